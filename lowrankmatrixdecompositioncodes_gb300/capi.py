@@ -1,0 +1,331 @@
+"""ctypes mirror of RSVDPACK's C API.
+
+The reference exposes plain C: column-major ``mat``/``vec`` structs
+(multi_core_mkl_code/matrix_vector_functions_intel_mkl.h:18-27) and the
+decomposition routines of multi_core_mkl_code/rank_revealing_algorithms_intel_mkl.h.
+``RsvdLibrary`` binds any shared library that exports that API -- the GPU engine
+(librsvdpack.so), or a CPU build of the same API -- and offers numpy-in /
+numpy-out wrappers with the reference's names, argument meanings and output
+conventions (0-based indices returned as float64, S as a dense k x k matrix,
+singular-value order as the reference gives it).
+
+Ownership follows the reference: inputs are borrowed, outputs are allocated by the
+callee with ``matrix_new``/``vector_new`` and released here with
+``matrix_delete``/``vector_delete`` after copying into numpy.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from typing import Callable, Optional
+
+import numpy as np
+
+
+class Mat(C.Structure):
+    _fields_ = [("nrows", C.c_int), ("ncols", C.c_int), ("d", C.POINTER(C.c_double))]
+
+
+class Vec(C.Structure):
+    _fields_ = [("nrows", C.c_int), ("d", C.POINTER(C.c_double))]
+
+
+PMat = C.POINTER(Mat)
+PVec = C.POINTER(Vec)
+OMEGA_FN = C.CFUNCTYPE(None, C.c_void_p, C.c_int, C.c_int, C.c_int, C.POINTER(C.c_double))
+
+_I, _D = C.c_int, C.c_double
+_PI = C.POINTER(C.c_int)
+_PPM = C.POINTER(PMat)
+_PPV = C.POINTER(PVec)
+
+# name -> argtypes for the reference API (rank_revealing_algorithms_intel_mkl.h:3-110)
+_ALGOS = {
+    "low_rank_svd_rand_decomp_fixed_rank": [PMat, _I, _I, _I, _I, _I, _PI, _PPM, _PPM, _PPM],
+    "low_rank_svd_blockrand_decomp_fixed_rank_or_prec":
+        [PMat, _I, _I, _D, _I, _I, _I, _I, _PI, _PPM, _PPM, _PPM],
+    "randQB_pb_new": [PMat, _I, _I, _D, _I, _I, _PI, _PPM, _PPM],
+    "pivotedQR_mkl": [PMat, _PPM, _PPM, _PPV],
+    "pivoted_QR_of_specified_rank_or_prec": [PMat, _I, _D, _PI, _PPM, _PPM, _PPV],
+    "id_decomp_fixed_rank_or_prec": [PMat, _I, _D, _PI, _PPV, _PPM],
+    "id_rand_decomp_fixed_rank": [PMat, _I, _I, _I, _I, _PPV, _PPM],
+    "id_blockrand_decomp_fixed_rank_or_prec": [PMat, _I, _I, _D, _I, _I, _I, _PI, _PPV, _PPM],
+    "id_two_sided_decomp_fixed_rank_or_prec": [PMat, _I, _D, _PI, _PPV, _PPV, _PPM, _PPM],
+    "id_two_sided_rand_decomp_fixed_rank": [PMat, _I, _I, _I, _I, _PPV, _PPV, _PPM, _PPM],
+    "id_two_sided_blockrand_decomp_fixed_rank_or_prec":
+        [PMat, _I, _I, _D, _I, _I, _I, _PI, _PPV, _PPV, _PPM, _PPM],
+    "cur_decomp_fixed_rank_or_prec": [PMat, _I, _D, _PI, _PPM, _PPM, _PPM],
+    "cur_rand_decomp_fixed_rank": [PMat, _I, _I, _I, _I, _PPM, _PPM, _PPM],
+    "cur_blockrand_decomp_fixed_rank_or_prec":
+        [PMat, _I, _I, _D, _I, _I, _I, _PI, _PPM, _PPM, _PPM],
+}
+
+
+class SeededOmega:
+    """Gaussian test matrices from a seed: request c of N values is
+    ``default_rng([seed, c]).standard_normal(N)`` rounded through float32 (the
+    reference draws float Gaussians, matrix_vector_functions_intel_mkl.c:458-486).
+    Values depend on the element count only, not on the requested shape."""
+
+    def __init__(self, seed: int = 0):
+        self.seed = int(seed)
+        self.served: list[np.ndarray] = []
+        self.record = False
+
+    def __call__(self, call_index: int, count: int) -> np.ndarray:
+        g = np.random.default_rng([self.seed, int(call_index)])
+        v = g.standard_normal(count).astype(np.float32)
+        if self.record:
+            self.served.append(v.copy())
+        return v
+
+
+class ListOmega:
+    """Serves a fixed list of float32 arrays, one per request, in order."""
+
+    def __init__(self, arrays):
+        self.arrays = [np.asarray(a, dtype=np.float32).ravel() for a in arrays]
+
+    def __call__(self, call_index: int, count: int) -> np.ndarray:
+        a = self.arrays[call_index]
+        if a.size != count:
+            raise ValueError(f"omega request {call_index}: want {count} values, have {a.size}")
+        return a
+
+
+class RsvdLibrary:
+    """Binds one shared library exporting the reference C API."""
+
+    def __init__(self, path: str):
+        self.path = str(path)
+        self.lib = C.CDLL(self.path)
+        L = self.lib
+        L.matrix_new.restype = PMat
+        L.matrix_new.argtypes = [_I, _I]
+        L.vector_new.restype = PVec
+        L.vector_new.argtypes = [_I]
+        L.matrix_delete.argtypes = [PMat]
+        L.vector_delete.argtypes = [PVec]
+        L.matrix_delete.restype = None
+        L.vector_delete.restype = None
+        L.get_matrix_frobenius_norm.restype = _D
+        L.get_matrix_frobenius_norm.argtypes = [PMat]
+        L.get_percent_error_between_two_mats.restype = _D
+        L.get_percent_error_between_two_mats.argtypes = [PMat, PMat]
+        for name, args in _ALGOS.items():
+            f = getattr(L, name, None)
+            if f is not None:
+                f.argtypes = args
+                f.restype = None
+        L.rsvdpack_set_omega_provider.argtypes = [OMEGA_FN, C.c_void_p]
+        L.rsvdpack_set_omega_provider.restype = None
+        L.rsvdpack_reset_omega_counter.argtypes = []
+        L.rsvdpack_reset_omega_counter.restype = None
+        L.rsvdpack_omega_calls.restype = C.c_int
+        self._omega_cb = None
+        self._omega = None
+
+    # ---------------------------------------------------------------- helpers
+    def has(self, name: str) -> bool:
+        return hasattr(self.lib, name)
+
+    def to_mat(self, A) -> PMat:
+        A = np.asarray(A, dtype=np.float64)
+        if A.ndim != 2:
+            raise ValueError("matrix must be 2-D")
+        m, n = A.shape
+        pM = self.lib.matrix_new(m, n)
+        if m * n:
+            buf = np.ctypeslib.as_array(pM.contents.d, shape=(m * n,))
+            buf[:] = A.ravel(order="F")
+        return pM
+
+    def from_mat(self, pM: PMat, free: bool = True) -> np.ndarray:
+        m, n = pM.contents.nrows, pM.contents.ncols
+        if m * n:
+            out = np.ctypeslib.as_array(pM.contents.d, shape=(m * n,)).copy()
+            out = out.reshape((m, n), order="F")
+        else:
+            out = np.zeros((m, n))
+        if free:
+            self.lib.matrix_delete(pM)
+        return out
+
+    def from_vec(self, pv: PVec, free: bool = True) -> np.ndarray:
+        n = pv.contents.nrows
+        out = np.ctypeslib.as_array(pv.contents.d, shape=(n,)).copy() if n else np.zeros(0)
+        if free:
+            self.lib.vector_delete(pv)
+        return out
+
+    def set_omega(self, provider: Optional[Callable[[int, int], np.ndarray]]):
+        """Register the Gaussian test-matrix provider (None: library default)."""
+        if provider is None:
+            self._omega_cb = None
+            self._omega = None
+            self.lib.rsvdpack_set_omega_provider(OMEGA_FN(), None)
+            return
+
+        def _cb(ctx, call_index, nrows, ncols, out):
+            count = int(nrows) * int(ncols)
+            vals = provider(int(call_index), count)
+            np.ctypeslib.as_array(out, shape=(count,))[:] = vals
+
+        self._omega = provider
+        self._omega_cb = OMEGA_FN(_cb)
+        self.lib.rsvdpack_set_omega_provider(self._omega_cb, None)
+
+    def omega_calls(self) -> int:
+        return int(self.lib.rsvdpack_omega_calls())
+
+    def _call(self, name, M, *scalars, nm=0, nv=0, frank=False):
+        pm = [PMat() for _ in range(nm)]
+        pv = [PVec() for _ in range(nv)]
+        fr = C.c_int(-1)
+        args = [M, *scalars]
+        if frank:
+            args.append(C.byref(fr))
+        return pm, pv, fr, args
+
+    # ------------------------------------------------------------ algorithms
+    def low_rank_svd_rand_decomp_fixed_rank(self, A, k, p, vnum, q, s):
+        M = self.to_mat(A)
+        U, S, V, fr = PMat(), PMat(), PMat(), C.c_int(-1)
+        try:
+            self.lib.low_rank_svd_rand_decomp_fixed_rank(
+                M, k, p, vnum, q, s, C.byref(fr), C.byref(U), C.byref(S), C.byref(V))
+        finally:
+            self.lib.matrix_delete(M)
+        return self.from_mat(U), self.from_mat(S), self.from_mat(V)
+
+    def low_rank_svd_blockrand_decomp_fixed_rank_or_prec(self, A, k, p, TOL, vnum, kstep, q, s):
+        M = self.to_mat(A)
+        U, S, V, fr = PMat(), PMat(), PMat(), C.c_int(-1)
+        try:
+            self.lib.low_rank_svd_blockrand_decomp_fixed_rank_or_prec(
+                M, k, p, float(TOL), vnum, kstep, q, s, C.byref(fr),
+                C.byref(U), C.byref(S), C.byref(V))
+        finally:
+            self.lib.matrix_delete(M)
+        return self.from_mat(U), self.from_mat(S), self.from_mat(V), fr.value
+
+    def randQB_pb_new(self, A, kstep, nstep, TOL, q, s):
+        M = self.to_mat(A)
+        Q, B, fr = PMat(), PMat(), C.c_int(-1)
+        try:
+            self.lib.randQB_pb_new(M, kstep, nstep, float(TOL), q, s, C.byref(fr),
+                                   C.byref(Q), C.byref(B))
+        finally:
+            self.lib.matrix_delete(M)
+        return self.from_mat(Q), self.from_mat(B), fr.value
+
+    def pivotedQR_mkl(self, A):
+        M = self.to_mat(A)
+        Q, R, I = PMat(), PMat(), PVec()
+        try:
+            self.lib.pivotedQR_mkl(M, C.byref(Q), C.byref(R), C.byref(I))
+        finally:
+            self.lib.matrix_delete(M)
+        return self.from_mat(Q), self.from_mat(R), self.from_vec(I)
+
+    def pivoted_QR_of_specified_rank_or_prec(self, A, k, TOL):
+        M = self.to_mat(A)
+        Q, R, I, fr = PMat(), PMat(), PVec(), C.c_int(-1)
+        try:
+            self.lib.pivoted_QR_of_specified_rank_or_prec(
+                M, k, float(TOL), C.byref(fr), C.byref(Q), C.byref(R), C.byref(I))
+        finally:
+            self.lib.matrix_delete(M)
+        return self.from_mat(Q), self.from_mat(R), self.from_vec(I), fr.value
+
+    def id_decomp_fixed_rank_or_prec(self, A, k, TOL):
+        M = self.to_mat(A)
+        I, T, fr = PVec(), PMat(), C.c_int(-1)
+        try:
+            self.lib.id_decomp_fixed_rank_or_prec(M, k, float(TOL), C.byref(fr),
+                                                  C.byref(I), C.byref(T))
+        finally:
+            self.lib.matrix_delete(M)
+        return self.from_vec(I), self.from_mat(T), fr.value
+
+    def id_rand_decomp_fixed_rank(self, A, k, p, q, s):
+        M = self.to_mat(A)
+        I, T = PVec(), PMat()
+        try:
+            self.lib.id_rand_decomp_fixed_rank(M, k, p, q, s, C.byref(I), C.byref(T))
+        finally:
+            self.lib.matrix_delete(M)
+        return self.from_vec(I), self.from_mat(T)
+
+    def id_blockrand_decomp_fixed_rank_or_prec(self, A, k, p, TOL, kstep, q, s):
+        M = self.to_mat(A)
+        I, T, fr = PVec(), PMat(), C.c_int(-1)
+        try:
+            self.lib.id_blockrand_decomp_fixed_rank_or_prec(
+                M, k, p, float(TOL), kstep, q, s, C.byref(fr), C.byref(I), C.byref(T))
+        finally:
+            self.lib.matrix_delete(M)
+        return self.from_vec(I), self.from_mat(T), fr.value
+
+    def id_two_sided_decomp_fixed_rank_or_prec(self, A, k, TOL):
+        M = self.to_mat(A)
+        Ic, Ir, T, S, fr = PVec(), PVec(), PMat(), PMat(), C.c_int(-1)
+        try:
+            self.lib.id_two_sided_decomp_fixed_rank_or_prec(
+                M, k, float(TOL), C.byref(fr), C.byref(Ic), C.byref(Ir), C.byref(T), C.byref(S))
+        finally:
+            self.lib.matrix_delete(M)
+        return (self.from_vec(Ic), self.from_vec(Ir), self.from_mat(T), self.from_mat(S),
+                fr.value)
+
+    def id_two_sided_rand_decomp_fixed_rank(self, A, k, p, q, s):
+        M = self.to_mat(A)
+        Ic, Ir, T, S = PVec(), PVec(), PMat(), PMat()
+        try:
+            self.lib.id_two_sided_rand_decomp_fixed_rank(
+                M, k, p, q, s, C.byref(Ic), C.byref(Ir), C.byref(T), C.byref(S))
+        finally:
+            self.lib.matrix_delete(M)
+        return self.from_vec(Ic), self.from_vec(Ir), self.from_mat(T), self.from_mat(S)
+
+    def id_two_sided_blockrand_decomp_fixed_rank_or_prec(self, A, k, p, TOL, kstep, q, s):
+        M = self.to_mat(A)
+        Ic, Ir, T, S, fr = PVec(), PVec(), PMat(), PMat(), C.c_int(-1)
+        try:
+            self.lib.id_two_sided_blockrand_decomp_fixed_rank_or_prec(
+                M, k, p, float(TOL), kstep, q, s, C.byref(fr), C.byref(Ic), C.byref(Ir),
+                C.byref(T), C.byref(S))
+        finally:
+            self.lib.matrix_delete(M)
+        return (self.from_vec(Ic), self.from_vec(Ir), self.from_mat(T), self.from_mat(S),
+                fr.value)
+
+    def cur_decomp_fixed_rank_or_prec(self, A, k, TOL):
+        M = self.to_mat(A)
+        Cm, U, R, fr = PMat(), PMat(), PMat(), C.c_int(-1)
+        try:
+            self.lib.cur_decomp_fixed_rank_or_prec(M, k, float(TOL), C.byref(fr),
+                                                   C.byref(Cm), C.byref(U), C.byref(R))
+        finally:
+            self.lib.matrix_delete(M)
+        return self.from_mat(Cm), self.from_mat(U), self.from_mat(R), fr.value
+
+    def cur_rand_decomp_fixed_rank(self, A, k, p, q, s):
+        M = self.to_mat(A)
+        Cm, U, R = PMat(), PMat(), PMat()
+        try:
+            self.lib.cur_rand_decomp_fixed_rank(M, k, p, q, s, C.byref(Cm), C.byref(U),
+                                                C.byref(R))
+        finally:
+            self.lib.matrix_delete(M)
+        return self.from_mat(Cm), self.from_mat(U), self.from_mat(R)
+
+    def cur_blockrand_decomp_fixed_rank_or_prec(self, A, k, p, TOL, kstep, q, s):
+        M = self.to_mat(A)
+        Cm, U, R, fr = PMat(), PMat(), PMat(), C.c_int(-1)
+        try:
+            self.lib.cur_blockrand_decomp_fixed_rank_or_prec(
+                M, k, p, float(TOL), kstep, q, s, C.byref(fr), C.byref(Cm), C.byref(U),
+                C.byref(R))
+        finally:
+            self.lib.matrix_delete(M)
+        return self.from_mat(Cm), self.from_mat(U), self.from_mat(R), fr.value
