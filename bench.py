@@ -1,0 +1,389 @@
+#!/usr/bin/env python
+"""Benchmark: rSVD solves/sec on the mixed-precision single large rSVD workload.
+
+Workload (one "step" = one fixed-rank randomized SVD with the reference's semantics):
+  A 16384 x 8192 FP32 = U diag(s) V^T + 1e-4 G, s_i = i^-1.5, Haar U, V, G standard
+  Gaussian (seeded synthetic data); k=256, p=16, q=2 (reference semantics: one power
+  round), s=1, vnum=1.
+  value : solves/s with A resident in HBM, through rsvdpack_dev_svd_fixed_rank.
+  e2e   : solves/s through the reference C API (low_rank_svd_rand_decomp_fixed_rank)
+          from a pinned host FP64 matrix: H2D of A, solve, D2H of U, S, V every step.
+  A (512 MiB) is larger than L2 (129 MB), so no flush is needed between steps.
+  Residual ||A - U S V^T||_F / ||A||_F is checked against the FP64 path of the same
+  method on the same test matrix ("matched FP64-oracle error").
+
+--impl reference times the CPU oracle (oracle/port: the reference's algorithm on
+OpenBLAS, all host cores) on the same workload and prints the same JSON line.
+Multi-GPU (torchrun): independent replicas, one matrix per rank ("scaling": "weak").
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+M_ROWS, N_COLS, K, P, Q, S_ORTH, VNUM = 16384, 8192, 256, 16, 2, 1, 1
+METRIC = "rSVD solves/sec at matched FP64-oracle error (16384x8192 FP32, k=256, p=16, q=2)"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--precision", default=os.environ.get("RSVDPACK_BENCH_PRECISION", "tf32"),
+                    choices=["fp64", "fp32", "tf32", "bf16"])
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    return (int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)),
+            int(os.environ.get("LOCAL_RANK", 0)))
+
+
+def make_matrix(torch, device, seed):
+    """A = U diag(i^-1.5) V^T + 1e-4 G in FP32 on the GPU (Haar U, V from QR of Gaussians)."""
+    g = torch.Generator(device=device)
+    g.manual_seed(seed)
+    m, n = M_ROWS, N_COLS
+    Ug, _ = torch.linalg.qr(torch.randn(m, n, device=device, generator=g))
+    Vg, _ = torch.linalg.qr(torch.randn(n, n, device=device, generator=g))
+    s = torch.arange(1, n + 1, device=device, dtype=torch.float32) ** -1.5
+    A = (Ug * s) @ Vg.T + 1e-4 * torch.randn(m, n, device=device, generator=g)
+    del Ug, Vg
+    # column-major storage: the transpose of a row-major n x m tensor
+    At = A.T.contiguous()          # At[j, i] = A[i, j]; memory = A column-major, ld = m
+    del A
+    torch.cuda.synchronize()
+    return At
+
+
+class ClockSampler:
+    """nvidia-smi sampling during the timed region (SM clock, throttle reasons)."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            threading.Thread(target=self._read, daemon=True).start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [x.strip() for x in ln.split(",")]
+            if len(parts) < 7:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx = float(parts[1])
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[3:7]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        sm.sort()
+        med = sm[len(sm) // 2] if sm else None
+        return {"sm_mhz": med, "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), float(d["bf16_tflops"]), "measured"
+    except Exception:
+        return 6800.0, 1900.0, "fallback"
+
+
+def cpu_solve_seconds(A_host, threads, repeats=1):
+    """Time the CPU oracle (oracle/port) on the workload; returns seconds per solve."""
+    from lowrankmatrixdecompositioncodes_gb300.capi import RsvdLibrary, SeededOmega
+    so = os.path.join(ROOT, "oracle", "port", "librsvd_port.so")
+    if not os.path.exists(so):
+        subprocess.check_call(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "port"])
+    port = RsvdLibrary(so)
+    port.lib.rsvdpack_set_num_threads(threads)
+    port.set_omega(SeededOmega(1234))
+    M = port.to_mat(A_host)
+    from lowrankmatrixdecompositioncodes_gb300.capi import PMat
+    times = []
+    for _ in range(repeats):
+        U, S, V, fr = PMat(), PMat(), PMat(), C.c_int(0)
+        t0 = time.perf_counter()
+        port.lib.low_rank_svd_rand_decomp_fixed_rank(M, K, P, VNUM, Q, S_ORTH, C.byref(fr), C.byref(U),
+                                                     C.byref(S), C.byref(V))
+        times.append(time.perf_counter() - t0)
+        for x in (U, S, V):
+            port.lib.matrix_delete(x)
+    port.lib.matrix_delete(M)
+    return times
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return 0
+    import numpy as np
+    import torch
+    dev = "cuda:0" if torch.cuda.is_available() else "cpu"
+    if dev.startswith("cuda"):
+        At = make_matrix(torch, dev, seed=1)
+        A_host = At.T.double().cpu().numpy()       # m x n view of column-major data
+        del At
+        torch.cuda.empty_cache()
+    else:
+        g = np.random.default_rng(1)
+        A_host = g.standard_normal((M_ROWS, N_COLS))
+    threads = os.cpu_count() or 1
+    t_all = cpu_solve_seconds(A_host, threads, repeats=args.warmup + args.steps)
+    t = t_all[args.warmup:]
+    sec = sum(t) / len(t)
+    val = 1.0 / sec
+    line = {
+        "impl": "reference", "metric": METRIC, "value": val, "unit": "solves/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * sec, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": "single large rSVD 16384x8192 k=256 p=16 q=2 s=1 vnum=1", "m": M_ROWS,
+                   "n": N_COLS, "k": K, "p": P, "q": Q, "s": S_ORTH},
+        "cpu_baseline": {"value": val, "unit": "solves/s", "cores": threads, "kind": "port",
+                         "sample": f"{args.steps} full solves of the workload (after {args.warmup} warm-up)"},
+        "e2e": {"value": val, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_ours(args):
+    rank, world, local = dist_env()
+    os.environ["RSVDPACK_DEVICE"] = str(local)
+    import numpy as np
+    import torch
+    torch.cuda.set_device(local)
+    dev = f"cuda:{local}"
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device(dev))
+    from lowrankmatrixdecompositioncodes_gb300 import load_engine
+    from lowrankmatrixdecompositioncodes_gb300.capi import PMat
+
+    eng = load_engine()
+    sms, name, cc = eng.device_info()
+    if sms <= 0:
+        raise RuntimeError(f"engine unavailable: {eng.last_error()}")
+    eng.set_precision(args.precision)
+    eng.set_use_provider(False)
+    L = eng.lib
+    L.rsvdpack_dev_svd_fixed_rank.restype = C.c_int
+    L.rsvdpack_dev_svd_fixed_rank.argtypes = [C.c_void_p, C.c_int, C.c_longlong, C.c_int, C.c_int, C.c_int, C.c_int,
+                                              C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_longlong, C.c_void_p,
+                                              C.c_void_p, C.c_longlong]
+    L.rsvdpack_dev_sketch.restype = C.c_int
+    L.rsvdpack_dev_sketch.argtypes = [C.c_void_p, C.c_int, C.c_longlong, C.c_int, C.c_int, C.c_void_p,
+                                      C.c_longlong, C.c_int, C.c_void_p, C.c_longlong, C.c_int]
+    L.rsvdpack_stream.restype = C.c_void_p
+    L.rsvdpack_reset_omega_counter.restype = None
+
+    m, n, k, l = M_ROWS, N_COLS, K, K + P
+    At = make_matrix(torch, dev, seed=1 + rank)        # column-major A, ld = m
+    dA = At.data_ptr()
+    dt = 0 if args.precision == "fp64" else 1
+    if dt == 0:
+        At64 = At.double()
+        dA = At64.data_ptr()
+    tdt = torch.float64 if dt == 0 else torch.float32
+    U = torch.empty(k, m, device=dev, dtype=tdt)        # column-major m x k
+    V = torch.empty(k, n, device=dev, dtype=tdt)
+    Sv = torch.empty(k, device=dev, dtype=torch.float64)
+    stream = torch.cuda.ExternalStream(L.rsvdpack_stream())
+
+    def solve():
+        rc = L.rsvdpack_dev_svd_fixed_rank(dA, dt, m, m, n, k, P, VNUM, Q, S_ORTH, U.data_ptr(), m,
+                                           Sv.data_ptr(), V.data_ptr(), n)
+        if rc:
+            raise RuntimeError(f"solve failed: {eng.last_error()}")
+
+    def residual():
+        Ur, Vr = U.T.double(), V.T.double()
+        Ad = At.T.double()
+        R = Ad - (Ur * Sv) @ Vr.T
+        return float(torch.linalg.norm(R) / torch.linalg.norm(Ad))
+
+    # matched-error check: same test matrix for the working precision and for FP64
+    L.rsvdpack_reset_omega_counter()
+    solve()
+    res_mixed = residual()
+    res_fp64 = None
+    if args.precision != "fp64":
+        eng.set_precision("fp64")
+        A64 = At.double()
+        U64 = torch.empty(k, m, device=dev, dtype=torch.float64)
+        V64 = torch.empty(k, n, device=dev, dtype=torch.float64)
+        S64 = torch.empty(k, device=dev, dtype=torch.float64)
+        L.rsvdpack_reset_omega_counter()
+        rc = L.rsvdpack_dev_svd_fixed_rank(A64.data_ptr(), 0, m, m, n, k, P, VNUM, Q, S_ORTH, U64.data_ptr(), m,
+                                           S64.data_ptr(), V64.data_ptr(), n)
+        if rc:
+            raise RuntimeError(f"fp64 solve failed: {eng.last_error()}")
+        R = A64.T - (U64.T * S64) @ V64
+        res_fp64 = float(torch.linalg.norm(R) / torch.linalg.norm(A64))
+        del A64, U64, V64, S64, R
+        eng.set_precision(args.precision)
+        torch.cuda.empty_cache()
+
+    # ---------------- device-resident timed region
+    for _ in range(args.warmup):
+        solve()
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    sampler = ClockSampler(local)
+    sampler.start()
+    time.sleep(0.4)
+    launches = 0
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    ev0.record(stream)
+    for _ in range(args.steps):
+        solve()
+        launches += eng.last_timing().kernel_launches
+    ev1.record(stream)
+    ev1.synchronize()
+    torch.cuda.synchronize()
+    clocks = sampler.stop()
+    ms = ev0.elapsed_time(ev1) / args.steps
+    if world > 1:
+        t = torch.tensor([ms], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    value = world * 1000.0 / ms
+
+    # ---------------- dominant kernel: the sketch product, timed alone
+    X = torch.randn(l, n, device=dev, dtype=tdt)     # column-major n x l
+    Y = torch.empty(l, m, device=dev, dtype=tdt)
+    Xt = torch.randn(l, m, device=dev, dtype=tdt)
+    Z = torch.empty(l, n, device=dev, dtype=tdt)
+    kern = {}
+    for trans, (x, ldx, y, ldy) in ((0, (X, n, Y, m)), (1, (Xt, m, Z, n))):
+        for _ in range(2):
+            L.rsvdpack_dev_sketch(dA, dt, m, m, n, x.data_ptr(), ldx, l, y.data_ptr(), ldy, trans)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        reps = 5
+        e0.record(stream)
+        for _ in range(reps):
+            L.rsvdpack_dev_sketch(dA, dt, m, m, n, x.data_ptr(), ldx, l, y.data_ptr(), ldy, trans)
+        e1.record(stream)
+        e1.synchronize()
+        kern[trans] = e0.elapsed_time(e1) / reps
+    t_kern = 0.5 * (kern[0] + kern[1]) / 1000.0
+    esize = 8 if dt == 0 else 4
+    bytes_alg = m * n * esize + (n * l + m * l) * esize
+    flops_alg = 2.0 * m * n * l
+    hbm_peak, tc_peak, peak_kind = measured_peaks()
+    gbs = bytes_alg / t_kern / 1e9
+    tfs = flops_alg / t_kern / 1e12
+    if args.precision in ("tf32", "bf16"):
+        roof = {"bound": "hbm", "achieved": gbs, "peak": hbm_peak, "unit": "GB/s", "frac": gbs / hbm_peak,
+                "traffic": None, "peak_kind": peak_kind, "kernel": "sketch product (tcgen05)",
+                "tflops": tfs, "ms_per_launch": {"A*X": kern[0], "A^T*X": kern[1]}}
+    else:
+        roof = {"bound": "hbm", "achieved": gbs, "peak": hbm_peak, "unit": "GB/s", "frac": gbs / hbm_peak,
+                "traffic": None, "peak_kind": peak_kind, "kernel": "sketch product (CUDA-core GEMM)",
+                "tflops": tfs, "ms_per_launch": {"A*X": kern[0], "A^T*X": kern[1]}}
+    del X, Y, Xt, Z
+
+    # ---------------- end to end through the reference C API, pinned host FP64 A
+    e2e = None
+    if not args.no_e2e:
+        A_pin = torch.empty(n, m, dtype=torch.float64, pin_memory=True)   # column-major m x n
+        A_pin.copy_(At.double().cpu())
+        from lowrankmatrixdecompositioncodes_gb300.capi import Mat
+        Mh = Mat(m, n, C.cast(C.c_void_p(A_pin.data_ptr()), C.POINTER(C.c_double)))
+        t_e2e = []
+        for i in range(args.warmup + args.steps):
+            Uo, So, Vo, fr = PMat(), PMat(), PMat(), C.c_int(0)
+            t0 = time.perf_counter()
+            L.low_rank_svd_rand_decomp_fixed_rank(C.byref(Mh), k, P, VNUM, Q, S_ORTH, C.byref(fr), C.byref(Uo),
+                                                  C.byref(So), C.byref(Vo))
+            t1 = time.perf_counter()
+            eng.check()
+            for x in (Uo, So, Vo):
+                L.matrix_delete(x)
+            if i >= args.warmup:
+                t_e2e.append(t1 - t0)
+        sec = sum(t_e2e) / len(t_e2e)
+        e2e = {"value": world / sec, "unit": "solves/s", "h2d_bytes_per_step": m * n * 8,
+               "d2h_bytes_per_step": 8 * (m * k + n * k + k), "ms_per_step": 1000 * sec}
+        del A_pin
+
+    # ---------------- CPU baseline: the oracle on the host cores, one full solve
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        A_host = At.T.double().cpu().numpy()
+        threads = os.cpu_count() or 1
+        t_cpu = cpu_solve_seconds(A_host, threads, repeats=1)
+        cpu = {"value": 1.0 / t_cpu[0], "unit": "solves/s", "cores": threads, "kind": "port",
+               "sample": "1 full solve of the workload on the CPU oracle (reference algorithm, OpenBLAS)"}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": {"fp64": "f64", "fp32": "f32", "tf32": "tf32", "bf16": "bf16"}[args.precision],
+            "data": "synthetic (seeded; A = U diag(i^-1.5) V^T + 1e-4 G)",
+            "config": {"workload": "single large rSVD 16384x8192 k=256 p=16 q=2 s=1 vnum=1", "m": m, "n": n, "k": k,
+                       "p": P, "q": Q, "s": S_ORTH, "precision": args.precision,
+                       "l2": "inputs larger than L2 (A = 512 MiB)", "parallelism": f"replicas x{world}"},
+            "residual": {"rel_frobenius": res_mixed, "fp64_same_method": res_fp64,
+                         "matched": (res_fp64 is None) or (res_mixed <= (1 + 1e-3) * res_fp64)},
+            "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches, "clocks": clocks,
+            "device": name,
+        }
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,218 @@
+/*
+ * rsvdpack.h -- public C ABI of librsvdpack.so, the GB300 (sm_103a) engine for
+ * RSVDPACK's randomized low-rank decompositions.
+ *
+ * Part 1 reproduces the reference's C API as a drop-in: the same struct layouts,
+ * function names, argument meanings, output shapes and ownership rules.
+ *   - mat / vec and their helpers: multi_core_mkl_code/matrix_vector_functions_intel_mkl.h
+ *   - decompositions:             multi_core_mkl_code/rank_revealing_algorithms_intel_mkl.h
+ * Matrices are column-major doubles on the host (ld = nrows).  Inputs are
+ * borrowed and never modified; outputs are allocated by the callee with
+ * matrix_new / vector_new (calloc) and freed by the caller with
+ * matrix_delete / vector_delete.  Index vectors hold 0-based integers as doubles.
+ * All calls are synchronous: device work is finished when they return.
+ * Calls are re-entrant per host thread (each thread owns a CUDA stream).
+ *
+ * The reference returns void and ignores LAPACK's info; so does this drop-in.
+ * Failures (bad arguments, CUDA errors, device timeouts) never exit(): the
+ * outputs are set to NULL and rsvdpack_last_error() reports a non-zero code.
+ *
+ * Part 2 holds additive extensions (precision modes, sketch-matrix provider,
+ * device-resident entry points, residual reporting).  They have no counterpart
+ * in the reference unless stated.
+ */
+#ifndef RSVDPACK_H
+#define RSVDPACK_H
+
+#include <stddef.h>
+#include <stdint.h>
+#include <sys/time.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ============================== Part 1: reference API ============================== */
+
+/* matrix_vector_functions_intel_mkl.h:18-27 (LP64 int dimensions, column-major) */
+typedef struct {
+    int nrows, ncols;
+    double *d;
+} mat;
+
+typedef struct {
+    int nrows;
+    double *d;
+} vec;
+
+/* ---- storage and element access: matrix_vector_functions_intel_mkl.h:31-58 ---- */
+mat *matrix_new(int nrows, int ncols);
+vec *vector_new(int nrows);
+void matrix_delete(mat *M);
+void vector_delete(vec *v);
+void matrix_set_element(mat *M, int row_num, int col_num, double val);
+double matrix_get_element(mat *M, int row_num, int col_num);
+void vector_set_element(vec *v, int row_num, double val);
+double vector_get_element(vec *v, int row_num);
+
+/* ---- binary matrix files: matrix_vector_functions_intel_mkl.h:60-64 (format: int32 m,
+ *      int32 n, then m*n doubles in row-major order; matrix_vector_functions_intel_mkl.c:77-133) ---- */
+mat *matrix_load_from_binary_file(char *fname);
+void matrix_write_to_binary_file(mat *M, char *fname);
+
+/* ---- helpers callers use around the decompositions ---- */
+void matrix_copy(mat *D, mat *S);                                 /* :92-94 */
+void matrix_build_transpose(mat *Mt, mat *M);                     /* :100-101 */
+double get_matrix_frobenius_norm(mat *M);                         /* :116-117 */
+double get_percent_error_between_two_mats(mat *A, mat *B);        /* :288-289 */
+void initialize_random_matrix(mat *M);                            /* :128-129 */
+void matrix_matrix_mult(mat *A, mat *B, mat *C);                  /* :132-133 */
+void matrix_transpose_matrix_mult(mat *A, mat *B, mat *C);        /* :136-137 */
+void matrix_matrix_transpose_mult(mat *A, mat *B, mat *C);        /* :140-141 */
+void form_svd_product_matrix(mat *U, mat *S, mat *V, mat *P);     /* :343-344 */
+void form_cur_product_matrix(mat *C, mat *U, mat *R, mat *P);     /* :346-347 */
+double get_seconds_frac(struct timeval start_timeval, struct timeval end_timeval); /* :359-360 */
+
+/* ---- decompositions: rank_revealing_algorithms_intel_mkl.h ---- */
+/* :5  fixed-rank randomized SVD.  q means q-1 rounds of (M M^T); vnum 1 (or >2): QR of
+ *     B^T route, singular values descending; vnum 2: eig(B B^T) route, ascending.
+ *     U m x k, S k x k dense diagonal, V n x k.  frank is not written (as in the reference). */
+void low_rank_svd_rand_decomp_fixed_rank(mat *M, int k, int p, int vnum, int q, int s,
+                                         int *frank, mat **U, mat **S, mat **V);
+/* :7  blocked randomized SVD (rank k, or absolute Frobenius tolerance TOL when k <= 0) */
+void low_rank_svd_blockrand_decomp_fixed_rank_or_prec(mat *M, int k, int p, double TOL,
+                                                      int vnum, int kstep, int q, int s,
+                                                      int *frank, mat **U, mat **S, mat **V);
+/* :67 blocked randomized QB (nstep <= 0 selects the TOL mode) */
+void randQB_pb_new(mat *M, int kstep, int nstep, double TOL, int q, int s, int *frank,
+                   mat **Q, mat **B);
+/* :43 full column-pivoted QR, M(:,I) = Q R (LAPACK dgeqp3 pivoting, all columns free) */
+void pivotedQR_mkl(mat *M, mat **Q, mat **R, vec **I);
+/* :52 partial pivoted Householder QR of rank k, or of precision TOL when k <= 0 */
+void pivoted_QR_of_specified_rank_or_prec(mat *M, int k, double TOL, int *frank,
+                                          mat **Qk, mat **Rk, vec **I);
+/* :73 column ID, T = Rk1^-1 Rk2 */
+void id_decomp_fixed_rank_or_prec(mat *M, int k, double TOL, int *frank, vec **I, mat **T);
+/* :76 randomized column ID (row sketch (k+p) x n, q power rounds) */
+void id_rand_decomp_fixed_rank(mat *M, int k, int p, int q, int s, vec **I, mat **T);
+/* :79 blocked randomized column ID */
+void id_blockrand_decomp_fixed_rank_or_prec(mat *M, int k, int p, double TOL, int kstep,
+                                            int q, int s, int *frank, vec **I, mat **T);
+/* :84 two-sided ID */
+void id_two_sided_decomp_fixed_rank_or_prec(mat *M, int k, double TOL, int *frank,
+                                            vec **Icol, vec **Irow, mat **T, mat **S);
+/* :87 randomized two-sided ID.  The reference header names the parameters (k,l,p,s);
+ *     the definition (rank_revealing_algorithms_intel_mkl.c:2060) uses (k,p,q,s). */
+void id_two_sided_rand_decomp_fixed_rank(mat *M, int k, int p, int q, int s,
+                                         vec **Icol, vec **Irow, mat **T, mat **S);
+/* :90 blocked randomized two-sided ID */
+void id_two_sided_blockrand_decomp_fixed_rank_or_prec(mat *M, int k, int p, double TOL,
+                                                      int kstep, int q, int s, int *frank,
+                                                      vec **Icol, vec **Irow, mat **T, mat **S);
+/* :95 CUR */
+void cur_decomp_fixed_rank_or_prec(mat *M, int k, double TOL, int *frank,
+                                   mat **C, mat **U, mat **R);
+/* :98 randomized CUR */
+void cur_rand_decomp_fixed_rank(mat *M, int k, int p, int q, int s, mat **C, mat **U, mat **R);
+/* :101 blocked randomized CUR */
+void cur_blockrand_decomp_fixed_rank_or_prec(mat *M, int k, int p, double TOL, int kstep,
+                                             int q, int s, int *frank,
+                                             mat **C, mat **U, mat **R);
+/* :105-120 approximation reports (print norms and percent error, as the reference does).
+ * use_pivoted_QR_decomp_for_approximation frees Qk and Rk, as the reference does. */
+void use_low_rank_svd_for_approximation(mat *M, mat *U, mat *S, mat *V);
+void use_pivoted_QR_decomp_for_approximation(mat *M, mat *Qk, mat *Rk, vec *I);
+void use_QB_decomp_for_approximation(mat *M, mat *Q, mat *B);
+void use_id_decomp_for_approximation(mat *M, mat *T, vec *I, int k);
+void use_id_two_sided_decomp_for_approximation(mat *M, mat *T, mat *S, vec *Icol, vec *Irow, int k);
+void use_cur_decomp_for_approximation(mat *M, mat *C, mat *U, mat *R);
+
+/* ============================== Part 2: extensions ============================== */
+
+/* Status codes reported by rsvdpack_last_error() (per host thread). */
+enum {
+    RSVD_OK = 0,
+    RSVD_ERR_ARGUMENT = 1,     /* invalid sizes / parameters */
+    RSVD_ERR_CUDA = 2,         /* CUDA runtime error */
+    RSVD_ERR_NO_DEVICE = 3,    /* no usable sm_103a device */
+    RSVD_ERR_NUMERIC = 4,      /* non-finite input or breakdown that the fallbacks could not repair */
+    RSVD_ERR_TIMEOUT = 5,      /* a bounded device-side wait gave up */
+    RSVD_ERR_ALLOC = 6         /* device or host allocation failed */
+};
+int rsvdpack_last_error(void);
+const char *rsvdpack_last_error_string(void);
+void rsvdpack_clear_error(void);
+
+/* Arithmetic of the large products (sketch, power rounds, projections) and of the
+ * storage of A on the device.  Small k x k work (Cholesky, Jacobi, triangular
+ * solves, pivot decisions) is FP64 in every mode. */
+enum {
+    RSVD_PREC_FP64 = 0,   /* everything FP64: reproduces the reference (default) */
+    RSVD_PREC_FP32 = 1,   /* A and tall factors FP32, CUDA-core FP32 products */
+    RSVD_PREC_TF32 = 2,   /* A FP32, tcgen05 kind::tf32 products, FP32 accumulate */
+    RSVD_PREC_BF16 = 3    /* A FP32 + BF16 copy, tcgen05 kind::f16 (bf16) sketch products */
+};
+
+typedef struct {
+    int precision;            /* RSVD_PREC_* */
+    int use_provider;         /* 1: Gaussian test matrices come from the registered provider
+                                 when one is set (default 1); 0: always on-device Philox */
+    unsigned long long seed;  /* Philox key for on-device test matrices */
+    int verbose;              /* print the reference's progress lines (default 0) */
+    int reserved[8];
+} rsvdpack_opts;
+
+void rsvdpack_get_opts(rsvdpack_opts *opts);
+void rsvdpack_set_opts(const rsvdpack_opts *opts);
+
+/* Gaussian test-matrix provider.  The reference draws every test matrix with
+ * initialize_random_matrix (matrix_vector_functions_intel_mkl.c:458-486), time-seeded.
+ * A provider makes runs repeatable and lets a caller hand the engine the same test
+ * matrices it hands another implementation: request number call_index (0-based,
+ * counted since registration or the last reset) fills nrows*ncols doubles in
+ * column-major order.  Pass fn = NULL to go back to on-device Philox. */
+typedef void (*rsvd_omega_fn)(void *ctx, int call_index, int nrows, int ncols, double *out);
+void rsvdpack_set_omega_provider(rsvd_omega_fn fn, void *ctx);
+void rsvdpack_reset_omega_counter(void);
+int rsvdpack_omega_calls(void);
+
+/* Device and build information: fills name (>= 64 bytes); returns the SM count, or
+ * a negative value when no usable device is present. */
+int rsvdpack_device_info(char *name, int name_len, int *cc_major, int *cc_minor);
+
+/* ---- device-resident entry points (no counterpart in the reference) ----
+ * For callers whose matrices already live in GPU memory.  Pointers are device
+ * pointers; matrices are column-major with the given leading dimensions (elements).
+ * dtype: RSVD_DT_F64 or RSVD_DT_F32 (FP32 data is computed in the current precision
+ * mode's arithmetic; FP64 data always in FP64).  The work is queued on the calling
+ * thread's engine stream (rsvdpack_stream()); the call returns after it finishes.
+ * Return value: RSVD_OK or an RSVD_ERR_* code (also kept in rsvdpack_last_error()). */
+enum { RSVD_DT_F64 = 0, RSVD_DT_F32 = 1 };
+
+/* Fixed-rank rSVD with the reference's semantics (as low_rank_svd_rand_decomp_fixed_rank).
+ * Outputs: U (m x k, ldu), S (k values, double, reference order), V (n x k, ldv), all
+ * caller-allocated device buffers, U and V in the input dtype. */
+int rsvdpack_dev_svd_fixed_rank(const void *dA, int dtype, long long lda, int m, int n, int k, int p,
+                                int vnum, int q, int s, void *dU, long long ldu, double *dS, void *dV,
+                                long long ldv);
+
+/* One sketch product with the engine's product kernel for the current precision:
+ * trans == 0: Y (m x w) = A X with X (n x w);  trans == 1: Y (n x w) = A^T X with X (m x w). */
+int rsvdpack_dev_sketch(const void *dA, int dtype, long long lda, int m, int n, const void *dX, long long ldx,
+                        int w, void *dY, long long ldy, int trans);
+
+/* The calling thread's engine stream (a cudaStream_t), for event timing by callers. */
+void *rsvdpack_stream(void);
+
+/* Per-call phase timing of the last decomposition on this thread (milliseconds). */
+typedef struct {
+    double upload_ms, sketch_ms, orth_ms, small_ms, download_ms, total_ms;
+    long long gemm_launches, kernel_launches;
+} rsvdpack_timing;
+void rsvdpack_last_timing(rsvdpack_timing *t);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* RSVDPACK_H */

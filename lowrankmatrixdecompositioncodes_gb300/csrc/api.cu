@@ -1,0 +1,723 @@
+// api.cu -- extern "C" drop-in for RSVDPACK's C API (include/rsvdpack.h, Part 1).
+//
+// Each entry point: validate -> upload A (host double, column-major) to the device in the
+// engine's working precision -> run the device algorithm (engine.cu) -> allocate the
+// outputs with matrix_new / vector_new and copy them back.  Errors never exit(): the
+// outputs are set to NULL and rsvdpack_last_error() reports the cause.
+#include "engine.h"
+
+#include <chrono>
+#include <cmath>
+#include <cstdlib>
+#include <cstring>
+
+using namespace rsvd;
+
+namespace {
+
+using Clock = std::chrono::steady_clock;
+double ms_since(Clock::time_point t0) {
+    return std::chrono::duration<double, std::milli>(Clock::now() - t0).count();
+}
+
+template <typename F>
+void guarded(const char *fn, F &&body) {
+    try {
+        rsvdpack_clear_error();
+        body();
+    } catch (const Error &e) {
+        set_error(e.code, std::string(fn) + ": " + e.what());
+    } catch (const std::bad_alloc &) {
+        set_error(RSVD_ERR_ALLOC, std::string(fn) + ": host allocation failed");
+    } catch (const std::exception &e) {
+        set_error(RSVD_ERR_CUDA, std::string(fn) + ": " + e.what());
+    }
+}
+
+void need(bool ok, const char *what) {
+    if (!ok) fail(RSVD_ERR_ARGUMENT, what);
+}
+
+void check_mat(const mat *M) {
+    need(M != nullptr && M->d != nullptr, "null matrix");
+    need(M->nrows > 0 && M->ncols > 0, "empty matrix");
+}
+
+// Working precision of the tall products for this call.
+bool use_fp32_path() { return ctx().opts.precision != RSVD_PREC_FP64; }
+
+template <typename T>
+DMat<T> upload(const mat *M) {
+    cudaStream_t s = ctx().stream;
+    const i64 m = M->nrows, n = M->ncols;
+    if (std::is_same<T, double>::value) {
+        DMat<T> A(m, n, s, false);
+        RSVD_CK(cudaMemcpy2DAsync(A.v.p, sizeof(T) * A.v.ld, M->d, sizeof(double) * m, sizeof(double) * m, n,
+                                  cudaMemcpyHostToDevice, s));
+        return A;
+    }
+    DMat<double> tmp(m, n, s, false);
+    RSVD_CK(cudaMemcpy2DAsync(tmp.v.p, sizeof(double) * tmp.v.ld, M->d, sizeof(double) * m, sizeof(double) * m, n,
+                              cudaMemcpyHostToDevice, s));
+    DMat<T> A(m, n, s, false);
+    convert<double, T>(s, tmp.v, A.v);
+    RSVD_CK(cudaStreamSynchronize(s));
+    return A;
+}
+
+template <typename T>
+mat *download(DM<T> a) {
+    cudaStream_t s = ctx().stream;
+    mat *M = matrix_new((int)a.r, (int)a.c);
+    if (!M) throw std::bad_alloc();
+    if (a.r * a.c == 0) return M;
+    if (std::is_same<T, double>::value) {
+        RSVD_CK(cudaMemcpy2DAsync(M->d, sizeof(double) * a.r, a.p, sizeof(T) * a.ld, sizeof(double) * a.r, a.c,
+                                  cudaMemcpyDeviceToHost, s));
+    } else {
+        DMat<double> tmp(a.r, a.c, s, false);
+        convert<T, double>(s, a, tmp.v);
+        RSVD_CK(cudaMemcpy2DAsync(M->d, sizeof(double) * a.r, tmp.v.p, sizeof(double) * tmp.v.ld,
+                                  sizeof(double) * a.r, a.c, cudaMemcpyDeviceToHost, s));
+        RSVD_CK(cudaStreamSynchronize(s));
+    }
+    RSVD_CK(cudaStreamSynchronize(s));
+    return M;
+}
+
+mat *diag_mat(const std::vector<double> &d) {
+    const int k = (int)d.size();
+    mat *S = matrix_new(k, k);
+    for (int i = 0; i < k; i++) S->d[(size_t)i * k + i] = d[(size_t)i];
+    return S;
+}
+
+vec *index_vec(const std::vector<int> &I) {
+    vec *v = vector_new((int)I.size());
+    for (size_t i = 0; i < I.size(); i++) v->d[i] = (double)I[i];
+    return v;
+}
+
+void begin_call() {
+    Ctx &c = ctx();
+    c.opts = global_opts();
+    std::memset(&c.timing, 0, sizeof c.timing);
+    c.launches = 0;
+}
+
+void end_call(Clock::time_point t0) {
+    Ctx &c = ctx();
+    check_device_flags(c);
+    c.timing.total_ms = ms_since(t0);
+    c.timing.kernel_launches = c.launches;
+}
+
+template <typename T>
+void svd_outputs(SvdOut<T> &r, mat **U, mat **S, mat **V) {
+    *U = download<T>(r.U.v);
+    *V = download<T>(r.V.v);
+    *S = diag_mat(r.S);
+}
+
+template <typename T>
+void run_fixed_rank(mat *M, int k, int p, int vnum, int q, int s, mat **U, mat **S, mat **V) {
+    auto t0 = Clock::now();
+    DMat<T> A = upload<T>(M);
+    ctx().timing.upload_ms = ms_since(t0);
+    SvdOut<T> r = svd_fixed_rank<T>(A.v, k, p, vnum, q, s);
+    auto t1 = Clock::now();
+    svd_outputs<T>(r, U, S, V);
+    ctx().timing.download_ms = ms_since(t1);
+    end_call(t0);
+}
+
+template <typename T>
+void run_blockrand(mat *M, int k, int p, double TOL, int vnum, int kstep, int q, int s, int *frank, mat **U,
+                   mat **S, mat **V) {
+    auto t0 = Clock::now();
+    DMat<T> A = upload<T>(M);
+    int f = 0;
+    SvdOut<T> r = svd_blockrand<T>(A.v, k, p, TOL, vnum, kstep, q, s, &f);
+    svd_outputs<T>(r, U, S, V);
+    if (frank) *frank = f;
+    end_call(t0);
+}
+
+template <typename T>
+void run_qb(mat *M, int kstep, int nstep, double TOL, int q, int s, int *frank, mat **Q, mat **B) {
+    auto t0 = Clock::now();
+    DMat<T> A = upload<T>(M);
+    QBOut<T> r = qb_blocked<T>(A.v, kstep, nstep, TOL, q, s);
+    *Q = download<T>(r.Q.v);
+    *B = download<T>(r.B.v);
+    if (frank) *frank = r.frank;
+    end_call(t0);
+}
+
+}  // namespace
+
+extern "C" {
+
+// ============================================================ storage (MVF:8-63)
+mat *matrix_new(int nrows, int ncols) {
+    mat *M = (mat *)std::malloc(sizeof(mat));
+    if (!M) return nullptr;
+    M->nrows = nrows;
+    M->ncols = ncols;
+    const size_t n = (size_t)(nrows > 0 ? nrows : 0) * (size_t)(ncols > 0 ? ncols : 0);
+    M->d = (double *)std::calloc(n ? n : 1, sizeof(double));
+    return M;
+}
+
+vec *vector_new(int nrows) {
+    vec *v = (vec *)std::malloc(sizeof(vec));
+    if (!v) return nullptr;
+    v->nrows = nrows;
+    v->d = (double *)std::calloc(nrows > 0 ? (size_t)nrows : 1, sizeof(double));
+    return v;
+}
+
+void matrix_delete(mat *M) {
+    if (!M) return;
+    std::free(M->d);
+    std::free(M);
+}
+
+void vector_delete(vec *v) {
+    if (!v) return;
+    std::free(v->d);
+    std::free(v);
+}
+
+void matrix_set_element(mat *M, int i, int j, double val) { M->d[(size_t)j * M->nrows + i] = val; }
+double matrix_get_element(mat *M, int i, int j) { return M->d[(size_t)j * M->nrows + i]; }
+void vector_set_element(vec *v, int i, double val) { v->d[i] = val; }
+double vector_get_element(vec *v, int i) { return v->d[i]; }
+
+// int32 m, int32 n, then m*n doubles in row-major order (MVF:77-133)
+mat *matrix_load_from_binary_file(char *fname) {
+    FILE *fp = std::fopen(fname, "rb");
+    if (!fp) {
+        set_error(RSVD_ERR_ARGUMENT, std::string("cannot open ") + fname);
+        return nullptr;
+    }
+    int hdr[2] = {0, 0};
+    if (std::fread(hdr, sizeof(int), 2, fp) != 2 || hdr[0] <= 0 || hdr[1] <= 0) {
+        std::fclose(fp);
+        set_error(RSVD_ERR_ARGUMENT, "bad matrix file header");
+        return nullptr;
+    }
+    mat *M = matrix_new(hdr[0], hdr[1]);
+    std::vector<double> row((size_t)hdr[1]);
+    for (int i = 0; i < hdr[0]; i++) {
+        if (std::fread(row.data(), sizeof(double), (size_t)hdr[1], fp) != (size_t)hdr[1]) {
+            std::fclose(fp);
+            matrix_delete(M);
+            set_error(RSVD_ERR_ARGUMENT, "truncated matrix file");
+            return nullptr;
+        }
+        for (int j = 0; j < hdr[1]; j++) M->d[(size_t)j * hdr[0] + i] = row[(size_t)j];
+    }
+    std::fclose(fp);
+    return M;
+}
+
+void matrix_write_to_binary_file(mat *M, char *fname) {
+    FILE *fp = std::fopen(fname, "wb");
+    if (!fp) {
+        set_error(RSVD_ERR_ARGUMENT, std::string("cannot open ") + fname);
+        return;
+    }
+    const int hdr[2] = {M->nrows, M->ncols};
+    std::fwrite(hdr, sizeof(int), 2, fp);
+    std::vector<double> row((size_t)M->ncols);
+    for (int i = 0; i < M->nrows; i++) {
+        for (int j = 0; j < M->ncols; j++) row[(size_t)j] = M->d[(size_t)j * M->nrows + i];
+        std::fwrite(row.data(), sizeof(double), (size_t)M->ncols, fp);
+    }
+    std::fclose(fp);
+}
+
+void matrix_copy(mat *D, mat *S) {
+    std::memcpy(D->d, S->d, sizeof(double) * (size_t)S->nrows * (size_t)S->ncols);
+}
+
+void matrix_build_transpose(mat *Mt, mat *M) {
+    for (int j = 0; j < M->ncols; j++)
+        for (int i = 0; i < M->nrows; i++) Mt->d[(size_t)i * Mt->nrows + j] = M->d[(size_t)j * M->nrows + i];
+}
+
+double get_matrix_frobenius_norm(mat *M) {
+    double acc = 0.0;
+    const size_t n = (size_t)M->nrows * (size_t)M->ncols;
+    for (size_t i = 0; i < n; i++) acc += M->d[i] * M->d[i];
+    return std::sqrt(acc);
+}
+
+double get_percent_error_between_two_mats(mat *A, mat *B) {
+    double num = 0.0;
+    const size_t n = (size_t)A->nrows * (size_t)A->ncols;
+    for (size_t i = 0; i < n; i++) {
+        const double d = A->d[i] - B->d[i];
+        num += d * d;
+    }
+    return 100.0 * std::sqrt(num) / get_matrix_frobenius_norm(A);
+}
+
+double get_seconds_frac(struct timeval start_timeval, struct timeval end_timeval) {
+    const long secs = end_timeval.tv_sec - start_timeval.tv_sec;
+    const long micros = secs * 1000000 + end_timeval.tv_usec - start_timeval.tv_usec;
+    return micros / 1e6;
+}
+
+void initialize_random_matrix(mat *M) {
+    guarded("initialize_random_matrix", [&] {
+        check_mat(M);
+        begin_call();
+        DMat<double> Om = make_omega<double>(M->nrows, M->ncols);
+        mat *tmp = download<double>(Om.v);
+        std::memcpy(M->d, tmp->d, sizeof(double) * (size_t)M->nrows * (size_t)M->ncols);
+        matrix_delete(tmp);
+    });
+}
+
+static void host_gemm(const char *fn, bool ta, bool tb, mat *A, mat *B, mat *C) {
+    guarded(fn, [&] {
+        check_mat(A); check_mat(B); check_mat(C);
+        begin_call();
+        DMat<double> dA = upload<double>(A), dB = upload<double>(B);
+        DMat<double> dC(C->nrows, C->ncols, ctx().stream, false);
+        gemm<double>(ctx().stream, ta, tb, 1.0, dA.v, dB.v, 0.0, dC.v);
+        mat *r = download<double>(dC.v);
+        std::memcpy(C->d, r->d, sizeof(double) * (size_t)C->nrows * (size_t)C->ncols);
+        matrix_delete(r);
+    });
+}
+
+void matrix_matrix_mult(mat *A, mat *B, mat *C) { host_gemm("matrix_matrix_mult", false, false, A, B, C); }
+void matrix_transpose_matrix_mult(mat *A, mat *B, mat *C) { host_gemm("matrix_transpose_matrix_mult", true, false, A, B, C); }
+void matrix_matrix_transpose_mult(mat *A, mat *B, mat *C) { host_gemm("matrix_matrix_transpose_mult", false, true, A, B, C); }
+
+// P = U S V^T (MVF:1304-1318)
+void form_svd_product_matrix(mat *U, mat *S, mat *V, mat *P) {
+    mat *SVt = matrix_new(S->nrows, V->nrows);
+    matrix_matrix_transpose_mult(S, V, SVt);
+    matrix_matrix_mult(U, SVt, P);
+    matrix_delete(SVt);
+}
+
+// P = C U R (MVF:1322-1336)
+void form_cur_product_matrix(mat *C, mat *U, mat *R, mat *P) {
+    mat *CU = matrix_new(C->nrows, U->ncols);
+    matrix_matrix_mult(C, U, CU);
+    matrix_matrix_mult(CU, R, P);
+    matrix_delete(CU);
+}
+
+// ============================================================ decompositions
+void low_rank_svd_rand_decomp_fixed_rank(mat *M, int k, int p, int vnum, int q, int s, int *frank, mat **U,
+                                         mat **S, mat **V) {
+    (void)frank;   // not written by the reference (RRA:73-234)
+    *U = *S = *V = nullptr;
+    guarded("low_rank_svd_rand_decomp_fixed_rank", [&] {
+        check_mat(M);
+        need(k >= 1 && p >= 0, "need k >= 1 and p >= 0");
+        need(k + p <= std::min(M->nrows, M->ncols), "k + p exceeds min(m, n)");
+        need(q < 2 || s >= 1, "s must be >= 1 when q >= 2");
+        begin_call();
+        if (use_fp32_path()) run_fixed_rank<float>(M, k, p, vnum, q, s, U, S, V);
+        else run_fixed_rank<double>(M, k, p, vnum, q, s, U, S, V);
+    });
+}
+
+void low_rank_svd_blockrand_decomp_fixed_rank_or_prec(mat *M, int k, int p, double TOL, int vnum, int kstep, int q,
+                                                      int s, int *frank, mat **U, mat **S, mat **V) {
+    *U = *S = *V = nullptr;
+    guarded("low_rank_svd_blockrand_decomp_fixed_rank_or_prec", [&] {
+        check_mat(M);
+        need(kstep >= 1 && p >= 0, "need kstep >= 1 and p >= 0");
+        need(q < 1 || s >= 1, "s must be >= 1");
+        begin_call();
+        if (use_fp32_path()) run_blockrand<float>(M, k, p, TOL, vnum, kstep, q, s, frank, U, S, V);
+        else run_blockrand<double>(M, k, p, TOL, vnum, kstep, q, s, frank, U, S, V);
+    });
+}
+
+void randQB_pb_new(mat *M, int kstep, int nstep, double TOL, int q, int s, int *frank, mat **Q, mat **B) {
+    *Q = *B = nullptr;
+    guarded("randQB_pb_new", [&] {
+        check_mat(M);
+        need(kstep >= 1, "need kstep >= 1");
+        need(q < 1 || s >= 1, "s must be >= 1");
+        need((long long)kstep * nstep <= (long long)std::min(M->nrows, M->ncols) || kstep > std::min(M->nrows, M->ncols) / 2,
+             "kstep * nstep exceeds min(m, n)");
+        begin_call();
+        if (use_fp32_path()) run_qb<float>(M, kstep, nstep, TOL, q, s, frank, Q, B);
+        else run_qb<double>(M, kstep, nstep, TOL, q, s, frank, Q, B);
+    });
+}
+
+void pivotedQR_mkl(mat *M, mat **Q, mat **R, vec **I) {
+    *Q = *R = nullptr;
+    *I = nullptr;
+    guarded("pivotedQR_mkl", [&] {
+        check_mat(M);
+        begin_call();
+        auto t0 = Clock::now();
+        DMat<double> A = upload<double>(M);
+        PivQROut r = pivoted_qr_full(A.v);
+        *Q = download<double>(r.Q.v);
+        *R = download<double>(r.R.v);
+        *I = index_vec(r.I);
+        end_call(t0);
+    });
+}
+
+void pivoted_QR_of_specified_rank_or_prec(mat *M, int k, double TOL, int *frank, mat **Qk, mat **Rk, vec **I) {
+    *Qk = *Rk = nullptr;
+    *I = nullptr;
+    guarded("pivoted_QR_of_specified_rank_or_prec", [&] {
+        check_mat(M);
+        need(k <= std::min(M->nrows, M->ncols), "k exceeds min(m, n)");
+        begin_call();
+        auto t0 = Clock::now();
+        DMat<double> A = upload<double>(M);
+        PivQROut r = pivoted_qr_partial(A.v, k, TOL);
+        *Qk = download<double>(r.Q.v);
+        *Rk = download<double>(r.R.v);
+        *I = index_vec(r.I);
+        if (frank) *frank = r.frank;
+        end_call(t0);
+    });
+}
+
+void id_decomp_fixed_rank_or_prec(mat *M, int k, double TOL, int *frank, vec **I, mat **T) {
+    *I = nullptr;
+    *T = nullptr;
+    guarded("id_decomp_fixed_rank_or_prec", [&] {
+        check_mat(M);
+        need(k <= std::min(M->nrows, M->ncols), "k exceeds min(m, n)");
+        begin_call();
+        auto t0 = Clock::now();
+        DMat<double> A = upload<double>(M);
+        IdOut r = id_det(A.v, k, TOL);
+        *I = index_vec(r.I);
+        *T = download<double>(r.T.v);
+        if (frank) *frank = r.frank;
+        end_call(t0);
+    });
+}
+
+void id_rand_decomp_fixed_rank(mat *M, int k, int p, int q, int s, vec **I, mat **T) {
+    *I = nullptr;
+    *T = nullptr;
+    guarded("id_rand_decomp_fixed_rank", [&] {
+        check_mat(M);
+        need(k >= 1 && p >= 0 && k + p <= std::min(M->nrows, M->ncols), "need 1 <= k, k + p <= min(m, n)");
+        need(q < 1 || s >= 1, "s must be >= 1");
+        begin_call();
+        auto t0 = Clock::now();
+        DMat<double> A = upload<double>(M);
+        IdOut r = id_rand(A.v, k, p, q, s);
+        *I = index_vec(r.I);
+        *T = download<double>(r.T.v);
+        end_call(t0);
+    });
+}
+
+void id_blockrand_decomp_fixed_rank_or_prec(mat *M, int k, int p, double TOL, int kstep, int q, int s, int *frank,
+                                            vec **I, mat **T) {
+    *I = nullptr;
+    *T = nullptr;
+    guarded("id_blockrand_decomp_fixed_rank_or_prec", [&] {
+        check_mat(M);
+        need(kstep >= 1, "need kstep >= 1");
+        need(q < 1 || s >= 1, "s must be >= 1");
+        begin_call();
+        auto t0 = Clock::now();
+        DMat<double> A = upload<double>(M);
+        IdOut r = id_blockrand(A.v, k, p, TOL, kstep, q, s);
+        *I = index_vec(r.I);
+        *T = download<double>(r.T.v);
+        if (frank) *frank = r.frank;
+        end_call(t0);
+    });
+}
+
+static void two_sided_outputs(TwoSidedOut &r, vec **Icol, vec **Irow, mat **T, mat **S) {
+    *Icol = index_vec(r.Icol);
+    *Irow = index_vec(r.Irow);
+    *T = download<double>(r.T.v);
+    *S = download<double>(r.S.v);
+}
+
+void id_two_sided_decomp_fixed_rank_or_prec(mat *M, int k, double TOL, int *frank, vec **Icol, vec **Irow, mat **T,
+                                            mat **S) {
+    *Icol = *Irow = nullptr;
+    *T = *S = nullptr;
+    guarded("id_two_sided_decomp_fixed_rank_or_prec", [&] {
+        check_mat(M);
+        need(k <= std::min(M->nrows, M->ncols), "k exceeds min(m, n)");
+        begin_call();
+        auto t0 = Clock::now();
+        DMat<double> A = upload<double>(M);
+        TwoSidedOut r = id_two_sided(A.v, id_det(A.v, k, TOL));
+        two_sided_outputs(r, Icol, Irow, T, S);
+        if (frank) *frank = r.frank;
+        end_call(t0);
+    });
+}
+
+void id_two_sided_rand_decomp_fixed_rank(mat *M, int k, int p, int q, int s, vec **Icol, vec **Irow, mat **T,
+                                         mat **S) {
+    *Icol = *Irow = nullptr;
+    *T = *S = nullptr;
+    guarded("id_two_sided_rand_decomp_fixed_rank", [&] {
+        check_mat(M);
+        need(k >= 1 && p >= 0 && k + p <= std::min(M->nrows, M->ncols), "need 1 <= k, k + p <= min(m, n)");
+        need(q < 1 || s >= 1, "s must be >= 1");
+        begin_call();
+        auto t0 = Clock::now();
+        DMat<double> A = upload<double>(M);
+        TwoSidedOut r = id_two_sided(A.v, id_rand(A.v, k, p, q, s));
+        two_sided_outputs(r, Icol, Irow, T, S);
+        end_call(t0);
+    });
+}
+
+void id_two_sided_blockrand_decomp_fixed_rank_or_prec(mat *M, int k, int p, double TOL, int kstep, int q, int s,
+                                                      int *frank, vec **Icol, vec **Irow, mat **T, mat **S) {
+    *Icol = *Irow = nullptr;
+    *T = *S = nullptr;
+    guarded("id_two_sided_blockrand_decomp_fixed_rank_or_prec", [&] {
+        check_mat(M);
+        need(kstep >= 1, "need kstep >= 1");
+        need(q < 1 || s >= 1, "s must be >= 1");
+        begin_call();
+        auto t0 = Clock::now();
+        DMat<double> A = upload<double>(M);
+        TwoSidedOut r = id_two_sided(A.v, id_blockrand(A.v, k, p, TOL, kstep, q, s));
+        two_sided_outputs(r, Icol, Irow, T, S);
+        if (frank) *frank = r.frank;
+        end_call(t0);
+    });
+}
+
+static void cur_outputs(CurOut &r, mat **C, mat **U, mat **R) {
+    *C = download<double>(r.C.v);
+    *U = download<double>(r.U.v);
+    *R = download<double>(r.R.v);
+}
+
+void cur_decomp_fixed_rank_or_prec(mat *M, int k, double TOL, int *frank, mat **C, mat **U, mat **R) {
+    *C = *U = *R = nullptr;
+    guarded("cur_decomp_fixed_rank_or_prec", [&] {
+        check_mat(M);
+        need(k <= std::min(M->nrows, M->ncols), "k exceeds min(m, n)");
+        begin_call();
+        auto t0 = Clock::now();
+        DMat<double> A = upload<double>(M);
+        TwoSidedOut ts = id_two_sided(A.v, id_det(A.v, k, TOL));
+        CurOut r = cur_from_two_sided(A.v, ts.frank, ts);
+        cur_outputs(r, C, U, R);
+        if (frank) *frank = ts.frank;
+        end_call(t0);
+    });
+}
+
+void cur_rand_decomp_fixed_rank(mat *M, int k, int p, int q, int s, mat **C, mat **U, mat **R) {
+    *C = *U = *R = nullptr;
+    guarded("cur_rand_decomp_fixed_rank", [&] {
+        check_mat(M);
+        need(k >= 1 && p >= 0 && k + p <= std::min(M->nrows, M->ncols), "need 1 <= k, k + p <= min(m, n)");
+        need(q < 1 || s >= 1, "s must be >= 1");
+        begin_call();
+        auto t0 = Clock::now();
+        DMat<double> A = upload<double>(M);
+        TwoSidedOut ts = id_two_sided(A.v, id_rand(A.v, k, p, q, s));
+        CurOut r = cur_from_two_sided(A.v, k, ts);
+        cur_outputs(r, C, U, R);
+        end_call(t0);
+    });
+}
+
+void cur_blockrand_decomp_fixed_rank_or_prec(mat *M, int k, int p, double TOL, int kstep, int q, int s, int *frank,
+                                             mat **C, mat **U, mat **R) {
+    *C = *U = *R = nullptr;
+    guarded("cur_blockrand_decomp_fixed_rank_or_prec", [&] {
+        check_mat(M);
+        need(kstep >= 1, "need kstep >= 1");
+        need(q < 1 || s >= 1, "s must be >= 1");
+        begin_call();
+        auto t0 = Clock::now();
+        DMat<double> A = upload<double>(M);
+        TwoSidedOut ts = id_two_sided(A.v, id_blockrand(A.v, k, p, TOL, kstep, q, s));
+        CurOut r = cur_from_two_sided(A.v, ts.frank, ts);
+        cur_outputs(r, C, U, R);
+        if (frank) *frank = ts.frank;
+        end_call(t0);
+    });
+}
+
+// ============================================================ device-resident entry points
+}  // extern "C"
+template <typename T>
+static void dev_svd(const void *dA, long long lda, int m, int n, int k, int p, int vnum, int q, int s, void *dU,
+                    long long ldu, double *dS, void *dV, long long ldv) {
+    cudaStream_t st = ctx().stream;
+    DM<T> A{(T *)const_cast<void *>(dA), m, n, lda};
+    SvdOut<T> r = svd_fixed_rank<T>(A, k, p, vnum, q, s);
+    RSVD_CK(cudaMemcpy2DAsync(dU, sizeof(T) * ldu, r.U.v.p, sizeof(T) * r.U.v.ld, sizeof(T) * m, k,
+                              cudaMemcpyDeviceToDevice, st));
+    RSVD_CK(cudaMemcpy2DAsync(dV, sizeof(T) * ldv, r.V.v.p, sizeof(T) * r.V.v.ld, sizeof(T) * n, k,
+                              cudaMemcpyDeviceToDevice, st));
+    RSVD_CK(cudaMemcpyAsync(dS, r.S.data(), sizeof(double) * k, cudaMemcpyHostToDevice, st));
+    RSVD_CK(cudaStreamSynchronize(st));
+}
+extern "C" {
+
+int rsvdpack_dev_svd_fixed_rank(const void *dA, int dtype, long long lda, int m, int n, int k, int p, int vnum,
+                                int q, int s, void *dU, long long ldu, double *dS, void *dV, long long ldv) {
+    guarded("rsvdpack_dev_svd_fixed_rank", [&] {
+        need(dA && dU && dS && dV, "null device pointer");
+        need(m > 0 && n > 0 && k >= 1 && p >= 0 && k + p <= std::min(m, n), "bad sizes");
+        need(lda >= m && ldu >= m && ldv >= n, "bad leading dimension");
+        need(q < 2 || s >= 1, "s must be >= 1 when q >= 2");
+        begin_call();
+        auto t0 = Clock::now();
+        if (dtype == RSVD_DT_F64) dev_svd<double>(dA, lda, m, n, k, p, vnum, q, s, dU, ldu, dS, dV, ldv);
+        else if (dtype == RSVD_DT_F32) dev_svd<float>(dA, lda, m, n, k, p, vnum, q, s, dU, ldu, dS, dV, ldv);
+        else fail(RSVD_ERR_ARGUMENT, "unknown dtype");
+        end_call(t0);
+    });
+    return rsvdpack_last_error();
+}
+
+int rsvdpack_dev_sketch(const void *dA, int dtype, long long lda, int m, int n, const void *dX, long long ldx, int w,
+                        void *dY, long long ldy, int trans) {
+    guarded("rsvdpack_dev_sketch", [&] {
+        need(dA && dX && dY, "null device pointer");
+        need(m > 0 && n > 0 && w > 0 && lda >= m, "bad sizes");
+        begin_call();
+        cudaStream_t st = ctx().stream;
+        const i64 xr = trans ? m : n, yr = trans ? n : m;
+        need(ldx >= xr && ldy >= yr, "bad leading dimension");
+        if (dtype == RSVD_DT_F64) {
+            DM<double> A{(double *)const_cast<void *>(dA), m, n, lda}, X{(double *)const_cast<void *>(dX), xr, w, ldx};
+            DM<double> Y{(double *)dY, yr, w, ldy};
+            prod<double>(st, trans != 0, false, 1.0, A, X, 0.0, Y);
+        } else if (dtype == RSVD_DT_F32) {
+            DM<float> A{(float *)const_cast<void *>(dA), m, n, lda}, X{(float *)const_cast<void *>(dX), xr, w, ldx};
+            DM<float> Y{(float *)dY, yr, w, ldy};
+            prod<float>(st, trans != 0, false, 1.0f, A, X, 0.0f, Y);
+        } else {
+            fail(RSVD_ERR_ARGUMENT, "unknown dtype");
+        }
+        RSVD_CK(cudaStreamSynchronize(st));
+        check_device_flags(ctx());
+    });
+    return rsvdpack_last_error();
+}
+
+void *rsvdpack_stream(void) {
+    try {
+        return (void *)ctx().stream;
+    } catch (const Error &e) {
+        set_error(e.code, e.what());
+        return nullptr;
+    }
+}
+
+// ============================================================ approximation reports (RRA:2337-2573)
+void use_low_rank_svd_for_approximation(mat *M, mat *U, mat *S, mat *V) {
+    mat *P = matrix_new(M->nrows, M->ncols);
+    form_svd_product_matrix(U, S, V, P);
+    std::printf("norm(M,fro) = %f\n", get_matrix_frobenius_norm(M));
+    std::printf("norm(P,fro) = %f\n", get_matrix_frobenius_norm(P));
+    std::printf("percent error = %f\n", get_percent_error_between_two_mats(M, P));
+    matrix_delete(P);
+}
+
+void use_pivoted_QR_decomp_for_approximation(mat *M, mat *Qk, mat *Rk, vec *I) {
+    const int m = M->nrows, n = M->ncols;
+    mat *QR = matrix_new(m, n), *QRPt = matrix_new(m, n);
+    matrix_matrix_mult(Qk, Rk, QR);
+    // (Qk Rk) P^T : column j of the product goes back to column I[j]
+    for (int j = 0; j < n; j++)
+        std::memcpy(QRPt->d + (size_t)((int)I->d[j]) * m, QR->d + (size_t)j * m, sizeof(double) * m);
+    std::printf("percent_error between M and QkRkPt = %f\n", get_percent_error_between_two_mats(M, QRPt));
+    matrix_delete(Qk);
+    matrix_delete(Rk);
+    matrix_delete(QR);
+    matrix_delete(QRPt);
+}
+
+void use_QB_decomp_for_approximation(mat *M, mat *Q, mat *B) {
+    mat *P = matrix_new(M->nrows, M->ncols);
+    matrix_matrix_mult(Q, B, P);
+    std::printf("norm(M,fro) = %f\n", get_matrix_frobenius_norm(M));
+    std::printf("norm(P,fro) = %f\n", get_matrix_frobenius_norm(P));
+    std::printf("percent error = %f\n", get_percent_error_between_two_mats(M, P));
+    matrix_delete(P);
+}
+
+// V = [I_k; T^T](Iinv,:) ; MA = M(:,I(1:k)) V^T
+static mat *id_basis(mat *T, vec *I, int k) {
+    const int n = I->nrows;
+    std::vector<int> inv((size_t)n);
+    for (int j = 0; j < n; j++) inv[(size_t)((int)I->d[j])] = j;
+    mat *V = matrix_new(n, k);
+    for (int i = 0; i < n; i++) {
+        const int r = inv[(size_t)i];
+        for (int c = 0; c < k; c++)
+            V->d[(size_t)c * n + i] = (r < k) ? (r == c ? 1.0 : 0.0) : T->d[(size_t)(r - k) * T->nrows + c];
+    }
+    return V;
+}
+
+void use_id_decomp_for_approximation(mat *M, mat *T, vec *I, int k) {
+    const int m = M->nrows, n = M->ncols;
+    mat *V = id_basis(T, I, k);
+    mat *MI = matrix_new(m, k);
+    for (int c = 0; c < k; c++) std::memcpy(MI->d + (size_t)c * m, M->d + (size_t)((int)I->d[c]) * m, sizeof(double) * m);
+    mat *MA = matrix_new(m, n);
+    matrix_matrix_transpose_mult(MI, V, MA);
+    std::printf("norm(M,fro) = %f\n", get_matrix_frobenius_norm(M));
+    std::printf("norm(MA,fro) = %f\n", get_matrix_frobenius_norm(MA));
+    std::printf("percent error = %f\n", get_percent_error_between_two_mats(M, MA));
+    matrix_delete(V);
+    matrix_delete(MI);
+    matrix_delete(MA);
+}
+
+void use_id_two_sided_decomp_for_approximation(mat *M, mat *T, mat *S, vec *Icol, vec *Irow, int k) {
+    const int m = M->nrows, n = M->ncols;
+    mat *V = id_basis(T, Icol, k);
+    mat *Uu = id_basis(S, Irow, k);
+    mat *MIJ = matrix_new(k, k);
+    for (int c = 0; c < k; c++)
+        for (int r = 0; r < k; r++)
+            MIJ->d[(size_t)c * k + r] = M->d[(size_t)((int)Icol->d[c]) * m + (size_t)((int)Irow->d[r])];
+    mat *UM = matrix_new(m, k), *MA = matrix_new(m, n);
+    matrix_matrix_mult(Uu, MIJ, UM);
+    matrix_matrix_transpose_mult(UM, V, MA);
+    std::printf("norm(M,fro) = %f\n", get_matrix_frobenius_norm(M));
+    std::printf("norm(MA,fro) = %f\n", get_matrix_frobenius_norm(MA));
+    std::printf("percent error = %f\n", get_percent_error_between_two_mats(M, MA));
+    matrix_delete(V);
+    matrix_delete(Uu);
+    matrix_delete(MIJ);
+    matrix_delete(UM);
+    matrix_delete(MA);
+}
+
+void use_cur_decomp_for_approximation(mat *M, mat *C, mat *U, mat *R) {
+    mat *P = matrix_new(M->nrows, M->ncols);
+    form_cur_product_matrix(C, U, R, P);
+    std::printf("norm(M,fro) = %f\n", get_matrix_frobenius_norm(M));
+    std::printf("norm(P,fro) = %f\n", get_matrix_frobenius_norm(P));
+    std::printf("percent error = %f\n", get_percent_error_between_two_mats(M, P));
+    matrix_delete(P);
+}
+
+}  // extern "C"

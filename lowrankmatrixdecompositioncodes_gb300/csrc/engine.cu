@@ -1,0 +1,484 @@
+// engine.cu -- device-resident decompositions (see engine.h).
+#include "engine.h"
+#include "k_common.cuh"
+
+#include <algorithm>
+#include <cmath>
+#include <type_traits>
+
+namespace rsvd {
+
+namespace {
+
+// dst(:, j) = scale[j] * src(:, perm[j])   (small l x l helpers; perm/scale uploaded)
+template <typename Ts, typename Td>
+__global__ void select_cols_kernel(const Ts *src, i64 lds, const int *perm, const double *scale, Td *dst, i64 ldd,
+                                   i64 r, i64 c) {
+    for (i64 e = blockIdx.x * (i64)blockDim.x + threadIdx.x; e < r * c; e += (i64)gridDim.x * blockDim.x) {
+        const i64 i = e % r, j = e / r;
+        double v = (double)src[i + (i64)perm[j] * lds];
+        if (scale) v *= scale[j];
+        dst[i + j * ldd] = (Td)v;
+    }
+}
+
+template <typename Ts, typename Td>
+void select_cols(cudaStream_t s, DM<Ts> src, const std::vector<int> &perm, const std::vector<double> *scale,
+                 DM<Td> dst) {
+    const i64 c = (i64)perm.size();
+    if (c == 0 || dst.r == 0) return;
+    DBuf pb(sizeof(int) * c, s);
+    DBuf sb(sizeof(double) * c, s);
+    int *dperm = (int *)pb.get();
+    double *dscale = scale ? (double *)sb.get() : nullptr;
+    RSVD_CK(cudaMemcpyAsync(dperm, perm.data(), sizeof(int) * c, cudaMemcpyHostToDevice, s));
+    if (scale) RSVD_CK(cudaMemcpyAsync(dscale, scale->data(), sizeof(double) * c, cudaMemcpyHostToDevice, s));
+    select_cols_kernel<Ts, Td><<<ceil_div(dst.r * c, 256), 256, 0, s>>>(src.p, src.ld, dperm, dscale, dst.p, dst.ld,
+                                                                         dst.r, c);
+    RSVD_LAUNCH_CK();
+    // keep pb/sb alive until the kernel has consumed them
+    RSVD_CK(cudaStreamSynchronize(s));
+}
+
+template <typename T>
+void copy_dm(cudaStream_t s, DM<T> src, DM<T> dst) {
+    if (src.r * src.c == 0) return;
+    RSVD_CK(cudaMemcpy2DAsync(dst.p, sizeof(T) * dst.ld, src.p, sizeof(T) * src.ld, sizeof(T) * src.r, src.c,
+                              cudaMemcpyDeviceToDevice, s));
+}
+
+template <typename T>
+constexpr double chol_tol() { return std::is_same<T, double>::value ? 1e-14 : 1e-5; }
+
+
+}  // namespace
+
+// Products of the tall / large operands.  Dispatches on the precision mode: CUDA-core
+// GEMM for FP64 and FP32; tcgen05 tensor-core GEMM for TF32 / BF16 (k_gemm_tc.cu).
+template <typename T>
+void prod(cudaStream_t s, bool ta, bool tb, T alpha, DM<T> A, DM<T> B, T beta, DM<T> C) {
+    gemm<T>(s, ta, tb, alpha, A, B, beta, C);
+}
+template void prod<double>(cudaStream_t, bool, bool, double, DM<double>, DM<double>, double, DM<double>);
+template void prod<float>(cudaStream_t, bool, bool, float, DM<float>, DM<float>, float, DM<float>);
+
+namespace {
+
+std::vector<int> download_ints(cudaStream_t s, const int *d, i64 n) {
+    std::vector<int> h((size_t)n);
+    if (n) RSVD_CK(cudaMemcpyAsync(h.data(), d, sizeof(int) * n, cudaMemcpyDeviceToHost, s));
+    RSVD_CK(cudaStreamSynchronize(s));
+    return h;
+}
+
+}  // namespace
+
+// ------------------------------------------------------------------ test matrices
+template <typename T>
+DMat<T> make_omega(i64 r, i64 c) {
+    Ctx &cx = ctx();
+    cudaStream_t s = cx.stream;
+    DMat<T> Om(r, c, s, false);
+    if (cx.opts.use_provider && omega_provider_active()) {
+        std::vector<double> h((size_t)(r * c));
+        omega_fill_host((int)r, (int)c, h.data());
+        DMat<double> tmp(r, c, s, false);
+        RSVD_CK(cudaMemcpy2DAsync(tmp.v.p, sizeof(double) * tmp.v.ld, h.data(), sizeof(double) * r,
+                                  sizeof(double) * r, c, cudaMemcpyHostToDevice, s));
+        convert<double, T>(s, tmp.v, Om.v);
+        RSVD_CK(cudaStreamSynchronize(s));   // h leaves scope
+    } else {
+        philox_gaussian(s, cx.opts.seed, philox_calls()++, Om.v);
+    }
+    return Om;
+}
+template DMat<double> make_omega<double>(i64, i64);
+template DMat<float> make_omega<float>(i64, i64);
+
+// ------------------------------------------------------------------ orthonormalisation
+template <typename T>
+void orth(DM<T> Y, DM<T> Q, DM<double> *R) {
+    Ctx &cx = ctx();
+    cudaStream_t s = cx.stream;
+    const i64 c = Y.c;
+    if (Y.r < c) fail(RSVD_ERR_ARGUMENT, "orth: more columns than rows");
+    int *flag = cx.d_flags + FLAG_CHOL_BREAKDOWN;
+    DMat<double> G1(c, c, s, false);
+    gram<T>(s, Y, G1.v);
+    if (cholesky_upper(s, G1.v, chol_tol<T>(), flag)) {
+        trsm_right_upper<T>(s, Y, G1.v, Q);
+        DMat<double> G2(c, c, s, false);
+        gram<T>(s, Q, G2.v);
+        if (cholesky_upper(s, G2.v, chol_tol<T>(), flag)) {
+            trsm_right_upper<T>(s, Q, G2.v, Q);
+            if (R) gemm<double>(s, false, false, 1.0, G2.v, G1.v, 0.0, *R);   // R = R2 R1
+            return;
+        }
+    }
+    // Householder fallback on a copy of Y
+    DMat<T> W(Y.r, c, s, false);
+    copy_dm<T>(s, Y, W.v);
+    DMat<double> Rh(c, c, s, true);
+    householder_qr<T>(s, W.v, Q, Rh.v);
+    if (R) copy_dm<double>(s, Rh.v, *R);
+}
+template void orth<double>(DM<double>, DM<double>, DM<double> *);
+template void orth<float>(DM<float>, DM<float>, DM<double> *);
+
+// ------------------------------------------------------------------ SVD back end
+// From an orthonormal Q (m x l) spanning the sketch: RRA:133-224.
+template <typename T>
+static SvdOut<T> svd_from_q(DM<T> A, DM<T> Q, int k, int vnum) {
+    Ctx &cx = ctx();
+    cudaStream_t s = cx.stream;
+    const i64 m = A.r, n = A.c, l = Q.c;
+    SvdOut<T> out;
+    DMat<T> Bt(n, l, s, false);
+    prod<T>(s, true, false, T(1), A, Q, T(0), Bt.v);                    // Bt = A^T Q
+    DMat<double> Uh(l, l, s, false), Vh(l, l, s, false);
+    DBuf svb(sizeof(double) * l, s);
+    std::vector<double> sv((size_t)l);
+    out.U = DMat<T>(m, k, s, false);
+    out.V = DMat<T>(n, k, s, false);
+    if (vnum == 1 || vnum > 2) {
+        // [Qh, Rh] = qr(Bt); Rh = Uh S Vh^T; U = Q Vh; V = Qh Uh   (RRA:133-174)
+        DMat<T> Qh(n, l, s, false);
+        DMat<double> Rh(l, l, s, true);
+        orth<T>(Bt.v, Qh.v, &Rh.v);
+        jacobi_svd(s, Rh.v, Uh.v, Vh.v, (double *)svb.get(), cx.d_flags + FLAG_JACOBI_NOCONV);
+        RSVD_CK(cudaMemcpyAsync(sv.data(), svb.get(), sizeof(double) * l, cudaMemcpyDeviceToHost, s));
+        std::vector<int> first((size_t)k);
+        for (int j = 0; j < k; j++) first[j] = j;
+        DMat<T> Vk(l, k, s, false), Uk(l, k, s, false);
+        select_cols<double, T>(s, Vh.v, first, nullptr, Vk.v);
+        select_cols<double, T>(s, Uh.v, first, nullptr, Uk.v);
+        prod<T>(s, false, false, T(1), Q, Vk.v, T(0), out.U.v);
+        prod<T>(s, false, false, T(1), Qh.v, Uk.v, T(0), out.V.v);
+        out.S.assign(sv.begin(), sv.begin() + k);
+    } else {
+        // eig(B B^T) ascending, keep the last k; U = Q Uh; V = B^T Uh S^-1   (RRA:176-224)
+        DMat<double> BBt(l, l, s, false);
+        gram<T>(s, Bt.v, BBt.v);                                         // B B^T = Bt^T Bt
+        jacobi_svd(s, BBt.v, Uh.v, Vh.v, (double *)svb.get(), cx.d_flags + FLAG_JACOBI_NOCONV);
+        RSVD_CK(cudaMemcpyAsync(sv.data(), svb.get(), sizeof(double) * l, cudaMemcpyDeviceToHost, s));
+        RSVD_CK(cudaStreamSynchronize(s));
+        // ascending order position i in [0,k) <- descending position k-1-i
+        std::vector<int> perm((size_t)k);
+        std::vector<double> inv((size_t)k);
+        out.S.resize((size_t)k);
+        for (int i = 0; i < k; i++) {
+            const int d = k - 1 - i;
+            perm[i] = d;
+            out.S[i] = std::sqrt(sv[d]);
+            inv[i] = 1.0 / out.S[i];
+        }
+        DMat<T> Uk(l, k, s, false), Uks(l, k, s, false);
+        select_cols<double, T>(s, Vh.v, perm, nullptr, Uk.v);
+        select_cols<double, T>(s, Vh.v, perm, &inv, Uks.v);
+        prod<T>(s, false, false, T(1), Q, Uk.v, T(0), out.U.v);
+        prod<T>(s, false, false, T(1), Bt.v, Uks.v, T(0), out.V.v);
+    }
+    RSVD_CK(cudaStreamSynchronize(s));
+    return out;
+}
+
+// ------------------------------------------------------------------ fixed-rank rSVD (RRA:73-234)
+template <typename T>
+SvdOut<T> svd_fixed_rank(DM<T> A, int k, int p, int vnum, int q, int s_) {
+    Ctx &cx = ctx();
+    cudaStream_t s = cx.stream;
+    const i64 m = A.r, n = A.c, l = (i64)k + p;
+    DMat<T> Om = make_omega<T>(n, l);
+    DMat<T> Y(m, l, s, false), Z(n, l, s, false), Yo(m, l, s, false), Zo(n, l, s, false);
+    prod<T>(s, false, false, T(1), A, Om.v, T(0), Y.v);                 // Y = A Om
+    for (int j = 1; j < q; j++) {                                         // q-1 rounds (RRA:101)
+        if ((2 * j - 2) % s_ == 0) { orth<T>(Y.v, Yo.v, nullptr); prod<T>(s, true, false, T(1), A, Yo.v, T(0), Z.v); }
+        else prod<T>(s, true, false, T(1), A, Y.v, T(0), Z.v);
+        if ((2 * j - 1) % s_ == 0) { orth<T>(Z.v, Zo.v, nullptr); prod<T>(s, false, false, T(1), A, Zo.v, T(0), Y.v); }
+        else prod<T>(s, false, false, T(1), A, Z.v, T(0), Y.v);
+    }
+    DMat<T> Q(m, l, s, false);
+    orth<T>(Y.v, Q.v, nullptr);
+    return svd_from_q<T>(A, Q.v, k, vnum);
+}
+template SvdOut<double> svd_fixed_rank<double>(DM<double>, int, int, int, int, int);
+template SvdOut<float> svd_fixed_rank<float>(DM<float>, int, int, int, int, int);
+
+// ------------------------------------------------------------------ blocked QB (RRA:1576-1801)
+template <typename T>
+QBOut<T> qb_blocked(DM<T> A, int kstep, int nstep, double TOL, int q, int s_) {
+    Ctx &cx = ctx();
+    cudaStream_t s = cx.stream;
+    const i64 m = A.r, n = A.c, mn = std::min(m, n);
+    if (kstep > (int)(mn / 2)) kstep = (int)mn / 10;                      // RRA:1589-1592
+    if (kstep <= 0) fail(RSVD_ERR_ARGUMENT, "randQB_pb_new: block size collapses to zero");
+    const bool tol_mode = nstep <= 0;
+    if (tol_mode) nstep = (int)(mn / kstep);
+    const i64 l = (i64)kstep * nstep;
+    DMat<T> Om = make_omega<T>(n, l);
+    DMat<T> Aw(m, n, s, false);
+    copy_dm<T>(s, A, Aw.v);
+    QBOut<T> out;
+    out.Q = DMat<T>(m, l, s, true);
+    out.B = DMat<T>(l, n, s, true);
+    DMat<T> Yp(m, kstep, s, false), Qp(m, kstep, s, false), AtQp(n, kstep, s, false), AtQp2(n, kstep, s, false);
+    DMat<T> Bp(kstep, n, s, false), Bpt(n, kstep, s, false);
+    int frank = 0;
+    for (int step = 0; step < nstep; step++) {
+        const i64 c0 = (i64)step * kstep;
+        prod<T>(s, false, false, T(1), Aw.v, Om.v.cols(c0, kstep), T(0), Yp.v);
+        for (int j = 1; j <= q; j++) {                                    // q rounds (RRA:1652)
+            if ((2 * j - 2) % s_ == 0) { orth<T>(Yp.v, Qp.v, nullptr); prod<T>(s, true, false, T(1), Aw.v, Qp.v, T(0), AtQp.v); }
+            else prod<T>(s, true, false, T(1), Aw.v, Yp.v, T(0), AtQp.v);
+            if ((2 * j - 1) % s_ == 0) { orth<T>(AtQp.v, AtQp2.v, nullptr); prod<T>(s, false, false, T(1), Aw.v, AtQp2.v, T(0), Yp.v); }
+            else prod<T>(s, false, false, T(1), Aw.v, AtQp.v, T(0), Yp.v);
+        }
+        orth<T>(Yp.v, Qp.v, nullptr);
+        if (step > 0 && step % 2 == 0) {                                  // RRA:1703-1732
+            DM<T> Qj = out.Q.v.cols(0, c0);
+            DMat<T> QjtQp(c0, kstep, s, false);
+            prod<T>(s, true, false, T(1), Qj, Qp.v, T(0), QjtQp.v);
+            copy_dm<T>(s, Qp.v, Yp.v);
+            prod<T>(s, false, false, T(-1), Qj, QjtQp.v, T(1), Yp.v);    // Yp = Qp - Qj (Qj^T Qp)
+            orth<T>(Yp.v, Qp.v, nullptr);
+        }
+        prod<T>(s, true, false, T(1), Qp.v, Aw.v, T(0), Bp.v);           // Bp = Qp^T A
+        prod<T>(s, false, false, T(-1), Qp.v, Bp.v, T(1), Aw.v);         // A -= Qp Bp (in place)
+        copy_dm<T>(s, Qp.v, out.Q.v.cols(c0, kstep));
+        copy_dm<T>(s, Bp.v, out.B.v.sub(c0, 0, kstep, n));
+        frank = (step + 1) * kstep;
+        if (tol_mode && frob_norm<T>(s, Aw.v) < TOL) break;               // RRA:1770-1778
+    }
+    out.frank = frank;
+    if (tol_mode) {
+        out.Q.v.c = frank;   // views keep the leading columns / rows
+        out.B.v.r = frank;
+    }
+    RSVD_CK(cudaStreamSynchronize(s));
+    return out;
+}
+template QBOut<double> qb_blocked<double>(DM<double>, int, int, double, int, int);
+template QBOut<float> qb_blocked<float>(DM<float>, int, int, double, int, int);
+
+// ------------------------------------------------------------------ blocked rSVD (RRA:239-381)
+template <typename T>
+SvdOut<T> svd_blockrand(DM<T> A, int k, int p, double TOL, int vnum, int kstep, int q, int s_, int *frank) {
+    const i64 m = A.r, n = A.c;
+    const bool rank_mode = k > 0;
+    if (p < kstep && (p + kstep) < std::min(m, n)) p = kstep;            // RRA:260-262
+    const int nstep = (k + p) / kstep;                                    // RRA:263 (integer division)
+    QBOut<T> qb = qb_blocked<T>(A, kstep, nstep, TOL, q, s_);
+    int f = qb.frank;
+    if (rank_mode) f = k;
+    else f = (int)std::round((double)(f / (f + p + 1e-6)) * f);          // RRA:278
+    *frank = f;
+    if (f > qb.Q.v.c) fail(RSVD_ERR_ARGUMENT, "blockrand: rank exceeds the sampled basis");
+    return svd_from_q<T>(A, qb.Q.v, f, vnum);
+}
+template SvdOut<double> svd_blockrand<double>(DM<double>, int, int, double, int, int, int, int, int *);
+template SvdOut<float> svd_blockrand<float>(DM<float>, int, int, double, int, int, int, int, int *);
+
+// ------------------------------------------------------------------ pivoted QR
+PivQROut pivoted_qr_full(DM<double> A) {
+    // RRA:924-976 : dgeqp3 + dorgqr
+    Ctx &cx = ctx();
+    cudaStream_t s = cx.stream;
+    const i64 m = A.r, n = A.c, k = std::min(m, n);
+    DMat<double> W(m, n, s, false);
+    copy_dm<double>(s, A, W.v);
+    DBuf taub(sizeof(double) * std::max<i64>(1, k), s), jb(sizeof(int) * std::max<i64>(1, n), s);
+    pivqr_lapack(s, W.v, (double *)taub.get(), (int *)jb.get());
+    const i64 qr_ = (m <= n) ? k : m, qc = k, rr = k, rc = (m <= n) ? n : k;
+    PivQROut out;
+    out.R = DMat<double>(rr, rc, s, true);
+    // upper triangle of W(0:rr, 0:rc)
+    {
+        DMat<double> tmp(rr, rc, s, false);
+        copy_dm<double>(s, W.v.sub(0, 0, rr, rc), tmp.v);
+        std::vector<double> h((size_t)(rr * rc));
+        RSVD_CK(cudaMemcpy2DAsync(h.data(), sizeof(double) * rr, tmp.v.p, sizeof(double) * tmp.v.ld,
+                                  sizeof(double) * rr, rc, cudaMemcpyDeviceToHost, s));
+        RSVD_CK(cudaStreamSynchronize(s));
+        for (i64 j = 0; j < rc; j++)
+            for (i64 i = j + 1; i < rr; i++) h[i + j * rr] = 0.0;
+        RSVD_CK(cudaMemcpy2DAsync(out.R.v.p, sizeof(double) * out.R.v.ld, h.data(), sizeof(double) * rr,
+                                  sizeof(double) * rr, rc, cudaMemcpyHostToDevice, s));
+        RSVD_CK(cudaStreamSynchronize(s));
+    }
+    out.Q = DMat<double>(qr_, qc, s, false);
+    form_q_from_reflectors(s, W.v.sub(0, 0, qr_, n), (const double *)taub.get(), (int)k, out.Q.v);
+    out.I = download_ints(s, (const int *)jb.get(), n);
+    out.frank = (int)k;
+    return out;
+}
+
+PivQROut pivoted_qr_partial(DM<double> A, int k, double TOL) {
+    // RRA:1159-1334 : the reference's own pivoting; Qk = first frank columns of the
+    // accumulated reflectors, Rk = first frank rows of the transformed matrix
+    Ctx &cx = ctx();
+    cudaStream_t s = cx.stream;
+    const i64 m = A.r, n = A.c;
+    const bool tol_mode = k <= 0;
+    if (tol_mode) k = (int)std::min(m, n);
+    DMat<double> R(m, n, s, false);
+    copy_dm<double>(s, A, R.v);
+    DMat<double> Qk(m, std::max(1, k), s, false);
+    DBuf jb(sizeof(int) * std::max<i64>(1, n), s);
+    const int f = pivqr_rsvdpack(s, R.v, Qk.v, k, TOL, tol_mode, (int *)jb.get());
+    PivQROut out;
+    out.frank = f;
+    out.Q = DMat<double>(m, f, s, false);
+    out.R = DMat<double>(f, n, s, false);
+    copy_dm<double>(s, Qk.v.cols(0, f), out.Q.v);
+    copy_dm<double>(s, R.v.sub(0, 0, f, n), out.R.v);
+    out.I = download_ints(s, (const int *)jb.get(), n);
+    return out;
+}
+
+// T = triu(Rk(:, 0:r))^-1 Rk(:, r:n)
+static DMat<double> interp_coeffs(DM<double> Rk, int r) {
+    cudaStream_t s = ctx().stream;
+    const i64 n = Rk.c;
+    DMat<double> T(r, n - r, s, false);
+    if (n - r > 0 && r > 0) trsm_left_upper(s, Rk.sub(0, 0, r, r), Rk.sub(0, r, r, n - r), T.v);
+    return T;
+}
+
+// ------------------------------------------------------------------ IDs (RRA:1807-2111)
+IdOut id_det(DM<double> A, int k, double TOL) {
+    IdOut out;
+    PivQROut pq;
+    if (k < std::min(A.r, A.c)) {
+        pq = pivoted_qr_partial(A, k, TOL);
+        out.frank = pq.frank;
+    } else {
+        pq = pivoted_qr_full(A);
+        out.frank = k;
+    }
+    out.I = pq.I;
+    out.T = interp_coeffs(pq.R.v.sub(0, 0, out.frank, pq.R.v.c), out.frank);
+    RSVD_CK(cudaStreamSynchronize(ctx().stream));
+    return out;
+}
+
+IdOut id_rand(DM<double> A, int k, int p, int q, int s_) {
+    // Row sketch Y = Om A ((k+p) x n) with q rounds; carried transposed (Yt = Y^T, n x l)
+    // so that Z = qr(Y^T,0)^T is the orthonormalisation of Yt (RRA:1863-1965).
+    Ctx &cx = ctx();
+    cudaStream_t s = cx.stream;
+    const i64 m = A.r, n = A.c, l = (i64)k + p;
+    DMat<double> Om = make_omega<double>(l, m);
+    DMat<double> Yt(n, l, s, false), Z1(n, l, s, false), Y2(m, l, s, false), Z2(m, l, s, false);
+    gemm<double>(s, true, true, 1.0, A, Om.v, 0.0, Yt.v);               // Yt = A^T Om^T
+    for (int j = 1; j <= q; j++) {
+        DM<double> z1 = Yt.v;
+        if ((2 * j - 2) % s_ == 0) { orth<double>(Yt.v, Z1.v, nullptr); z1 = Z1.v; }
+        gemm<double>(s, false, false, 1.0, A, z1, 0.0, Y2.v);            // (Z M^T)^T = M Z^T
+        DM<double> z2 = Y2.v;
+        if ((2 * j - 1) % s_ == 0) { orth<double>(Y2.v, Z2.v, nullptr); z2 = Z2.v; }
+        gemm<double>(s, true, false, 1.0, A, z2, 0.0, Yt.v);             // (Z M)^T = M^T Z^T
+    }
+    DMat<double> Y(l, n, s, false);
+    transpose<double>(s, Yt.v, Y.v);
+    DBuf taub(sizeof(double) * std::max<i64>(1, std::min(l, n)), s), jb(sizeof(int) * std::max<i64>(1, n), s);
+    pivqr_lapack(s, Y.v, (double *)taub.get(), (int *)jb.get());
+    IdOut out;
+    out.I = download_ints(s, (const int *)jb.get(), n);
+    out.T = interp_coeffs(Y.v.sub(0, 0, k, n), k);
+    out.frank = k;
+    RSVD_CK(cudaStreamSynchronize(s));
+    return out;
+}
+
+IdOut id_blockrand(DM<double> A, int k, int p, double TOL, int kstep, int q, int s_) {
+    // RRA:1969-2027
+    Ctx &cx = ctx();
+    cudaStream_t s = cx.stream;
+    int nstep = (k + p) / kstep;
+    const bool rank_mode = k > 0;
+    if (!rank_mode) nstep = 0;
+    QBOut<double> qb = qb_blocked<double>(A, kstep, nstep, TOL, q, s_);
+    DM<double> B = qb.B.v;
+    const i64 lb = B.r, n = B.c;
+    DMat<double> W(lb, n, s, false);
+    copy_dm<double>(s, B, W.v);
+    DBuf taub(sizeof(double) * std::max<i64>(1, std::min(lb, n)), s), jb(sizeof(int) * std::max<i64>(1, n), s);
+    pivqr_lapack(s, W.v, (double *)taub.get(), (int *)jb.get());
+    IdOut out;
+    int f = qb.frank;
+    if (rank_mode) f = k;
+    else f = (int)std::round((double)(f / (f + p + 1e-6)) * f);
+    out.frank = f;
+    out.I = download_ints(s, (const int *)jb.get(), n);
+    out.T = interp_coeffs(W.v.sub(0, 0, f, n), f);
+    RSVD_CK(cudaStreamSynchronize(s));
+    return out;
+}
+
+namespace {
+__global__ void build_v_kernel(const double *T, i64 ldt, const int *inv, int k, i64 n, double *V, i64 ldv) {
+    // V(i,:) = row inv[i] of [I_k ; T^T]
+    for (i64 e = blockIdx.x * (i64)blockDim.x + threadIdx.x; e < n * k; e += (i64)gridDim.x * blockDim.x) {
+        const i64 i = e % n;
+        const int c = (int)(e / n);
+        const int r = inv[i];
+        V[i + (i64)c * ldv] = (r < k) ? (r == c ? 1.0 : 0.0) : T[c + (i64)(r - k) * ldt];
+    }
+}
+}  // namespace
+
+TwoSidedOut id_two_sided(DM<double> A, IdOut col) {
+    // MIt = A(:, Icol(1:k))^T, then a full-rank deterministic row ID of it (RRA:2042-2051)
+    Ctx &cx = ctx();
+    cudaStream_t s = cx.stream;
+    const int k = col.frank;
+    const i64 m = A.r;
+    DBuf ib(sizeof(int) * std::max(1, k), s);
+    RSVD_CK(cudaMemcpyAsync(ib.get(), col.I.data(), sizeof(int) * k, cudaMemcpyHostToDevice, s));
+    DMat<double> MI(m, k, s, false), MIt(k, m, s, false);
+    gather_cols<double>(s, A, (const int *)ib.get(), MI.v);
+    transpose<double>(s, MI.v, MIt.v);
+    IdOut row = id_det(MIt.v, k, 0.0);
+    TwoSidedOut out;
+    out.Icol = std::move(col.I);
+    out.T = std::move(col.T);
+    out.Irow = std::move(row.I);
+    out.S = std::move(row.T);
+    out.frank = k;
+    return out;
+}
+
+CurOut cur_from_two_sided(DM<double> A, int k, const TwoSidedOut &ts) {
+    // RRA:2191-2258: V = [I; T^T](Icolinv,:), C = A(:,Icol(1:k)), R = A(Irow(1:k),:),
+    // (R R^T) Ut = R V solved by LU with partial pivoting, U = Ut^T
+    Ctx &cx = ctx();
+    cudaStream_t s = cx.stream;
+    const i64 m = A.r, n = A.c;
+    std::vector<int> inv((size_t)n);
+    for (i64 j = 0; j < n; j++) inv[(size_t)ts.Icol[(size_t)j]] = (int)j;
+    DBuf ib(sizeof(int) * (n + 2 * (i64)k + 2), s);
+    int *d_inv = (int *)ib.get(), *d_icol = d_inv + n, *d_irow = d_icol + k;
+    RSVD_CK(cudaMemcpyAsync(d_inv, inv.data(), sizeof(int) * n, cudaMemcpyHostToDevice, s));
+    RSVD_CK(cudaMemcpyAsync(d_icol, ts.Icol.data(), sizeof(int) * k, cudaMemcpyHostToDevice, s));
+    RSVD_CK(cudaMemcpyAsync(d_irow, ts.Irow.data(), sizeof(int) * k, cudaMemcpyHostToDevice, s));
+    DMat<double> V(n, k, s, false);
+    build_v_kernel<<<ceil_div(n * k, 256), 256, 0, s>>>(ts.T.v.p, ts.T.v.ld, d_inv, k, n, V.v.p, V.v.ld);
+    RSVD_LAUNCH_CK();
+    CurOut out;
+    out.frank = k;
+    out.R = DMat<double>(k, n, s, false);
+    out.C = DMat<double>(m, k, s, false);
+    gather_rows<double>(s, A, d_irow, out.R.v);
+    gather_cols<double>(s, A, d_icol, out.C.v);
+    DMat<double> RRt(k, k, s, false), RV(k, k, s, false);
+    gemm<double>(s, false, true, 1.0, out.R.v, out.R.v, 0.0, RRt.v);
+    gemm<double>(s, false, false, 1.0, out.R.v, V.v, 0.0, RV.v);
+    if (!lu_solve(s, RRt.v, RV.v, cx.d_flags + FLAG_NONFINITE))
+        set_error(RSVD_ERR_NUMERIC, "cur: R R^T is singular");
+    out.U = DMat<double>(k, k, s, false);
+    transpose<double>(s, RV.v, out.U.v);
+    RSVD_CK(cudaStreamSynchronize(s));
+    return out;
+}
+
+}  // namespace rsvd

@@ -1,0 +1,78 @@
+// engine.h -- device-resident decompositions (called by api.cu).
+//
+// Every routine takes A as a device view and leaves its results on the device.  The
+// steps follow multi_core_mkl_code/rank_revealing_algorithms_intel_mkl.c ("RRA"); the
+// products and orthonormalisations are GPU kernels:
+//   Q = orth(Y)  : CholeskyQR2 (FP64 Cholesky of an FP64-accumulated Gram), Householder
+//                  QR when Cholesky breaks down.  Same column space as the reference's
+//                  dgeqrf+dorgqr Q; columns may differ in sign, which no output depends on
+//                  beyond the sign of singular-vector pairs.
+//   l x l SVD    : one-sided Jacobi (FP64).
+//   pivoting     : k_pivqr.cu (dgeqp3 rule / the reference's own rule).
+#pragma once
+#include "rsvd_internal.h"
+
+namespace rsvd {
+
+template <typename T>
+struct SvdOut {
+    DMat<T> U, V;
+    std::vector<double> S;   // length k, in the reference's order for vnum
+};
+
+template <typename T>
+struct QBOut {
+    DMat<T> Q, B;
+    int frank = 0;
+};
+
+struct IdOut {
+    std::vector<int> I;      // 0-based permutation (length n)
+    DMat<double> T;          // k x (n - k)
+    int frank = 0;
+};
+
+struct TwoSidedOut {
+    std::vector<int> Icol, Irow;
+    DMat<double> T, S;
+    int frank = 0;
+};
+
+struct CurOut {
+    DMat<double> C, U, R;
+    int frank = 0;
+};
+
+struct PivQROut {
+    DMat<double> Q, R;
+    std::vector<int> I;
+    int frank = 0;
+};
+
+// Large products (sketch, power rounds, projections): precision-mode dispatch.
+template <typename T>
+void prod(cudaStream_t s, bool ta, bool tb, T alpha, DM<T> A, DM<T> B, T beta, DM<T> C);
+
+// Gaussian test matrix (r x c): provider when registered (and enabled), else Philox.
+template <typename T>
+DMat<T> make_omega(i64 r, i64 c);
+
+template <typename T>
+void orth(DM<T> Y, DM<T> Q, DM<double> *R);
+
+template <typename T>
+SvdOut<T> svd_fixed_rank(DM<T> A, int k, int p, int vnum, int q, int s);
+template <typename T>
+SvdOut<T> svd_blockrand(DM<T> A, int k, int p, double TOL, int vnum, int kstep, int q, int s, int *frank);
+template <typename T>
+QBOut<T> qb_blocked(DM<T> A, int kstep, int nstep, double TOL, int q, int s);
+
+PivQROut pivoted_qr_full(DM<double> A);
+PivQROut pivoted_qr_partial(DM<double> A, int k, double TOL);
+IdOut id_det(DM<double> A, int k, double TOL);
+IdOut id_rand(DM<double> A, int k, int p, int q, int s);
+IdOut id_blockrand(DM<double> A, int k, int p, double TOL, int kstep, int q, int s);
+TwoSidedOut id_two_sided(DM<double> A, IdOut col);
+CurOut cur_from_two_sided(DM<double> A, int k, const TwoSidedOut &ts);
+
+}  // namespace rsvd

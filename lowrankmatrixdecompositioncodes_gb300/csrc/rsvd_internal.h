@@ -1,0 +1,165 @@
+// rsvd_internal.h -- internal C++ interfaces of librsvdpack (not installed).
+//
+// Layering:
+//   api.cpp        extern "C" reference API: host mat/vec in, host mat/vec out
+//   engine.cu      device-resident algorithms on DM<T> views (rsvd, QB, ID, CUR)
+//   k_*.cu         kernels + their launchers declared below
+// All device matrices are column-major views {ptr, rows, cols, ld}.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cuda_bf16.h>
+
+#include <cstdint>
+#include <cstdio>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "rsvdpack.h"
+
+namespace rsvd {
+
+using i64 = long long;
+
+// ----------------------------------------------------------------- errors
+struct Error : std::runtime_error {
+    int code;
+    Error(int c, const std::string &m) : std::runtime_error(m), code(c) {}
+};
+[[noreturn]] void throw_cuda(cudaError_t e, const char *what, const char *file, int line);
+[[noreturn]] void fail(int code, const std::string &msg);
+void set_error(int code, const std::string &msg);   // thread-local last error
+
+#define RSVD_CK(x)                                                              \
+    do {                                                                        \
+        cudaError_t e_ = (x);                                                   \
+        if (e_ != cudaSuccess) ::rsvd::throw_cuda(e_, #x, __FILE__, __LINE__);  \
+    } while (0)
+#define RSVD_LAUNCH_CK() RSVD_CK(cudaGetLastError())
+
+// ----------------------------------------------------------------- device views
+template <typename T>
+struct DM {
+    T *p = nullptr;
+    i64 r = 0, c = 0, ld = 0;
+    __host__ __device__ T *col(i64 j) const { return p + j * ld; }
+    __host__ __device__ T &at(i64 i, i64 j) const { return p[i + j * ld]; }
+    DM sub(i64 r0, i64 c0, i64 nr, i64 nc) const { return DM{p + r0 + c0 * ld, nr, nc, ld}; }
+    DM cols(i64 c0, i64 nc) const { return sub(0, c0, r, nc); }
+};
+
+// Stream-ordered device buffer (cudaMallocAsync on the calling thread's stream).
+class DBuf {
+  public:
+    DBuf() = default;
+    DBuf(size_t bytes, cudaStream_t s);
+    ~DBuf();
+    DBuf(const DBuf &) = delete;
+    DBuf &operator=(const DBuf &) = delete;
+    DBuf(DBuf &&o) noexcept : p_(o.p_), n_(o.n_), s_(o.s_) { o.p_ = nullptr; o.n_ = 0; }
+    DBuf &operator=(DBuf &&o) noexcept;
+    void *get() const { return p_; }
+    size_t bytes() const { return n_; }
+
+  private:
+    void *p_ = nullptr;
+    size_t n_ = 0;
+    cudaStream_t s_ = nullptr;
+};
+
+// Leading dimension used for device copies: rows rounded up to 32 elements so that
+// every column starts on a 128-byte boundary (TMA needs 16-byte strides).
+inline i64 pad_ld(i64 rows) { return ((rows + 31) / 32) * 32; }
+
+template <typename T>
+struct DMat {  // owning device matrix
+    DBuf buf;
+    DM<T> v;
+    DMat() = default;
+    DMat(i64 r, i64 c, cudaStream_t s, bool zero = true);
+    operator DM<T>() const { return v; }
+};
+
+// ----------------------------------------------------------------- per-thread context
+struct Ctx {
+    cudaStream_t stream = nullptr;
+    int device = -1;
+    int sms = 0;
+    int cc_major = 0, cc_minor = 0;
+    int *d_flags = nullptr;       // device status words (see k_common.cuh: FLAG_*)
+    rsvdpack_opts opts{};
+    rsvdpack_timing timing{};
+    long long launches = 0;
+};
+Ctx &ctx();                       // initialises the device on first use; throws RSVD_ERR_NO_DEVICE
+const rsvdpack_opts &global_opts();
+void check_device_flags(Ctx &c);  // throws if a kernel reported a timeout / breakdown
+
+// Gaussian test-matrix provider (host side).
+bool omega_provider_active();
+unsigned long long &philox_calls();   // per-thread Philox stream counter (reset with the provider counter)
+void omega_fill_host(int nrows, int ncols, double *out);  // serves the next request
+
+// ----------------------------------------------------------------- kernel launchers (k_dense.cu)
+// C = alpha * op(A) * op(B) + beta * C  (CUDA cores; double or float)
+template <typename T>
+void gemm_simt(cudaStream_t s, bool ta, bool tb, i64 M, i64 N, i64 K, T alpha, const T *A,
+               i64 lda, const T *B, i64 ldb, T beta, T *C, i64 ldc);
+template <typename T>
+void gemm(cudaStream_t s, bool ta, bool tb, T alpha, DM<T> A, DM<T> B, T beta, DM<T> C);
+
+template <typename Ts, typename Td>
+void convert(cudaStream_t s, DM<Ts> src, DM<Td> dst);      // dst = (Td)src, same shape
+template <typename T>
+void fill_zero(cudaStream_t s, DM<T> a);
+template <typename T>
+void set_identity(cudaStream_t s, DM<T> a);
+template <typename T>
+void transpose(cudaStream_t s, DM<T> src, DM<T> dst);      // dst (c x r) = src^T
+template <typename T>
+void gather_cols(cudaStream_t s, DM<T> src, const int *idx, DM<T> dst);  // dst(:,j)=src(:,idx[j])
+template <typename T>
+void gather_rows(cudaStream_t s, DM<T> src, const int *idx, DM<T> dst);  // dst(i,:)=src(idx[i],:)
+template <typename T>
+void sub_inplace(cudaStream_t s, DM<T> a, DM<T> b);        // a -= b
+template <typename T>
+double frob_norm(cudaStream_t s, DM<T> a);                  // synchronous
+void philox_gaussian(cudaStream_t s, unsigned long long seed, unsigned long long offset, DM<double> out);
+void philox_gaussian(cudaStream_t s, unsigned long long seed, unsigned long long offset, DM<float> out);
+
+// Small dense FP64 kernels.
+// Upper Cholesky G = R^T R in place (upper triangle); lower triangle zeroed.
+// Returns false on breakdown (pivot <= rel_tol * original diagonal).  Synchronous.
+bool cholesky_upper(cudaStream_t s, DM<double> G, double rel_tol, int *d_flag);
+// Q = Y * R^-1 for upper-triangular R (FP64), row by row.
+template <typename T>
+void trsm_right_upper(cudaStream_t s, DM<T> Y, DM<double> R, DM<T> Q);
+// X = triu(R)^-1 * B  (left, upper, FP64), one column of B per warp.
+void trsm_left_upper(cudaStream_t s, DM<double> R, DM<double> B, DM<double> X);
+// One-sided Jacobi SVD of square G (n x n, FP64): G = U diag(sv) V^T, sorted descending.
+// G is overwritten.  U, V: n x n.  Returns the sweep count.
+int jacobi_svd(cudaStream_t s, DM<double> G, DM<double> U, DM<double> V, double *d_sv, int *d_flag);
+// Householder QR of a tall matrix: Q (r x c) explicit, R (c x c) upper.  FP64/FP32 tall data.
+template <typename T>
+void householder_qr(cudaStream_t s, DM<T> Y, DM<T> Q, DM<double> R);
+
+// ----------------------------------------------------------------- pivoted QR (k_pivqr.cu)
+// Column-pivoted Householder QR with LAPACK dgeqp3 pivoting (all columns free):
+// on exit A holds R in its upper triangle and the reflectors below it, tau[min(m,n)],
+// jpvt[n] holds 0-based source columns.
+void pivqr_lapack(cudaStream_t s, DM<double> A, double *d_tau, int *d_jpvt);
+// Form Q (m x qc) from the reflectors stored in A (dorgqr).
+void form_q_from_reflectors(cudaStream_t s, DM<double> A, const double *d_tau, int nrefl, DM<double> Q);
+// The reference's own partial pivoted QR (rank_revealing_algorithms_intel_mkl.c:1159-1334).
+// Returns frank; fills Q (m x m workspace) and R (m x n) in place.
+int pivqr_rsvdpack(cudaStream_t s, DM<double> R, DM<double> Q, int k, double TOL, bool tol_mode,
+                   int *d_jpvt);
+// Solve A X = B in place (B <- X) by LU with partial pivoting (dgesv); false if singular.
+bool lu_solve(cudaStream_t s, DM<double> A, DM<double> B, int *d_flag);
+// G = Y^T Y (c x c, FP64) for tall Y: FP64 products for double data; for float data,
+// FP32 products summed in FP32 over 256-row chunks and in FP64 across chunks.
+template <typename T>
+void gram(cudaStream_t s, DM<T> Y, DM<double> G);
+
+}  // namespace rsvd
