@@ -107,6 +107,7 @@ void begin_call() {
 
 void end_call(Clock::time_point t0) {
     Ctx &c = ctx();
+    release_operand_cache();
     check_device_flags(c);
     c.timing.total_ms = ms_since(t0);
     c.timing.kernel_launches = c.launches;
@@ -614,7 +615,9 @@ int rsvdpack_dev_sketch(const void *dA, int dtype, long long lda, int m, int n, 
             fail(RSVD_ERR_ARGUMENT, "unknown dtype");
         }
         RSVD_CK(cudaStreamSynchronize(st));
+        release_operand_cache();
         check_device_flags(ctx());
+        ctx().timing.kernel_launches = ctx().launches;
     });
     return rsvdpack_last_error();
 }

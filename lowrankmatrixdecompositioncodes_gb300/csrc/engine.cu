@@ -55,8 +55,69 @@ constexpr double chol_tol() { return std::is_same<T, double>::value ? 1e-14 : 1e
 
 // Products of the tall / large operands.  Dispatches on the precision mode: CUDA-core
 // GEMM for FP64 and FP32; tcgen05 tensor-core GEMM for TF32 / BF16 (k_gemm_tc.cu).
+namespace {
+bool tc_ok_ptr(const void *p, i64 ld, int esz) { return ((uintptr_t)p % 16 == 0) && ((ld * esz) % 16 == 0); }
+
+// BF16 copies of operands for kind::f16 products, kept for the duration of one API call
+// (the large A is converted once per solve, not once per product).
+struct Bf16Cache {
+    const void *src = nullptr;
+    i64 r = 0, c = 0, ld = 0;
+    DMat<__nv_bfloat16> m;
+};
+thread_local Bf16Cache t_bf16_a;
+
+DM<__nv_bfloat16> to_bf16(cudaStream_t s, DM<float> X, DMat<__nv_bfloat16> &tmp, bool cache) {
+    if (cache && t_bf16_a.src == X.p && t_bf16_a.r == X.r && t_bf16_a.c == X.c && t_bf16_a.ld == X.ld)
+        return t_bf16_a.m.v;
+    DMat<__nv_bfloat16> d(X.r, X.c, s, false);
+    convert<float, __nv_bfloat16>(s, X, d.v);
+    if (cache) {
+        t_bf16_a.m = std::move(d);
+        t_bf16_a.src = X.p; t_bf16_a.r = X.r; t_bf16_a.c = X.c; t_bf16_a.ld = X.ld;
+        return t_bf16_a.m.v;
+    }
+    tmp = std::move(d);
+    return tmp.v;
+}
+}  // namespace
+
+void release_operand_cache() { t_bf16_a = Bf16Cache{}; }
+
+// Tensor-core routing (FP32 data, TF32 / BF16 modes, store form C = alpha op(A) B):
+//   op(A) = A^T (A is the K-major operand): TF32 mode -> kind::tf32 on the FP32 data as is;
+//                                           BF16 mode -> kind::f16 on the BF16 copy.
+//   op(A) = A   (A is the MN-major operand): kind::f16 on the BF16 copy in both modes --
+//       kind::tf32 with an MN-major operand gave wrong products on GB300 (tests/test_gpu_tc.py),
+//       so the transposed-operand products always read a BF16 copy of A, made once per call.
+// Deflation updates (beta != 0) and small products stay on the CUDA cores in FP32.
 template <typename T>
 void prod(cudaStream_t s, bool ta, bool tb, T alpha, DM<T> A, DM<T> B, T beta, DM<T> C) {
+    if (std::is_same<T, float>::value && !tb && beta == T(0)) {
+        const int prec = ctx().opts.precision;
+        const i64 M = ta ? A.c : A.r, K = ta ? A.r : A.c, N = B.c;
+        const bool big = (double)M * (double)N * (double)K >= 4.0e6 && M >= 64 && K >= 32;
+        if ((prec == RSVD_PREC_TF32 || prec == RSVD_PREC_BF16) && big && B.r == K && C.r == M && C.c == N &&
+            tc_ok_ptr(A.p, A.ld, 4) && tc_ok_ptr(B.p, B.ld, 4) && M < (1ll << 31) && N < (1ll << 31) &&
+            K < (1ll << 31)) {
+            if (prec == RSVD_PREC_TF32 && ta) {
+                tc_gemm(s, 0, false, A.p, A.ld, B.p, B.ld, (int)M, (int)N, (int)K, (float)alpha, (float *)C.p, C.ld,
+                        0, nullptr, 0, nullptr, 0);
+            } else {
+                // bf16 operands: the larger operand (normally A) is converted once per call
+                DMat<__nv_bfloat16> ta_tmp, tb_tmp;
+                const bool a_big = A.r * A.c >= B.r * B.c;
+                DM<__nv_bfloat16> Ab = to_bf16(s, *(DM<float> *)&A, ta_tmp, a_big);
+                DM<__nv_bfloat16> Bb = to_bf16(s, *(DM<float> *)&B, tb_tmp, !a_big);
+                tc_gemm(s, 1, !ta, Ab.p, Ab.ld, Bb.p, Bb.ld, (int)M, (int)N, (int)K, (float)alpha, (float *)C.p, C.ld,
+                        0, nullptr, 0, nullptr, 0);
+                RSVD_CK(cudaStreamSynchronize(s));   // temporaries leave scope
+            }
+            if (t_bf16_a.src == (const void *)C.p) release_operand_cache();   // C was overwritten
+            return;
+        }
+    }
+    if (t_bf16_a.src == (const void *)C.p) release_operand_cache();
     gemm<T>(s, ta, tb, alpha, A, B, beta, C);
 }
 template void prod<double>(cudaStream_t, bool, bool, double, DM<double>, DM<double>, double, DM<double>);
@@ -152,8 +213,9 @@ static SvdOut<T> svd_from_q(DM<T> A, DM<T> Q, int k, int vnum) {
         DMat<T> Vk(l, k, s, false), Uk(l, k, s, false);
         select_cols<double, T>(s, Vh.v, first, nullptr, Vk.v);
         select_cols<double, T>(s, Uh.v, first, nullptr, Uk.v);
-        prod<T>(s, false, false, T(1), Q, Vk.v, T(0), out.U.v);
-        prod<T>(s, false, false, T(1), Qh.v, Uk.v, T(0), out.V.v);
+        // factor formation stays in the working precision (never rounded to bf16)
+        gemm<T>(s, false, false, T(1), Q, Vk.v, T(0), out.U.v);
+        gemm<T>(s, false, false, T(1), Qh.v, Uk.v, T(0), out.V.v);
         out.S.assign(sv.begin(), sv.begin() + k);
     } else {
         // eig(B B^T) ascending, keep the last k; U = Q Uh; V = B^T Uh S^-1   (RRA:176-224)
@@ -175,8 +237,8 @@ static SvdOut<T> svd_from_q(DM<T> A, DM<T> Q, int k, int vnum) {
         DMat<T> Uk(l, k, s, false), Uks(l, k, s, false);
         select_cols<double, T>(s, Vh.v, perm, nullptr, Uk.v);
         select_cols<double, T>(s, Vh.v, perm, &inv, Uks.v);
-        prod<T>(s, false, false, T(1), Q, Uk.v, T(0), out.U.v);
-        prod<T>(s, false, false, T(1), Bt.v, Uks.v, T(0), out.V.v);
+        gemm<T>(s, false, false, T(1), Q, Uk.v, T(0), out.U.v);
+        gemm<T>(s, false, false, T(1), Bt.v, Uks.v, T(0), out.V.v);
     }
     RSVD_CK(cudaStreamSynchronize(s));
     return out;

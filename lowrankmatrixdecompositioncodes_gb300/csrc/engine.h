@@ -52,6 +52,8 @@ struct PivQROut {
 // Large products (sketch, power rounds, projections): precision-mode dispatch.
 template <typename T>
 void prod(cudaStream_t s, bool ta, bool tb, T alpha, DM<T> A, DM<T> B, T beta, DM<T> C);
+// Drop the per-call BF16 operand copies (called at the end of every API call).
+void release_operand_cache();
 
 // Gaussian test matrix (r x c): provider when registered (and enabled), else Philox.
 template <typename T>

@@ -1,0 +1,465 @@
+// k_gemm_tc.cu -- tensor-core GEMM for sm_103a: TMA -> shared memory (128B swizzle)
+// -> tcgen05.mma (kind::tf32 or kind::f16 with bf16 operands) -> TMEM accumulator ->
+// tcgen05.ld epilogue.  This carries every large product of the mixed-precision modes:
+//   form N : D (m x w) = A X        A column-major: operand A is MN-major (m contiguous)
+//   form T : D (n x w) = A^T X      A column-major: operand A is K-major (m contiguous)
+//   update : A (m x n) -= Qp Bp     (blocked QB deflation, fused: no m x n temporary)
+// In every form the second operand is K-major: X (column-major, K = its rows).
+//
+// CTA = 128 threads: thread 0 issues TMA loads, thread 32 issues MMAs, warp 2 owns the
+// TMEM allocation, all four warps run the epilogue (warp w reads TMEM lanes 32w..32w+31,
+// i.e. rows m0+32w..).  One CTA computes a 128-row tile for all N <= 512 columns, so A is
+// streamed from HBM exactly once per product; split-K over grid.z (deterministic
+// two-phase reduction) raises the CTA count when there are few row tiles.
+// Every mbarrier wait is bounded (~1 s); on timeout the kernel sets FLAG_TIMEOUT, skips
+// the remaining work, frees its TMEM and returns.
+#include "rsvd_internal.h"
+#include "k_common.cuh"
+
+#include <cuda.h>
+
+#include <algorithm>
+#include <cstring>
+#include <mutex>
+
+namespace rsvd {
+namespace tc {
+
+constexpr int BM = 128;          // UMMA M (cta_group::1): one TMEM lane per output row
+constexpr int KB = 128;          // bytes of K per pipeline stage (one 128B swizzle row)
+constexpr int NTHR = 128;
+constexpr int A_BYTES = BM * KB; // 16 KB per stage for operand A
+constexpr int MAX_BN = 512;      // TMEM columns available to one CTA
+
+enum { KIND_TF32 = 0, KIND_BF16 = 1 };
+enum { EPI_STORE = 0, EPI_UPDATE = 1, EPI_PARTIAL = 2 };
+
+struct Params {
+    float *D;          // output (or partial workspace base for EPI_PARTIAL)
+    long long ldd;
+    long long part_stride;   // EPI_PARTIAL: elements between split slabs
+    const float *C;    // EPI_UPDATE: D = C - alpha * acc (C may equal D)
+    long long ldc;
+    int M, N, K;
+    int BN;            // columns per CTA (multiple of 16, <= 512)
+    int chunk_n0, chunk_n1;   // MMA N of the (up to) two column chunks (chunk_n1 may be 0)
+    int kb_per_split;  // K blocks handled by one split
+    int num_kb;        // total K blocks
+    int stages;
+    float alpha;
+    double *fro_part;  // EPI_UPDATE: per-CTA sum of squares of the new D (or null)
+    int *flag;         // FLAG_TIMEOUT word
+};
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}\n"
+        : "=r"(ok)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+// Bounded wait: gives up after ~2^31 SM cycles (about one second), or as soon as another
+// thread of the CTA has given up.
+__device__ bool mbar_wait(uint32_t bar, uint32_t parity, volatile int *abort_flag, int *gflag) {
+    if (mbar_try_wait(bar, parity)) return true;
+    const long long t0 = clock64();
+    while (!mbar_try_wait(bar, parity)) {
+        if (*abort_flag) return false;
+        if (clock64() - t0 > (1ll << 31)) {
+            *abort_flag = 1;
+            atomicExch(gflag, 1);
+            return false;
+        }
+    }
+    return true;
+}
+
+__device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap *tm, uint32_t bar, int c0, int c1) {
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%3, %4}], [%2];" ::"r"(dst),
+        "l"((unsigned long long)tm), "r"(bar), "r"(c0), "r"(c1)
+        : "memory");
+}
+
+// UMMA shared-memory descriptor, SM100 layout: start>>4 [0,14), LBO>>4 [16,30),
+// SBO>>4 [32,46), version 1 at bit 46, layout SWIZZLE_128B (2) at bits [61,64).
+__device__ __forceinline__ uint64_t sdesc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
+    uint64_t d = (uint64_t)((saddr >> 4) & 0x3FFFu);
+    d |= (uint64_t)((lbo >> 4) & 0x3FFFu) << 16;
+    d |= (uint64_t)((sbo >> 4) & 0x3FFFu) << 32;
+    d |= (uint64_t)1 << 46;
+    d |= (uint64_t)2 << 61;
+    return d;
+}
+
+// Instruction descriptor (kind::tf32 / kind::f16): D f32 (bits 4-5 = 1), A/B format
+// (bits 7-9 / 10-12: bf16 = 1, tf32 = 2), A major (bit 15: 1 = MN-major), B K-major,
+// N>>3 at bits 17-22, M>>4 at bits 24-28.
+__host__ __device__ constexpr uint32_t make_idesc(int kind, bool a_mn, int n) {
+    return (1u << 4) | ((kind == KIND_TF32 ? 2u : 1u) << 7) | ((kind == KIND_TF32 ? 2u : 1u) << 10) |
+           ((a_mn ? 1u : 0u) << 15) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(BM >> 4) << 24);
+}
+
+template <int KIND>
+__device__ __forceinline__ void umma(uint32_t dt, uint64_t ad, uint64_t bd, uint32_t id, uint32_t acc) {
+    if (KIND == KIND_TF32)
+        asm volatile(
+            "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+            "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(dt),
+            "l"(ad), "l"(bd), "r"(id), "r"(acc)
+            : "memory");
+    else
+        asm volatile(
+            "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+            "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(dt),
+            "l"(ad), "l"(bd), "r"(id), "r"(acc)
+            : "memory");
+}
+__device__ __forceinline__ void umma_commit(uint32_t bar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar) : "memory");
+}
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
+    uint32_t r[16];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int i = 0; i < 16; i++) v[i] = __uint_as_float(r[i]);
+}
+
+template <int KIND, bool A_MN, int EPI>
+__global__ void __launch_bounds__(NTHR, 1)
+    tc_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, Params P) {
+    extern __shared__ uint8_t smem_raw[];
+    // 1024-byte alignment for the 128B-swizzled tiles
+    const uint32_t raw = smem_u32(smem_raw);
+    const uint32_t base = (raw + 1023u) & ~1023u;
+    uint8_t *sbase = smem_raw + (base - raw);
+    const int stages = P.stages;
+    const uint32_t b_bytes = (uint32_t)P.BN * KB;
+    const uint32_t stage_bytes = A_BYTES + b_bytes;
+    uint64_t *bars = (uint64_t *)(sbase + (size_t)stages * stage_bytes);
+    uint64_t *full = bars, *empty = bars + stages, *done = bars + 2 * stages;
+    uint32_t *tmem_holder = (uint32_t *)(done + 1);
+    volatile int *abort_flag = (volatile int *)(tmem_holder + 1);
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int m0 = blockIdx.x * BM;
+    const int n0 = blockIdx.y * P.BN;
+    const int kb0 = blockIdx.z * P.kb_per_split;
+    const int kb1 = min(P.num_kb, kb0 + P.kb_per_split);
+    const int nkb = max(0, kb1 - kb0);
+
+    uint32_t ncols = 32;
+    while ((int)ncols < P.BN) ncols <<= 1;
+
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < stages; s++) {
+            mbar_init(smem_u32(&full[s]), 1);
+            mbar_init(smem_u32(&empty[s]), 1);
+        }
+        mbar_init(smem_u32(done), 1);
+        *abort_flag = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 2) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_holder)),
+                     "r"(ncols)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = *tmem_holder;
+
+    // K elements per stage and per MMA
+    constexpr int ESZ = (KIND == KIND_TF32) ? 4 : 2;
+    constexpr int KE = KB / ESZ;                  // 32 (tf32) or 64 (bf16)
+    constexpr int ATOM_M = KB / ESZ;              // MN-major: M elements per 128B row
+    constexpr int KSTEP = 32 / ESZ;               // K per MMA instruction: 8 (tf32) / 16 (bf16)
+
+    if (threadIdx.x == 0 && nkb > 0) {
+        // ---------------- TMA producer
+        for (int i = 0; i < nkb; i++) {
+            const int s = i % stages;
+            const uint32_t ph = (uint32_t)(i / stages) & 1u;
+            if (!mbar_wait(smem_u32(&empty[s]), ph ^ 1u, abort_flag, P.flag)) break;
+            const uint32_t sa = base + (uint32_t)s * stage_bytes;
+            const uint32_t sb = sa + A_BYTES;
+            const int kidx = (kb0 + i) * KE;
+            uint32_t bytes = 0;
+            int nbox_a = 0;
+            if (A_MN) {
+                for (int j = 0; j < BM / ATOM_M; j++)
+                    if (m0 + j * ATOM_M < P.M) { bytes += (uint32_t)ATOM_M * KE * ESZ; nbox_a++; }
+            } else {
+                bytes += A_BYTES;
+            }
+            bytes += (uint32_t)P.chunk_n0 * KB;
+            if (P.chunk_n1 > 0) bytes += (uint32_t)P.chunk_n1 * KB;
+            const uint32_t fb = smem_u32(&full[s]);
+            mbar_expect_tx(fb, bytes);
+            if (A_MN) {
+                for (int j = 0; j < nbox_a; j++)
+                    tma_load_2d(sa + (uint32_t)j * (uint32_t)(KE * KB), &tmA, fb, m0 + j * ATOM_M, kidx);
+            } else {
+                tma_load_2d(sa, &tmA, fb, kidx, m0);
+            }
+            tma_load_2d(sb, &tmB, fb, kidx, n0);
+            if (P.chunk_n1 > 0) tma_load_2d(sb + (uint32_t)P.chunk_n0 * KB, &tmB, fb, kidx, n0 + P.chunk_n0);
+        }
+    } else if (threadIdx.x == 32 && nkb > 0) {
+        // ---------------- MMA issuer
+        const uint32_t id0 = make_idesc(KIND, A_MN, P.chunk_n0);
+        const uint32_t id1 = make_idesc(KIND, A_MN, P.chunk_n1 > 0 ? P.chunk_n1 : 16);
+        for (int i = 0; i < nkb; i++) {
+            const int s = i % stages;
+            const uint32_t ph = (uint32_t)(i / stages) & 1u;
+            if (!mbar_wait(smem_u32(&full[s]), ph, abort_flag, P.flag)) break;
+            tc_fence_after();
+            const uint32_t sa = base + (uint32_t)s * stage_bytes;
+            const uint32_t sb = sa + A_BYTES;
+#pragma unroll
+            for (int ks = 0; ks < KB / 32; ks++) {
+                uint64_t ad;
+                if (A_MN) ad = sdesc(sa + (uint32_t)ks * (uint32_t)(KSTEP * KB), (uint32_t)(KE * KB), 1024u);
+                else ad = sdesc(sa + (uint32_t)ks * 32u, 16u, 1024u);
+                const uint32_t acc = (i > 0 || ks > 0) ? 1u : 0u;
+                umma<KIND>(tmem, ad, sdesc(sb + (uint32_t)ks * 32u, 16u, 1024u), id0, acc);
+                if (P.chunk_n1 > 0)
+                    umma<KIND>(tmem + (uint32_t)P.chunk_n0, ad,
+                               sdesc(sb + (uint32_t)P.chunk_n0 * KB + (uint32_t)ks * 32u, 16u, 1024u), id1, acc);
+            }
+            umma_commit(smem_u32(&empty[s]));
+        }
+        umma_commit(smem_u32(done));
+    }
+    __syncwarp();
+
+    // ---------------- epilogue: TMEM -> registers -> global
+    bool ok = true;
+    if (nkb > 0) ok = mbar_wait(smem_u32(done), 0u, abort_flag, P.flag);
+    __syncwarp();
+    tc_fence_after();
+    const int row = m0 + warp * 32 + lane;
+    double fro = 0.0;
+    if (ok) {
+        for (int c0 = 0; c0 < P.BN; c0 += 16) {
+            float v[16];
+            if (nkb > 0) tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, v);
+            else {
+#pragma unroll
+                for (int t = 0; t < 16; t++) v[t] = 0.f;
+            }
+            if (row < P.M) {
+#pragma unroll
+                for (int t = 0; t < 16; t++) {
+                    const int col = n0 + c0 + t;
+                    if (col >= P.N) break;
+                    if (EPI == EPI_STORE) {
+                        P.D[(long long)row + (long long)col * P.ldd] = P.alpha * v[t];
+                    } else if (EPI == EPI_PARTIAL) {
+                        P.D[(long long)blockIdx.z * P.part_stride + (long long)row + (long long)col * P.ldd] = v[t];
+                    } else {
+                        const float nv = P.C[(long long)row + (long long)col * P.ldc] - P.alpha * v[t];
+                        P.D[(long long)row + (long long)col * P.ldd] = nv;
+                        fro += (double)nv * (double)nv;
+                    }
+                }
+            }
+        }
+    }
+    if (EPI == EPI_UPDATE && P.fro_part) {
+        __shared__ double red[32];
+        fro = block_sum(fro, red);
+        if (threadIdx.x == 0) P.fro_part[blockIdx.x + (long long)gridDim.x * blockIdx.y] = fro;
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 2) {
+        tc_fence_after();
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(ncols) : "memory");
+    }
+}
+
+__global__ void splitk_reduce_kernel(const float *part, long long stride, int splits, int M, int N, long long ldp,
+                                     float *D, long long ldd, float alpha) {
+    const long long total = (long long)M * N;
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total; e += (long long)gridDim.x * blockDim.x) {
+        const long long i = e % M, j = e / M;
+        float acc = 0.f;
+        for (int z = 0; z < splits; z++) acc += part[z * stride + i + j * ldp];
+        D[i + j * ldd] = alpha * acc;
+    }
+}
+
+// ------------------------------------------------------------------ host side
+using EncodeFn = CUresult (*)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                              const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
+                              CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+static EncodeFn encode_fn() {
+    static std::once_flag once;
+    static EncodeFn fn = nullptr;
+    std::call_once(once, [] {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = (EncodeFn)p;
+    });
+    if (!fn) fail(RSVD_ERR_CUDA, "cuTensorMapEncodeTiled is not available");
+    return fn;
+}
+
+// 2-D tensor map over a column-major-ish buffer: dim0 contiguous (extent e0), dim1 with
+// stride (bytes); box {b0, b1}; 128B swizzle; out-of-bounds elements read as zero.
+static CUtensorMap make_map(const void *ptr, int esz, long long e0, long long e1, long long stride_bytes, int b0,
+                            int b1) {
+    if (((uintptr_t)ptr & 15) || (stride_bytes & 15)) fail(RSVD_ERR_ARGUMENT, "tensor map: 16-byte alignment");
+    if (b0 * esz > 128 || b1 > 256 || b0 <= 0 || b1 <= 0) fail(RSVD_ERR_ARGUMENT, "tensor map: bad box");
+    CUtensorMap m;
+    std::memset(&m, 0, sizeof m);
+    cuuint64_t dims[2] = {(cuuint64_t)e0, (cuuint64_t)e1};
+    cuuint64_t strides[1] = {(cuuint64_t)stride_bytes};
+    cuuint32_t box[2] = {(cuuint32_t)b0, (cuuint32_t)b1};
+    cuuint32_t es[2] = {1, 1};
+    CUresult r = encode_fn()(&m, esz == 4 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2,
+                             const_cast<void *>(ptr), dims, strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                             CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) fail(RSVD_ERR_CUDA, "cuTensorMapEncodeTiled failed");
+    return m;
+}
+
+template <int KIND, bool A_MN, int EPI>
+static void launch(cudaStream_t s, dim3 grid, size_t smem, const CUtensorMap &ta, const CUtensorMap &tb,
+                   const Params &P) {
+    auto k = tc_gemm_kernel<KIND, A_MN, EPI>;
+    static bool attr_set = false;   // per instantiation
+    if (!attr_set) {
+        RSVD_CK(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, 232448));
+        attr_set = true;
+    }
+    k<<<grid, NTHR, smem, s>>>(ta, tb, P);
+    RSVD_LAUNCH_CK();
+    ctx().launches++;
+    ctx().timing.gemm_launches++;
+}
+
+}  // namespace tc
+
+// Public launcher (declared in rsvd_internal.h).
+// D (M x N, fp32, ldd) = alpha * op(A) X^T-contracted ... see rsvd_internal.h.
+void tc_gemm(cudaStream_t s, int kind, bool a_mn, const void *A, long long lda, const void *X, long long ldx,
+             int M, int N, int K, float alpha, float *D, long long ldd, int epi, const float *C, long long ldc,
+             double *fro_part, int splits_hint) {
+    using namespace tc;
+    const int esz = (kind == KIND_TF32) ? 4 : 2;
+    const int KE = KB / esz;
+    if (M <= 0 || N <= 0 || K <= 0) fail(RSVD_ERR_ARGUMENT, "tc_gemm: empty");
+    // kind::tf32 with an MN-major A operand produced wrong products on GB300; only the
+    // K-major form is used with tf32 (MN-major operands go through kind::f16 / bf16).
+    if (kind == KIND_TF32 && a_mn) fail(RSVD_ERR_ARGUMENT, "tc_gemm: tf32 needs a K-major A operand");
+    // column tiling: one CTA covers up to 512 columns as one MMA chunk (<= 256 columns) or
+    // two EQUAL chunks (both use the same TMA box, so each box fills exactly its half of
+    // the stage buffer); wider products tile N by 256.
+    const int Npad16 = (N + 15) / 16 * 16;
+    int BN, c0, c1;
+    if (Npad16 <= 256) { BN = Npad16; c0 = BN; c1 = 0; }
+    else if (N <= MAX_BN) { BN = (N + 31) / 32 * 32; c0 = c1 = BN / 2; }
+    else { BN = 256; c0 = 256; c1 = 0; }
+    const int ntiles = (N + BN - 1) / BN;
+    const int mtiles = (M + BM - 1) / BM;
+    const int num_kb = (K + KE - 1) / KE;
+    // split-K so that the grid fills the GPU when row tiles are few
+    int splits = 1;
+    const int sms = std::max(1, ctx().sms);
+    if (epi == EPI_STORE && splits_hint != 1) {
+        const int tiles = mtiles * ntiles;
+        double best = (double)((tiles + sms - 1) / sms) * sms / tiles;   // waves / useful
+        for (int z = 2; z <= 8; z++) {
+            if (num_kb / z < 4) break;
+            const double eff = (double)((tiles * z + sms - 1) / sms) * sms / ((double)tiles * z);
+            if (eff < best - 0.05) { best = eff; splits = z; }
+        }
+        if (splits_hint > 1) splits = splits_hint;
+    }
+    const int kb_per_split = (num_kb + splits - 1) / splits;
+    splits = (num_kb + kb_per_split - 1) / kb_per_split;
+
+    const size_t stage_bytes = (size_t)A_BYTES + (size_t)BN * KB;
+    int stages = (int)std::min<size_t>(8, (220 * 1024) / stage_bytes);
+    if (stages < 2) fail(RSVD_ERR_ARGUMENT, "tc_gemm: tile does not fit in shared memory");
+    const size_t smem = (size_t)stages * stage_bytes + 1024 + 64 + 16 * stages;
+
+    // tensor maps: A either MN-major (dim0 = M) or K-major (dim0 = K); X K-major (dim0 = K)
+    CUtensorMap ta = a_mn ? make_map(A, esz, M, K, lda * esz, KE, KE) : make_map(A, esz, K, M, lda * esz, KE, BM);
+    CUtensorMap tb = make_map(X, esz, K, N, ldx * esz, KE, c0);
+    Params P{};
+    P.M = M; P.N = N; P.K = K; P.BN = BN; P.chunk_n0 = c0; P.chunk_n1 = c1;
+    P.num_kb = num_kb; P.kb_per_split = kb_per_split; P.stages = stages; P.alpha = alpha;
+    P.flag = ctx().d_flags + FLAG_TIMEOUT;
+    P.fro_part = fro_part;
+    P.C = C; P.ldc = ldc;
+    dim3 grid(mtiles, ntiles, splits);
+    if (epi == EPI_UPDATE) {
+        P.D = D; P.ldd = ldd;
+        if (kind == KIND_TF32) {
+            if (a_mn) launch<KIND_TF32, true, EPI_UPDATE>(s, grid, smem, ta, tb, P);
+            else launch<KIND_TF32, false, EPI_UPDATE>(s, grid, smem, ta, tb, P);
+        } else {
+            if (a_mn) launch<KIND_BF16, true, EPI_UPDATE>(s, grid, smem, ta, tb, P);
+            else launch<KIND_BF16, false, EPI_UPDATE>(s, grid, smem, ta, tb, P);
+        }
+        return;
+    }
+    if (splits == 1) {
+        P.D = D; P.ldd = ldd;
+        if (kind == KIND_TF32) {
+            if (a_mn) launch<KIND_TF32, true, EPI_STORE>(s, grid, smem, ta, tb, P);
+            else launch<KIND_TF32, false, EPI_STORE>(s, grid, smem, ta, tb, P);
+        } else {
+            if (a_mn) launch<KIND_BF16, true, EPI_STORE>(s, grid, smem, ta, tb, P);
+            else launch<KIND_BF16, false, EPI_STORE>(s, grid, smem, ta, tb, P);
+        }
+        return;
+    }
+    const long long ldp = ((long long)M + 31) / 32 * 32;
+    const long long stride = ldp * N;
+    DBuf part(sizeof(float) * (size_t)stride * splits, s);
+    P.D = (float *)part.get(); P.ldd = ldp; P.part_stride = stride;
+    if (kind == KIND_TF32) {
+        if (a_mn) launch<KIND_TF32, true, EPI_PARTIAL>(s, grid, smem, ta, tb, P);
+        else launch<KIND_TF32, false, EPI_PARTIAL>(s, grid, smem, ta, tb, P);
+    } else {
+        if (a_mn) launch<KIND_BF16, true, EPI_PARTIAL>(s, grid, smem, ta, tb, P);
+        else launch<KIND_BF16, false, EPI_PARTIAL>(s, grid, smem, ta, tb, P);
+    }
+    const long long total = (long long)M * N;
+    const unsigned g = (unsigned)std::min<long long>((total + 255) / 256, (long long)sms * 8);
+    splitk_reduce_kernel<<<g, 256, 0, s>>>((const float *)part.get(), stride, splits, M, N, ldp, D, ldd, alpha);
+    RSVD_LAUNCH_CK();
+    ctx().launches++;
+}
+
+}  // namespace rsvd

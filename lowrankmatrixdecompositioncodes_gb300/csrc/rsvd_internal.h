@@ -163,3 +163,19 @@ template <typename T>
 void gram(cudaStream_t s, DM<T> Y, DM<double> G);
 
 }  // namespace rsvd
+
+namespace rsvd {
+// ----------------------------------------------------------------- tensor-core GEMM (k_gemm_tc.cu)
+// kind 0: tf32 operands (fp32 in memory), kind 1: bf16 operands.
+// D (M x N, fp32, column-major, ldd) = alpha * sum_k Aop(i,k) X(k,j), where
+//   a_mn == true : Aop(i,k) = A[i + k*lda]   (A column-major M x K: the "A X" form)
+//   a_mn == false: Aop(i,k) = A[k + i*lda]   (A column-major K x M: the "A^T X" form)
+//   X(k,j) = X[k + j*ldx]                    (X column-major K x N)
+// epi 0: D = alpha*acc (split-K allowed: splits_hint 0 = auto, 1 = none, >1 = forced);
+// epi 1: D = C - alpha*acc, with per-CTA sums of squares of D written to fro_part
+//        (gridDim.x * gridDim.y doubles) when fro_part is not null.
+// Requirements: A, X 16-byte aligned; lda*esize and ldx*esize multiples of 16 bytes.
+void tc_gemm(cudaStream_t s, int kind, bool a_mn, const void *A, long long lda, const void *X, long long ldx,
+             int M, int N, int K, float alpha, float *D, long long ldd, int epi, const float *C, long long ldc,
+             double *fro_part, int splits_hint);
+}  // namespace rsvd
