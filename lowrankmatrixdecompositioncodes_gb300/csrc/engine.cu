@@ -157,8 +157,29 @@ template DMat<double> make_omega<double>(i64, i64);
 template DMat<float> make_omega<float>(i64, i64);
 
 // ------------------------------------------------------------------ orthonormalisation
+// X = Y R^-1 for the upper-triangular Cholesky factor R (FP64 storage): Rinv by warp-per-
+// column back substitution, then one product in the working precision.
 template <typename T>
-void orth(DM<T> Y, DM<T> Q, DM<double> *R) {
+static void apply_rinv(cudaStream_t s, DM<T> Y, DM<double> R, DM<T> X) {
+    const i64 c = R.r;
+    DMat<double> Ri(c, c, s, false);
+    tri_inv_upper<T>(s, R, Ri.v);
+    if (std::is_same<T, double>::value) {
+        gemm<T>(s, false, false, T(1), Y, *(DM<T> *)&Ri.v, T(0), X);
+    } else {
+        DMat<T> Rt(c, c, s, false);
+        convert<double, T>(s, Ri.v, Rt.v);
+        gemm<T>(s, false, false, T(1), Y, Rt.v, T(0), X);
+        RSVD_CK(cudaStreamSynchronize(s));
+    }
+}
+
+// Q = orth(Y) by CholeskyQR (passes = 1: enough for the power-round bases, whose span is
+// all that matters) or CholeskyQR2 (passes = 2: the final bases).  Falls back to
+// Householder QR when a Cholesky factorisation breaks down.  R (optional) receives the
+// triangular factor (R2 R1 for two passes).
+template <typename T>
+void orth(DM<T> Y, DM<T> Q, DM<double> *R, int passes) {
     Ctx &cx = ctx();
     cudaStream_t s = cx.stream;
     const i64 c = Y.c;
@@ -166,12 +187,18 @@ void orth(DM<T> Y, DM<T> Q, DM<double> *R) {
     int *flag = cx.d_flags + FLAG_CHOL_BREAKDOWN;
     DMat<double> G1(c, c, s, false);
     gram<T>(s, Y, G1.v);
-    if (cholesky_upper(s, G1.v, chol_tol<T>(), flag)) {
-        trsm_right_upper<T>(s, Y, G1.v, Q);
+    if (cholesky_small<T>(s, G1.v, chol_tol<T>(), flag)) {
+        if (passes < 2) {
+            apply_rinv<T>(s, Y, G1.v, Q);
+            if (R) copy_dm<double>(s, G1.v, *R);
+            return;
+        }
+        DMat<T> W(Y.r, c, s, false);
+        apply_rinv<T>(s, Y, G1.v, W.v);
         DMat<double> G2(c, c, s, false);
-        gram<T>(s, Q, G2.v);
-        if (cholesky_upper(s, G2.v, chol_tol<T>(), flag)) {
-            trsm_right_upper<T>(s, Q, G2.v, Q);
+        gram<T>(s, W.v, G2.v);
+        if (cholesky_small<T>(s, G2.v, chol_tol<T>(), flag)) {
+            apply_rinv<T>(s, W.v, G2.v, Q);
             if (R) gemm<double>(s, false, false, 1.0, G2.v, G1.v, 0.0, *R);   // R = R2 R1
             return;
         }
@@ -183,8 +210,8 @@ void orth(DM<T> Y, DM<T> Q, DM<double> *R) {
     householder_qr<T>(s, W.v, Q, Rh.v);
     if (R) copy_dm<double>(s, Rh.v, *R);
 }
-template void orth<double>(DM<double>, DM<double>, DM<double> *);
-template void orth<float>(DM<float>, DM<float>, DM<double> *);
+template void orth<double>(DM<double>, DM<double>, DM<double> *, int);
+template void orth<float>(DM<float>, DM<float>, DM<double> *, int);
 
 // ------------------------------------------------------------------ SVD back end
 // From an orthonormal Q (m x l) spanning the sketch: RRA:133-224.
@@ -205,8 +232,8 @@ static SvdOut<T> svd_from_q(DM<T> A, DM<T> Q, int k, int vnum) {
         // [Qh, Rh] = qr(Bt); Rh = Uh S Vh^T; U = Q Vh; V = Qh Uh   (RRA:133-174)
         DMat<T> Qh(n, l, s, false);
         DMat<double> Rh(l, l, s, true);
-        orth<T>(Bt.v, Qh.v, &Rh.v);
-        jacobi_svd(s, Rh.v, Uh.v, Vh.v, (double *)svb.get(), cx.d_flags + FLAG_JACOBI_NOCONV);
+        orth<T>(Bt.v, Qh.v, &Rh.v, 2);
+        jacobi_small<T>(s, Rh.v, Uh.v, Vh.v, (double *)svb.get(), cx.d_flags + FLAG_JACOBI_NOCONV);
         RSVD_CK(cudaMemcpyAsync(sv.data(), svb.get(), sizeof(double) * l, cudaMemcpyDeviceToHost, s));
         std::vector<int> first((size_t)k);
         for (int j = 0; j < k; j++) first[j] = j;
@@ -221,7 +248,7 @@ static SvdOut<T> svd_from_q(DM<T> A, DM<T> Q, int k, int vnum) {
         // eig(B B^T) ascending, keep the last k; U = Q Uh; V = B^T Uh S^-1   (RRA:176-224)
         DMat<double> BBt(l, l, s, false);
         gram<T>(s, Bt.v, BBt.v);                                         // B B^T = Bt^T Bt
-        jacobi_svd(s, BBt.v, Uh.v, Vh.v, (double *)svb.get(), cx.d_flags + FLAG_JACOBI_NOCONV);
+        jacobi_small<T>(s, BBt.v, Uh.v, Vh.v, (double *)svb.get(), cx.d_flags + FLAG_JACOBI_NOCONV);
         RSVD_CK(cudaMemcpyAsync(sv.data(), svb.get(), sizeof(double) * l, cudaMemcpyDeviceToHost, s));
         RSVD_CK(cudaStreamSynchronize(s));
         // ascending order position i in [0,k) <- descending position k-1-i
@@ -254,13 +281,13 @@ SvdOut<T> svd_fixed_rank(DM<T> A, int k, int p, int vnum, int q, int s_) {
     DMat<T> Y(m, l, s, false), Z(n, l, s, false), Yo(m, l, s, false), Zo(n, l, s, false);
     prod<T>(s, false, false, T(1), A, Om.v, T(0), Y.v);                 // Y = A Om
     for (int j = 1; j < q; j++) {                                         // q-1 rounds (RRA:101)
-        if ((2 * j - 2) % s_ == 0) { orth<T>(Y.v, Yo.v, nullptr); prod<T>(s, true, false, T(1), A, Yo.v, T(0), Z.v); }
+        if ((2 * j - 2) % s_ == 0) { orth<T>(Y.v, Yo.v, nullptr, 1); prod<T>(s, true, false, T(1), A, Yo.v, T(0), Z.v); }
         else prod<T>(s, true, false, T(1), A, Y.v, T(0), Z.v);
-        if ((2 * j - 1) % s_ == 0) { orth<T>(Z.v, Zo.v, nullptr); prod<T>(s, false, false, T(1), A, Zo.v, T(0), Y.v); }
+        if ((2 * j - 1) % s_ == 0) { orth<T>(Z.v, Zo.v, nullptr, 1); prod<T>(s, false, false, T(1), A, Zo.v, T(0), Y.v); }
         else prod<T>(s, false, false, T(1), A, Z.v, T(0), Y.v);
     }
     DMat<T> Q(m, l, s, false);
-    orth<T>(Y.v, Q.v, nullptr);
+    orth<T>(Y.v, Q.v, nullptr, 2);
     return svd_from_q<T>(A, Q.v, k, vnum);
 }
 template SvdOut<double> svd_fixed_rank<double>(DM<double>, int, int, int, int, int);
@@ -290,19 +317,19 @@ QBOut<T> qb_blocked(DM<T> A, int kstep, int nstep, double TOL, int q, int s_) {
         const i64 c0 = (i64)step * kstep;
         prod<T>(s, false, false, T(1), Aw.v, Om.v.cols(c0, kstep), T(0), Yp.v);
         for (int j = 1; j <= q; j++) {                                    // q rounds (RRA:1652)
-            if ((2 * j - 2) % s_ == 0) { orth<T>(Yp.v, Qp.v, nullptr); prod<T>(s, true, false, T(1), Aw.v, Qp.v, T(0), AtQp.v); }
+            if ((2 * j - 2) % s_ == 0) { orth<T>(Yp.v, Qp.v, nullptr, 1); prod<T>(s, true, false, T(1), Aw.v, Qp.v, T(0), AtQp.v); }
             else prod<T>(s, true, false, T(1), Aw.v, Yp.v, T(0), AtQp.v);
-            if ((2 * j - 1) % s_ == 0) { orth<T>(AtQp.v, AtQp2.v, nullptr); prod<T>(s, false, false, T(1), Aw.v, AtQp2.v, T(0), Yp.v); }
+            if ((2 * j - 1) % s_ == 0) { orth<T>(AtQp.v, AtQp2.v, nullptr, 1); prod<T>(s, false, false, T(1), Aw.v, AtQp2.v, T(0), Yp.v); }
             else prod<T>(s, false, false, T(1), Aw.v, AtQp.v, T(0), Yp.v);
         }
-        orth<T>(Yp.v, Qp.v, nullptr);
+        orth<T>(Yp.v, Qp.v, nullptr, 2);
         if (step > 0 && step % 2 == 0) {                                  // RRA:1703-1732
             DM<T> Qj = out.Q.v.cols(0, c0);
             DMat<T> QjtQp(c0, kstep, s, false);
             prod<T>(s, true, false, T(1), Qj, Qp.v, T(0), QjtQp.v);
             copy_dm<T>(s, Qp.v, Yp.v);
             prod<T>(s, false, false, T(-1), Qj, QjtQp.v, T(1), Yp.v);    // Yp = Qp - Qj (Qj^T Qp)
-            orth<T>(Yp.v, Qp.v, nullptr);
+            orth<T>(Yp.v, Qp.v, nullptr, 2);
         }
         prod<T>(s, true, false, T(1), Qp.v, Aw.v, T(0), Bp.v);           // Bp = Qp^T A
         prod<T>(s, false, false, T(-1), Qp.v, Bp.v, T(1), Aw.v);         // A -= Qp Bp (in place)
@@ -434,10 +461,10 @@ IdOut id_rand(DM<double> A, int k, int p, int q, int s_) {
     gemm<double>(s, true, true, 1.0, A, Om.v, 0.0, Yt.v);               // Yt = A^T Om^T
     for (int j = 1; j <= q; j++) {
         DM<double> z1 = Yt.v;
-        if ((2 * j - 2) % s_ == 0) { orth<double>(Yt.v, Z1.v, nullptr); z1 = Z1.v; }
+        if ((2 * j - 2) % s_ == 0) { orth<double>(Yt.v, Z1.v, nullptr, 1); z1 = Z1.v; }
         gemm<double>(s, false, false, 1.0, A, z1, 0.0, Y2.v);            // (Z M^T)^T = M Z^T
         DM<double> z2 = Y2.v;
-        if ((2 * j - 1) % s_ == 0) { orth<double>(Y2.v, Z2.v, nullptr); z2 = Z2.v; }
+        if ((2 * j - 1) % s_ == 0) { orth<double>(Y2.v, Z2.v, nullptr, 1); z2 = Z2.v; }
         gemm<double>(s, true, false, 1.0, A, z2, 0.0, Yt.v);             // (Z M)^T = M^T Z^T
     }
     DMat<double> Y(l, n, s, false);

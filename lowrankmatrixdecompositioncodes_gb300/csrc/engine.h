@@ -60,7 +60,7 @@ template <typename T>
 DMat<T> make_omega(i64 r, i64 c);
 
 template <typename T>
-void orth(DM<T> Y, DM<T> Q, DM<double> *R);
+void orth(DM<T> Y, DM<T> Q, DM<double> *R, int passes = 2);
 
 template <typename T>
 SvdOut<T> svd_fixed_rank(DM<T> A, int k, int p, int vnum, int q, int s);

@@ -87,10 +87,106 @@ __global__ void __launch_bounds__(256) gemm_simt_kernel(i64 M, i64 N, i64 K, T a
 }
 }  // namespace
 
+// FP32 CUDA-core GEMM for op(B) = B: 128 x 64 tile, 256 threads, 8 x 4 outputs per thread
+// (rows ty*4+{0..3} and 64+ty*4+{0..3}, columns tx*4+{0..3}), K staged 16 at a time with
+// the next stage prefetched into registers while the current one is consumed.
+template <bool TA>
+__global__ void __launch_bounds__(256) sgemm_128x64_kernel(i64 M, i64 N, i64 K, float alpha,
+                                                           const float *__restrict__ A, i64 lda,
+                                                           const float *__restrict__ B, i64 ldb, float beta,
+                                                           float *__restrict__ C, i64 ldc) {
+    __shared__ __align__(16) float As[16][128];
+    __shared__ __align__(16) float Bs[16][64];
+    const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
+    const i64 m0 = (i64)blockIdx.x * 128, n0 = (i64)blockIdx.y * 64;
+    float ra[8], rb[4];
+    auto load = [&](i64 k0) {
+#pragma unroll
+        for (int e = 0; e < 8; e++) {
+            const int idx = tid + 256 * e;
+            int i, kk;
+            if (!TA) { i = idx & 127; kk = idx >> 7; }
+            else { kk = idx & 15; i = idx >> 4; }
+            const i64 gi = m0 + i, gk = k0 + kk;
+            ra[e] = (gi < M && gk < K) ? (TA ? A[gk + gi * lda] : A[gi + gk * lda]) : 0.f;
+        }
+#pragma unroll
+        for (int e = 0; e < 4; e++) {
+            const int idx = tid + 256 * e;
+            const int kk = idx & 15, j = idx >> 4;
+            const i64 gj = n0 + j, gk = k0 + kk;
+            rb[e] = (gj < N && gk < K) ? B[gk + gj * ldb] : 0.f;
+        }
+    };
+    auto store = [&]() {
+#pragma unroll
+        for (int e = 0; e < 8; e++) {
+            const int idx = tid + 256 * e;
+            int i, kk;
+            if (!TA) { i = idx & 127; kk = idx >> 7; }
+            else { kk = idx & 15; i = idx >> 4; }
+            As[kk][i] = ra[e];
+        }
+#pragma unroll
+        for (int e = 0; e < 4; e++) {
+            const int idx = tid + 256 * e;
+            Bs[idx & 15][idx >> 4] = rb[e];
+        }
+    };
+    float acc[8][4];
+#pragma unroll
+    for (int a = 0; a < 8; a++)
+#pragma unroll
+        for (int b = 0; b < 4; b++) acc[a][b] = 0.f;
+    load(0);
+    for (i64 k0 = 0; k0 < K; k0 += 16) {
+        store();
+        __syncthreads();
+        if (k0 + 16 < K) load(k0 + 16);
+#pragma unroll
+        for (int kk = 0; kk < 16; kk++) {
+            const float4 a0 = *reinterpret_cast<const float4 *>(&As[kk][ty * 4]);
+            const float4 a1 = *reinterpret_cast<const float4 *>(&As[kk][64 + ty * 4]);
+            const float4 b0 = *reinterpret_cast<const float4 *>(&Bs[kk][tx * 4]);
+            const float av[8] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w};
+            const float bv[4] = {b0.x, b0.y, b0.z, b0.w};
+#pragma unroll
+            for (int x = 0; x < 8; x++)
+#pragma unroll
+                for (int y = 0; y < 4; y++) acc[x][y] = fmaf(av[x], bv[y], acc[x][y]);
+        }
+        __syncthreads();
+    }
+#pragma unroll
+    for (int x = 0; x < 8; x++) {
+        const i64 gi = m0 + (x < 4 ? ty * 4 + x : 64 + ty * 4 + (x - 4));
+        if (gi >= M) continue;
+#pragma unroll
+        for (int y = 0; y < 4; y++) {
+            const i64 gj = n0 + tx * 4 + y;
+            if (gj >= N) continue;
+            float *c = C + gi + gj * ldc;
+            *c = (beta == 0.f) ? alpha * acc[x][y] : alpha * acc[x][y] + beta * (*c);
+        }
+    }
+}
+
 template <typename T>
 void gemm_simt(cudaStream_t s, bool ta, bool tb, i64 M, i64 N, i64 K, T alpha, const T *A,
                i64 lda, const T *B, i64 ldb, T beta, T *C, i64 ldc) {
     if (M <= 0 || N <= 0) return;
+    if (std::is_same<T, float>::value && !tb && M >= 128) {
+        dim3 grid(ceil_div(M, 128), ceil_div(N, 64));
+        if (grid.y <= 65535) {
+            if (ta) sgemm_128x64_kernel<true><<<grid, 256, 0, s>>>(M, N, K, (float)alpha, (const float *)A, lda,
+                                                                  (const float *)B, ldb, (float)beta, (float *)C, ldc);
+            else sgemm_128x64_kernel<false><<<grid, 256, 0, s>>>(M, N, K, (float)alpha, (const float *)A, lda,
+                                                                (const float *)B, ldb, (float)beta, (float *)C, ldc);
+            RSVD_LAUNCH_CK();
+            ctx().launches++;
+            return;
+        }
+    }
     dim3 grid(ceil_div(M, GB_M), ceil_div(N, GB_N));
     if (grid.y > 65535) fail(RSVD_ERR_ARGUMENT, "gemm: N too large for the SIMT tiling");
     if (!ta && !tb) gemm_simt_kernel<T, false, false><<<grid, 256, 0, s>>>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc);

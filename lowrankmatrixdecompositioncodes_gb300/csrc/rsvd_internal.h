@@ -179,3 +179,14 @@ void tc_gemm(cudaStream_t s, int kind, bool a_mn, const void *A, long long lda, 
              int M, int N, int K, float alpha, float *D, long long ldd, int epi, const float *C, long long ldc,
              double *fro_part, int splits_hint);
 }  // namespace rsvd
+
+namespace rsvd {
+// ----------------------------------------------------------------- small l x l steps (k_small.cu)
+// Compute type S: double in the FP64 mode, float in the mixed modes (storage is FP64).
+template <typename S>
+bool cholesky_small(cudaStream_t s, DM<double> G, double rel_tol, int *d_flag);
+template <typename S>
+void tri_inv_upper(cudaStream_t s, DM<double> R, DM<double> X);
+template <typename S>
+int jacobi_small(cudaStream_t s, DM<double> G, DM<double> U, DM<double> V, double *d_sv, int *d_flag);
+}  // namespace rsvd
