@@ -105,6 +105,15 @@ void begin_call() {
     c.launches = 0;
 }
 
+// Device entry points read caller memory: order the engine stream (non-blocking) after
+// all work already queued on the legacy default stream.
+void order_after_default_stream() {
+    thread_local cudaEvent_t ev = nullptr;
+    if (!ev) RSVD_CK(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+    RSVD_CK(cudaEventRecord(ev, 0));
+    RSVD_CK(cudaStreamWaitEvent(ctx().stream, ev, 0));
+}
+
 void end_call(Clock::time_point t0) {
     Ctx &c = ctx();
     release_operand_cache();
@@ -585,6 +594,7 @@ int rsvdpack_dev_svd_fixed_rank(const void *dA, int dtype, long long lda, int m,
         need(lda >= m && ldu >= m && ldv >= n, "bad leading dimension");
         need(q < 2 || s >= 1, "s must be >= 1 when q >= 2");
         begin_call();
+        order_after_default_stream();
         auto t0 = Clock::now();
         if (dtype == RSVD_DT_F64) dev_svd<double>(dA, lda, m, n, k, p, vnum, q, s, dU, ldu, dS, dV, ldv);
         else if (dtype == RSVD_DT_F32) dev_svd<float>(dA, lda, m, n, k, p, vnum, q, s, dU, ldu, dS, dV, ldv);
@@ -600,6 +610,7 @@ int rsvdpack_dev_sketch(const void *dA, int dtype, long long lda, int m, int n, 
         need(dA && dX && dY, "null device pointer");
         need(m > 0 && n > 0 && w > 0 && lda >= m, "bad sizes");
         begin_call();
+        order_after_default_stream();
         cudaStream_t st = ctx().stream;
         const i64 xr = trans ? m : n, yr = trans ? n : m;
         need(ldx >= xr && ldy >= yr, "bad leading dimension");

@@ -50,6 +50,7 @@ def test_tc_product_matches_fp64(engine, prec, trans, m, n, w):
     ldx, ldy = (xr + 31) // 32 * 32, (yr + 31) // 32 * 32
     X = colmajor(xr, w, ldx, g)
     Y = torch.full((w, ldy), float("nan"), device="cuda", dtype=torch.float32)
+    torch.cuda.synchronize()
     rc = engine.lib.rsvdpack_dev_sketch(A.data_ptr(), 1, lda, m, n, X.data_ptr(), ldx, w, Y.data_ptr(), ldy, trans)
     assert rc == 0, engine.last_error()
     t = engine.last_timing()
