@@ -185,7 +185,9 @@ int rsvdpack_device_info(char *name, int name_len, int *cc_major, int *cc_minor)
  * pointers; matrices are column-major with the given leading dimensions (elements).
  * dtype: RSVD_DT_F64 or RSVD_DT_F32 (FP32 data is computed in the current precision
  * mode's arithmetic; FP64 data always in FP64).  The work is queued on the calling
- * thread's engine stream (rsvdpack_stream()); the call returns after it finishes.
+ * thread's engine stream (rsvdpack_stream()), ordered after all work already queued on the
+ * legacy default stream (work on other streams must be complete or ordered by the caller);
+ * the call returns after it finishes.
  * Return value: RSVD_OK or an RSVD_ERR_* code (also kept in rsvdpack_last_error()). */
 enum { RSVD_DT_F64 = 0, RSVD_DT_F32 = 1 };
 
@@ -203,6 +205,20 @@ int rsvdpack_dev_sketch(const void *dA, int dtype, long long lda, int m, int n, 
 
 /* The calling thread's engine stream (a cudaStream_t), for event timing by callers. */
 void *rsvdpack_stream(void);
+
+/* Allocation-free sketch product Y (n x w) = A^T X (A m x n, X m x w; FP32, tcgen05 kind::tf32,
+ * split-K).  No counterpart in the reference.  For callers that cannot allocate GPU memory at
+ * the point of the call -- code under an external memory manager or a budget that forbids
+ * driver allocations, or code that must not take the implicit device synchronisation of
+ * cudaMalloc / cudaFree.  It allocates nothing and creates nothing: it uses the caller's buffers,
+ * the caller's stream (a cudaStream_t, may be 0), and a 32 MiB scratch array inside the library
+ * that each GPU loading the library holds until exit.  Limit: round_up(n, 32) * w <= 4,194,272
+ * and m > 32; larger products return RSVD_ERR_ARGUMENT.  The first call on each device (made
+ * with that device current) looks up the scratch address; make it before any stream capture.
+ * Calls share the scratch: calls that overlap on the GPU race, so serialise them.
+ * A, X, Y 16-byte aligned; lda, ldx multiples of 4.  Synchronous; returns RSVD_OK or RSVD_ERR_*. */
+int rsvdpack_dev_sketch_t_noalloc(const float *dA, long long lda, int m, int n, const float *dX,
+                                  long long ldx, int w, float *dY, long long ldy, void *stream);
 
 /* Per-call phase timing of the last decomposition on this thread (milliseconds). */
 typedef struct {

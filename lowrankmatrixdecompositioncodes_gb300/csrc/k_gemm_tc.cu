@@ -462,4 +462,127 @@ void tc_gemm(cudaStream_t s, int kind, bool a_mn, const void *A, long long lda, 
     ctx().launches++;
 }
 
+// =====================================================================================
+// Allocation-free variant of the split-K sketch product Y = A^T X (kind::tf32).
+//
+// For callers that cannot allocate GPU memory at the point of the call: code running
+// under an external memory manager or budget that forbids driver allocations, callers
+// that must not trigger the implicit synchronisation of cudaMalloc / cudaFree, and hosts
+// that reserve all device memory up front.  Every other entry point of this library
+// allocates stream-ordered workspace (and its first call creates a per-thread context);
+// this one uses only the caller's buffers, the caller's stream, and a file-scope scratch
+// array that every GPU that loads the library holds until process exit:
+//   bytes [0, 256)   : device status word (bounded-wait timeout flag), cleared every call
+//   bytes [256, ...) : split-K partial slabs (fully written before they are read)
+// Limit: 2 slabs of round_up(n, 32) x w floats must fit in the scratch (32 MiB), i.e.
+// round_up(n, 32) * w <= 4,194,272; larger products are rejected with RSVD_ERR_ARGUMENT.
+// Set-up (once per device, on the first call made while that device is current) looks
+// up the scratch array's device address with cudaGetSymbolAddress and sets the kernel's
+// shared-memory limit; make that first call before any stream capture.  All calls share
+// the one array, so calls that overlap on the GPU (other streams, other host threads on
+// the same device) race on it: serialise them.
+// =====================================================================================
+namespace {
+constexpr size_t NOALLOC_SCRATCH_BYTES = (size_t)32 << 20;
+constexpr size_t NOALLOC_HEADER = 256;
+}  // namespace
+
+static __device__ __align__(256) unsigned char rsvd_noalloc_scratch[NOALLOC_SCRATCH_BYTES];
+
+namespace {
+std::mutex g_noalloc_mu;
+void *g_noalloc_ptr[128] = {nullptr};
+
+// Per-device set-up: the scratch array's device address and the kernel attribute.
+void *noalloc_setup(int dev) {
+    if (dev < 0 || dev >= 128) fail(RSVD_ERR_NO_DEVICE, "device ordinal out of range");
+    std::lock_guard<std::mutex> g(g_noalloc_mu);
+    if (g_noalloc_ptr[dev]) return g_noalloc_ptr[dev];
+    void *p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, rsvd_noalloc_scratch);
+    if (e != cudaSuccess || !p) {
+        cudaGetLastError();
+        fail(RSVD_ERR_CUDA, std::string("cudaGetSymbolAddress(scratch) failed: ") + cudaGetErrorString(e));
+    }
+    RSVD_CK(cudaFuncSetAttribute(tc::tc_gemm_kernel<tc::KIND_TF32, false, tc::EPI_PARTIAL>,
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize, 232448));
+    g_noalloc_ptr[dev] = p;
+    return p;
+}
+}  // namespace
+
+}  // namespace rsvd
+
+extern "C" int rsvdpack_dev_sketch_t_noalloc(const float *dA, long long lda, int m, int n, const float *dX,
+                                             long long ldx, int w, float *dY, long long ldy, void *stream) {
+    using namespace rsvd;
+    using namespace rsvd::tc;
+    try {
+        rsvdpack_clear_error();
+        cudaStream_t s = (cudaStream_t)stream;
+        if (!dA || !dX || !dY) fail(RSVD_ERR_ARGUMENT, "null device pointer");
+        if (m <= 0 || n <= 0 || w <= 0) fail(RSVD_ERR_ARGUMENT, "empty product");
+        if (lda < m || ldx < m || ldy < n) fail(RSVD_ERR_ARGUMENT, "bad leading dimension");
+        int dev = -1;
+        RSVD_CK(cudaGetDevice(&dev));
+        int major = 0, minor = 0, sms = 0;
+        RSVD_CK(cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, dev));
+        RSVD_CK(cudaDeviceGetAttribute(&minor, cudaDevAttrComputeCapabilityMinor, dev));
+        RSVD_CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+        if (!(major == 10 && minor == 3)) fail(RSVD_ERR_NO_DEVICE, "needs an sm_103 (GB300) device");
+        unsigned char *scratch = (unsigned char *)noalloc_setup(dev);
+
+        // Y (n x w) = A^T X : M = n, N = w, K = m, A is the K-major operand
+        const int M = n, N = w, K = m;
+        const int KE = KB / 4;
+        const int Npad16 = (N + 15) / 16 * 16;
+        int BN, c0, c1;
+        if (Npad16 <= 256) { BN = Npad16; c0 = BN; c1 = 0; }
+        else if (N <= MAX_BN) { BN = (N + 31) / 32 * 32; c0 = c1 = BN / 2; }
+        else { BN = 256; c0 = 256; c1 = 0; }
+        const int ntiles = (N + BN - 1) / BN, mtiles = (M + BM - 1) / BM;
+        const int num_kb = (K + KE - 1) / KE;
+        const long long ldp = ((long long)M + 31) / 32 * 32;
+        const long long stride = ldp * N;
+        const long long max_slabs = (long long)((NOALLOC_SCRATCH_BYTES - NOALLOC_HEADER) / (sizeof(float) * (size_t)stride));
+        if (max_slabs < 2)
+            fail(RSVD_ERR_ARGUMENT, "product too large for the no-allocation scratch: need round_up(n,32)*w <= 4194272");
+        if (num_kb < 2) fail(RSVD_ERR_ARGUMENT, "m too small to split (needs m > 32)");
+        int splits = 2;
+        const int tiles = mtiles * ntiles;
+        for (int z = 2; z <= 8 && z <= max_slabs && z <= num_kb; z++)
+            if ((long long)tiles * z <= (long long)sms) splits = z;
+        const int kb_per_split = (num_kb + splits - 1) / splits;
+        splits = (num_kb + kb_per_split - 1) / kb_per_split;
+
+        const size_t stage_bytes = (size_t)A_BYTES + (size_t)BN * KB;
+        const int stages = (int)std::min<size_t>(8, (220 * 1024) / stage_bytes);
+        const size_t smem = (size_t)stages * stage_bytes + 1024 + 64 + 16 * stages;
+        CUtensorMap ta = make_map(dA, 4, K, M, lda * 4, KE, BM);
+        CUtensorMap tb = make_map(dX, 4, K, N, ldx * 4, KE, c0);
+        int *flag = (int *)scratch;
+        float *part = (float *)(scratch + NOALLOC_HEADER);
+        Params P{};
+        P.M = M; P.N = N; P.K = K; P.BN = BN; P.chunk_n0 = c0; P.chunk_n1 = c1;
+        P.num_kb = num_kb; P.kb_per_split = kb_per_split; P.stages = stages; P.alpha = 1.0f;
+        P.flag = flag; P.D = part; P.ldd = ldp; P.part_stride = stride;
+        RSVD_CK(cudaMemsetAsync(flag, 0, sizeof(int), s));
+        tc_gemm_kernel<KIND_TF32, false, EPI_PARTIAL><<<dim3(mtiles, ntiles, splits), NTHR, smem, s>>>(ta, tb, P);
+        RSVD_LAUNCH_CK();
+        const long long total = (long long)M * N;
+        const unsigned g = (unsigned)std::min<long long>((total + 255) / 256, (long long)std::max(1, sms) * 8);
+        splitk_reduce_kernel<<<g, 256, 0, s>>>(part, stride, splits, M, N, ldp, dY, ldy, 1.0f);
+        RSVD_LAUNCH_CK();
+        int h = 0;
+        RSVD_CK(cudaMemcpyAsync(&h, flag, sizeof(int), cudaMemcpyDeviceToHost, s));
+        RSVD_CK(cudaStreamSynchronize(s));
+        if (h) fail(RSVD_ERR_TIMEOUT, "a bounded device-side wait gave up");
+        return RSVD_OK;
+    } catch (const Error &e) {
+        set_error(e.code, std::string("rsvdpack_dev_sketch_t_noalloc: ") + e.what());
+        return e.code;
+    }
+}
+
+namespace rsvd {
 }  // namespace rsvd
