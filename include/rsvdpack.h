@@ -206,6 +206,15 @@ int rsvdpack_dev_sketch(const void *dA, int dtype, long long lda, int m, int n, 
 /* The calling thread's engine stream (a cudaStream_t), for event timing by callers. */
 void *rsvdpack_stream(void);
 
+/* The l x l steps on their own (device FP64 storage, column-major; compute in FP32 when
+ * fp32 != 0, else FP64).  rsvdpack_dev_small_svd: G (n x n) = U diag(S) V^T, S descending,
+ * by one-sided Jacobi (the engine's l x l SVD); G is overwritten; returns the sweep count or
+ * a negative RSVD_ERR_* code.  rsvdpack_dev_small_cholesky: G = R^T R in place (upper R, lower
+ * part zeroed); returns RSVD_OK, RSVD_ERR_NUMERIC on breakdown, or another RSVD_ERR_* code. */
+int rsvdpack_dev_small_svd(double *dG, int n, long long ldg, double *dU, long long ldu, double *dS, double *dV,
+                           long long ldv, int fp32);
+int rsvdpack_dev_small_cholesky(double *dG, int n, long long ldg, int fp32);
+
 /* Allocation-free sketch product Y (n x w) = A^T X (A m x n, X m x w; FP32, tcgen05 kind::tf32,
  * split-K).  No counterpart in the reference.  For callers that cannot allocate GPU memory at
  * the point of the call -- code under an external memory manager or a budget that forbids

@@ -5,6 +5,7 @@
 // outputs with matrix_new / vector_new and copy them back.  Errors never exit(): the
 // outputs are set to NULL and rsvdpack_last_error() reports the cause.
 #include "engine.h"
+#include "k_common.cuh"
 
 #include <chrono>
 #include <cmath>
@@ -629,6 +630,38 @@ int rsvdpack_dev_sketch(const void *dA, int dtype, long long lda, int m, int n, 
         release_operand_cache();
         check_device_flags(ctx());
         ctx().timing.kernel_launches = ctx().launches;
+    });
+    return rsvdpack_last_error();
+}
+
+int rsvdpack_dev_small_svd(double *dG, int n, long long ldg, double *dU, long long ldu, double *dS, double *dV,
+                           long long ldv, int fp32) {
+    int sweeps = -1;
+    guarded("rsvdpack_dev_small_svd", [&] {
+        need(dG && dU && dS && dV, "null device pointer");
+        need(n > 0 && ldg >= n && ldu >= n && ldv >= n, "bad sizes");
+        begin_call();
+        order_after_default_stream();
+        cudaStream_t st = ctx().stream;
+        DM<double> G{dG, n, n, ldg}, U{dU, n, n, ldu}, V{dV, n, n, ldv};
+        int *flag = ctx().d_flags + FLAG_JACOBI_NOCONV;
+        sweeps = fp32 ? jacobi_small<float>(st, G, U, V, dS, flag) : jacobi_small<double>(st, G, U, V, dS, flag);
+        RSVD_CK(cudaStreamSynchronize(st));
+    });
+    const int e = rsvdpack_last_error();
+    return e ? -e : sweeps;
+}
+
+int rsvdpack_dev_small_cholesky(double *dG, int n, long long ldg, int fp32) {
+    guarded("rsvdpack_dev_small_cholesky", [&] {
+        need(dG && n > 0 && ldg >= n, "bad arguments");
+        begin_call();
+        order_after_default_stream();
+        cudaStream_t st = ctx().stream;
+        DM<double> G{dG, n, n, ldg};
+        int *flag = ctx().d_flags + FLAG_CHOL_BREAKDOWN;
+        const bool ok = fp32 ? cholesky_small<float>(st, G, 0.0, flag) : cholesky_small<double>(st, G, 0.0, flag);
+        if (!ok) fail(RSVD_ERR_NUMERIC, "Cholesky breakdown (matrix not positive definite)");
     });
     return rsvdpack_last_error();
 }

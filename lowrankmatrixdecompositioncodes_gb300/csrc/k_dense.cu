@@ -798,11 +798,94 @@ __global__ void gram_reduce_kernel(const double *part, i64 part_stride, int nsla
 }
 }  // namespace
 
+// FP32 Gram, symmetric tiles only: 64 x 64 tile (bi <= bj) of G per block over a 1024-row
+// slab, 256 threads with 4 x 4 outputs each, FP32 sums flushed to FP64 every 256 rows.
+// Off-diagonal tiles are written to both (bi,bj) and (bj,bi) of the slab partial.
+namespace {
+constexpr int GS_SLAB = 1024;
+__global__ void __launch_bounds__(256) gram_sym_f32_kernel(const float *__restrict__ Y, i64 ld, i64 m, int c,
+                                                           int ntile, double *__restrict__ part, i64 part_stride) {
+    __shared__ __align__(16) float As[32][64];
+    __shared__ __align__(16) float Bs[32][64];
+    // upper-triangular tile list: blockIdx.x -> (bi, bj), bi <= bj
+    int bj = 0;
+    while ((bj + 1) * (bj + 2) / 2 <= (int)blockIdx.x) bj++;
+    const int bi = (int)blockIdx.x - bj * (bj + 1) / 2;
+    const int i0 = bi * 64, j0 = bj * 64;
+    const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
+    const i64 r0 = (i64)blockIdx.y * GS_SLAB, r1 = min(m, r0 + GS_SLAB);
+    float acc[4][4];
+    double dacc[4][4];
+#pragma unroll
+    for (int a = 0; a < 4; a++)
+#pragma unroll
+        for (int b = 0; b < 4; b++) { acc[a][b] = 0.f; dacc[a][b] = 0.0; }
+    int since = 0;
+    for (i64 rb = r0; rb < r1; rb += 32) {
+#pragma unroll
+        for (int e = 0; e < 8; e++) {
+            const int idx = tid + 256 * e;
+            const int kk = idx & 31, cc = idx >> 5;
+            const i64 row = rb + kk;
+            As[kk][cc] = (row < r1 && i0 + cc < c) ? Y[row + (i64)(i0 + cc) * ld] : 0.f;
+            Bs[kk][cc] = (row < r1 && j0 + cc < c) ? Y[row + (i64)(j0 + cc) * ld] : 0.f;
+        }
+        __syncthreads();
+#pragma unroll 8
+        for (int kk = 0; kk < 32; kk++) {
+            const float4 a = *reinterpret_cast<const float4 *>(&As[kk][ty * 4]);
+            const float4 b = *reinterpret_cast<const float4 *>(&Bs[kk][tx * 4]);
+            const float av[4] = {a.x, a.y, a.z, a.w}, bv[4] = {b.x, b.y, b.z, b.w};
+#pragma unroll
+            for (int x = 0; x < 4; x++)
+#pragma unroll
+                for (int y = 0; y < 4; y++) acc[x][y] = fmaf(av[x], bv[y], acc[x][y]);
+        }
+        __syncthreads();
+        if (++since == 8) {
+#pragma unroll
+            for (int x = 0; x < 4; x++)
+#pragma unroll
+                for (int y = 0; y < 4; y++) { dacc[x][y] += (double)acc[x][y]; acc[x][y] = 0.f; }
+            since = 0;
+        }
+    }
+    double *P = part + (i64)blockIdx.y * part_stride;
+#pragma unroll
+    for (int x = 0; x < 4; x++)
+#pragma unroll
+        for (int y = 0; y < 4; y++) {
+            const double v = dacc[x][y] + (double)acc[x][y];
+            const int gi = i0 + ty * 4 + x, gj = j0 + tx * 4 + y;
+            if (gi < c && gj < c) {
+                P[gi + (i64)gj * c] = v;
+                if (bi != bj) P[gj + (i64)gi * c] = v;
+            }
+        }
+    (void)ntile;
+}
+}  // namespace
+
 template <typename T>
 void gram(cudaStream_t s, DM<T> Y, DM<double> G) {
     const int c = (int)Y.c;
     if (G.r != c || G.c != c) fail(RSVD_ERR_ARGUMENT, "gram: shape mismatch");
     if (c == 0) return;
+    if (std::is_same<T, float>::value && c >= 64) {
+        const int nt = (c + 63) / 64, ntiles = nt * (nt + 1) / 2;
+        const int nslab = (int)std::max<i64>(1, (Y.r + GS_SLAB - 1) / GS_SLAB);
+        const i64 stride = (i64)c * c;
+        if (nslab <= 65535) {
+            DBuf part(sizeof(double) * (size_t)stride * nslab, s);
+            gram_sym_f32_kernel<<<dim3(ntiles, nslab), 256, 0, s>>>((const float *)Y.p, Y.ld, Y.r, c, ntiles,
+                                                                    (double *)part.get(), stride);
+            gram_reduce_kernel<<<grid_for(stride), 256, 0, s>>>((const double *)part.get(), stride, nslab, c, G.p,
+                                                                G.ld);
+            RSVD_LAUNCH_CK();
+            ctx().launches += 2;
+            return;
+        }
+    }
     const int nslab = (int)std::max<i64>(1, (Y.r + GR_SLAB - 1) / GR_SLAB);
     const i64 stride = (i64)c * c;
     DBuf part(sizeof(double) * (size_t)stride * nslab, s);
