@@ -206,6 +206,23 @@ int rsvdpack_dev_sketch(const void *dA, int dtype, long long lda, int m, int n, 
 /* The calling thread's engine stream (a cudaStream_t), for event timing by callers. */
 void *rsvdpack_stream(void);
 
+/* ---- batched fixed-rank rSVD (no counterpart in the reference, which takes one matrix per
+ * call): low_rank_svd_rand_decomp_fixed_rank with vnum = 1 on `count` independent FP32
+ * device matrices of uneven size, in one persistent launch captured in a CUDA graph.
+ * Matrix i: A_i (m[i] x n[i], lda[i]) -> U_i (m[i] x k[i], ldu[i]), S_i (k[i] doubles,
+ * descending), V_i (n[i] x k[i], ldv[i]); the arrays hold device pointers and are copied at
+ * plan creation.  Test matrices are Philox Gaussians (stream = seed, item index).
+ * Limits: k[i] + p <= min(m[i], n[i]), k[i] + p <= 72, n[i] * (k[i] + p) <= 54,000.
+ * Execute returns RSVD_OK, or RSVD_ERR_NUMERIC if some item broke down (its outputs are
+ * then left unwritten). */
+typedef struct rsvdpack_batch_plan rsvdpack_batch_plan;
+rsvdpack_batch_plan *rsvdpack_batch_plan_create(int count, const int *m, const int *n, const int *k, int p, int q,
+                                                int s, const float *const *dA, const long long *lda,
+                                                float *const *dU, const long long *ldu, double *const *dS,
+                                                float *const *dV, const long long *ldv, unsigned long long seed);
+int rsvdpack_batch_plan_execute(rsvdpack_batch_plan *plan);
+void rsvdpack_batch_plan_destroy(rsvdpack_batch_plan *plan);
+
 /* The l x l steps on their own (device FP64 storage, column-major; compute in FP32 when
  * fp32 != 0, else FP64).  rsvdpack_dev_small_svd: G (n x n) = U diag(S) V^T, S descending,
  * by one-sided Jacobi (the engine's l x l SVD); G is overwritten; returns the sweep count or

@@ -1,0 +1,583 @@
+// k_batch.cu -- batched fixed-rank rSVD: many independent FP32 matrices of uneven size in one
+// persistent launch (the reference has one matrix per call; low_rank_svd_rand_decomp_fixed_rank,
+// rank_revealing_algorithms_intel_mkl.c:73-174, is applied to every matrix of the batch with
+// vnum = 1).
+//
+// Each CTA pops matrices from a device work queue and runs the whole pipeline on one matrix:
+//   Om (n x l)   Philox4x32-10 Gaussians, drawn straight into shared memory (never in HBM)
+//   Y = A Om     A streamed in 64 x 32 tiles
+//   [q-1 power rounds: Yo = cqr(Y); Z = A^T Yo; Zo = cqr(Z); Y = A Zo]
+//   Q = cqr2(Y) ; Bt = A^T Q ; (Qh, Rh) = cqr2(Bt) ; Rh = Uh S Vh^T (Jacobi in shared memory)
+//   U = Q Vh(:, 1:k) ; V = Qh Uh(:, 1:k)
+// cqr = CholeskyQR (Gram, Cholesky and triangular inverse in shared memory), all FP32.
+// Tall intermediates live in a per-CTA slab of global memory (L2-resident across the CTA's
+// work).  Matrices are taken largest-first (the host sorts the queue) to balance the tail.
+#include "rsvd_internal.h"
+#include "k_common.cuh"
+
+#include <algorithm>
+#include <cmath>
+#include <numeric>
+#include <vector>
+
+namespace rsvd {
+
+struct BatchItem {
+    const float *A;
+    long long lda;
+    float *U;
+    long long ldu;
+    double *S;
+    float *V;
+    long long ldv;
+    int m, n, k, l;
+    int index;     // position in the caller's batch (Philox stream offset)
+    int pad;
+};
+
+namespace {
+
+constexpr int BT = 256;   // threads per CTA
+
+struct U4b { uint32_t x, y, z, w; };
+__device__ __forceinline__ U4b philox_b(U4b c, uint32_t k0, uint32_t k1) {
+#pragma unroll
+    for (int r = 0; r < 10; r++) {
+        const uint32_t lo0 = 0xD2511F53u * c.x, hi0 = __umulhi(0xD2511F53u, c.x);
+        const uint32_t lo1 = 0xCD9E8D57u * c.z, hi1 = __umulhi(0xCD9E8D57u, c.z);
+        c = U4b{hi1 ^ c.y ^ k0, lo1, hi0 ^ c.w ^ k1, lo0};
+        k0 += 0x9E3779B9u;
+        k1 += 0xBB67AE85u;
+    }
+    return c;
+}
+
+// Om (n x l, column-major element e = row + col*n) into shared memory, row-major Bsm[j*l + c].
+// Same counter layout as the single-matrix generator: group g = e/4 -> counter (g, offset).
+__device__ void gen_omega(float *Bsm, int n, int l, uint64_t seed, uint64_t offset) {
+    const long long total = (long long)n * l, groups = (total + 3) / 4;
+    for (long long g = threadIdx.x; g < groups; g += blockDim.x) {
+        const U4b v = philox_b(U4b{(uint32_t)g, (uint32_t)(g >> 32), (uint32_t)offset, (uint32_t)(offset >> 32)},
+                               (uint32_t)seed, (uint32_t)(seed >> 32));
+        const uint32_t u[4] = {v.x, v.y, v.z, v.w};
+        float z[4];
+#pragma unroll
+        for (int h = 0; h < 2; h++) {
+            const float u1 = ((float)u[2 * h] + 1.0f) * 2.3283064365386963e-10f;
+            const float u2 = (float)u[2 * h + 1] * 2.3283064365386963e-10f;
+            const float rad = sqrtf(-2.0f * logf(u1));
+            float sn, cs;
+            sincospif(2.0f * u2, &sn, &cs);
+            z[2 * h] = rad * cs;
+            z[2 * h + 1] = rad * sn;
+        }
+#pragma unroll
+        for (int t = 0; t < 4; t++) {
+            const long long e = 4 * g + t;
+            if (e < total) {
+                const int row = (int)(e % n), col = (int)(e / n);
+                Bsm[(size_t)row * l + col] = z[t];
+            }
+        }
+    }
+}
+
+// Y (m x l, ldy) = A (m x n) * B, B row-major in shared memory (B[j*l + c]).
+// 64-row tiles of A staged 32 columns at a time; thread -> (row, column group of 4).
+__device__ void gemm_A_B(const float *A, long long lda, int m, int n, const float *Bsm, int l, float *Y, long long ldy,
+                         float *At) {
+    const int tid = threadIdx.x, row = tid & 63, grp = tid >> 6;   // 4 groups
+    constexpr int MAXC = 20;                                         // l <= 4 * 20 = 80
+    for (int r0 = 0; r0 < m; r0 += 64) {
+        float acc[MAXC];
+#pragma unroll
+        for (int u = 0; u < MAXC; u++) acc[u] = 0.f;
+        for (int j0 = 0; j0 < n; j0 += 32) {
+            __syncthreads();
+            for (int e = tid; e < 64 * 32; e += BT) {
+                const int rr = e & 63, jj = e >> 6;
+                At[jj * 64 + rr] = (r0 + rr < m && j0 + jj < n) ? A[(r0 + rr) + (long long)(j0 + jj) * lda] : 0.f;
+            }
+            __syncthreads();
+            const int jn = min(32, n - j0);
+            for (int jj = 0; jj < jn; jj++) {
+                const float a = At[jj * 64 + row];
+                const float *b = Bsm + (size_t)(j0 + jj) * l;
+#pragma unroll
+                for (int u = 0; u < MAXC; u++) {
+                    const int c = grp + 4 * u;
+                    if (c < l) acc[u] = fmaf(a, b[c], acc[u]);
+                }
+            }
+        }
+        if (r0 + row < m) {
+#pragma unroll
+            for (int u = 0; u < MAXC; u++) {
+                const int c = grp + 4 * u;
+                if (c < l) Y[(r0 + row) + (long long)c * ldy] = acc[u];
+            }
+        }
+    }
+    __syncthreads();
+}
+
+// Z (n x l, ldz) = A^T (n x m) * Q (m x l, ldq, global).  32-column tiles of A; Q rows staged.
+__device__ void gemm_At_Q(const float *A, long long lda, int m, int n, const float *Q, long long ldq, int l, float *Z,
+                          long long ldz, float *At, float *Qs) {
+    const int tid = threadIdx.x, col = tid & 31, grp = tid >> 5;    // 8 groups
+    constexpr int MAXC = 10;                                          // l <= 8 * 10 = 80
+    for (int j0 = 0; j0 < n; j0 += 32) {
+        float acc[MAXC];
+#pragma unroll
+        for (int u = 0; u < MAXC; u++) acc[u] = 0.f;
+        for (int i0 = 0; i0 < m; i0 += 32) {
+            __syncthreads();
+            for (int e = tid; e < 32 * 32; e += BT) {
+                const int ii = e & 31, jj = e >> 5;
+                At[jj * 33 + ii] = (i0 + ii < m && j0 + jj < n) ? A[(i0 + ii) + (long long)(j0 + jj) * lda] : 0.f;
+            }
+            for (int e = tid; e < 32 * l; e += BT) {
+                const int ii = e % 32, c = e / 32;
+                Qs[ii * l + c] = (i0 + ii < m) ? Q[(i0 + ii) + (long long)c * ldq] : 0.f;
+            }
+            __syncthreads();
+            for (int ii = 0; ii < 32; ii++) {
+                const float a = At[col * 33 + ii];
+                const float *qr = Qs + ii * l;
+#pragma unroll
+                for (int u = 0; u < MAXC; u++) {
+                    const int c = grp + 8 * u;
+                    if (c < l) acc[u] = fmaf(a, qr[c], acc[u]);
+                }
+            }
+        }
+        if (j0 + col < n) {
+#pragma unroll
+            for (int u = 0; u < MAXC; u++) {
+                const int c = grp + 8 * u;
+                if (c < l) Z[(j0 + col) + (long long)c * ldz] = acc[u];
+            }
+        }
+    }
+    __syncthreads();
+}
+
+// G (l x l, shared, ldg = l) = Y^T Y for Y (rows x l) in global; 32-row chunks staged.
+__device__ void gram_cta(const float *Y, long long ldy, int rows, int l, float *G, float *Ys) {
+    const int tid = threadIdx.x;
+    const int npairs = l * (l + 1) / 2;
+    constexpr int MAXP = 12;                                          // npairs <= 256 * 12
+    float acc[MAXP];
+    int pa[MAXP], pb[MAXP];
+#pragma unroll
+    for (int u = 0; u < MAXP; u++) {
+        acc[u] = 0.f;
+        const int e = tid + BT * u;
+        int b = 0;
+        if (e < npairs) {
+            while ((b + 1) * (b + 2) / 2 <= e) b++;
+        }
+        pb[u] = b;
+        pa[u] = e - b * (b + 1) / 2;
+    }
+    for (int r0 = 0; r0 < rows; r0 += 32) {
+        __syncthreads();
+        for (int e = tid; e < 32 * l; e += BT) {
+            const int rr = e % 32, c = e / 32;
+            Ys[c * 33 + rr] = (r0 + rr < rows) ? Y[(r0 + rr) + (long long)c * ldy] : 0.f;
+        }
+        __syncthreads();
+#pragma unroll
+        for (int u = 0; u < MAXP; u++) {
+            if (tid + BT * u < npairs) {
+                const float *ya = Ys + pa[u] * 33, *yb = Ys + pb[u] * 33;
+                float s = acc[u];
+#pragma unroll 8
+                for (int rr = 0; rr < 32; rr++) s = fmaf(ya[rr], yb[rr], s);
+                acc[u] = s;
+            }
+        }
+    }
+#pragma unroll
+    for (int u = 0; u < MAXP; u++)
+        if (tid + BT * u < npairs) {
+            G[pa[u] + pb[u] * l] = acc[u];
+            G[pb[u] + pa[u] * l] = acc[u];
+        }
+    __syncthreads();
+}
+
+// In-place upper Cholesky of G (l x l, shared); returns false on breakdown (CTA-uniform).
+__device__ bool chol_cta(float *G, int l, int *bad) {
+    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+    if (tid == 0) *bad = 0;
+    __syncthreads();
+    for (int j = 0; j < l; j++) {
+        if (tid == 0) {
+            const float d = G[j + j * l];
+            if (!(d > 0.f) || !isfinite(d)) { *bad = 1; G[j + j * l] = 1.f; }
+            else G[j + j * l] = sqrtf(d);
+        }
+        __syncthreads();
+        const float p = G[j + j * l];
+        for (int k = j + 1 + tid; k < l; k += BT) G[j + k * l] /= p;
+        __syncthreads();
+        for (int k = j + 1 + wid; k < l; k += BT / 32) {
+            const float rjk = G[j + k * l];
+            for (int i = j + 1 + lane; i <= k; i += 32) G[i + k * l] -= G[j + i * l] * rjk;
+        }
+        __syncthreads();
+    }
+    for (int e = tid; e < l * l; e += BT) {
+        const int i = e % l, k = e / l;
+        if (i > k) G[e] = 0.f;
+    }
+    __syncthreads();
+    return *bad == 0;
+}
+
+// X = R^-1 (upper, l x l, shared), one warp per column.
+__device__ void trinv_cta(const float *R, int l, float *X) {
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    for (int e = threadIdx.x; e < l * l; e += BT) X[e] = 0.f;
+    __syncthreads();
+    for (int c = wid; c < l; c += BT / 32) {
+        float b[3];   // rows lane, lane+32, lane+64 (l <= 96)
+#pragma unroll
+        for (int t = 0; t < 3; t++) b[t] = (lane + 32 * t == c) ? 1.f : 0.f;
+        for (int j = c; j >= 0; j--) {
+            const int slot = j >> 5, owner = j & 31;
+            float bj = (slot == 0) ? b[0] : (slot == 1 ? b[1] : b[2]);
+            bj = __shfl_sync(0xffffffffu, bj, owner);
+            const float xj = bj / R[j + j * l];
+            if (lane == 0) X[j + c * l] = xj;
+#pragma unroll
+            for (int t = 0; t < 3; t++) {
+                const int r = lane + 32 * t;
+                if (r < j) b[t] -= xj * R[r + j * l];
+            }
+        }
+    }
+    __syncthreads();
+}
+
+// Y (rows x l, global) <- Y * X (X upper l x l in shared); one thread per row, in place.
+__device__ void apply_upper_cta(float *Y, long long ldy, int rows, int l, const float *X) {
+    constexpr int MAXL = 80;
+    for (int r = threadIdx.x; r < rows; r += BT) {
+        float y[MAXL];
+#pragma unroll
+        for (int c = 0; c < MAXL; c++) y[c] = (c < l) ? Y[r + (long long)c * ldy] : 0.f;
+        for (int c = l - 1; c >= 0; c--) {
+            float s = 0.f;
+#pragma unroll
+            for (int t = 0; t < MAXL; t++)
+                if (t <= c) s = fmaf(y[t], X[t + c * l], s);
+            Y[r + (long long)c * ldy] = s;
+        }
+    }
+    __syncthreads();
+}
+
+// CholeskyQR (passes 1 or 2) of Y (rows x l, global) in place; R (shared l x l) = R2 R1.
+// A pass whose Cholesky breaks down (Y too ill-conditioned for an FP32 Gram) is redone as
+// shifted CholeskyQR: the Gram's diagonal is raised by 8 l u trace(G), which keeps it
+// positive definite, and one extra plain pass restores the orthogonality (shifted
+// CholeskyQR3, Fukaya et al. 2020).
+__device__ bool cqr_cta(float *Y, long long ldy, int rows, int l, int passes, float *R, float *G, float *X, float *T,
+                        float *Ys, int *bad) {
+    for (int e = threadIdx.x; e < l * l; e += BT) R[e] = ((e % l) == (e / l)) ? 1.f : 0.f;
+    __syncthreads();
+    __shared__ float trace_sh;
+    int shifted = 0;
+    for (int pass = 0; pass < passes; pass++) {
+        gram_cta(Y, ldy, rows, l, G, Ys);
+        for (int e = threadIdx.x; e < l * l; e += BT) T[e] = G[e];
+        __syncthreads();
+        if (!chol_cta(G, l, bad)) {
+            if (shifted) return false;
+            if (threadIdx.x == 0) {
+                float tr = 0.f;
+                for (int j = 0; j < l; j++) tr += T[j + j * l];
+                trace_sh = tr;
+            }
+            __syncthreads();
+            const float shift = 8.f * (float)l * 1.1920929e-7f * trace_sh;
+            for (int e = threadIdx.x; e < l * l; e += BT) G[e] = T[e] + (((e % l) == (e / l)) ? shift : 0.f);
+            __syncthreads();
+            if (!chol_cta(G, l, bad)) return false;
+            shifted = 1;
+            passes++;
+        }
+        trinv_cta(G, l, X);
+        apply_upper_cta(Y, ldy, rows, l, X);
+        // R <- G R  (both upper)
+        for (int e = threadIdx.x; e < l * l; e += BT) {
+            const int i = e % l, k = e / l;
+            float s = 0.f;
+            for (int t = i; t <= k; t++) s = fmaf(G[i + t * l], R[t + k * l], s);
+            T[e] = (i <= k) ? s : 0.f;
+        }
+        __syncthreads();
+        for (int e = threadIdx.x; e < l * l; e += BT) R[e] = T[e];
+        __syncthreads();
+    }
+    return true;
+}
+
+// One-sided Jacobi on W (l x l, shared), V accumulated; then sort descending.
+__device__ int jacobi_cta(float *W, float *V, int l, float *sv, int *rot) {
+    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+    for (int e = tid; e < l * l; e += BT) V[e] = ((e % l) == (e / l)) ? 1.f : 0.f;
+    const int np = l + (l & 1);
+    const float tol = 4.f * sqrtf((float)l) * 1.1920929e-7f;
+    int sweep = 0;
+    for (; sweep < 40; sweep++) {
+        if (tid == 0) *rot = 0;
+        __syncthreads();
+        for (int r = 0; r < np - 1; r++) {
+            for (int pi = wid; pi < np / 2; pi += BT / 32) {
+                int p, q;
+                const int mm = np - 1;
+                if (pi == 0) { p = 0; q = (r % mm) + 1; }
+                else { p = ((r + pi) % mm) + 1; q = ((r - pi + mm) % mm) + 1; }
+                if (p >= l || q >= l) continue;
+                if (p > q) { const int t = p; p = q; q = t; }
+                float *wp = W + p * l, *wq = W + q * l;
+                float a = 0, b = 0, d = 0;
+                for (int i = lane; i < l; i += 32) {
+                    const float x = wp[i], y = wq[i];
+                    a = fmaf(x, x, a); b = fmaf(y, y, b); d = fmaf(x, y, d);
+                }
+                a = warp_sum(a); b = warp_sum(b); d = warp_sum(d);
+                if (d == 0.f || fabsf(d) <= tol * sqrtf(a * b)) continue;
+                const float zeta = (b - a) / (2.f * d);
+                const float t = copysignf(1.f, zeta) / (fabsf(zeta) + sqrtf(1.f + zeta * zeta));
+                const float cs = rsqrtf(1.f + t * t), sn = cs * t;
+                float *vp = V + p * l, *vq = V + q * l;
+                for (int i = lane; i < l; i += 32) {
+                    const float x = wp[i], y = wq[i];
+                    wp[i] = cs * x - sn * y;
+                    wq[i] = sn * x + cs * y;
+                    const float u = vp[i], v = vq[i];
+                    vp[i] = cs * u - sn * v;
+                    vq[i] = sn * u + cs * v;
+                }
+                if (lane == 0) *rot = 1;
+            }
+            __syncthreads();
+        }
+        const int any = *rot;
+        __syncthreads();
+        if (!any) break;
+    }
+    for (int c = wid; c < l; c += BT / 32) {
+        float s = 0.f;
+        for (int i = lane; i < l; i += 32) s = fmaf(W[i + c * l], W[i + c * l], s);
+        s = warp_sum(s);
+        if (lane == 0) sv[c] = sqrtf(s);
+    }
+    __syncthreads();
+    return sweep;
+}
+
+__global__ void __launch_bounds__(BT, 1)
+    batch_rsvd_kernel(const BatchItem *items, int count, int *queue, float *work, long long slab, long long ldw,
+                      uint64_t seed, int q, int s, int *flag) {
+    extern __shared__ __align__(16) float sm[];
+    __shared__ int item_idx, bad, rot;
+    float *slabp = work + (long long)blockIdx.x * slab;
+    float *Yg = slabp, *Zg = slabp + ldw * 96;   // two tall buffers (<= 96 columns each), ld = ldw
+    for (;;) {
+        if (threadIdx.x == 0) item_idx = atomicAdd(queue, 1);
+        __syncthreads();
+        const int it = item_idx;
+        __syncthreads();
+        if (it >= count) break;
+        const BatchItem B = items[it];
+        const int m = B.m, n = B.n, l = B.l, k = B.k;
+        // shared layout: [Bsm: n*l][At: 64*32]  (phase 1)  /  small l x l work areas (later)
+        float *Bsm = sm, *At = sm + (size_t)n * l;
+        gen_omega(Bsm, n, l, seed, (uint64_t)B.index);
+        __syncthreads();
+        gemm_A_B(B.A, B.lda, m, n, Bsm, l, Yg, ldw, At);
+        // small-matrix areas after the phase-1 region is no longer needed
+        const int L2 = l * l;
+        float *R = sm, *G = R + L2, *X = G + L2, *T = X + L2, *Ys = T + L2, *W = Ys + 33 * 96, *Vs = W + L2;
+        float *sv = Vs + L2, *Qs = sv + 96;
+        bool ok = true;
+        for (int j = 1; j < q && ok; j++) {                            // q-1 power rounds, s=1 schedule
+            if ((2 * j - 2) % s == 0) ok = cqr_cta(Yg, ldw, m, l, 1, R, G, X, T, Ys, &bad);
+            gemm_At_Q(B.A, B.lda, m, n, Yg, ldw, l, Zg, ldw, Qs + 32 * 96, Qs);
+            if ((2 * j - 1) % s == 0 && ok) ok = cqr_cta(Zg, ldw, n, l, 1, R, G, X, T, Ys, &bad);
+            // Y = A Zo : stage Zo row-major in shared memory as the B operand
+            for (int e = threadIdx.x; e < n * l; e += BT) Bsm[(e % n) * l + e / n] = Zg[(e % n) + (long long)(e / n) * ldw];
+            __syncthreads();
+            gemm_A_B(B.A, B.lda, m, n, Bsm, l, Yg, ldw, At);
+        }
+        if (ok) ok = cqr_cta(Yg, ldw, m, l, 2, R, G, X, T, Ys, &bad);                // Q in Yg
+        if (ok) gemm_At_Q(B.A, B.lda, m, n, Yg, ldw, l, Zg, ldw, Qs + 32 * 96, Qs);  // Bt in Zg
+        if (ok) ok = cqr_cta(Zg, ldw, n, l, 2, R, G, X, T, Ys, &bad);                // Qh in Zg, Rh in R
+        if (!ok) {
+            if (threadIdx.x == 0) atomicAdd(flag, 1);
+            continue;
+        }
+        for (int e = threadIdx.x; e < L2; e += BT) W[e] = R[e];
+        __syncthreads();
+        jacobi_cta(W, Vs, l, sv, &rot);
+        // order: rank of each column by descending sv
+        __shared__ int rank_of[96];
+        for (int c = threadIdx.x; c < l; c += BT) {
+            int r = 0;
+            for (int t = 0; t < l; t++) r += (sv[t] > sv[c]) || (sv[t] == sv[c] && t < c);
+            rank_of[c] = r;
+        }
+        __syncthreads();
+        // Rh = Uh S Vh^T with Uh = W / sv, Vh = Vs.  U = Q Vh(:, :k) ; V = Qh Uh(:, :k)
+        // stage the k selected columns (by rank) of Vh and Uh in shared memory (G and X areas)
+        for (int e = threadIdx.x; e < L2; e += BT) {
+            const int i = e % l, c = e / l, r = rank_of[c];
+            if (r < k) {
+                G[i + r * l] = Vs[i + c * l];
+                X[i + r * l] = (sv[c] > 0.f) ? W[i + c * l] / sv[c] : 0.f;
+            }
+        }
+        __syncthreads();
+        for (int c = threadIdx.x; c < l; c += BT)
+            if (rank_of[c] < k) B.S[rank_of[c]] = (double)sv[c];
+        for (long long e = threadIdx.x; e < (long long)m * k; e += BT) {
+            const int i = (int)(e % m), c = (int)(e / m);
+            float acc = 0.f;
+            for (int t = 0; t < l; t++) acc = fmaf(Yg[i + (long long)t * ldw], G[t + c * l], acc);
+            B.U[i + (long long)c * B.ldu] = acc;
+        }
+        for (long long e = threadIdx.x; e < (long long)n * k; e += BT) {
+            const int i = (int)(e % n), c = (int)(e / n);
+            float acc = 0.f;
+            for (int t = 0; t < l; t++) acc = fmaf(Zg[i + (long long)t * ldw], X[t + c * l], acc);
+            B.V[i + (long long)c * B.ldv] = acc;
+        }
+        __syncthreads();
+    }
+}
+
+}  // namespace
+
+// Shared memory and slab sizes for a batch whose largest matrix is (mmax x nmax), l <= lmax.
+size_t batch_smem_bytes(int nmax, int lmax) {
+    const size_t phase1 = (size_t)nmax * lmax + 64 * 32;
+    const size_t L2 = (size_t)lmax * lmax;
+    const size_t small = 4 * L2 + 33 * 96 + 2 * L2 + 96 + 32 * 96 + 32 * 33 + 64;
+    return sizeof(float) * std::max(phase1, small) + 64;
+}
+
+void batch_rsvd_launch(cudaStream_t s, const BatchItem *d_items, int count, int *d_queue, float *d_work, long long slab,
+                       long long ldw, unsigned long long seed, int q, int s_, int *d_flag, int nctas, size_t smem) {
+    auto k = batch_rsvd_kernel;
+    RSVD_CK(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    k<<<nctas, BT, smem, s>>>(d_items, count, d_queue, d_work, slab, ldw, seed, q, s_, d_flag);
+    RSVD_LAUNCH_CK();
+}
+
+}  // namespace rsvd
+
+// ============================================================ plan API (extern "C")
+struct rsvdpack_batch_plan {
+    int count = 0;
+    rsvd::DBuf items, queue, work, flag;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    cudaStream_t stream = nullptr;
+};
+
+extern "C" {
+
+rsvdpack_batch_plan *rsvdpack_batch_plan_create(int count, const int *m, const int *n, const int *k, int p, int q,
+                                                int s, const float *const *dA, const long long *lda,
+                                                float *const *dU, const long long *ldu, double *const *dS,
+                                                float *const *dV, const long long *ldv, unsigned long long seed) {
+    using namespace rsvd;
+    rsvdpack_batch_plan *plan = nullptr;
+    try {
+        rsvdpack_clear_error();
+        if (count <= 0 || !m || !n || !k || !dA || !lda || !dU || !ldu || !dS || !dV || !ldv)
+            fail(RSVD_ERR_ARGUMENT, "null or empty batch description");
+        if (p < 0 || (q >= 2 && s < 1)) fail(RSVD_ERR_ARGUMENT, "need p >= 0 and s >= 1");
+        Ctx &cx = ctx();
+        std::vector<BatchItem> items((size_t)count);
+        int mmax = 1, nmax = 1, lmax = 1;
+        for (int i = 0; i < count; i++) {
+            const int l = k[i] + p;
+            if (m[i] <= 0 || n[i] <= 0 || k[i] < 1 || l > std::min(m[i], n[i]))
+                fail(RSVD_ERR_ARGUMENT, "batch item " + std::to_string(i) + ": need 1 <= k, k + p <= min(m, n)");
+            if (l > 72) fail(RSVD_ERR_ARGUMENT, "batch item " + std::to_string(i) + ": k + p above 72");
+            if (lda[i] < m[i] || ldu[i] < m[i] || ldv[i] < n[i]) fail(RSVD_ERR_ARGUMENT, "bad leading dimension");
+            items[(size_t)i] = BatchItem{dA[i], lda[i], dU[i], ldu[i], dS[i], dV[i], ldv[i], m[i], n[i], k[i], l, i, 0};
+            mmax = std::max(mmax, m[i]);
+            nmax = std::max(nmax, n[i]);
+            lmax = std::max(lmax, l);
+        }
+        const size_t smem = batch_smem_bytes(nmax, lmax);
+        if (smem > 220 * 1024) fail(RSVD_ERR_ARGUMENT, "batch: n * (k + p) too large for shared memory (n <= 760 at k+p = 72)");
+        // largest problems first: the queue hands them out early, small ones fill the tail
+        std::stable_sort(items.begin(), items.end(), [](const BatchItem &a, const BatchItem &b) {
+            return (long long)a.m * a.n * a.l > (long long)b.m * b.n * b.l;
+        });
+        plan = new rsvdpack_batch_plan();
+        plan->count = count;
+        plan->stream = cx.stream;
+        cudaStream_t st = cx.stream;
+        plan->items = DBuf(sizeof(BatchItem) * (size_t)count, st);
+        RSVD_CK(cudaMemcpyAsync(plan->items.get(), items.data(), sizeof(BatchItem) * (size_t)count,
+                                cudaMemcpyHostToDevice, st));
+        const int nctas = std::max(1, std::min(cx.sms, count));
+        const long long ldw = pad_ld(std::max(mmax, nmax));
+        const long long slab = 2 * ldw * 96;
+        plan->work = DBuf(sizeof(float) * (size_t)slab * nctas, st);
+        plan->queue = DBuf(sizeof(int), st);
+        plan->flag = DBuf(sizeof(int), st);
+        RSVD_CK(cudaStreamSynchronize(st));
+        // one persistent launch (plus the two counter resets) captured in a CUDA graph
+        RSVD_CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+        cudaMemsetAsync(plan->queue.get(), 0, sizeof(int), st);
+        cudaMemsetAsync(plan->flag.get(), 0, sizeof(int), st);
+        batch_rsvd_launch(st, (const BatchItem *)plan->items.get(), count, (int *)plan->queue.get(),
+                          (float *)plan->work.get(), slab, ldw, seed, q, s, (int *)plan->flag.get(), nctas, smem);
+        RSVD_CK(cudaStreamEndCapture(st, &plan->graph));
+        RSVD_CK(cudaGraphInstantiate(&plan->exec, plan->graph, 0));
+        return plan;
+    } catch (const Error &e) {
+        set_error(e.code, std::string("rsvdpack_batch_plan_create: ") + e.what());
+        if (plan) {
+            cudaStreamEndCapture(plan->stream, &plan->graph);
+            delete plan;
+        }
+        return nullptr;
+    }
+}
+
+int rsvdpack_batch_plan_execute(rsvdpack_batch_plan *plan) {
+    using namespace rsvd;
+    try {
+        rsvdpack_clear_error();
+        if (!plan || !plan->exec) fail(RSVD_ERR_ARGUMENT, "null plan");
+        RSVD_CK(cudaGraphLaunch(plan->exec, plan->stream));
+        int bad = 0;
+        RSVD_CK(cudaMemcpyAsync(&bad, plan->flag.get(), sizeof(int), cudaMemcpyDeviceToHost, plan->stream));
+        RSVD_CK(cudaStreamSynchronize(plan->stream));
+        if (bad) fail(RSVD_ERR_NUMERIC, std::to_string(bad) + " batch item(s) broke down in CholeskyQR");
+        return RSVD_OK;
+    } catch (const Error &e) {
+        set_error(e.code, std::string("rsvdpack_batch_plan_execute: ") + e.what());
+        return e.code;
+    }
+}
+
+void rsvdpack_batch_plan_destroy(rsvdpack_batch_plan *plan) {
+    if (!plan) return;
+    if (plan->exec) cudaGraphExecDestroy(plan->exec);
+    if (plan->graph) cudaGraphDestroy(plan->graph);
+    delete plan;
+}
+
+}  // extern "C"
