@@ -32,6 +32,10 @@ sys.path.insert(0, ROOT)
 
 M_ROWS, N_COLS, K, P, Q, S_ORTH, VNUM = 16384, 8192, 256, 16, 2, 1, 1
 METRIC = "rSVD solves/sec at matched FP64-oracle error (16384x8192 FP32, k=256, p=16, q=2)"
+# DRAM bytes (read + write) per tensor-core sketch launch on this workload, mean of the A*X
+# (BF16 A) and A^T*X (TF32) forms, from one ncu capture of this script
+# (profiles/tc_gemm_sketch_16384x8192.txt); None until a capture exists.
+TC_TRAFFIC_PER_LAUNCH = None
 
 
 def parse():
@@ -44,6 +48,7 @@ def parse():
                     choices=["fp64", "fp32", "tf32", "bf16"])
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-plain", action="store_true")
     return ap.parse_args()
 
 
@@ -291,39 +296,66 @@ def run_ours(args):
         ms = float(t.item())
     value = world * 1000.0 / ms
 
-    # ---------------- dominant kernel: the sketch product, timed alone
+    # ---------------- dominant kernel: the sketch product, timed alone.  The engine times
+    # each product with CUDA events on its own stream (rsvdpack_last_timing().sketch_ms).
+    # Mixed modes: the solve's A X products read a BF16 copy of A (made once per solve) and its
+    # A^T X products read the FP32 A through kind::tf32 (TF32 mode) or the BF16 copy (BF16
+    # mode); both forms are timed here on the same resident operands.
     X = torch.randn(l, n, device=dev, dtype=tdt)     # column-major n x l
     Y = torch.empty(l, m, device=dev, dtype=tdt)
     Xt = torch.randn(l, m, device=dev, dtype=tdt)
     Z = torch.empty(l, n, device=dev, dtype=tdt)
-    kern = {}
-    for trans, (x, ldx, y, ldy) in ((0, (X, n, Y, m)), (1, (Xt, m, Z, n))):
+    mixed = args.precision in ("tf32", "bf16")
+    Abf = At.to(torch.bfloat16) if mixed else None
+    forms = {}
+    for name, trans, (x, ldx, y, ldy) in (("A*X", 0, (X, n, Y, m)), ("A^T*X", 1, (Xt, m, Z, n))):
+        if mixed and (trans == 0 or args.precision == "bf16"):
+            a_ptr, a_dt, a_es, kname = Abf.data_ptr(), 2, 2, "bf16 (kind::f16)"
+        else:
+            a_ptr, a_dt, a_es = dA, dt, (8 if dt == 0 else 4)
+            kname = "tf32 (kind::tf32)" if mixed else ("fp64 CUDA-core" if dt == 0 else "fp32 CUDA-core")
+        x_es = 2 if a_dt == 2 else a_es
+        times = []
+        for i in range(7):
+            rc = L.rsvdpack_dev_sketch(a_ptr, a_dt, m, m, n, x.data_ptr(), ldx, l, y.data_ptr(), ldy, trans)
+            if rc:
+                raise RuntimeError(f"sketch failed: {eng.last_error()}")
+            if i >= 2:
+                times.append(eng.last_timing().sketch_ms)
+        ms_k = sum(times) / len(times)
+        xr, yr = (m, n) if trans else (n, m)
+        nbytes = m * n * a_es + xr * l * x_es + yr * l * (8 if dt == 0 else 4)
+        forms[name] = {"ms": ms_k, "operand": kname, "bytes": nbytes, "gbs": nbytes / ms_k / 1e6,
+                       "tflops": 2.0 * m * n * l / ms_k / 1e9}
+    del X, Y, Xt, Z, Abf
+    hbm_peak, tc_peak, peak_kind = measured_peaks()
+    tot_bytes = sum(f["bytes"] for f in forms.values())
+    tot_ms = sum(f["ms"] for f in forms.values())
+    gbs = tot_bytes / tot_ms / 1e6
+    roof = {"bound": "hbm", "achieved": gbs, "peak": hbm_peak, "unit": "GB/s", "frac": gbs / hbm_peak,
+            "traffic": TC_TRAFFIC_PER_LAUNCH if mixed else None, "peak_kind": peak_kind,
+            "kernel": "sketch product " + ("(tcgen05, one A*X and one A^T*X launch)" if mixed else "(CUDA-core GEMM)"),
+            "tflops": 2.0 * m * n * l * len(forms) / tot_ms / 1e9, "tensor_peak_tflops": tc_peak, "forms": forms}
+
+    # ---------------- the plain FP32 GPU form of the same method (CUDA-core GEMMs, no
+    # tensor cores), same matrix and sizes: the comparison point for the mixed modes
+    plain = None
+    if mixed and not args.no_plain:
+        eng.set_precision("fp32")
         for _ in range(2):
-            L.rsvdpack_dev_sketch(dA, dt, m, m, n, x.data_ptr(), ldx, l, y.data_ptr(), ldy, trans)
+            solve()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        reps = 5
+        torch.cuda.synchronize()
         e0.record(stream)
-        for _ in range(reps):
-            L.rsvdpack_dev_sketch(dA, dt, m, m, n, x.data_ptr(), ldx, l, y.data_ptr(), ldy, trans)
+        for _ in range(3):
+            solve()
         e1.record(stream)
         e1.synchronize()
-        kern[trans] = e0.elapsed_time(e1) / reps
-    t_kern = 0.5 * (kern[0] + kern[1]) / 1000.0
-    esize = 8 if dt == 0 else 4
-    bytes_alg = m * n * esize + (n * l + m * l) * esize
-    flops_alg = 2.0 * m * n * l
-    hbm_peak, tc_peak, peak_kind = measured_peaks()
-    gbs = bytes_alg / t_kern / 1e9
-    tfs = flops_alg / t_kern / 1e12
-    if args.precision in ("tf32", "bf16"):
-        roof = {"bound": "hbm", "achieved": gbs, "peak": hbm_peak, "unit": "GB/s", "frac": gbs / hbm_peak,
-                "traffic": None, "peak_kind": peak_kind, "kernel": "sketch product (tcgen05)",
-                "tflops": tfs, "ms_per_launch": {"A*X": kern[0], "A^T*X": kern[1]}}
-    else:
-        roof = {"bound": "hbm", "achieved": gbs, "peak": hbm_peak, "unit": "GB/s", "frac": gbs / hbm_peak,
-                "traffic": None, "peak_kind": peak_kind, "kernel": "sketch product (CUDA-core GEMM)",
-                "tflops": tfs, "ms_per_launch": {"A*X": kern[0], "A^T*X": kern[1]}}
-    del X, Y, Xt, Z
+        ms_plain = e0.elapsed_time(e1) / 3
+        res_plain = residual()
+        eng.set_precision(args.precision)
+        plain = {"precision": "fp32", "value": 1000.0 / ms_plain, "ms_per_step": ms_plain,
+                 "rel_frobenius": res_plain, "speedup_of_value": ms_plain / ms}
 
     # ---------------- end to end through the reference C API, pinned host FP64 A
     e2e = None
@@ -369,7 +401,7 @@ def run_ours(args):
                        "l2": "inputs larger than L2 (A = 512 MiB)", "parallelism": f"replicas x{world}"},
             "residual": {"rel_frobenius": res_mixed, "fp64_same_method": res_fp64,
                          "matched": (res_fp64 is None) or (res_mixed <= (1 + 1e-3) * res_fp64)},
-            "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches, "clocks": clocks,
+            "roofline": roof, "plain_gpu": plain, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches, "clocks": clocks,
             "device": name,
         }
         print(json.dumps(line), flush=True)

@@ -189,7 +189,7 @@ int rsvdpack_device_info(char *name, int name_len, int *cc_major, int *cc_minor)
  * legacy default stream (work on other streams must be complete or ordered by the caller);
  * the call returns after it finishes.
  * Return value: RSVD_OK or an RSVD_ERR_* code (also kept in rsvdpack_last_error()). */
-enum { RSVD_DT_F64 = 0, RSVD_DT_F32 = 1 };
+enum { RSVD_DT_F64 = 0, RSVD_DT_F32 = 1, RSVD_DT_BF16 = 2 /* rsvdpack_dev_sketch only */ };
 
 /* Fixed-rank rSVD with the reference's semantics (as low_rank_svd_rand_decomp_fixed_rank).
  * Outputs: U (m x k, ldu), S (k values, double, reference order), V (n x k, ldv), all
@@ -199,7 +199,10 @@ int rsvdpack_dev_svd_fixed_rank(const void *dA, int dtype, long long lda, int m,
                                 long long ldv);
 
 /* One sketch product with the engine's product kernel for the current precision:
- * trans == 0: Y (m x w) = A X with X (n x w);  trans == 1: Y (n x w) = A^T X with X (m x w). */
+ * trans == 0: Y (m x w) = A X with X (n x w);  trans == 1: Y (n x w) = A^T X with X (m x w).
+ * dtype RSVD_DT_BF16: A is a BF16 matrix (16-byte aligned, lda a multiple of 8), X and Y are
+ * FP32; X is rounded to BF16 and the product is one tensor-core kernel with FP32 accumulation
+ * (the form the mixed-precision solve uses after its once-per-call BF16 copy of A). */
 int rsvdpack_dev_sketch(const void *dA, int dtype, long long lda, int m, int n, const void *dX, long long ldx,
                         int w, void *dY, long long ldy, int trans);
 

@@ -615,18 +615,37 @@ int rsvdpack_dev_sketch(const void *dA, int dtype, long long lda, int m, int n, 
         cudaStream_t st = ctx().stream;
         const i64 xr = trans ? m : n, yr = trans ? n : m;
         need(ldx >= xr && ldy >= yr, "bad leading dimension");
+        // device time of the product itself (events on the engine stream) -> timing.sketch_ms
+        thread_local cudaEvent_t ev[2] = {nullptr, nullptr};
+        for (auto &e : ev)
+            if (!e) RSVD_CK(cudaEventCreate(&e));
         if (dtype == RSVD_DT_F64) {
             DM<double> A{(double *)const_cast<void *>(dA), m, n, lda}, X{(double *)const_cast<void *>(dX), xr, w, ldx};
             DM<double> Y{(double *)dY, yr, w, ldy};
+            RSVD_CK(cudaEventRecord(ev[0], st));
             prod<double>(st, trans != 0, false, 1.0, A, X, 0.0, Y);
         } else if (dtype == RSVD_DT_F32) {
             DM<float> A{(float *)const_cast<void *>(dA), m, n, lda}, X{(float *)const_cast<void *>(dX), xr, w, ldx};
             DM<float> Y{(float *)dY, yr, w, ldy};
+            RSVD_CK(cudaEventRecord(ev[0], st));
             prod<float>(st, trans != 0, false, 1.0f, A, X, 0.0f, Y);
+        } else if (dtype == RSVD_DT_BF16) {
+            // BF16-resident A: one kind::f16 tensor-core product on X rounded to BF16
+            need(((uintptr_t)dA % 16 == 0) && (lda * 2) % 16 == 0, "BF16 A must be 16-byte aligned, lda % 8 == 0");
+            DM<float> X{(float *)const_cast<void *>(dX), xr, w, ldx};
+            DMat<__nv_bfloat16> Xb(xr, w, st, false);
+            convert<float, __nv_bfloat16>(st, X, Xb.v);
+            RSVD_CK(cudaEventRecord(ev[0], st));
+            tc_gemm(st, 1, trans == 0, dA, lda, Xb.v.p, Xb.v.ld, (int)yr, w, (int)xr, 1.0f, (float *)dY, ldy, 0,
+                    nullptr, 0, nullptr, 0);
         } else {
             fail(RSVD_ERR_ARGUMENT, "unknown dtype");
         }
+        RSVD_CK(cudaEventRecord(ev[1], st));
         RSVD_CK(cudaStreamSynchronize(st));
+        float ms = 0.f;
+        RSVD_CK(cudaEventElapsedTime(&ms, ev[0], ev[1]));
+        ctx().timing.sketch_ms = ms;
         release_operand_cache();
         check_device_flags(ctx());
         ctx().timing.kernel_launches = ctx().launches;

@@ -157,21 +157,31 @@ template DMat<double> make_omega<double>(i64, i64);
 template DMat<float> make_omega<float>(i64, i64);
 
 // ------------------------------------------------------------------ orthonormalisation
-// X = Y R^-1 for the upper-triangular Cholesky factor R (FP64 storage): Rinv by warp-per-
-// column back substitution, then one product in the working precision.
+// One CholeskyQR pass: G (in: Y^T Y, out: R) -> Q = Y R^-1.  The factorisation runs in
+// the compute type T (FP32 in the mixed modes, FP64 in the FP64 mode); Q comes from the
+// slab triangular solve (orders <= 288) or from R^-1 and one product.
 template <typename T>
-static void apply_rinv(cudaStream_t s, DM<T> Y, DM<double> R, DM<T> X) {
-    const i64 c = R.r;
-    DMat<double> Ri(c, c, s, false);
-    tri_inv_upper<T>(s, R, Ri.v);
-    if (std::is_same<T, double>::value) {
-        gemm<T>(s, false, false, T(1), Y, *(DM<T> *)&Ri.v, T(0), X);
-    } else {
-        DMat<T> Rt(c, c, s, false);
-        convert<double, T>(s, Ri.v, Rt.v);
-        gemm<T>(s, false, false, T(1), Y, Rt.v, T(0), X);
-        RSVD_CK(cudaStreamSynchronize(s));
-    }
+static bool chol_apply(cudaStream_t s, DM<T> Y, DM<double> G, DM<T> Q, int *flag) {
+    const i64 c = G.r;
+    const i64 nb = (c + 31) / 32;
+    DBuf dinv(sizeof(T) * nb * 32 * 32, s);
+    if (!chol_factor<T>(s, G, chol_tol<T>(), flag, (T *)dinv.get())) return false;
+    if (trsm_right_tiles<T>(s, Y, G, (const T *)dinv.get(), Q)) return true;
+    DMat<T> Ri(c, c, s, false);
+    tri_inv_tiles<T, T>(s, G, (const T *)dinv.get(), Ri.v);
+    gemm<T>(s, false, false, T(1), Y, Ri.v, T(0), Q);
+    return true;
+}
+
+// One FP32 CholeskyQR pass on packed 32 x 32 tiles (orders <= 288): Gram straight into
+// FP32 tiles, one-CTA factorisation, slab triangular solve.  Rout (optional): R in FP64.
+static bool chol_pass_f32(cudaStream_t s, DM<float> Y, DM<float> Q, DM<double> *Rout, int *flag) {
+    const i64 c = Y.c, nb = (c + 31) / 32;
+    DBuf gt(sizeof(float) * (size_t)(nb * (nb + 1) / 2) * 1024, s), dinv(sizeof(float) * (size_t)nb * 1024, s);
+    gram_tiles_f32(s, Y, (float *)gt.get(), nullptr);
+    if (!chol_tiles_f32(s, (float *)gt.get(), (int)c, chol_tol<float>(), flag, (float *)dinv.get(), Rout)) return false;
+    trsm_right_tiles_f32(s, Y, (int)c, (const float *)gt.get(), (const float *)dinv.get(), Q);
+    return true;
 }
 
 // Q = orth(Y) by CholeskyQR (passes = 1: enough for the power-round bases, whose span is
@@ -185,22 +195,43 @@ void orth(DM<T> Y, DM<T> Q, DM<double> *R, int passes) {
     const i64 c = Y.c;
     if (Y.r < c) fail(RSVD_ERR_ARGUMENT, "orth: more columns than rows");
     int *flag = cx.d_flags + FLAG_CHOL_BREAKDOWN;
+    if constexpr (std::is_same<T, float>::value) {
+        if (c <= 288) {
+            if (passes < 2) {
+                if (chol_pass_f32(s, Y, Q, R, flag)) return;
+            } else {
+                DMat<float> W(Y.r, c, s, false);
+                DMat<double> R1(R ? c : 1, R ? c : 1, s, false), R2(R ? c : 1, R ? c : 1, s, false);
+                if (chol_pass_f32(s, Y, W.v, R ? &R1.v : nullptr, flag) &&
+                    chol_pass_f32(s, W.v, Q, R ? &R2.v : nullptr, flag)) {
+                    if (R) tri_mul_upper<float>(s, R2.v, R1.v, *R);   // R = R2 R1
+                    return;
+                }
+            }
+            DMat<float> W(Y.r, c, s, false);
+            copy_dm<float>(s, Y, W.v);
+            DMat<double> Rh(c, c, s, true);
+            householder_qr<float>(s, W.v, Q, Rh.v);
+            if (R) copy_dm<double>(s, Rh.v, *R);
+            return;
+        }
+    }
     DMat<double> G1(c, c, s, false);
     gram<T>(s, Y, G1.v);
-    if (cholesky_small<T>(s, G1.v, chol_tol<T>(), flag)) {
-        if (passes < 2) {
-            apply_rinv<T>(s, Y, G1.v, Q);
+    if (passes < 2) {
+        if (chol_apply<T>(s, Y, G1.v, Q, flag)) {
             if (R) copy_dm<double>(s, G1.v, *R);
             return;
         }
+    } else {
         DMat<T> W(Y.r, c, s, false);
-        apply_rinv<T>(s, Y, G1.v, W.v);
-        DMat<double> G2(c, c, s, false);
-        gram<T>(s, W.v, G2.v);
-        if (cholesky_small<T>(s, G2.v, chol_tol<T>(), flag)) {
-            apply_rinv<T>(s, W.v, G2.v, Q);
-            if (R) gemm<double>(s, false, false, 1.0, G2.v, G1.v, 0.0, *R);   // R = R2 R1
-            return;
+        if (chol_apply<T>(s, Y, G1.v, W.v, flag)) {
+            DMat<double> G2(c, c, s, false);
+            gram<T>(s, W.v, G2.v);
+            if (chol_apply<T>(s, W.v, G2.v, Q, flag)) {
+                if (R) tri_mul_upper<T>(s, G2.v, G1.v, *R);   // R = R2 R1
+                return;
+            }
         }
     }
     // Householder fallback on a copy of Y
@@ -229,11 +260,18 @@ static SvdOut<T> svd_from_q(DM<T> A, DM<T> Q, int k, int vnum) {
     out.U = DMat<T>(m, k, s, false);
     out.V = DMat<T>(n, k, s, false);
     if (vnum == 1 || vnum > 2) {
-        // [Qh, Rh] = qr(Bt); Rh = Uh S Vh^T; U = Q Vh; V = Qh Uh   (RRA:133-174)
+        // [Qh, Rh] = qr(Bt); Rh = Uh S Vh^T; U = Q Vh; V = Qh Uh   (RRA:133-174).
+        // The one-sided Jacobi runs on Rh^T = Vh S Uh^T: the rows of a triangular factor of a
+        // graded matrix are close to orthogonal, so Jacobi on its transpose needs far fewer
+        // sweeps (Drmac & Veselic 2008, "New fast and accurate Jacobi SVD algorithm I").
         DMat<T> Qh(n, l, s, false);
         DMat<double> Rh(l, l, s, true);
         orth<T>(Bt.v, Qh.v, &Rh.v, 2);
-        jacobi_small<T>(s, Rh.v, Uh.v, Vh.v, (double *)svb.get(), cx.d_flags + FLAG_JACOBI_NOCONV);
+        {
+            DMat<double> RhT(l, l, s, false);
+            transpose<double>(s, Rh.v, RhT.v);
+            jacobi_small<T>(s, RhT.v, Vh.v, Uh.v, (double *)svb.get(), cx.d_flags + FLAG_JACOBI_NOCONV);
+        }
         RSVD_CK(cudaMemcpyAsync(sv.data(), svb.get(), sizeof(double) * l, cudaMemcpyDeviceToHost, s));
         std::vector<int> first((size_t)k);
         for (int j = 0; j < k; j++) first[j] = j;

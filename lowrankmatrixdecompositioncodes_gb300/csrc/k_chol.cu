@@ -1,0 +1,781 @@
+// k_chol.cu -- the triangular l x l steps of CholeskyQR / CholeskyQR2 on 32 x 32 tiles:
+//
+//   chol_factor<S>    G = R^T R (upper R), right-looking blocked Cholesky.  Each step
+//                     factors the diagonal tile in one warp and inverts it by back
+//                     substitution, so the panel R_JK = R_JJ^-T G_JK and the trailing update
+//                     G_IK -= R_JI^T R_JK are plain tile products (one warp per tile).
+//                     Orders up to 288 (FP32) / 192 (FP64) run in one CTA with every
+//                     tile resident in shared memory; larger orders run one launch per
+//                     panel and per trailing update over tiles in global memory (L2).
+//   tri_inv_tiles     X = R^-1 from R and the inverted diagonal tiles: one CTA per block
+//                     column, X_IJ = -R_II^-1 sum_{K=I+1..J} R_IK X_KJ from I = J-1 down.
+//   trsm_right_tiles  Q = Y R^-1 for tall Y: one CTA per slab of rows solves Q R = Y by
+//                     block columns, the slab's Q resident in shared memory.
+//   tri_mul_upper     C = A B for upper-triangular A, B (the R2 R1 of CholeskyQR2).
+//
+// Compute type S: float in the mixed-precision modes, double in the FP64 mode; the
+// l x l matrices are stored in FP64 at the interface.  The factorisation follows the
+// semantics of the Householder-based QR it replaces in the reference's range finder
+// (QR_factorization_getQ, matrix_vector_functions_intel_mkl.c:1251-1263): the R factor
+// of Y is the Cholesky factor of Y^T Y.
+#include "rsvd_internal.h"
+#include "k_common.cuh"
+
+#include <algorithm>
+#include <cmath>
+#include <type_traits>
+
+namespace rsvd {
+
+namespace {
+
+constexpr int TB = 32;            // tile order
+constexpr int TP = 36;            // row pitch of a tile in shared memory (16-byte rows)
+constexpr int TE = TB * TP;       // shared-memory elements per tile
+constexpr unsigned FULL = 0xffffffffu;
+
+__host__ __device__ __forceinline__ int tix(int I, int K) { return K * (K + 1) / 2 + I; }   // I <= K
+
+// (I, K) of packed upper tile index t
+__device__ __forceinline__ void untix(int t, int &I, int &K) {
+    int k = (int)((sqrtf(8.0f * (float)t + 1.0f) - 1.0f) * 0.5f);
+    while (k * (k + 1) / 2 > t) k--;
+    while ((k + 1) * (k + 2) / 2 <= t) k++;
+    K = k;
+    I = t - k * (k + 1) / 2;
+}
+
+// Lane -> 4 x 8 block of a 32 x 32 tile: rows r0..r0+3, columns c0..c0+7.
+__device__ __forceinline__ int lane_r0() { return ((threadIdx.x & 31) >> 2) * 4; }
+__device__ __forceinline__ int lane_c0() { return ((threadIdx.x & 31) & 3) * 8; }
+
+template <typename S>
+__device__ __forceinline__ void ld4(const S *p, S (&o)[4]) {
+    if constexpr (sizeof(S) == 4) {
+        const float4 v = *reinterpret_cast<const float4 *>(p);
+        o[0] = v.x; o[1] = v.y; o[2] = v.z; o[3] = v.w;
+    } else {
+        const double2 a = *reinterpret_cast<const double2 *>(p), b = *reinterpret_cast<const double2 *>(p + 2);
+        o[0] = a.x; o[1] = a.y; o[2] = b.x; o[3] = b.y;
+    }
+}
+
+template <typename S>
+__device__ __forceinline__ void zero_acc(S (&acc)[4][8]) {
+#pragma unroll
+    for (int a = 0; a < 4; a++)
+#pragma unroll
+        for (int b = 0; b < 8; b++) acc[a][b] = S(0);
+}
+
+// acc(r, c) += sum_{k0 <= k < k1} P[k][r] Q[k][c]     (P^T Q, row-major tiles of pitch TP)
+template <typename S>
+__device__ __forceinline__ void tile_tn(const S *P, const S *Q, int k0, int k1, S (&acc)[4][8]) {
+    const int r0 = lane_r0(), c0 = lane_c0();
+    for (int k = k0; k < k1; k++) {
+        S p[4], q[8], q2[4];
+        ld4<S>(P + k * TP + r0, p);
+        ld4<S>(Q + k * TP + c0, *reinterpret_cast<S(*)[4]>(q));
+        ld4<S>(Q + k * TP + c0 + 4, q2);
+#pragma unroll
+        for (int b = 0; b < 4; b++) q[4 + b] = q2[b];
+#pragma unroll
+        for (int a = 0; a < 4; a++)
+#pragma unroll
+            for (int b = 0; b < 8; b++) acc[a][b] = fma(p[a], q[b], acc[a][b]);
+    }
+}
+
+// acc(r, c) += sum_{k0 <= k < k1} P[r][k] Q[k][c]     (P Q)
+template <typename S>
+__device__ __forceinline__ void tile_nn(const S *P, const S *Q, int k0, int k1, S (&acc)[4][8]) {
+    const int r0 = lane_r0(), c0 = lane_c0();
+    for (int k = k0; k < k1; k++) {
+        S p[4], q[8], q2[4];
+#pragma unroll
+        for (int a = 0; a < 4; a++) p[a] = P[(r0 + a) * TP + k];
+        ld4<S>(Q + k * TP + c0, *reinterpret_cast<S(*)[4]>(q));
+        ld4<S>(Q + k * TP + c0 + 4, q2);
+#pragma unroll
+        for (int b = 0; b < 4; b++) q[4 + b] = q2[b];
+#pragma unroll
+        for (int a = 0; a < 4; a++)
+#pragma unroll
+            for (int b = 0; b < 8; b++) acc[a][b] = fma(p[a], q[b], acc[a][b]);
+    }
+}
+
+// Factor the upper 32 x 32 tile D (row-major, pitch TP) in place, D = R^T R, and write
+// R^-1 (upper) into Di.  One warp.  diag0: the original diagonal of the whole matrix at
+// this tile (relative breakdown test d_j > rel_tol * diag0_j).  Returns false on breakdown.
+template <typename S>
+__device__ __noinline__ bool factor_diag_warp(S *D, S *Di, const S *diag0, S rel_tol) {
+    const int lane = threadIdx.x & 31;
+    // lane t keeps column t of the tile in registers; row j of R is broadcast by shuffles
+    S c[32];
+#pragma unroll
+    for (int i = 0; i < 32; i++) c[i] = (i <= lane) ? D[i * TP + lane] : S(0);
+    bool bad = false;
+#pragma unroll
+    for (int j = 0; j < 32; j++) {
+        const S d = __shfl_sync(FULL, c[j], j);
+        const bool ok = (d > S(0)) && isfinite(d) && (d > rel_tol * diag0[j]);
+        bad |= !ok;
+        const S p = ok ? sqrt(d) : S(1);
+        const S inv = S(1) / p;
+        if (lane == j) c[j] = p;
+        else if (lane > j) c[j] *= inv;                 // lane t now holds R(j, t)
+#pragma unroll
+        for (int i = j + 1; i < 32; i++) {
+            const S rji = __shfl_sync(FULL, c[j], i);   // R(j, i) from lane i
+            if (lane >= i) c[i] -= rji * c[j];
+        }
+    }
+    __syncwarp();
+#pragma unroll
+    for (int i = 0; i < 32; i++) D[i * TP + lane] = (i <= lane) ? c[i] : S(0);
+    __syncwarp();
+    // column `lane` of R^-1 by back substitution, R read back from the tile (broadcast
+    // reads: every lane reads the same R(i, k)); x[k] = 0 for k > lane
+    S x[32];
+#pragma unroll
+    for (int i = 31; i >= 0; i--) {
+        S acc = S(0);
+#pragma unroll
+        for (int k = i + 1; k < 32; k++) acc = fma(D[i * TP + k], x[k], acc);
+        const S rii = D[i * TP + i];
+        x[i] = (i == lane) ? S(1) / rii : ((i < lane) ? -acc / rii : S(0));
+    }
+#pragma unroll
+    for (int i = 0; i < 32; i++) Di[i * TP + lane] = x[i];
+    __syncwarp();
+    return !bad;
+}
+
+// Store a lane's 4 x 8 block (optionally subtracting from the tile).
+template <typename S>
+__device__ __forceinline__ void put_acc(S *T, const S (&acc)[4][8], bool subtract) {
+    const int r0 = lane_r0(), c0 = lane_c0();
+#pragma unroll
+    for (int a = 0; a < 4; a++)
+#pragma unroll
+        for (int b = 0; b < 8; b++) {
+            S &t = T[(r0 + a) * TP + c0 + b];
+            t = subtract ? t - acc[a][b] : acc[a][b];
+        }
+}
+
+// Load a 32 x 32 tile of a column-major FP64 matrix into a shared-memory tile (one warp).
+// Outside [0, n): identity (so padded diagonal blocks factor trivially).  upper_only:
+// entries below the diagonal of the whole matrix read as 0.
+template <typename S>
+__device__ void load_tile_g(S *T, const double *G, long long ldg, int n, int I, int K, bool upper_only) {
+    const int lane = threadIdx.x & 31;
+    for (int c = 0; c < TB; c++) {
+        const int gi = I * TB + lane, gk = K * TB + c;
+        S v;
+        if (gi < n && gk < n) v = (!upper_only || gi <= gk) ? (S)G[gi + (long long)gk * ldg] : S(0);
+        else v = (gi == gk) ? S(1) : S(0);
+        T[lane * TP + c] = v;
+    }
+}
+
+// The J loop of the one-CTA factorisation over tiles resident in shared memory (T: packed
+// upper tiles, Dw: scratch tile, diag0: original diagonal).  *bad is set on breakdown.
+template <typename S>
+__device__ void chol_steps(S *T, S *Dw, const S *diag0, int nb, double rel_tol, S *dinv, int *bad) {
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    for (int J = 0; J < nb; J++) {
+        if (wid == 0) {
+            const bool ok = factor_diag_warp<S>(T + (size_t)tix(J, J) * TE, Dw, diag0 + J * TB, (S)rel_tol);
+            if (!ok && lane == 0) *bad = 1;
+        }
+        __syncthreads();
+        if (*bad) break;
+        // panel R_JK = R_JJ^-T G_JK (in place; R_JJ^-1 upper: only k <= r contributes)
+        for (int K = J + 1 + wid; K < nb; K += nw) {
+            S *W = T + (size_t)tix(J, K) * TE;
+            S acc[4][8];
+            zero_acc(acc);
+            tile_tn<S>(Dw, W, 0, lane_r0() + 4, acc);
+            __syncwarp();
+            put_acc<S>(W, acc, false);
+        }
+        for (int e = threadIdx.x; e < TB * TB; e += blockDim.x) dinv[(size_t)J * TB * TB + e] = Dw[(e >> 5) * TP + (e & 31)];
+        __syncthreads();
+        // trailing update G_IK -= R_JI^T R_JK, J < I <= K
+        const int nt = nb - J - 1;
+        for (int t = wid; t < nt * (nt + 1) / 2; t += nw) {
+            int Ip, Kp;
+            untix(t, Ip, Kp);
+            const int I = J + 1 + Ip, K = J + 1 + Kp;
+            S acc[4][8];
+            zero_acc(acc);
+            tile_tn<S>(T + (size_t)tix(J, I) * TE, T + (size_t)tix(J, K) * TE, 0, TB, acc);
+            put_acc<S>(T + (size_t)tix(I, K) * TE, acc, true);
+        }
+        __syncthreads();
+    }
+}
+
+// ---------------------------------------------------------------- one CTA, all tiles in smem
+// Shared memory: nb(nb+1)/2 tiles + 1 scratch tile (diagonal inverse) + nb*32 diagonal.
+// Outputs: R in G (upper, zero below), the inverted diagonal tiles in dinv (nb row-major
+// 32 x 32 tiles, compute type).
+template <typename S>
+constexpr int chol_smem_threads() { return 256; }   // the register factorisation needs > 128 per thread
+
+template <typename S>
+__global__ void __launch_bounds__(chol_smem_threads<S>()) chol_smem_kernel(double *G, long long ldg, int n, int nb, double rel_tol,
+                                                        S *dinv, int *flag) {
+    extern __shared__ __align__(16) unsigned char shraw[];
+    S *T = (S *)shraw;
+    const int ntile = tix(0, nb);
+    S *Dw = T + (size_t)ntile * TE;
+    S *diag0 = Dw + TE;
+    __shared__ int bad;
+    const int wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    for (int t = wid; t < ntile; t += nw) {
+        int I, K;
+        untix(t, I, K);
+        load_tile_g<S>(T + (size_t)t * TE, G, ldg, n, I, K, true);
+    }
+    for (int j = threadIdx.x; j < nb * TB; j += blockDim.x) diag0[j] = (j < n) ? (S)G[j + (long long)j * ldg] : S(1);
+    if (threadIdx.x == 0) bad = 0;
+    __syncthreads();
+    chol_steps<S>(T, Dw, diag0, nb, rel_tol, dinv, &bad);
+    if (bad) {
+        if (threadIdx.x == 0) atomicExch(flag, 1);
+        return;
+    }
+    // R -> G (column-major, zero below the diagonal)
+    for (long long e = threadIdx.x; e < (long long)n * n; e += blockDim.x) {
+        const int k = (int)(e / n), i = (int)(e - (long long)k * n);
+        double v = 0.0;
+        if (i <= k) v = (double)T[(size_t)tix(i >> 5, k >> 5) * TE + (i & 31) * TP + (k & 31)];
+        G[i + (long long)k * ldg] = v;
+    }
+}
+
+// ---------------------------------------------------------------- FP32, packed tiles in/out
+// Gt: the Gram as FP32 packed upper tiles (32 x 32 row-major, pitch 32, padded with the
+// identity; written by gram_tiles_f32).  All tiles come into shared memory by 16-byte
+// asynchronous copies; on return Gt holds R in the same layout (zero below the diagonal
+// of the diagonal tiles).  Rout (optional): R as FP64, column-major, zero below.
+__device__ __forceinline__ void cp_async16(void *smem, const void *gmem) {
+    const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(sa), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() {
+    asm volatile("cp.async.commit_group;\n" ::: "memory");
+    asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+}
+
+__global__ void __launch_bounds__(256) chol_tiles_f32_kernel(float *Gt, int n, int nb, double rel_tol, float *dinv,
+                                                             double *Rout, long long ldr, int *flag) {
+    extern __shared__ __align__(16) unsigned char shraw[];
+    float *T = (float *)shraw;
+    const int ntile = tix(0, nb);
+    float *Dw = T + (size_t)ntile * TE;
+    float *diag0 = Dw + TE;
+    __shared__ int bad;
+    const int nchunk = ntile * TB * 8;                     // 16-byte chunks: 8 per tile row
+    for (int e = threadIdx.x; e < nchunk; e += blockDim.x) {
+        const int t = e >> 8, r = (e >> 3) & 31, q = e & 7;
+        cp_async16(T + (size_t)t * TE + r * TP + q * 4, Gt + (size_t)t * TB * TB + r * TB + q * 4);
+    }
+    cp_async_wait_all();
+    if (threadIdx.x == 0) bad = 0;
+    __syncthreads();
+    for (int j = threadIdx.x; j < nb * TB; j += blockDim.x) {
+        const int J = j >> 5, jj = j & 31;
+        diag0[j] = T[(size_t)tix(J, J) * TE + jj * TP + jj];
+    }
+    __syncthreads();
+    chol_steps<float>(T, Dw, diag0, nb, rel_tol, dinv, &bad);
+    if (bad) {
+        if (threadIdx.x == 0) atomicExch(flag, 1);
+        return;
+    }
+    // R tiles back to Gt (16-byte stores)
+    for (int e = threadIdx.x; e < nchunk; e += blockDim.x) {
+        const int t = e >> 8, r = (e >> 3) & 31, q = e & 7;
+        *reinterpret_cast<float4 *>(Gt + (size_t)t * TB * TB + r * TB + q * 4) =
+            *reinterpret_cast<const float4 *>(T + (size_t)t * TE + r * TP + q * 4);
+    }
+    if (Rout) {
+        // column k by one warp, rows by lanes (coalesced)
+        const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+        for (int k = wid; k < n; k += nw)
+            for (int i = lane; i < n; i += 32)
+                Rout[i + (long long)k * ldr] =
+                    (i <= k) ? (double)T[(size_t)tix(i >> 5, k >> 5) * TE + (i & 31) * TP + (k & 31)] : 0.0;
+    }
+}
+
+// ---------------------------------------------------------------- tiles in global memory
+// Working storage: packed upper tiles, each 32 x 32 row-major (pitch 32), compute type.
+template <typename S>
+__global__ void chol_gload_kernel(const double *G, long long ldg, int n, int nb, S *Wt, S *diag0) {
+    const long long tot = (long long)tix(0, nb) * TB * TB;
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < tot; e += (long long)gridDim.x * blockDim.x) {
+        const int t = (int)(e >> 10), w = (int)(e & 1023), r = w >> 5, c = w & 31;
+        int I, K;
+        untix(t, I, K);
+        const int gi = I * TB + r, gk = K * TB + c;
+        S v;
+        if (gi < n && gk < n) v = (gi <= gk) ? (S)G[gi + (long long)gk * ldg] : S(0);
+        else v = (gi == gk) ? S(1) : S(0);
+        Wt[e] = v;
+        if (I == K && r == c) diag0[gi] = (gi < n) ? (S)G[gi + (long long)gi * ldg] : S(1);
+    }
+}
+
+template <typename S>
+__device__ __forceinline__ void gtile_to_smem(S *T, const S *g) {
+    const int lane = threadIdx.x & 31;
+    for (int r = 0; r < TB; r++) T[r * TP + lane] = g[r * TB + lane];
+}
+template <typename S>
+__device__ __forceinline__ void acc_to_gtile(S *g, const S (&acc)[4][8], bool subtract) {
+    const int r0 = lane_r0(), c0 = lane_c0();
+#pragma unroll
+    for (int a = 0; a < 4; a++)
+#pragma unroll
+        for (int b = 0; b < 8; b++) {
+            S &t = g[(r0 + a) * TB + c0 + b];
+            t = subtract ? t - acc[a][b] : acc[a][b];
+        }
+}
+
+// Step J, panel: CTA b (one warp) factors the diagonal tile itself (all CTAs agree) and
+// forms R_JK, K = J + b.  CTA 0 writes R_JJ to Rd (not over the tile the other CTAs are
+// reading) and its inverse to dinv.
+template <typename S>
+__global__ void __launch_bounds__(32) chol_gpanel_kernel(S *Wt, int nb, int J, const S *diag0, double rel_tol,
+                                                         S *dinv, S *Rd, int *flag) {
+    __shared__ __align__(16) S D[TE], Di[TE], W[TE];
+    const int K = J + blockIdx.x;
+    gtile_to_smem<S>(D, Wt + (size_t)tix(J, J) * TB * TB);
+    __syncwarp();
+    const bool ok = factor_diag_warp<S>(D, Di, diag0 + J * TB, (S)rel_tol);
+    if (!ok) {
+        if (blockIdx.x == 0 && threadIdx.x == 0) atomicExch(flag, 1);
+        return;
+    }
+    const int lane = threadIdx.x;
+    if (K == J) {
+        for (int r = 0; r < TB; r++) {
+            Rd[(size_t)J * TB * TB + r * TB + lane] = D[r * TP + lane];
+            dinv[(size_t)J * TB * TB + r * TB + lane] = Di[r * TP + lane];
+        }
+        return;
+    }
+    S *g = Wt + (size_t)tix(J, K) * TB * TB;
+    gtile_to_smem<S>(W, g);
+    __syncwarp();
+    S acc[4][8];
+    zero_acc(acc);
+    tile_tn<S>(Di, W, 0, lane_r0() + 4, acc);
+    acc_to_gtile<S>(g, acc, false);
+}
+
+// Step J, trailing update: CTA t (one warp) updates tile (I, K), J < I <= K.
+template <typename S>
+__global__ void __launch_bounds__(32) chol_gupdate_kernel(S *Wt, int nb, int J) {
+    __shared__ __align__(16) S P[TE], Q[TE];
+    int Ip, Kp;
+    untix(blockIdx.x, Ip, Kp);
+    const int I = J + 1 + Ip, K = J + 1 + Kp;
+    gtile_to_smem<S>(P, Wt + (size_t)tix(J, I) * TB * TB);
+    gtile_to_smem<S>(Q, Wt + (size_t)tix(J, K) * TB * TB);
+    __syncwarp();
+    S acc[4][8];
+    zero_acc(acc);
+    tile_tn<S>(P, Q, 0, TB, acc);
+    acc_to_gtile<S>(Wt + (size_t)tix(I, K) * TB * TB, acc, true);
+}
+
+template <typename S>
+__global__ void chol_gstore_kernel(const S *Wt, const S *Rd, int n, double *G, long long ldg) {
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < (long long)n * n;
+         e += (long long)gridDim.x * blockDim.x) {
+        const int k = (int)(e / n), i = (int)(e - (long long)k * n);
+        double v = 0.0;
+        const int I = i >> 5, K = k >> 5;
+        if (i <= k) v = (double)((I == K) ? Rd[(size_t)I * TB * TB + (i & 31) * TB + (k & 31)]
+                                          : Wt[(size_t)tix(I, K) * TB * TB + (i & 31) * TB + (k & 31)]);
+        G[i + (long long)k * ldg] = v;
+    }
+}
+
+// ---------------------------------------------------------------- triangular inverse
+// CTA J computes block column J of X = R^-1 (R: FP64, column-major, upper).  Warps split
+// the K-sum of each row block I, accumulate into a shared tile, and warp 0 applies
+// -R_II^-1.  X_KJ for K > I are read back from X (written earlier by this CTA).
+template <typename S, typename To>
+__global__ void __launch_bounds__(512) tri_inv_tiles_kernel(const double *R, long long ldr, int n, int nb,
+                                                            const S *dinv, To *X, long long ldx) {
+    extern __shared__ __align__(16) unsigned char shraw[];
+    const int J = blockIdx.x;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    S *Acc = (S *)shraw;                  // the K-sum
+    S *Dt = Acc + TE;                     // R_II^-1
+    S *Pw = Dt + TE + (size_t)wid * 2 * TE, *Qw = Pw + TE;   // per-warp R_IK, X_KJ
+    const int jw = min(TB, n - J * TB);
+    // X_JJ = R_JJ^-1; below the diagonal of the block column: zero
+    for (int e = threadIdx.x; e < TB * TB; e += blockDim.x) {
+        const int r = e & 31, c = e >> 5;
+        const int gi = J * TB + r, gk = J * TB + c;
+        if (gi < n && gk < n) X[gi + (long long)gk * ldx] = (To)((r <= c) ? dinv[(size_t)J * TB * TB + r * TB + c] : S(0));
+    }
+    for (long long e = threadIdx.x; e < (long long)jw * n; e += blockDim.x) {
+        const int c = (int)(e / n), gi = (int)(e - (long long)c * n);
+        if (gi >= (J + 1) * TB) X[gi + (long long)(J * TB + c) * ldx] = (To)0;
+    }
+    for (int e = threadIdx.x; e < TE; e += blockDim.x) Acc[e] = S(0);
+    __syncthreads();
+    for (int I = J - 1; I >= 0; I--) {
+        // partial sums over K = I+1 .. J, one tile product per warp at a time
+        S acc[4][8];
+        zero_acc(acc);
+        bool any = false;
+        for (int K = I + 1 + wid; K <= J; K += nw) {
+            any = true;
+            for (int c = 0; c < TB; c++) {
+                const int gi = I * TB + lane, gk = K * TB + c;                 // R_IK (row lane, col c)
+                Pw[lane * TP + c] = (gi < n && gk < n) ? (S)R[gi + (long long)gk * ldr] : S(0);
+                const int xi = K * TB + lane, xk = J * TB + c;                 // X_KJ
+                Qw[lane * TP + c] = (xi < n && xk < n) ? (S)X[xi + (long long)xk * ldx] : S(0);
+            }
+            __syncwarp();
+            tile_nn<S>(Pw, Qw, 0, TB, acc);
+            __syncwarp();
+        }
+        if (any) {
+            const int r0 = lane_r0(), c0 = lane_c0();
+#pragma unroll
+            for (int a = 0; a < 4; a++)
+#pragma unroll
+                for (int b = 0; b < 8; b++) atomicAdd(&Acc[(r0 + a) * TP + c0 + b], acc[a][b]);
+        }
+        for (int e = threadIdx.x; e < TB * TB; e += blockDim.x) Dt[(e >> 5) * TP + (e & 31)] = dinv[(size_t)I * TB * TB + e];
+        __syncthreads();
+        if (wid == 0) {
+            S o[4][8];
+            zero_acc(o);
+            tile_nn<S>(Dt, Acc, 0, TB, o);
+            const int r0 = lane_r0(), c0 = lane_c0();
+#pragma unroll
+            for (int a = 0; a < 4; a++)
+#pragma unroll
+                for (int b = 0; b < 8; b++) {
+                    const int gi = I * TB + r0 + a, gk = J * TB + c0 + b;
+                    if (gi < n && gk < n) X[gi + (long long)gk * ldx] = (To)(-o[a][b]);
+                }
+        }
+        __syncthreads();
+        for (int e = threadIdx.x; e < TE; e += blockDim.x) Acc[e] = S(0);
+        __syncthreads();
+    }
+}
+
+// ---------------------------------------------------------------- C = A B, A and B upper
+// CTA t: tile (I, K) of C (upper tiles first, then the strictly lower tiles, which are
+// zeroed).  256 threads stage A_IL and B_LK; warp 0 accumulates the products.
+template <typename S>
+__global__ void __launch_bounds__(256) tri_mul_upper_kernel(const double *A, long long lda, const double *B,
+                                                            long long ldb, double *C, long long ldc, int n, int nb) {
+    __shared__ __align__(16) S P[TE], Q[TE];
+    const int t = blockIdx.x;
+    const int ntile = tix(0, nb);
+    int I, K;
+    if (t >= ntile) {
+        int Kp, Ip;
+        untix(t - ntile, Kp, Ip);                      // Kp <= Ip
+        I = Ip + 1;
+        K = Kp;
+        for (int e = threadIdx.x; e < TB * TB; e += blockDim.x) {
+            const int gi = I * TB + (e & 31), gk = K * TB + (e >> 5);
+            if (gi < n && gk < n) C[gi + (long long)gk * ldc] = 0.0;
+        }
+        return;
+    }
+    untix(t, I, K);
+    S acc[4][8];
+    zero_acc(acc);
+    for (int L = I; L <= K; L++) {
+        for (int e = threadIdx.x; e < TB * TB; e += blockDim.x) {
+            const int r = e & 31, c = e >> 5;
+            const int gi = I * TB + r, gl = L * TB + c;
+            P[r * TP + c] = (gi < n && gl < n && gi <= gl) ? (S)A[gi + (long long)gl * lda] : S(0);
+            const int bi = L * TB + r, bk = K * TB + c;
+            Q[r * TP + c] = (bi < n && bk < n && bi <= bk) ? (S)B[bi + (long long)bk * ldb] : S(0);
+        }
+        __syncthreads();
+        if (threadIdx.x < 32) tile_nn<S>(P, Q, 0, TB, acc);
+        __syncthreads();
+    }
+    if (threadIdx.x < 32) {
+        const int r0 = lane_r0(), c0 = lane_c0();
+#pragma unroll
+        for (int a = 0; a < 4; a++)
+#pragma unroll
+            for (int b = 0; b < 8; b++) {
+                const int gi = I * TB + r0 + a, gk = K * TB + c0 + b;
+                if (gi < n && gk < n) C[gi + (long long)gk * ldc] = (gi <= gk) ? (double)acc[a][b] : 0.0;
+            }
+    }
+}
+
+// ---------------------------------------------------------------- Q = Y R^-1 by slabs
+// One CTA per slab of BM rows of Y (m x n): block column J of Q is
+//   Q_J = (Y_J - Q_{:, 0:J} R_{0:J, J}) R_JJ^-1,
+// with the slab's finished columns of Q kept in shared memory (column-major, pitch BM + 4,
+// so a thread's RPT rows are one 16-byte load) and R's block column J staged per step
+// (R_JJ^-1 from the factorisation's inverted diagonal tiles).  Thread t: rows
+// (t / 8) * RPT .. + RPT - 1 of the slab, columns (t % 8) * 4 .. + 3 of the block.
+constexpr int TRSM_THREADS = 256;
+// R comes either as FP64 column-major (R, ldr) or, when Rt is given, as packed upper
+// tiles in the compute type (the layout chol_tiles_f32_kernel leaves), staged by 16-byte
+// asynchronous copies.
+template <typename T, typename S, int BM>
+__global__ void __launch_bounds__(TRSM_THREADS) trsm_slab_kernel(const T *Y, long long ldy, const double *R,
+                                                                 long long ldr, const S *Rt, const S *dinv, T *Q,
+                                                                 long long ldq, long long m, int n, int nb) {
+    constexpr int RPT = BM / 32;
+    static_assert(RPT == 4, "one 16-byte row group per thread");
+    constexpr int BP = BM + 4;                        // column pitch of the slab
+    extern __shared__ __align__(16) unsigned char shraw[];
+    S *Qs = (S *)shraw;                               // (nb * 32) columns x BP
+    S *Rc = Qs + (size_t)nb * TB * BP;                // (nb * 32) x TP: block column J of R
+    S *Dv = Rc + (size_t)nb * TB * TP;                // 32 x TP: R_JJ^-1
+    const long long row0 = (long long)blockIdx.x * BM;
+    const int t = threadIdx.x;
+    const int rg = (t >> 3) * RPT, cg = (t & 7) * 4;
+    for (int J = 0; J < nb; J++) {
+        const int kr = J * TB;                        // rows of R above the diagonal tile
+        if constexpr (sizeof(S) == 4) {
+            if (Rt) {
+                constexpr int CPR = TB * sizeof(S) / 16;      // 16-byte chunks per tile row
+                for (int e = t; e < kr * CPR; e += TRSM_THREADS) {
+                    const int I = e / (TB * CPR), r = (e / CPR) % TB, q = e % CPR;
+                    cp_async16(Rc + (I * TB + r) * TP + q * 4, Rt + (size_t)tix(I, J) * TB * TB + r * TB + q * 4);
+                }
+                for (int e = t; e < TB * CPR; e += TRSM_THREADS) {
+                    const int r = e / CPR, q = e % CPR;
+                    cp_async16(Dv + r * TP + q * 4, dinv + (size_t)J * TB * TB + r * TB + q * 4);
+                }
+                cp_async_wait_all();
+            }
+        }
+        if (!Rt) {
+            for (int e = t; e < kr * TB; e += TRSM_THREADS) {
+                const int k = e % kr, c = e / kr;
+                const int gc = kr + c;
+                Rc[k * TP + c] = (gc < n) ? (S)R[k + (long long)gc * ldr] : S(0);
+            }
+            for (int e = t; e < TB * TB; e += TRSM_THREADS) Dv[(e >> 5) * TP + (e & 31)] = dinv[(size_t)J * TB * TB + e];
+        }
+        S acc[RPT][4];
+#pragma unroll
+        for (int a = 0; a < RPT; a++)
+#pragma unroll
+            for (int b = 0; b < 4; b++) {
+                const long long gr = row0 + rg + a;
+                const int gc = kr + cg + b;
+                acc[a][b] = (gr < m && gc < n) ? (S)Y[gr + (long long)gc * ldy] : S(0);
+            }
+        __syncthreads();
+        for (int k = 0; k < kr; k++) {
+            S r4[4], q[RPT];
+            ld4<S>(Rc + k * TP + cg, r4);
+            ld4<S>(Qs + (size_t)k * BP + rg, q);
+#pragma unroll
+            for (int a = 0; a < RPT; a++)
+#pragma unroll
+                for (int b = 0; b < 4; b++) acc[a][b] = fma(-q[a], r4[b], acc[a][b]);
+        }
+        // the diagonal block: Q_J = T R_JJ^-1 (T staged through the slab's column block J)
+#pragma unroll
+        for (int a = 0; a < RPT; a++)
+#pragma unroll
+            for (int b = 0; b < 4; b++) Qs[(size_t)(kr + cg + b) * BP + rg + a] = acc[a][b];
+        __syncthreads();
+        S o[RPT][4];
+#pragma unroll
+        for (int a = 0; a < RPT; a++)
+#pragma unroll
+            for (int b = 0; b < 4; b++) o[a][b] = S(0);
+#pragma unroll 4
+        for (int k = 0; k < TB; k++) {
+            S d4[4], q[RPT];
+            ld4<S>(Dv + k * TP + cg, d4);
+            ld4<S>(Qs + (size_t)(kr + k) * BP + rg, q);
+#pragma unroll
+            for (int a = 0; a < RPT; a++)
+#pragma unroll
+                for (int b = 0; b < 4; b++) o[a][b] = fma(q[a], d4[b], o[a][b]);
+        }
+        __syncthreads();
+#pragma unroll
+        for (int a = 0; a < RPT; a++)
+#pragma unroll
+            for (int b = 0; b < 4; b++) {
+                Qs[(size_t)(kr + cg + b) * BP + rg + a] = o[a][b];
+                const long long gr = row0 + rg + a;
+                const int gc = kr + cg + b;
+                if (gr < m && gc < n) Q[gr + (long long)gc * ldq] = (T)o[a][b];
+            }
+        __syncthreads();
+    }
+}
+
+template <typename S>
+constexpr int smem_nb_max() { return sizeof(S) == 4 ? 9 : 6; }
+
+template <typename T>
+constexpr int trsm_bm() { return 128; }
+
+template <typename T>
+size_t trsm_smem(int nb) {
+    using S = T;
+    return sizeof(S) * ((size_t)nb * TB * (trsm_bm<T>() + 4) + (size_t)nb * TB * TP + (size_t)TE);
+}
+
+}  // namespace
+
+// G (n x n, FP64, symmetric positive definite; upper triangle read) -> R (upper, zero
+// below).  When dinv is given (nb = ceil(n/32) tiles of 32 x 32, compute type), it
+// receives the inverses of the diagonal tiles of R.  Returns false on breakdown
+// (a pivot d_j <= rel_tol * G_jj, or not finite); d_flag is left set then.
+template <typename S>
+bool chol_factor(cudaStream_t s, DM<double> G, double rel_tol, int *d_flag, S *dinv) {
+    const int n = (int)G.r;
+    if (G.r != G.c) fail(RSVD_ERR_ARGUMENT, "cholesky: not square");
+    if (n == 0) return true;
+    const int nb = (n + TB - 1) / TB;
+    RSVD_CK(cudaMemsetAsync(d_flag, 0, sizeof(int), s));
+    DBuf own(dinv ? 16 : sizeof(S) * (size_t)nb * TB * TB, s);
+    S *di = dinv ? dinv : (S *)own.get();
+    if (nb <= smem_nb_max<S>()) {
+        const size_t smem = sizeof(S) * ((size_t)(tix(0, nb) + 1) * TE + (size_t)nb * TB);
+        auto k = chol_smem_kernel<S>;
+        RSVD_CK(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        k<<<1, chol_smem_threads<S>(), smem, s>>>(G.p, G.ld, n, nb, rel_tol, di, d_flag);
+        RSVD_LAUNCH_CK();
+        ctx().launches++;
+    } else {
+        const size_t ntile = (size_t)tix(0, nb);
+        DBuf wt(sizeof(S) * ntile * TB * TB, s), d0(sizeof(S) * (size_t)nb * TB, s), rd(sizeof(S) * (size_t)nb * TB * TB, s);
+        S *Wt = (S *)wt.get(), *diag0 = (S *)d0.get(), *Rd = (S *)rd.get();
+        const long long tot = (long long)ntile * TB * TB;
+        const unsigned g = (unsigned)std::min<long long>((tot + 255) / 256, (long long)std::max(1, ctx().sms) * 16);
+        chol_gload_kernel<S><<<g, 256, 0, s>>>(G.p, G.ld, n, nb, Wt, diag0);
+        for (int J = 0; J < nb; J++) {
+            chol_gpanel_kernel<S><<<nb - J, 32, 0, s>>>(Wt, nb, J, diag0, rel_tol, di, Rd, d_flag);
+            const int nt = nb - J - 1;
+            if (nt > 0) chol_gupdate_kernel<S><<<nt * (nt + 1) / 2, 32, 0, s>>>(Wt, nb, J);
+        }
+        const unsigned g2 = (unsigned)std::min<long long>(((long long)n * n + 255) / 256, (long long)std::max(1, ctx().sms) * 16);
+        chol_gstore_kernel<S><<<g2, 256, 0, s>>>(Wt, Rd, n, G.p, G.ld);
+        RSVD_LAUNCH_CK();
+        ctx().launches += 2 * nb + 2;
+    }
+    int h = 0;
+    RSVD_CK(cudaMemcpyAsync(&h, d_flag, sizeof(int), cudaMemcpyDeviceToHost, s));
+    RSVD_CK(cudaStreamSynchronize(s));
+    return h == 0;
+}
+
+// X = R^-1 (upper, zero below), given the inverted diagonal tiles from chol_factor.
+template <typename S, typename To>
+void tri_inv_tiles(cudaStream_t s, DM<double> R, const S *dinv, DM<To> X) {
+    const int n = (int)R.r;
+    if (n == 0) return;
+    const int nb = (n + TB - 1) / TB;
+    const int threads = sizeof(S) == 4 ? 512 : 256, nw = threads / 32;
+    const size_t smem = sizeof(S) * (size_t)(2 + 2 * nw) * TE;
+    auto k = tri_inv_tiles_kernel<S, To>;
+    RSVD_CK(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    k<<<nb, threads, smem, s>>>(R.p, R.ld, n, nb, dinv, X.p, X.ld);
+    RSVD_LAUNCH_CK();
+    ctx().launches++;
+}
+
+// Q = Y R^-1 by the slab solve when the slab and R's block column fit in shared memory
+// (order <= 288); returns false (nothing queued) otherwise.
+template <typename T>
+bool trsm_right_tiles(cudaStream_t s, DM<T> Y, DM<double> R, const T *dinv, DM<T> Q) {
+    const int n = (int)R.r;
+    if (n == 0 || Y.r == 0) return true;
+    const int nb = (n + TB - 1) / TB;
+    if (nb > 9) return false;
+    const size_t smem = trsm_smem<T>(nb);
+    if (smem > 220 * 1024) return false;
+    constexpr int BM = trsm_bm<T>();
+    auto k = trsm_slab_kernel<T, T, BM>;
+    RSVD_CK(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    const long long slabs = (Y.r + BM - 1) / BM;
+    if (slabs > 0x7fffffffll) fail(RSVD_ERR_ARGUMENT, "trsm: too many rows");
+    k<<<(unsigned)slabs, TRSM_THREADS, smem, s>>>(Y.p, Y.ld, R.p, R.ld, nullptr, dinv, Q.p, Q.ld, Y.r, n, nb);
+    RSVD_LAUNCH_CK();
+    ctx().launches++;
+    return true;
+}
+
+// FP32 packed-tile Cholesky (order <= 288): Gt in, R tiles out (see chol_tiles_f32_kernel).
+bool chol_tiles_f32(cudaStream_t s, float *Gt, int n, double rel_tol, int *d_flag, float *dinv, DM<double> *Rout) {
+    if (n == 0) return true;
+    const int nb = (n + TB - 1) / TB;
+    if (nb > smem_nb_max<float>()) fail(RSVD_ERR_ARGUMENT, "chol_tiles_f32: order above 288");
+    RSVD_CK(cudaMemsetAsync(d_flag, 0, sizeof(int), s));
+    const size_t smem = sizeof(float) * ((size_t)(tix(0, nb) + 1) * TE + (size_t)nb * TB);
+    RSVD_CK(cudaFuncSetAttribute(chol_tiles_f32_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    chol_tiles_f32_kernel<<<1, 256, smem, s>>>(Gt, n, nb, rel_tol, dinv, Rout ? Rout->p : nullptr,
+                                               Rout ? Rout->ld : 0, d_flag);
+    RSVD_LAUNCH_CK();
+    ctx().launches++;
+    int h = 0;
+    RSVD_CK(cudaMemcpyAsync(&h, d_flag, sizeof(int), cudaMemcpyDeviceToHost, s));
+    RSVD_CK(cudaStreamSynchronize(s));
+    return h == 0;
+}
+
+// Q = Y R^-1 from R's packed FP32 tiles (order <= 288).
+void trsm_right_tiles_f32(cudaStream_t s, DM<float> Y, int n, const float *Rt, const float *dinv, DM<float> Q) {
+    if (n == 0 || Y.r == 0) return;
+    const int nb = (n + TB - 1) / TB;
+    if (nb > 9) fail(RSVD_ERR_ARGUMENT, "trsm_right_tiles_f32: order above 288");
+    const size_t smem = trsm_smem<float>(nb);
+    constexpr int BM = trsm_bm<float>();
+    auto k = trsm_slab_kernel<float, float, BM>;
+    RSVD_CK(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    const long long slabs = (Y.r + BM - 1) / BM;
+    k<<<(unsigned)slabs, TRSM_THREADS, smem, s>>>(Y.p, Y.ld, nullptr, 0, Rt, dinv, Q.p, Q.ld, Y.r, n, nb);
+    RSVD_LAUNCH_CK();
+    ctx().launches++;
+}
+
+template <typename S>
+void tri_mul_upper(cudaStream_t s, DM<double> A, DM<double> B, DM<double> C) {
+    const int n = (int)A.r;
+    if (n == 0) return;
+    const int nb = (n + TB - 1) / TB;
+    const int tiles = nb * nb;     // upper tiles + strictly lower tiles (zeroed)
+    tri_mul_upper_kernel<S><<<tiles, 256, 0, s>>>(A.p, A.ld, B.p, B.ld, C.p, C.ld, n, nb);
+    RSVD_LAUNCH_CK();
+    ctx().launches++;
+}
+
+template bool chol_factor<float>(cudaStream_t, DM<double>, double, int *, float *);
+template bool chol_factor<double>(cudaStream_t, DM<double>, double, int *, double *);
+template void tri_inv_tiles<float, float>(cudaStream_t, DM<double>, const float *, DM<float>);
+template void tri_inv_tiles<float, double>(cudaStream_t, DM<double>, const float *, DM<double>);
+template void tri_inv_tiles<double, double>(cudaStream_t, DM<double>, const double *, DM<double>);
+template bool trsm_right_tiles<float>(cudaStream_t, DM<float>, DM<double>, const float *, DM<float>);
+template bool trsm_right_tiles<double>(cudaStream_t, DM<double>, DM<double>, const double *, DM<double>);
+template void tri_mul_upper<float>(cudaStream_t, DM<double>, DM<double>, DM<double>);
+template void tri_mul_upper<double>(cudaStream_t, DM<double>, DM<double>, DM<double>);
+
+}  // namespace rsvd

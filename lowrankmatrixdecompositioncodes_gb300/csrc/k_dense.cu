@@ -217,10 +217,23 @@ template void gemm<float>(cudaStream_t, bool, bool, float, DM<float>, DM<float>,
 // =====================================================================================
 namespace {
 template <typename Ts, typename Td>
+// 2-D launch: blockIdx.x covers 1024 rows (4 per thread, coalesced), blockIdx.y strides columns
 __global__ void convert_kernel(const Ts *src, i64 lds, Td *dst, i64 ldd, i64 r, i64 c) {
-    for (i64 e = blockIdx.x * (i64)blockDim.x + threadIdx.x; e < r * c; e += (i64)gridDim.x * blockDim.x) {
-        const i64 i = e % r, j = e / r;
-        dst[i + j * ldd] = (Td)src[i + j * lds];
+    const i64 i0 = (i64)blockIdx.x * 1024 + threadIdx.x;
+    for (i64 j = blockIdx.y; j < c; j += gridDim.y) {
+        const Ts *sc = src + j * lds;
+        Td *dc = dst + j * ldd;
+        Ts v[4];
+#pragma unroll
+        for (int t = 0; t < 4; t++) {
+            const i64 i = i0 + 256 * t;
+            v[t] = (i < r) ? sc[i] : Ts(0);
+        }
+#pragma unroll
+        for (int t = 0; t < 4; t++) {
+            const i64 i = i0 + 256 * t;
+            if (i < r) dc[i] = (Td)v[t];
+        }
     }
 }
 template <typename T>
@@ -287,7 +300,8 @@ unsigned grid_for(i64 n) {
 template <typename Ts, typename Td>
 void convert(cudaStream_t s, DM<Ts> src, DM<Td> dst) {
     if (src.r * src.c == 0) return;
-    convert_kernel<Ts, Td><<<grid_for(src.r * src.c), 256, 0, s>>>(src.p, src.ld, dst.p, dst.ld, src.r, src.c);
+    const dim3 grid((unsigned)((src.r + 1023) / 1024), (unsigned)std::min<i64>(src.c, 65535));
+    convert_kernel<Ts, Td><<<grid, 256, 0, s>>>(src.p, src.ld, dst.p, dst.ld, src.r, src.c);
     RSVD_LAUNCH_CK();
     ctx().launches++;
 }
@@ -387,21 +401,27 @@ __global__ void philox_kernel(uint64_t seed, uint64_t offset, T *out, i64 ld, i6
         const U4 v = philox4x32_10(U4{(uint32_t)g, (uint32_t)(g >> 32), (uint32_t)offset, (uint32_t)(offset >> 32)},
                                    (uint32_t)seed, (uint32_t)(seed >> 32));
         const uint32_t u[4] = {v.x, v.y, v.z, v.w};
-        double z[4];
+        // Box-Muller in FP32 (the values are FP32 in every mode; FP64 transcendental
+        // throughput is low on this part).  Same formulas as the batched kernel's generator.
+        float z[4];
 #pragma unroll
         for (int h = 0; h < 2; h++) {
-            const double u1 = ((double)u[2 * h] + 1.0) * 2.3283064365386963e-10;   // (0,1]
-            const double u2 = (double)u[2 * h + 1] * 2.3283064365386963e-10;       // [0,1)
-            const double rad = sqrt(-2.0 * log(u1));
-            double sn, cs;
-            sincospi(2.0 * u2, &sn, &cs);
+            const float u1 = ((float)u[2 * h] + 1.0f) * 2.3283064365386963e-10f;   // (0,1]
+            const float u2 = (float)u[2 * h + 1] * 2.3283064365386963e-10f;       // [0,1)
+            const float rad = sqrtf(-2.0f * logf(u1));
+            float sn, cs;
+            sincospif(2.0f * u2, &sn, &cs);
             z[2 * h] = rad * cs;
             z[2 * h + 1] = rad * sn;
         }
+        const i64 e0 = 4 * g;
+        i64 col = e0 / r, row = e0 - col * r;
 #pragma unroll
         for (int t = 0; t < 4; t++) {
-            const i64 e = 4 * g + t;
-            if (e < n) out[(e % r) + (e / r) * ld] = (T)(float)z[t];
+            if (e0 + t < n) {
+                out[row + col * ld] = (T)z[t];
+                if (++row == r) { row = 0; ++col; }
+            }
         }
     }
 }
@@ -796,6 +816,29 @@ __global__ void gram_reduce_kernel(const double *part, i64 part_stride, int nsla
         G[(e % c) + (e / c) * ldg] = acc;
     }
 }
+// Reduce into FP32 packed upper 32 x 32 tiles (tile (I, K), I <= K, at (K(K+1)/2 + I) *
+// 1024, row-major), padded to np = 32 * ceil(c / 32) with the identity; optionally also
+// into the full symmetric FP64 G.
+__global__ void gram_reduce_tiles_kernel(const double *part, i64 part_stride, int nslab, int c, int np, float *Gt,
+                                         double *G, i64 ldg) {
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < np * np; e += gridDim.x * blockDim.x) {
+        const int i = e % np, j = e / np;
+        if (i > j) continue;
+        double v;
+        if (i < c && j < c) {
+            v = 0.0;
+            for (int z = 0; z < nslab; z++) v += part[z * part_stride + i + (i64)j * c];
+            if (G) {
+                G[i + (i64)j * ldg] = v;
+                G[j + (i64)i * ldg] = v;
+            }
+        } else {
+            v = (i == j) ? 1.0 : 0.0;
+        }
+        const int I = i >> 5, K = j >> 5;
+        Gt[(size_t)(K * (K + 1) / 2 + I) * 1024 + (i & 31) * 32 + (j & 31)] = (float)v;
+    }
+}
 }  // namespace
 
 // FP32 Gram, symmetric tiles only: 64 x 64 tile (bi <= bj) of G per block over a 1024-row
@@ -805,8 +848,11 @@ namespace {
 constexpr int GS_SLAB = 1024;
 __global__ void __launch_bounds__(256) gram_sym_f32_kernel(const float *__restrict__ Y, i64 ld, i64 m, int c,
                                                            int ntile, double *__restrict__ part, i64 part_stride) {
-    __shared__ __align__(16) float As[32][64];
-    __shared__ __align__(16) float Bs[32][64];
+    // column-major staging tiles [column][row], pitch 33: the staging stores (32 rows of
+    // one column per warp) and the compute loads (16 distinct columns per warp) are
+    // free of bank conflicts
+    __shared__ float As[64][33];
+    __shared__ float Bs[64][33];
     // upper-triangular tile list: blockIdx.x -> (bi, bj), bi <= bj
     int bj = 0;
     while ((bj + 1) * (bj + 2) / 2 <= (int)blockIdx.x) bj++;
@@ -827,15 +873,17 @@ __global__ void __launch_bounds__(256) gram_sym_f32_kernel(const float *__restri
             const int idx = tid + 256 * e;
             const int kk = idx & 31, cc = idx >> 5;
             const i64 row = rb + kk;
-            As[kk][cc] = (row < r1 && i0 + cc < c) ? Y[row + (i64)(i0 + cc) * ld] : 0.f;
-            Bs[kk][cc] = (row < r1 && j0 + cc < c) ? Y[row + (i64)(j0 + cc) * ld] : 0.f;
+            As[cc][kk] = (row < r1 && i0 + cc < c) ? Y[row + (i64)(i0 + cc) * ld] : 0.f;
+            Bs[cc][kk] = (row < r1 && j0 + cc < c) ? Y[row + (i64)(j0 + cc) * ld] : 0.f;
         }
         __syncthreads();
 #pragma unroll 8
         for (int kk = 0; kk < 32; kk++) {
-            const float4 a = *reinterpret_cast<const float4 *>(&As[kk][ty * 4]);
-            const float4 b = *reinterpret_cast<const float4 *>(&Bs[kk][tx * 4]);
-            const float av[4] = {a.x, a.y, a.z, a.w}, bv[4] = {b.x, b.y, b.z, b.w};
+            float av[4], bv[4];
+#pragma unroll
+            for (int x = 0; x < 4; x++) av[x] = As[ty + 16 * x][kk];
+#pragma unroll
+            for (int y = 0; y < 4; y++) bv[y] = Bs[tx + 16 * y][kk];
 #pragma unroll
             for (int x = 0; x < 4; x++)
 #pragma unroll
@@ -856,7 +904,7 @@ __global__ void __launch_bounds__(256) gram_sym_f32_kernel(const float *__restri
 #pragma unroll
         for (int y = 0; y < 4; y++) {
             const double v = dacc[x][y] + (double)acc[x][y];
-            const int gi = i0 + ty * 4 + x, gj = j0 + tx * 4 + y;
+            const int gi = i0 + ty + 16 * x, gj = j0 + tx + 16 * y;
             if (gi < c && gj < c) {
                 P[gi + (i64)gj * c] = v;
                 if (bi != bj) P[gj + (i64)gi * c] = v;
@@ -897,5 +945,30 @@ void gram(cudaStream_t s, DM<T> Y, DM<double> G) {
 }
 template void gram<double>(cudaStream_t, DM<double>, DM<double>);
 template void gram<float>(cudaStream_t, DM<float>, DM<double>);
+
+void gram_tiles_f32(cudaStream_t s, DM<float> Y, float *Gt, DM<double> *G) {
+    const int c = (int)Y.c;
+    if (c == 0) return;
+    if (G && (G->r != c || G->c != c)) fail(RSVD_ERR_ARGUMENT, "gram: shape mismatch");
+    const int np = (c + 31) / 32 * 32;
+    const i64 stride = (i64)c * c;
+    int nslab;
+    DBuf part;
+    if (c >= 64 && (Y.r + GS_SLAB - 1) / GS_SLAB <= 65535) {
+        const int nt = (c + 63) / 64, ntiles = nt * (nt + 1) / 2;
+        nslab = (int)std::max<i64>(1, (Y.r + GS_SLAB - 1) / GS_SLAB);
+        part = DBuf(sizeof(double) * (size_t)stride * nslab, s);
+        gram_sym_f32_kernel<<<dim3(ntiles, nslab), 256, 0, s>>>(Y.p, Y.ld, Y.r, c, ntiles, (double *)part.get(), stride);
+    } else {
+        nslab = (int)std::max<i64>(1, (Y.r + GR_SLAB - 1) / GR_SLAB);
+        part = DBuf(sizeof(double) * (size_t)stride * nslab, s);
+        dim3 grid(ceil_div(c, 32), ceil_div(c, 32), nslab);
+        gram_kernel<float><<<grid, 256, 0, s>>>(Y.p, Y.ld, Y.r, c, (double *)part.get(), stride);
+    }
+    gram_reduce_tiles_kernel<<<grid_for((i64)np * np), 256, 0, s>>>((const double *)part.get(), stride, nslab, c, np,
+                                                                     Gt, G ? G->p : nullptr, G ? G->ld : 0);
+    RSVD_LAUNCH_CK();
+    ctx().launches += 2;
+}
 
 }  // namespace rsvd

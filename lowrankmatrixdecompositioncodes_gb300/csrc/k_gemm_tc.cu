@@ -395,12 +395,23 @@ void tc_gemm(cudaStream_t s, int kind, bool a_mn, const void *A, long long lda, 
     int splits = 1;
     const int sms = std::max(1, ctx().sms);
     if (epi == EPI_STORE && splits_hint != 1) {
+        // time model in units of one k-block of one CTA (one CTA per SM; a k-block moves
+        // (BM + BN) x 128 bytes through shared memory at ~80 GB/s per SM on GB300):
+        //   waves(z) x ceil(num_kb / z)  +  the split-K reduce, which writes and reads z
+        //   FP32 partial slabs of M x N at ~6 TB/s.
         const int tiles = mtiles * ntiles;
-        double best = (double)((tiles + sms - 1) / sms) * sms / tiles;   // waves / useful
+        const double t_kb = (double)(BM + BN) * KB / 80e9;
+        auto cost = [&](int z) {
+            const double waves = (double)((tiles * z + sms - 1) / sms);
+            const double main = waves * (double)((num_kb + z - 1) / z);
+            const double red = (z > 1) ? (double)z * 8.0 * (double)M * (double)N / 6e12 / t_kb : 0.0;
+            return main + red;
+        };
+        double best = cost(1);
         for (int z = 2; z <= 8; z++) {
             if (num_kb / z < 4) break;
-            const double eff = (double)((tiles * z + sms - 1) / sms) * sms / ((double)tiles * z);
-            if (eff < best - 0.05) { best = eff; splits = z; }
+            const double c = cost(z);
+            if (c < best * 0.97) { best = c; splits = z; }
         }
         if (splits_hint > 1) splits = splits_hint;
     }

@@ -7,9 +7,7 @@
 // milliseconds in FP64 and tens of microseconds in FP32.  In the mixed modes the inputs
 // of these steps (Grams of FP32 data) are only FP32-accurate anyway.
 //
-//   cholesky_small  : G = R^T R, one CTA; the upper triangle is kept packed in shared
-//                     memory when it fits (else in global memory / L2)
-//   tri_inv_upper   : Rinv = R^-1, one warp per column (back substitution), many SMs
+//   cholesky_small  : G = R^T R through the tiled factorisation of k_chol.cu
 //   jacobi_small    : one-sided Jacobi SVD, one CTA, round-robin pair ordering
 #include "rsvd_internal.h"
 #include "k_common.cuh"
@@ -25,260 +23,11 @@ namespace rsvd {
 
 namespace {
 
-__host__ __device__ __forceinline__ long long pk(int i, int k) { return (long long)k * (k + 1) / 2 + i; }  // i <= k
-
 template <typename S>
 __device__ __forceinline__ S warp_sum_t(S v) {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
     return v;
-}
-
-// ------------------------------------------------------------------ Cholesky
-// Packed upper triangle P (column k holds rows 0..k).  Right-looking with deferred row
-// scaling: step j updates the trailing triangle with P(j,i) P(j,k) / d_j (d_j the pivot)
-// and leaves row j unscaled; rows are scaled by 1/sqrt(d_j) once at the end.  Two block
-// barriers per step; the original diagonal (for the breakdown test) sits in shared memory.
-template <typename S>
-__global__ void __launch_bounds__(1024) chol_kernel(double *G, long long ldg, int n, double rel_tol, int *flag,
-                                                    S *gbuf, int use_smem) {
-    extern __shared__ __align__(16) unsigned char shraw[];
-    S *P = use_smem ? (S *)shraw : gbuf;
-    S *piv = use_smem ? (S *)(shraw + sizeof(S) * ((size_t)n * (n + 1) / 2)) : gbuf + (size_t)n * (n + 1) / 2;
-    S *diag0 = piv + n;
-    __shared__ int bad;
-    __shared__ S inv_d;
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    if (threadIdx.x == 0) bad = 0;
-    for (int k = wid; k < n; k += nw)
-        for (int i = lane; i <= k; i += 32) P[pk(i, k)] = (S)G[i + (long long)k * ldg];
-    for (int j = threadIdx.x; j < n; j += blockDim.x) diag0[j] = (S)G[j + (long long)j * ldg];
-    __syncthreads();
-    for (int j = 0; j < n; j++) {
-        if (threadIdx.x == 0) {
-            const S d = P[pk(j, j)];
-            if (!(d > S(0)) || !isfinite((double)d) || !((double)d > rel_tol * (double)diag0[j])) { bad = 1; inv_d = S(0); }
-            else inv_d = S(1) / d;
-            piv[j] = d;
-        }
-        __syncthreads();
-        if (bad) break;
-        const S id = inv_d;
-        for (int k = j + 1 + wid; k < n; k += nw) {
-            const S f = P[pk(j, k)] * id;
-            const long long ck = (long long)k * (k + 1) / 2;
-            for (int i = j + 1 + lane; i <= k; i += 32) P[ck + i] -= P[pk(j, i)] * f;
-        }
-        __syncthreads();
-    }
-    if (bad) {
-        if (threadIdx.x == 0) atomicExch(flag, 1);
-        return;
-    }
-    for (long long e = threadIdx.x; e < (long long)n * n; e += blockDim.x) {
-        const int i = (int)(e % n), k = (int)(e / n);
-        double v = 0.0;
-        if (i < k) v = (double)(P[pk(i, k)] / sqrt(piv[i]));
-        else if (i == k) v = (double)sqrt(piv[i]);
-        G[i + (long long)k * ldg] = v;
-    }
-}
-
-// Blocked right-looking Cholesky on the packed upper triangle in shared memory (one CTA,
-// 1024 threads, 32-column blocks):
-//   A: warp 0 factors the diagonal block (unblocked, warp-synchronous);
-//   B: the block row to its right, R_JK = R_JJ^-T G_JK, one warp per column (forward
-//      substitution with the 32 rows of the column held one per lane);
-//   C: trailing update G_IK -= R_JI^T R_JK over 32 x 32 tiles, 4 x 4 outputs per thread.
-template <typename S>
-__global__ void __launch_bounds__(1024) chol_blocked_kernel(double *G, long long ldg, int n, double rel_tol,
-                                                            int *flag) {
-    extern __shared__ __align__(16) unsigned char shraw[];
-    S *P = (S *)shraw;
-    S *diag0 = P + (size_t)n * (n + 1) / 2;
-    __shared__ int bad;
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    if (threadIdx.x == 0) bad = 0;
-    for (int k = wid; k < n; k += nw)
-        for (int i = lane; i <= k; i += 32) P[pk(i, k)] = (S)G[i + (long long)k * ldg];
-    for (int j = threadIdx.x; j < n; j += blockDim.x) diag0[j] = (S)G[j + (long long)j * ldg];
-    __syncthreads();
-    const int nb = (n + 31) / 32;
-    for (int J = 0; J < nb; J++) {
-        const int j0 = 32 * J, jw = min(32, n - j0);
-        // ---- A: diagonal block in registers: lane t holds column j0+t (rows j0..j0+31);
-        //      row j of R is broadcast from lane i's register c[j] by shuffles
-        if (wid == 0) {
-            S c[32];
-            const long long ct = (long long)(j0 + lane) * (j0 + lane + 1) / 2 + j0;
-#pragma unroll
-            for (int i = 0; i < 32; i++) c[i] = (lane < jw && i <= lane) ? P[ct + i] : S(0);
-            int bad_local = 0;
-#pragma unroll
-            for (int j = 0; j < 32; j++) {
-                if (j < jw) {
-                    const S d = __shfl_sync(0xffffffffu, c[j], j);
-                    const bool ok = (d > S(0)) && isfinite(d) && (d > (S)rel_tol * diag0[j0 + j]);
-                    bad_local |= !ok;
-                    const S p = ok ? sqrt(d) : S(1);
-                    const S inv = S(1) / p;
-                    if (lane == j) c[j] = p;
-                    else if (lane > j) c[j] *= inv;          // lane t now holds R(j, t)
-#pragma unroll
-                    for (int i = j + 1; i < 32; i++) {
-                        const S rji = __shfl_sync(0xffffffffu, c[j], i);
-                        if (lane >= i) c[i] -= rji * c[j];
-                    }
-                }
-            }
-            if (lane < jw) {
-#pragma unroll
-                for (int i = 0; i < 32; i++)
-                    if (i <= lane) P[ct + i] = c[i];
-            }
-            if (lane == 0 && bad_local) bad = 1;
-        }
-        __syncthreads();
-        if (bad) break;
-        // ---- B: block row to the right, one warp per column
-        S rdiag_inv = S(0);
-        if (lane < jw) rdiag_inv = S(1) / P[pk(j0 + lane, j0 + lane)];
-        const long long lrow = (long long)(j0 + lane) * (j0 + lane + 1) / 2 + j0;   // R(j0+t, j0+lane) = P[lrow + t]
-        for (int k = j0 + jw + wid; k < n; k += nw) {
-            const long long ck = (long long)k * (k + 1) / 2;
-            S g = (lane < jw) ? P[ck + j0 + lane] : S(0);
-            for (int t = 0; t < jw; t++) {
-                S xt = (lane == t) ? g * rdiag_inv : S(0);
-                xt = __shfl_sync(0xffffffffu, xt, t);
-                if (lane == t) g = xt;
-                else if (lane > t && lane < jw) g -= P[lrow + t] * xt;
-            }
-            if (lane < jw) P[ck + j0 + lane] = g;
-        }
-        __syncthreads();
-        // ---- C: trailing update over tiles (I, K), J < I <= K, 4 x 4 per thread
-        const int t0 = J + 1, nt = nb - t0;
-        const int ntiles = nt * (nt + 1) / 2;
-        const int sub = threadIdx.x & 63;             // 64 threads per tile: 8 x 8 threads x (4 x 4)
-        const int tslot = threadIdx.x >> 6;           // 16 tiles in flight
-        for (int tt = tslot; tt < ntiles; tt += 16) {
-            // tile index -> (I, K) with I <= K
-            int K = 0;
-            while ((K + 1) * (K + 2) / 2 <= tt) K++;
-            const int I = tt - K * (K + 1) / 2;
-            const int ib = 32 * (t0 + I), kb = 32 * (t0 + K);
-            const int ri = ib + (sub & 7) * 4, ck = kb + (sub >> 3) * 4;
-            S acc[4][4];
-#pragma unroll
-            for (int a = 0; a < 4; a++)
-#pragma unroll
-                for (int b = 0; b < 4; b++) acc[a][b] = S(0);
-            for (int t = 0; t < jw; t++) {
-                const int row = j0 + t;
-                S ra[4], rb[4];
-#pragma unroll
-                for (int a = 0; a < 4; a++) {
-                    const int i = ri + a, k = ck + a;
-                    ra[a] = (i < n) ? P[pk(row, i)] : S(0);
-                    rb[a] = (k < n) ? P[pk(row, k)] : S(0);
-                }
-#pragma unroll
-                for (int a = 0; a < 4; a++)
-#pragma unroll
-                    for (int b = 0; b < 4; b++) acc[a][b] = fma(ra[a], rb[b], acc[a][b]);
-            }
-#pragma unroll
-            for (int a = 0; a < 4; a++)
-#pragma unroll
-                for (int b = 0; b < 4; b++) {
-                    const int i = ri + a, k = ck + b;
-                    if (i <= k && k < n) P[pk(i, k)] -= acc[a][b];
-                }
-        }
-        __syncthreads();
-    }
-    if (bad) {
-        if (threadIdx.x == 0) atomicExch(flag, 1);
-        return;
-    }
-    for (long long e = threadIdx.x; e < (long long)n * n; e += blockDim.x) {
-        const int i = (int)(e % n), k = (int)(e / n);
-        G[i + (long long)k * ldg] = (i <= k) ? (double)P[pk(i, k)] : 0.0;
-    }
-}
-
-// ------------------------------------------------------------------ triangular inverse
-// Column c of X = R^-1 solves R x = e_c: back substitution from row c down to 0, the
-// pending right-hand side kept in registers (rows spread over the 32 lanes).
-template <typename S, int MAXR>
-__global__ void tri_inv_kernel(const double *R, long long ldr, int n, double *X, long long ldx) {
-    const int c = (int)((blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5);
-    const int lane = threadIdx.x & 31;
-    if (c >= n) return;
-    S b[MAXR];   // b[t] holds rhs row (lane + 32 t)
-#pragma unroll
-    for (int t = 0; t < MAXR; t++) {
-        const int r = lane + 32 * t;
-        b[t] = (r == c) ? S(1) : S(0);
-    }
-    double *x = X + (long long)c * ldx;
-    for (int r = lane; r < n; r += 32) x[r] = 0.0;
-    for (int j = c; j >= 0; j--) {
-        const int owner = j & 31, slot = j >> 5;
-        S bj = S(0);
-#pragma unroll
-        for (int t = 0; t < MAXR; t++)
-            if (t == slot) bj = b[t];
-        bj = __shfl_sync(0xffffffffu, bj, owner);
-        const S xj = bj / (S)R[j + (long long)j * ldr];
-        if (lane == 0) x[j] = (double)xj;
-        // b[0..j-1] -= xj * R(0..j-1, j)
-        const double *rc = R + (long long)j * ldr;
-#pragma unroll
-        for (int t = 0; t < MAXR; t++) {
-            const int r = lane + 32 * t;
-            if (r < j) b[t] -= xj * (S)rc[r];
-        }
-    }
-}
-
-// Shared-memory variant: CTA b solves columns [32b, 32b+32) (one warp each) against the
-// packed upper triangle of R(0:cmax, 0:cmax) staged in shared memory.
-template <typename S, int MAXR>
-__global__ void __launch_bounds__(1024) tri_inv_smem_kernel(const double *R, long long ldr, int n, double *X,
-                                                            long long ldx) {
-    extern __shared__ __align__(16) unsigned char shraw[];
-    S *Rs = (S *)shraw;
-    const int cmax = min(n, (int)(blockIdx.x + 1) * 32);
-    for (long long e = threadIdx.x; e < (long long)cmax * cmax; e += blockDim.x) {
-        const int i = (int)(e % cmax), k = (int)(e / cmax);
-        if (i <= k) Rs[pk(i, k)] = (S)R[i + (long long)k * ldr];
-    }
-    __syncthreads();
-    const int lane = threadIdx.x & 31;
-    const int c = blockIdx.x * 32 + (threadIdx.x >> 5);
-    if (c >= n) return;
-    S b[MAXR];
-#pragma unroll
-    for (int t = 0; t < MAXR; t++) b[t] = (lane + 32 * t == c) ? S(1) : S(0);
-    double *x = X + (long long)c * ldx;
-    for (int r = lane; r < n; r += 32) x[r] = 0.0;
-    for (int j = c; j >= 0; j--) {
-        const int owner = j & 31, slot = j >> 5;
-        S bj = S(0);
-#pragma unroll
-        for (int t = 0; t < MAXR; t++)
-            if (t == slot) bj = b[t];
-        bj = __shfl_sync(0xffffffffu, bj, owner);
-        const long long cj = (long long)j * (j + 1) / 2;
-        const S xj = bj / Rs[cj + j];
-        if (lane == 0) x[j] = (double)xj;
-#pragma unroll
-        for (int t = 0; t < MAXR; t++) {
-            const int r = lane + 32 * t;
-            if (r < j) b[t] -= xj * Rs[cj + r];
-        }
-    }
 }
 
 // ------------------------------------------------------------------ Jacobi SVD
@@ -675,71 +424,10 @@ unsigned gfor(long long n) {
 
 template <typename S>
 bool cholesky_small(cudaStream_t s, DM<double> G, double rel_tol, int *d_flag) {
-    const int n = (int)G.r;
-    if (G.r != G.c) fail(RSVD_ERR_ARGUMENT, "cholesky: not square");
-    if (n == 0) return true;
-    RSVD_CK(cudaMemsetAsync(d_flag, 0, sizeof(int), s));
-    const size_t bpacked = sizeof(S) * ((size_t)n * (n + 1) / 2 + (size_t)n);
-    if (bpacked <= 220 * 1024) {
-        auto kb = chol_blocked_kernel<S>;
-        RSVD_CK(cudaFuncSetAttribute(kb, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)std::max<size_t>(bpacked, 1024)));
-        kb<<<1, 1024, std::max<size_t>(bpacked, 1024), s>>>(G.p, G.ld, n, rel_tol, d_flag);
-        RSVD_LAUNCH_CK();
-        ctx().launches++;
-        int hb = 0;
-        RSVD_CK(cudaMemcpyAsync(&hb, d_flag, sizeof(int), cudaMemcpyDeviceToHost, s));
-        RSVD_CK(cudaStreamSynchronize(s));
-        return hb == 0;
-    }
-    const size_t packed = sizeof(S) * ((size_t)n * (n + 1) / 2 + 2 * (size_t)n);
-    const bool smem = packed <= 200 * 1024;
-    DBuf gb(smem ? 16 : packed, s);
-    auto k = chol_kernel<S>;
-    if (smem && packed > 48 * 1024)
-        RSVD_CK(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)packed));
-    k<<<1, 1024, smem ? packed : 0, s>>>(G.p, G.ld, n, rel_tol, d_flag, (S *)gb.get(), smem ? 1 : 0);
-    RSVD_LAUNCH_CK();
-    ctx().launches++;
-    int h = 0;
-    RSVD_CK(cudaMemcpyAsync(&h, d_flag, sizeof(int), cudaMemcpyDeviceToHost, s));
-    RSVD_CK(cudaStreamSynchronize(s));
-    return h == 0;
+    return chol_factor<S>(s, G, rel_tol, d_flag, nullptr);     // tiled factorisation (k_chol.cu)
 }
 template bool cholesky_small<double>(cudaStream_t, DM<double>, double, int *);
 template bool cholesky_small<float>(cudaStream_t, DM<double>, double, int *);
-
-template <typename S>
-void tri_inv_upper(cudaStream_t s, DM<double> R, DM<double> X) {
-    const int n = (int)R.r;
-    if (n == 0) return;
-    const size_t sm = sizeof(S) * (size_t)n * (n + 1) / 2;
-    if (sm <= 200 * 1024 && n <= 512) {
-        const unsigned nb = (unsigned)((n + 31) / 32);
-        if (n <= 256) {
-            auto k = tri_inv_smem_kernel<S, 8>;
-            RSVD_CK(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)std::max<size_t>(sm, 1024)));
-            k<<<nb, 1024, std::max<size_t>(sm, 1024), s>>>(R.p, R.ld, n, X.p, X.ld);
-        } else {
-            auto k = tri_inv_smem_kernel<S, 16>;
-            RSVD_CK(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-            k<<<nb, 1024, sm, s>>>(R.p, R.ld, n, X.p, X.ld);
-        }
-        RSVD_LAUNCH_CK();
-        ctx().launches++;
-        return;
-    }
-    const long long threads = (long long)n * 32;
-    const unsigned blocks = (unsigned)((threads + 127) / 128);
-    if (n <= 256) tri_inv_kernel<S, 8><<<blocks, 128, 0, s>>>(R.p, R.ld, n, X.p, X.ld);
-    else if (n <= 512) tri_inv_kernel<S, 16><<<blocks, 128, 0, s>>>(R.p, R.ld, n, X.p, X.ld);
-    else if (n <= 1024) tri_inv_kernel<S, 32><<<blocks, 128, 0, s>>>(R.p, R.ld, n, X.p, X.ld);
-    else if (n <= 4096) tri_inv_kernel<S, 128><<<blocks, 128, 0, s>>>(R.p, R.ld, n, X.p, X.ld);
-    else fail(RSVD_ERR_ARGUMENT, "tri_inv_upper: order above 4096");
-    RSVD_LAUNCH_CK();
-    ctx().launches++;
-}
-template void tri_inv_upper<double>(cudaStream_t, DM<double>, DM<double>);
-template void tri_inv_upper<float>(cudaStream_t, DM<double>, DM<double>);
 
 template <typename S>
 int jacobi_small(cudaStream_t s, DM<double> G, DM<double> U, DM<double> V, double *d_sv, int *d_flag) {

@@ -178,6 +178,27 @@ namespace rsvd {
 void tc_gemm(cudaStream_t s, int kind, bool a_mn, const void *A, long long lda, const void *X, long long ldx,
              int M, int N, int K, float alpha, float *D, long long ldd, int epi, const float *C, long long ldc,
              double *fro_part, int splits_hint);
+// ----------------------------------------------------------------- tiled triangular steps (k_chol.cu)
+// G (n x n, FP64, upper triangle read) -> R, G = R^T R (upper, zero below), compute type S.
+// dinv (optional): receives the inverses of R's 32 x 32 diagonal tiles (ceil(n/32) row-major
+// tiles), which tri_inv_tiles consumes.  false on breakdown (pivot <= rel_tol * G_jj).
+template <typename S>
+bool chol_factor(cudaStream_t s, DM<double> G, double rel_tol, int *d_flag, S *dinv);
+template <typename S, typename To>
+void tri_inv_tiles(cudaStream_t s, DM<double> R, const S *dinv, DM<To> X);   // X = R^-1
+template <typename S>
+void tri_mul_upper(cudaStream_t s, DM<double> A, DM<double> B, DM<double> C);   // C = A B (upper)
+// Q = Y R^-1 (R from chol_factor, dinv its inverted diagonal tiles), order <= 288;
+// false when the order is too large (nothing queued).
+template <typename T>
+bool trsm_right_tiles(cudaStream_t s, DM<T> Y, DM<double> R, const T *dinv, DM<T> Q);
+// The FP32 CholeskyQR pass on packed upper 32 x 32 tiles (orders <= 288): the Gram is
+// reduced straight into FP32 tiles (Gt: ceil(n/32)(ceil(n/32)+1)/2 tiles of 1024 floats),
+// factored in one CTA (Gt then holds R; Rout optional FP64 copy), and applied by the slab
+// triangular solve.
+void gram_tiles_f32(cudaStream_t s, DM<float> Y, float *Gt, DM<double> *G);
+bool chol_tiles_f32(cudaStream_t s, float *Gt, int n, double rel_tol, int *d_flag, float *dinv, DM<double> *Rout);
+void trsm_right_tiles_f32(cudaStream_t s, DM<float> Y, int n, const float *Rt, const float *dinv, DM<float> Q);
 }  // namespace rsvd
 
 namespace rsvd {
@@ -185,8 +206,6 @@ namespace rsvd {
 // Compute type S: double in the FP64 mode, float in the mixed modes (storage is FP64).
 template <typename S>
 bool cholesky_small(cudaStream_t s, DM<double> G, double rel_tol, int *d_flag);
-template <typename S>
-void tri_inv_upper(cudaStream_t s, DM<double> R, DM<double> X);
 template <typename S>
 int jacobi_small(cudaStream_t s, DM<double> G, DM<double> U, DM<double> V, double *d_sv, int *d_flag);
 }  // namespace rsvd

@@ -24,7 +24,7 @@ def _dev(A):
 
 
 @pytest.mark.parametrize("fp32", [0, 1])
-@pytest.mark.parametrize("n", [5, 33, 64, 110, 272, 300, 400])
+@pytest.mark.parametrize("n", [5, 33, 64, 110, 192, 200, 272, 288, 300, 400, 600])
 def test_small_cholesky(engine, n, fp32):
     _bind(engine.lib)
     g = np.random.default_rng(n)

@@ -70,11 +70,12 @@ def test_tc_product_matches_fp64(engine, prec, trans, m, n, w):
     engine.set_precision("fp64")
 
 
-@pytest.mark.parametrize("prec", ["tf32", "bf16"])
-def test_mixed_precision_rsvd_matches_fp64_error(engine, prec):
+@pytest.mark.parametrize("prec,k,p", [("tf32", 64, 8), ("bf16", 64, 8), ("fp32", 300, 20), ("tf32", 300, 20)])
+def test_mixed_precision_rsvd_matches_fp64_error(engine, prec, k, p):
     """Same method, same test matrix: the tensor-core path's relative Frobenius residual
-    is within 1e-3 (relative) of the FP64 path's."""
-    m, n, k, p = 3000, 1500, 64, 8
+    is within 1e-3 (relative) of the FP64 path's.  l = 320 exceeds the one-CTA Cholesky
+    (order 288 in FP32) and runs the tiled global-memory factorisation."""
+    m, n = 3000, 1500
     s = (1.0 + np.arange(n)) ** -1.5
     A = spectrum_matrix(m, n, s, seed=8) + 1e-4 * np.random.default_rng(9).standard_normal((m, n))
     res = {}
