@@ -33,9 +33,9 @@ sys.path.insert(0, ROOT)
 M_ROWS, N_COLS, K, P, Q, S_ORTH, VNUM = 16384, 8192, 256, 16, 2, 1, 1
 METRIC = "rSVD solves/sec at matched FP64-oracle error (16384x8192 FP32, k=256, p=16, q=2)"
 # DRAM bytes (read + write) per tensor-core sketch launch on this workload, mean of the A*X
-# (BF16 A) and A^T*X (TF32) forms, from one ncu capture of this script
-# (profiles/tc_gemm_sketch_16384x8192.txt); None until a capture exists.
-TC_TRAFFIC_PER_LAUNCH = None
+# (BF16 A: 276.3 MB) and A^T*X (TF32: 605.9 MB) forms, from one ncu capture of this script
+# (profiles/tc_gemm_sketch_16384x8192.txt).
+TC_TRAFFIC_PER_LAUNCH = 441.1e6
 
 
 def parse():
