@@ -159,7 +159,11 @@ typedef struct {
                                  when one is set (default 1); 0: always on-device Philox */
     unsigned long long seed;  /* Philox key for on-device test matrices */
     int verbose;              /* print the reference's progress lines (default 0) */
-    int reserved[8];
+    int learned;              /* randQB_pb_new in TOL mode, FP32 data: let the learned proposal
+                                 (rsvdpack_load_proposal_model) pick the sketch width and power
+                                 count of one single-shot QB, verified against TOL, with the
+                                 plain adaptive loop as the fallback (default 0) */
+    int reserved[7];
 } rsvdpack_opts;
 
 void rsvdpack_get_opts(rsvdpack_opts *opts);
@@ -250,9 +254,40 @@ int rsvdpack_dev_sketch_t_noalloc(const float *dA, long long lda, int m, int n, 
                                   long long ldx, int w, float *dY, long long ldy, void *stream);
 
 /* Per-call phase timing of the last decomposition on this thread (milliseconds). */
+/* ---- the learned rank / power-count proposal's network (no counterpart in the reference):
+ * an MLP 36 -> 64 -> 64 -> 2 (ReLU) whose inputs are the R-diagonal features of a 32-column
+ * probe sketch and whose outputs are log2(width / 32) of the single-shot range finder for
+ * q = 1 and q = 2 power iterations.  Parameters: one flat FP32 array (W_l row-major in x out,
+ * then b_l, layer by layer); norm = [mean(36), inv_std(36)] of the inputs.  All pointers are
+ * device pointers; calls run on the engine stream and return after it finishes. */
+int rsvdpack_mlp_info(int *dims /* 4 layer widths */, int *nparams);
+/* Fixed-rank or fixed-precision blocked QB on device data (randQB_pb_new semantics; nstep <= 0
+ * selects the TOL mode, TOL absolute).  Q (m x frank, ldq) and B (frank x n, ldb) go to
+ * caller buffers with room for cap columns / rows; *frank receives the rank.  With
+ * rsvdpack_opts.learned set, FP32 data and a proposal model installed, the TOL mode runs the
+ * learned proposal (rsvdpack_last_timing()->learned_path reports which path ran). */
+int rsvdpack_dev_qb(const void *dA, int dtype, long long lda, int m, int n, int kstep, int nstep, double TOL,
+                    int q, int s, void *dQ, long long ldq, void *dB, long long ldb, int cap, int *frank);
+
+/* Install the proposal network used when rsvdpack_opts.learned is set (host arrays, copied):
+ * params (nparams floats), norm (2 x input width), margin (one log2 safety margin per output).
+ * rsvdpack_load_proposal_model reads the same from a weights file (magic "RSVDMLP1"). */
+int rsvdpack_set_proposal_model(const float *params, int nparams, const float *norm, int nnorm,
+                                const float *margin, int nmargin);
+int rsvdpack_load_proposal_model(const char *path);
+int rsvdpack_mlp_forward(const float *dP, const float *dnorm, const float *dX, int batch, float *dY);
+/* One training step: forward, loss (squared error; a target whose run did not reach the
+ * tolerance, dReached[i] == 0, only penalises predictions below it), backward into dG, and an
+ * Adam update of dP (state dM, dV; step >= 1) when lr > 0.  *dloss receives the batch loss. */
+int rsvdpack_mlp_train_step(float *dP, float *dM, float *dV, const float *dnorm, const float *dX, const float *dT,
+                            const float *dReached, int batch, float lr, int step, float *dloss, float *dG);
+
 typedef struct {
     double upload_ms, sketch_ms, orth_ms, small_ms, download_ms, total_ms;
     long long gemm_launches, kernel_launches;
+    int learned_path;   /* last fixed-precision QB: 0 plain loop, 1 learned proposal accepted,
+                           2 learned proposal rejected by the residual check (plain loop ran) */
+    int pad_;
 } rsvdpack_timing;
 void rsvdpack_last_timing(rsvdpack_timing *t);
 

@@ -22,13 +22,14 @@ PREC = {"fp64": 0, "fp32": 1, "tf32": 2, "bf16": 3}
 
 class RsvdOpts(C.Structure):
     _fields_ = [("precision", C.c_int), ("use_provider", C.c_int), ("seed", C.c_ulonglong),
-                ("verbose", C.c_int), ("reserved", C.c_int * 8)]
+                ("verbose", C.c_int), ("learned", C.c_int), ("reserved", C.c_int * 7)]
 
 
 class RsvdTiming(C.Structure):
     _fields_ = [("upload_ms", C.c_double), ("sketch_ms", C.c_double), ("orth_ms", C.c_double),
                 ("small_ms", C.c_double), ("download_ms", C.c_double), ("total_ms", C.c_double),
-                ("gemm_launches", C.c_longlong), ("kernel_launches", C.c_longlong)]
+                ("gemm_launches", C.c_longlong), ("kernel_launches", C.c_longlong),
+                ("learned_path", C.c_int), ("pad_", C.c_int)]
 
 
 class EngineLibrary(RsvdLibrary):
@@ -67,6 +68,17 @@ class EngineLibrary(RsvdLibrary):
         o = self.get_opts()
         o.use_provider = 1 if flag else 0
         self.lib.rsvdpack_set_opts(C.byref(o))
+
+    def set_learned(self, flag: bool):
+        """Fixed-precision QB (randQB_pb_new, TOL mode, FP32 data) through the learned proposal."""
+        o = self.get_opts()
+        o.learned = 1 if flag else 0
+        self.lib.rsvdpack_set_opts(C.byref(o))
+
+    def load_proposal_model(self, path: str):
+        self.lib.rsvdpack_load_proposal_model.argtypes = [C.c_char_p]
+        if self.lib.rsvdpack_load_proposal_model(path.encode()) != 0:
+            raise RuntimeError(self.last_error())
 
     def device_info(self):
         name = C.create_string_buffer(128)

@@ -653,6 +653,122 @@ int rsvdpack_dev_sketch(const void *dA, int dtype, long long lda, int m, int n, 
     return rsvdpack_last_error();
 }
 
+// ---- the learned proposal's network (k_mlp.cu): device pointers, engine stream, synchronous
+int rsvdpack_mlp_info(int *dims, int *nparams) {
+    guarded("rsvdpack_mlp_info", [&] {
+        need(dims && nparams, "null pointer");
+        mlp_dims(dims);
+        *nparams = mlp_param_count();
+    });
+    return rsvdpack_last_error();
+}
+
+int rsvdpack_dev_qb(const void *dA, int dtype, long long lda, int m, int n, int kstep, int nstep, double TOL, int q,
+                    int s, void *dQ, long long ldq, void *dB, long long ldb, int cap, int *frank) {
+    guarded("rsvdpack_dev_qb", [&] {
+        need(dA && dQ && dB && frank, "null pointer");
+        need(m > 0 && n > 0 && lda >= m && ldq >= m && kstep > 0 && q >= 0 && s >= 1 && cap > 0 && ldb >= cap,
+             "bad sizes");
+        auto t0 = Clock::now();
+        begin_call();
+        order_after_default_stream();
+        cudaStream_t st = ctx().stream;
+        auto run = [&](auto tag) {
+            using T = decltype(tag);
+            DM<T> A{(T *)const_cast<void *>(dA), m, n, lda};
+            QBOut<T> r = qb_blocked<T>(A, kstep, nstep, TOL, q, s);
+            if (r.frank > cap) fail(RSVD_ERR_ARGUMENT, "rsvdpack_dev_qb: rank above the output capacity");
+            *frank = r.frank;
+            if (r.frank > 0) {
+                RSVD_CK(cudaMemcpy2DAsync(dQ, sizeof(T) * ldq, r.Q.v.p, sizeof(T) * r.Q.v.ld, sizeof(T) * m, r.frank,
+                                          cudaMemcpyDeviceToDevice, st));
+                RSVD_CK(cudaMemcpy2DAsync(dB, sizeof(T) * ldb, r.B.v.p, sizeof(T) * r.B.v.ld, sizeof(T) * r.frank, n,
+                                          cudaMemcpyDeviceToDevice, st));
+            }
+            RSVD_CK(cudaStreamSynchronize(st));
+        };
+        if (dtype == RSVD_DT_F64) run(double{});
+        else if (dtype == RSVD_DT_F32) run(float{});
+        else fail(RSVD_ERR_ARGUMENT, "unknown dtype");
+        end_call(t0);
+    });
+    return rsvdpack_last_error();
+}
+
+int rsvdpack_set_proposal_model(const float *params, int nparams, const float *norm, int nnorm, const float *margin,
+                                int nmargin) {
+    guarded("rsvdpack_set_proposal_model", [&] {
+        int dims[4];
+        mlp_dims(dims);
+        need(params && norm && margin, "null pointer");
+        need(nparams == mlp_param_count(), "parameter count does not match the network");
+        need(nnorm == 2 * dims[0] && nmargin == dims[3], "norm / margin length does not match the network");
+        ProposalModel m;
+        m.params.assign(params, params + nparams);
+        m.norm.assign(norm, norm + nnorm);
+        m.margin.assign(margin, margin + nmargin);
+        set_proposal_model(std::move(m));
+    });
+    return rsvdpack_last_error();
+}
+
+int rsvdpack_load_proposal_model(const char *path) {
+    guarded("rsvdpack_load_proposal_model", [&] {
+        need(path != nullptr, "null path");
+        FILE *fp = std::fopen(path, "rb");
+        if (!fp) fail(RSVD_ERR_ARGUMENT, std::string("cannot open ") + path);
+        std::vector<float> P, N, M;
+        char magic[8];
+        int nd = 0, dims[8] = {0}, np = 0, nn = 0;
+        bool ok = std::fread(magic, 1, 8, fp) == 8 && std::memcmp(magic, "RSVDMLP1", 8) == 0 &&
+                  std::fread(&nd, 4, 1, fp) == 1 && nd >= 2 && nd <= 8 && std::fread(dims, 4, nd, fp) == (size_t)nd &&
+                  std::fread(&np, 4, 1, fp) == 1 && std::fread(&nn, 4, 1, fp) == 1 && np > 0 && np < (1 << 24) &&
+                  nn > 0 && nn < (1 << 16);
+        if (ok) {
+            P.resize(np);
+            N.resize(nn);
+            M.resize(dims[nd - 1]);
+            ok = std::fread(P.data(), 4, np, fp) == (size_t)np && std::fread(N.data(), 4, nn, fp) == (size_t)nn &&
+                 std::fread(M.data(), 4, M.size(), fp) == M.size();
+        }
+        std::fclose(fp);
+        if (!ok) fail(RSVD_ERR_ARGUMENT, std::string("not a valid RSVDMLP1 weights file: ") + path);
+        if (rsvdpack_set_proposal_model(P.data(), np, N.data(), nn, M.data(), (int)M.size()) != RSVD_OK)
+            fail(RSVD_ERR_ARGUMENT, "weights file does not match the network");
+    });
+    return rsvdpack_last_error();
+}
+
+int rsvdpack_mlp_forward(const float *dP, const float *dnorm, const float *dX, int batch, float *dY) {
+    guarded("rsvdpack_mlp_forward", [&] {
+        need(dP && dnorm && dX && dY, "null device pointer");
+        need(batch > 0, "empty batch");
+        begin_call();
+        order_after_default_stream();
+        cudaStream_t st = ctx().stream;
+        mlp_forward(st, dP, dnorm, dX, batch, dY);
+        RSVD_CK(cudaStreamSynchronize(st));
+        check_device_flags(ctx());
+    });
+    return rsvdpack_last_error();
+}
+
+int rsvdpack_mlp_train_step(float *dP, float *dM, float *dV, const float *dnorm, const float *dX, const float *dT,
+                            const float *dReached, int batch, float lr, int step, float *dloss, float *dG) {
+    guarded("rsvdpack_mlp_train_step", [&] {
+        need(dP && dnorm && dX && dT && dReached && dloss && dG, "null device pointer");
+        need(lr <= 0.f || (dM && dV), "Adam state required when lr > 0");
+        need(batch > 0 && step >= 1, "bad batch or step");
+        begin_call();
+        order_after_default_stream();
+        cudaStream_t st = ctx().stream;
+        mlp_train_step(st, dP, dM, dV, dnorm, dX, dT, dReached, batch, lr, step, dloss, dG);
+        RSVD_CK(cudaStreamSynchronize(st));
+        check_device_flags(ctx());
+    });
+    return rsvdpack_last_error();
+}
+
 int rsvdpack_dev_small_svd(double *dG, int n, long long ldg, double *dU, long long ldu, double *dS, double *dV,
                            long long ldv, int fp32) {
     int sweeps = -1;

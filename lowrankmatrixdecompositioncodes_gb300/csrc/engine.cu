@@ -184,6 +184,39 @@ static bool chol_pass_f32(cudaStream_t s, DM<float> Y, DM<float> Q, DM<double> *
     return true;
 }
 
+// One FP32-accurate CholeskyQR pass for wide bases (orders > 288) on the tensor cores:
+// G = Y^T Y by 3xTF32, tiled Cholesky and R^-1 in FP32, and Q = Y R^-1 formed as
+// (R^-T Y^T)^T so that both 3xTF32 operands are K-major.  Rout (optional): R in FP64.
+static bool chol_pass_tc(cudaStream_t s, DM<float> Y, DM<float> Q, DM<double> *Rout, int *flag) {
+    const i64 m = Y.r, w = Y.c, nb = (w + 31) / 32;
+    DMat<float> Gf(w, w, s, false);
+    {
+        DMat<float> Yh(m, w, s, false), Yl(m, w, s, false);
+        split_tf32(s, Y.p, Y.ld, m, w, Yh.v.p, Yl.v.p, Yh.v.ld);
+        tc_gemm_3xtf32(s, Yh.v.p, Yl.v.p, Yh.v.ld, Yh.v.p, Yl.v.p, Yh.v.ld, (int)w, (int)w, (int)m, Gf.v.p, Gf.v.ld);
+        RSVD_CK(cudaStreamSynchronize(s));
+    }
+    DMat<double> G(w, w, s, false);
+    convert<float, double>(s, Gf.v, G.v);
+    DBuf dinv(sizeof(float) * (size_t)nb * 1024, s);
+    if (!chol_factor<float>(s, G.v, chol_tol<float>(), flag, (float *)dinv.get())) return false;
+    if (Rout) copy_dm<double>(s, G.v, *Rout);
+    DMat<float> Ri(w, w, s, false);
+    tri_inv_tiles<float, float>(s, G.v, (const float *)dinv.get(), Ri.v);
+    DMat<float> Yt(w, m, s, false), Qt(w, m, s, false);
+    transpose<float>(s, Y, Yt.v);
+    {
+        DMat<float> Rh(w, w, s, false), Rl(w, w, s, false), Th(w, m, s, false), Tl(w, m, s, false);
+        split_tf32(s, Ri.v.p, Ri.v.ld, w, w, Rh.v.p, Rl.v.p, Rh.v.ld);
+        split_tf32(s, Yt.v.p, Yt.v.ld, w, m, Th.v.p, Tl.v.p, Th.v.ld);
+        tc_gemm_3xtf32(s, Rh.v.p, Rl.v.p, Rh.v.ld, Th.v.p, Tl.v.p, Th.v.ld, (int)w, (int)m, (int)w, Qt.v.p, Qt.v.ld);
+        RSVD_CK(cudaStreamSynchronize(s));
+    }
+    transpose<float>(s, Qt.v, Q);
+    RSVD_CK(cudaStreamSynchronize(s));
+    return true;
+}
+
 // Q = orth(Y) by CholeskyQR (passes = 1: enough for the power-round bases, whose span is
 // all that matters) or CholeskyQR2 (passes = 2: the final bases).  Falls back to
 // Householder QR when a Cholesky factorisation breaks down.  R (optional) receives the
@@ -196,6 +229,20 @@ void orth(DM<T> Y, DM<T> Q, DM<double> *R, int passes) {
     if (Y.r < c) fail(RSVD_ERR_ARGUMENT, "orth: more columns than rows");
     int *flag = cx.d_flags + FLAG_CHOL_BREAKDOWN;
     if constexpr (std::is_same<T, float>::value) {
+        const int prec = cx.opts.precision;
+        if (c > 288 && (prec == RSVD_PREC_TF32 || prec == RSVD_PREC_BF16) && Y.r >= 128) {
+            if (passes < 2) {
+                if (chol_pass_tc(s, Y, Q, R, flag)) return;
+            } else {
+                DMat<float> W(Y.r, c, s, false);
+                DMat<double> R1(R ? c : 1, R ? c : 1, s, false), R2(R ? c : 1, R ? c : 1, s, false);
+                if (chol_pass_tc(s, Y, W.v, R ? &R1.v : nullptr, flag) &&
+                    chol_pass_tc(s, W.v, Q, R ? &R2.v : nullptr, flag)) {
+                    if (R) tri_mul_upper<float>(s, R2.v, R1.v, *R);
+                    return;
+                }
+            }
+        }
         if (c <= 288) {
             if (passes < 2) {
                 if (chol_pass_f32(s, Y, Q, R, flag)) return;
@@ -333,7 +380,7 @@ template SvdOut<float> svd_fixed_rank<float>(DM<float>, int, int, int, int, int)
 
 // ------------------------------------------------------------------ blocked QB (RRA:1576-1801)
 template <typename T>
-QBOut<T> qb_blocked(DM<T> A, int kstep, int nstep, double TOL, int q, int s_) {
+static QBOut<T> qb_plain(DM<T> A, int kstep, int nstep, double TOL, int q, int s_) {
     Ctx &cx = ctx();
     cudaStream_t s = cx.stream;
     const i64 m = A.r, n = A.c, mn = std::min(m, n);
@@ -383,6 +430,213 @@ QBOut<T> qb_blocked(DM<T> A, int kstep, int nstep, double TOL, int q, int s_) {
     }
     RSVD_CK(cudaStreamSynchronize(s));
     return out;
+}
+// ------------------------------------------------------------------ learned proposal
+// Fixed-precision QB (randQB_pb_new in TOL mode) with the block widths and power count set by
+// the learned network from a 32-column probe sketch:
+//   probe   Y0 = A Omega0 (n x 32, FP32 products), R0 = chol(Y0^T Y0); features = log10 of
+//           R0's diagonal relative to ||A||_F, the captured energy, log10 min(m, n),
+//           log10(m / n), log10(TOL / ||A||_F) (the training set's feature_vector);
+//   network 2 outputs = predicted log2(total width / 32) for q = 1, 2 (+ the calibrated
+//           margin); the q with the fewest passes x width is taken;
+//   blocks  the predicted width W is split into nb = ceil((2q+1) log10(||A||_F / TOL) / 2.5)
+//           blocks: a tensor-core (TF32 / BF16) sketch of the deflated matrix resolves ~2.5
+//           decades of its sketched spectrum sigma^(2q+1), so a block must not span more.  Per block: Y = A_res Omega, q power rounds, projection against the
+//           earlier blocks (twice), Q_j = orth(Y), B_j = Q_j^T A_res and A_res -= Q_j B_j by
+//           3xTF32 (FP32-accurate), ||A_res||_F from the update's epilogue.
+//   judge   the loop stops when ||A_res||_F <= TOL (the reference's criterion, exact up to
+//           FP32 rounding); when the proposed width is used up first, it continues with
+//           blocks of the same width, i.e. the adaptive loop is the fallback.
+static constexpr int kProbe = 32, kFeat = 36;
+static constexpr int kTf32 = 0, kEpiUpdate = 1;                          // tc_gemm kind / epilogue codes
+
+static bool learned_qb(DM<float> A, double TOL, QBOut<float> &out, int *q_used) {
+    Ctx &cx = ctx();
+    cudaStream_t s = cx.stream;
+    const ProposalModel *pm = proposal_model();
+    const i64 m = A.r, n = A.c, rmin = std::min(m, n);
+    const double fro = frob_norm<float>(s, A);
+    if (!(fro > 0.0) || !(TOL > 0.0)) return false;
+    // ---- probe
+    std::vector<double> rdiag(kProbe, 0.0);
+    {
+        DMat<float> Om0 = make_omega<float>(n, kProbe);
+        DMat<float> Y0(m, kProbe, s, false);
+        gemm<float>(s, false, false, 1.f, A, Om0.v, 0.f, Y0.v);
+        DMat<double> G0(kProbe, kProbe, s, false);
+        gram<float>(s, Y0.v, G0.v);
+        if (!cholesky_small<double>(s, G0.v, 0.0, cx.d_flags + FLAG_CHOL_BREAKDOWN)) return false;
+        std::vector<double> h((size_t)kProbe * kProbe);
+        RSVD_CK(cudaMemcpy2DAsync(h.data(), sizeof(double) * kProbe, G0.v.p, sizeof(double) * G0.v.ld,
+                                  sizeof(double) * kProbe, kProbe, cudaMemcpyDeviceToHost, s));
+        RSVD_CK(cudaStreamSynchronize(s));
+        for (int j = 0; j < kProbe; j++) rdiag[j] = std::fabs(h[(size_t)j * kProbe + j]);
+    }
+    float feat[kFeat];
+    double energy = 0.0;
+    for (int j = 0; j < kProbe; j++) {
+        const double rel = std::max(rdiag[j] / fro, 1e-30);
+        feat[j] = (float)std::log10(rel);
+        energy += rel * rel;
+    }
+    feat[kProbe] = (float)energy;
+    feat[kProbe + 1] = (float)std::log10((double)rmin);
+    feat[kProbe + 2] = (float)std::log10((double)m / (double)n);
+    feat[kProbe + 3] = (float)std::log10(TOL / fro);
+    // ---- network
+    float pred[2];
+    {
+        DBuf dp(sizeof(float) * pm->params.size(), s), dn(sizeof(float) * pm->norm.size(), s), dx(sizeof(feat), s),
+            dy(sizeof(pred), s);
+        RSVD_CK(cudaMemcpyAsync(dp.get(), pm->params.data(), dp.bytes(), cudaMemcpyHostToDevice, s));
+        RSVD_CK(cudaMemcpyAsync(dn.get(), pm->norm.data(), dn.bytes(), cudaMemcpyHostToDevice, s));
+        RSVD_CK(cudaMemcpyAsync(dx.get(), feat, sizeof(feat), cudaMemcpyHostToDevice, s));
+        mlp_forward(s, (const float *)dp.get(), (const float *)dn.get(), (const float *)dx.get(), 1, (float *)dy.get());
+        RSVD_CK(cudaMemcpyAsync(pred, dy.get(), sizeof(pred), cudaMemcpyDeviceToHost, s));
+        RSVD_CK(cudaStreamSynchronize(s));
+    }
+    int width = 0, q = 1;
+    long long best = -1;
+    for (int j = 0; j < 2; j++) {
+        const int qj = j + 1;
+        const double lw = (double)pred[j] + (double)pm->margin[j];
+        long long w = 32ll * (long long)std::ceil(std::pow(2.0, std::min(lw, 20.0)));
+        w = std::max<long long>(32, std::min<long long>(rmin, w));
+        const long long cost = (2ll * qj + 2) * w;
+        if (best < 0 || cost < best) { best = cost; width = (int)w; q = qj; }
+    }
+    if (cx.opts.verbose)
+        std::fprintf(stderr, "rsvdpack: learned proposal width %d q %d (log2 preds %.3f %.3f)\n", width, q, pred[0],
+                     pred[1]);
+    // ---- blocks on the deflated matrix
+    // a TF32 / BF16 sketch resolves ~2.5 decades of the sketched spectrum sigma^(2q+1), and
+    // the proposed width spans the log10(||A|| / TOL) decades of sigma that the tolerance needs
+    const double tol_rel = TOL / fro;
+    const double decades = -std::log10(std::max(tol_rel, 1e-12));
+    const int nb = std::max(1, (int)std::ceil((2 * q + 1) * decades / 2.5));
+    const int bw = (int)std::min<long long>(rmin, std::max(64ll, 32ll * ((width / nb + 31) / 32)));
+    const int bw_more = bw;
+    DMat<float> Ar(m, n, s, false);                                    // the residual A - Q B
+    copy_dm<float>(s, A, Ar.v);
+    DMat<float> Qall(m, rmin, s, false), Qt(rmin, m, s, false), Ball(rmin, n, s, false);
+    // tc_gemm's grid for an m x n update: 128-row tiles; one column tile up to 512 columns,
+    // else 256-column tiles (one sum of squares per CTA)
+    const i64 mt = (m + 127) / 128, ntl = (n <= 512) ? 1 : (n + 255) / 256;
+    DBuf frob_part(sizeof(double) * (size_t)(mt * ntl + 1024), s);
+    std::vector<double> hpart;
+    int f = 0;
+    double res = fro;
+    int blocks = 0;
+    while (res > TOL && f < rmin) {
+        const int b = (int)std::min<long long>(rmin - f, blocks < nb ? bw : bw_more);
+        DMat<float> Y(m, b, s, false), Yo(m, b, s, false), Z(n, b, s, false), Zo(n, b, s, false);
+        {
+            DMat<float> Om = make_omega<float>(n, b);
+            prod<float>(s, false, false, 1.f, Ar.v, Om.v, 0.f, Y.v);
+        }
+        for (int j = 1; j <= q; j++) {
+            orth<float>(Y.v, Yo.v, nullptr, 1);
+            prod<float>(s, true, false, 1.f, Ar.v, Yo.v, 0.f, Z.v);
+            orth<float>(Z.v, Zo.v, nullptr, 1);
+            prod<float>(s, false, false, 1.f, Ar.v, Zo.v, 0.f, Y.v);
+        }
+        // BCGS2 against the earlier blocks: (orth, project) twice, then CholeskyQR2; the
+        // projections Y^T -= (Q_f^T Y)^T Q_f^T are 3xTF32
+        orth<float>(Y.v, Yo.v, nullptr, f > 0 ? 1 : 2);
+        if (f > 0) {
+            for (int pass = 0; pass < 2; pass++) {
+                DMat<float> P(f, b, s, false), Yt(b, m, s, false);
+                {
+                    DMat<float> Qh(m, f, s, false), Ql(m, f, s, false), Yh(m, b, s, false), Yl(m, b, s, false);
+                    split_tf32(s, Qall.v.p, Qall.v.ld, m, f, Qh.v.p, Ql.v.p, Qh.v.ld);
+                    split_tf32(s, Yo.v.p, Yo.v.ld, m, b, Yh.v.p, Yl.v.p, Yh.v.ld);
+                    tc_gemm_3xtf32(s, Qh.v.p, Ql.v.p, Qh.v.ld, Yh.v.p, Yl.v.p, Yh.v.ld, f, b, (int)m, P.v.p, P.v.ld);
+                    RSVD_CK(cudaStreamSynchronize(s));
+                }
+                transpose<float>(s, Yo.v, Yt.v);
+                {
+                    DMat<float> Ph(f, b, s, false), Pl(f, b, s, false), Th(f, m, s, false), Tl(f, m, s, false);
+                    split_tf32(s, P.v.p, P.v.ld, f, b, Ph.v.p, Pl.v.p, Ph.v.ld);
+                    split_tf32(s, Qt.v.p, Qt.v.ld, f, m, Th.v.p, Tl.v.p, Th.v.ld);
+                    // Yt (b x m) = Yt - P^T Q_f^T : A^T X form with A = P (K = f), X = Q_f^T (K = f)
+                    tc_gemm(s, kTf32, false, Ph.v.p, Ph.v.ld, Th.v.p, Th.v.ld, b, (int)m, f, 1.f, Yt.v.p,
+                            Yt.v.ld, kEpiUpdate, Yt.v.p, Yt.v.ld, nullptr, 1);
+                    tc_gemm(s, kTf32, false, Pl.v.p, Pl.v.ld, Th.v.p, Th.v.ld, b, (int)m, f, 1.f, Yt.v.p,
+                            Yt.v.ld, kEpiUpdate, Yt.v.p, Yt.v.ld, nullptr, 1);
+                    tc_gemm(s, kTf32, false, Ph.v.p, Ph.v.ld, Tl.v.p, Tl.v.ld, b, (int)m, f, 1.f, Yt.v.p,
+                            Yt.v.ld, kEpiUpdate, Yt.v.p, Yt.v.ld, nullptr, 1);
+                    RSVD_CK(cudaStreamSynchronize(s));
+                }
+                transpose<float>(s, Yt.v, Y.v);
+                orth<float>(Y.v, Yo.v, nullptr, pass == 0 ? 1 : 2);
+            }
+        }
+        DM<float> Qj = Qall.v.cols(f, b);
+        copy_dm<float>(s, Yo.v, Qj);
+        DM<float> Qtj = Qt.v.sub(f, 0, b, m);
+        transpose<float>(s, Qj, Qtj);
+        // B_j (b x n) = Q_j^T A_res, as B_j^T = A_res^T Q_j (3xTF32)
+        DM<float> Bj = Ball.v.sub(f, 0, b, n);
+        {
+            DMat<float> Ah(m, n, s, false), Al(m, n, s, false), Qh(m, b, s, false), Ql(m, b, s, false);
+            split_tf32(s, Ar.v.p, Ar.v.ld, m, n, Ah.v.p, Al.v.p, Ah.v.ld);
+            split_tf32(s, Qj.p, Qj.ld, m, b, Qh.v.p, Ql.v.p, Qh.v.ld);
+            DMat<float> Bt(n, b, s, false);
+            tc_gemm_3xtf32(s, Ah.v.p, Al.v.p, Ah.v.ld, Qh.v.p, Ql.v.p, Qh.v.ld, (int)n, b, (int)m, Bt.v.p, Bt.v.ld);
+            transpose<float>(s, Bt.v, Bj);
+            RSVD_CK(cudaStreamSynchronize(s));
+        }
+        // A_res -= Q_j B_j (3xTF32, in place) with per-CTA sums of squares of the result
+        {
+            DMat<float> Th(b, m, s, false), Tl(b, m, s, false), Bh(b, n, s, false), Bl(b, n, s, false);
+            split_tf32(s, Qtj.p, Qtj.ld, b, m, Th.v.p, Tl.v.p, Th.v.ld);
+            split_tf32(s, Bj.p, Bj.ld, b, n, Bh.v.p, Bl.v.p, Bh.v.ld);
+            tc_gemm(s, kTf32, false, Th.v.p, Th.v.ld, Bh.v.p, Bh.v.ld, (int)m, (int)n, b, 1.f, Ar.v.p, Ar.v.ld,
+                    kEpiUpdate, Ar.v.p, Ar.v.ld, nullptr, 1);
+            tc_gemm(s, kTf32, false, Tl.v.p, Tl.v.ld, Bh.v.p, Bh.v.ld, (int)m, (int)n, b, 1.f, Ar.v.p, Ar.v.ld,
+                    kEpiUpdate, Ar.v.p, Ar.v.ld, nullptr, 1);
+            tc_gemm(s, kTf32, false, Th.v.p, Th.v.ld, Bl.v.p, Bl.v.ld, (int)m, (int)n, b, 1.f, Ar.v.p, Ar.v.ld,
+                    kEpiUpdate, Ar.v.p, Ar.v.ld, (double *)frob_part.get(), 1);
+            release_operand_cache();                                     // A_res changed
+            hpart.resize((size_t)(mt * ntl));
+            RSVD_CK(cudaMemcpyAsync(hpart.data(), frob_part.get(), sizeof(double) * hpart.size(),
+                                    cudaMemcpyDeviceToHost, s));
+            RSVD_CK(cudaStreamSynchronize(s));
+        }
+        double ss = 0.0;
+        for (double v : hpart) ss += v;
+        res = std::sqrt(ss);
+        f += b;
+        blocks++;
+        if (cx.opts.verbose)
+            std::fprintf(stderr, "rsvdpack: learned QB block %d width %d rank %d residual %.3e (TOL %.3e)\n", blocks,
+                         b, f, res, TOL);
+    }
+    out.Q = std::move(Qall);
+    out.B = std::move(Ball);
+    out.Q.v.c = f;
+    out.B.v.r = f;
+    out.frank = f;
+    *q_used = q;
+    return res <= TOL;
+}
+
+template <typename T>
+QBOut<T> qb_blocked(DM<T> A, int kstep, int nstep, double TOL, int q, int s_) {
+    Ctx &cx = ctx();
+    cx.timing.learned_path = 0;
+    if constexpr (std::is_same<T, float>::value) {
+        if (nstep <= 0 && cx.opts.learned && proposal_model() != nullptr) {
+            QBOut<float> out;
+            int q_used = 0;
+            if (learned_qb(A, TOL, out, &q_used)) {
+                cx.timing.learned_path = 1;
+                return out;
+            }
+            cx.timing.learned_path = 2;                                   // fell back
+        }
+    }
+    return qb_plain<T>(A, kstep, nstep, TOL, q, s_);
 }
 template QBOut<double> qb_blocked<double>(DM<double>, int, int, double, int, int);
 template QBOut<float> qb_blocked<float>(DM<float>, int, int, double, int, int);

@@ -306,9 +306,9 @@ __global__ void splitk_reduce_kernel(const float *part, long long stride, int sp
     const long long total = (long long)M * N;
     for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total; e += (long long)gridDim.x * blockDim.x) {
         const long long i = e % M, j = e / M;
-        float acc = 0.f;
-        for (int z = 0; z < splits; z++) acc += part[z * stride + i + j * ldp];
-        D[i + j * ldd] = alpha * acc;
+        double acc = 0.0;                        // FP64 sum of the FP32 partial sums
+        for (int z = 0; z < splits; z++) acc += (double)part[z * stride + i + j * ldp];
+        D[i + j * ldd] = (float)((double)alpha * acc);
     }
 }
 
@@ -357,7 +357,12 @@ static void launch(cudaStream_t s, dim3 grid, size_t smem, const CUtensorMap &ta
     auto k = tc_gemm_kernel<KIND, A_MN, EPI>;
     static bool attr_set = false;   // per instantiation
     if (!attr_set) {
-        RSVD_CK(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, 232448));
+        // 227 KB per CTA in total: the dynamic part is what the kernel's static shared
+        // memory (the update epilogue's reduction scratch) leaves
+        cudaFuncAttributes fa{};
+        RSVD_CK(cudaFuncGetAttributes(&fa, k));
+        RSVD_CK(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     232448 - (int)fa.sharedSizeBytes));
         attr_set = true;
     }
     k<<<grid, NTHR, smem, s>>>(ta, tb, P);
@@ -596,4 +601,46 @@ extern "C" int rsvdpack_dev_sketch_t_noalloc(const float *dA, long long lda, int
 }
 
 namespace rsvd {
+
+// ---------------------------------------------------------------- 3xTF32 products
+// FP32-accurate products on the tf32 tensor pipe: x = hi + lo with hi = x rounded to TF32
+// (10 mantissa bits, representable exactly, so the MMA's operand conversion leaves it
+// unchanged) and lo = x - hi (exact in FP32); A^T X = hi_A^T hi_X + lo_A^T hi_X + hi_A^T lo_X,
+// the dropped lo_A^T lo_X term and the TF32 rounding of lo being ~2^-22 relative.
+namespace {
+__global__ void split_tf32_kernel(const float *X, long long ldx, long long r, long long c, float *hi, float *lo,
+                                  long long ldo) {
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < r * c;
+         e += (long long)gridDim.x * blockDim.x) {
+        const long long j = e / r, i = e - j * r;
+        const float x = X[i + j * ldx];
+        const float h = __uint_as_float((__float_as_uint(x) + 0x1000u) & 0xFFFFE000u);
+        hi[i + j * ldo] = h;
+        lo[i + j * ldo] = x - h;
+    }
+}
+}  // namespace
+
+void split_tf32(cudaStream_t s, const float *X, long long ldx, long long r, long long c, float *hi, float *lo,
+                long long ldo) {
+    if (r * c == 0) return;
+    const long long want = (r * c + 255) / 256, cap = (long long)std::max(1, ctx().sms) * 16;
+    split_tf32_kernel<<<(unsigned)std::min(want, cap), 256, 0, s>>>(X, ldx, r, c, hi, lo, ldo);
+    RSVD_LAUNCH_CK();
+    ctx().launches++;
+}
+
+// D (M x N) = A^T X with A K-major (K x M, lda) and X (K x N, ldx), both given split.
+// The leading hi^T hi product is split along K into chunks of ~2048 (FP32 accumulation in
+// TMEM within a chunk, FP64 across chunks), so its accumulation error does not grow with K.
+void tc_gemm_3xtf32(cudaStream_t s, const float *Ahi, const float *Alo, long long lda, const float *Xhi,
+                    const float *Xlo, long long ldx, int M, int N, int K, float *D, long long ldd) {
+    const int splits = std::max(1, std::min(32, K / 2048));
+    tc_gemm(s, tc::KIND_TF32, false, Ahi, lda, Xhi, ldx, M, N, K, 1.0f, D, ldd, tc::EPI_STORE, nullptr, 0, nullptr,
+            splits);
+    // D = D - (-1) * (lo_A^T hi_X), then the hi_A^T lo_X term
+    tc_gemm(s, tc::KIND_TF32, false, Alo, lda, Xhi, ldx, M, N, K, -1.0f, D, ldd, tc::EPI_UPDATE, D, ldd, nullptr, 1);
+    tc_gemm(s, tc::KIND_TF32, false, Ahi, lda, Xlo, ldx, M, N, K, -1.0f, D, ldd, tc::EPI_UPDATE, D, ldd, nullptr, 1);
+}
+
 }  // namespace rsvd

@@ -94,6 +94,13 @@ struct Ctx {
 };
 Ctx &ctx();                       // initialises the device on first use; throws RSVD_ERR_NO_DEVICE
 const rsvdpack_opts &global_opts();
+
+// The learned proposal's network (host copy; null when none is installed).
+struct ProposalModel {
+    std::vector<float> params, norm, margin;
+};
+const ProposalModel *proposal_model();
+void set_proposal_model(ProposalModel m);
 void check_device_flags(Ctx &c);  // throws if a kernel reported a timeout / breakdown
 
 // Gaussian test-matrix provider (host side).
@@ -178,6 +185,12 @@ namespace rsvd {
 void tc_gemm(cudaStream_t s, int kind, bool a_mn, const void *A, long long lda, const void *X, long long ldx,
              int M, int N, int K, float alpha, float *D, long long ldd, int epi, const float *C, long long ldc,
              double *fro_part, int splits_hint);
+// 3xTF32 (FP32-accurate) products on the tf32 pipe: split_tf32 writes hi = tf32(X) and
+// lo = X - hi; tc_gemm_3xtf32 computes D = A^T X (A K-major, K x M) from split operands.
+void split_tf32(cudaStream_t s, const float *X, long long ldx, long long r, long long c, float *hi, float *lo,
+                long long ldo);
+void tc_gemm_3xtf32(cudaStream_t s, const float *Ahi, const float *Alo, long long lda, const float *Xhi,
+                    const float *Xlo, long long ldx, int M, int N, int K, float *D, long long ldd);
 // ----------------------------------------------------------------- tiled triangular steps (k_chol.cu)
 // G (n x n, FP64, upper triangle read) -> R, G = R^T R (upper, zero below), compute type S.
 // dinv (optional): receives the inverses of R's 32 x 32 diagonal tiles (ceil(n/32) row-major
@@ -199,6 +212,15 @@ bool trsm_right_tiles(cudaStream_t s, DM<T> Y, DM<double> R, const T *dinv, DM<T
 void gram_tiles_f32(cudaStream_t s, DM<float> Y, float *Gt, DM<double> *G);
 bool chol_tiles_f32(cudaStream_t s, float *Gt, int n, double rel_tol, int *d_flag, float *dinv, DM<double> *Rout);
 void trsm_right_tiles_f32(cudaStream_t s, DM<float> Y, int n, const float *Rt, const float *dinv, DM<float> Q);
+}  // namespace rsvd
+
+namespace rsvd {
+// ----------------------------------------------------------------- learned proposal MLP (k_mlp.cu)
+int mlp_param_count();
+void mlp_dims(int *d);                                      // 4 layer widths
+void mlp_forward(cudaStream_t s, const float *P, const float *norm, const float *X, int B, float *Y);
+void mlp_train_step(cudaStream_t s, float *P, float *M, float *V, const float *norm, const float *X, const float *T,
+                    const float *reached, int B, float lr, int step, float *loss, float *G);
 }  // namespace rsvd
 
 namespace rsvd {

@@ -5,6 +5,7 @@
 
 #include <cstdlib>
 #include <cstring>
+#include <memory>
 #include <mutex>
 #include <string>
 
@@ -59,6 +60,20 @@ const rsvdpack_opts &global_opts() {
     std::lock_guard<std::mutex> g(g_opts_mu);
     init_opts_locked();
     return g_opts;
+}
+
+namespace {
+std::mutex g_model_mu;
+std::unique_ptr<ProposalModel> g_model;
+}  // namespace
+
+const ProposalModel *proposal_model() {
+    std::lock_guard<std::mutex> g(g_model_mu);
+    return g_model.get();
+}
+void set_proposal_model(ProposalModel m) {
+    std::lock_guard<std::mutex> g(g_model_mu);
+    g_model.reset(new ProposalModel(std::move(m)));
 }
 
 // ------------------------------------------------------------------ provider
