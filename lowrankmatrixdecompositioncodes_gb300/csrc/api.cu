@@ -11,6 +11,10 @@
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
+#include <thread>
+#include <vector>
+
+#include <sys/mman.h>
 
 using namespace rsvd;
 
@@ -66,23 +70,84 @@ DMat<T> upload(const mat *M) {
     return A;
 }
 
+// An output matrix the engine overwrites entirely: same ownership as matrix_new (freed
+// with matrix_delete / free), but for large sizes 2 MB aligned with a transparent-huge-page
+// hint and not zeroed, so that filling it costs a few page faults instead of one per 4 KB.
+mat *matrix_new_output(int nrows, int ncols) {
+    const size_t bytes = sizeof(double) * (size_t)std::max(nrows, 0) * (size_t)std::max(ncols, 0);
+    if (bytes < ((size_t)4 << 20)) return matrix_new(nrows, ncols);
+    mat *M = (mat *)std::malloc(sizeof(mat));
+    if (!M) return nullptr;
+    void *p = nullptr;
+    const size_t align = (size_t)2 << 20;
+    if (posix_memalign(&p, align, (bytes + align - 1) / align * align) != 0) {
+        std::free(M);
+        return nullptr;
+    }
+    madvise(p, (bytes + align - 1) / align * align, MADV_HUGEPAGE);
+    M->nrows = nrows;
+    M->ncols = ncols;
+    M->d = (double *)p;
+    return M;
+}
+
+// Pinned host staging for device-to-host copies (per thread, grown on demand).
+struct PinnedStage {
+    void *p = nullptr;
+    size_t n = 0;
+    ~PinnedStage() {
+        if (p) cudaFreeHost(p);
+    }
+    void *get(size_t bytes) {
+        if (bytes > n) {
+            if (p) RSVD_CK(cudaFreeHost(p));
+            p = nullptr;
+            n = 0;
+            RSVD_CK(cudaHostAlloc(&p, bytes, cudaHostAllocDefault));
+            n = bytes;
+        }
+        return p;
+    }
+};
+thread_local PinnedStage t_stage;
+
+// Host copy from the pinned stage into the (pageable) output, split over a few threads.
+void parallel_copy(double *dst, const double *src, size_t count) {
+    const size_t bytes = count * sizeof(double);
+    const int nt = bytes < ((size_t)8 << 20) ? 1 : 8;
+    if (nt == 1) {
+        std::memcpy(dst, src, bytes);
+        return;
+    }
+    std::vector<std::thread> th;
+    const size_t per = (count + nt - 1) / nt;
+    for (int t = 0; t < nt; t++) {
+        const size_t a = std::min(count, (size_t)t * per), b = std::min(count, a + per);
+        if (a < b) th.emplace_back([=] { std::memcpy(dst + a, src + a, (b - a) * sizeof(double)); });
+    }
+    for (auto &x : th) x.join();
+}
+
 template <typename T>
 mat *download(DM<T> a) {
     cudaStream_t s = ctx().stream;
-    mat *M = matrix_new((int)a.r, (int)a.c);
+    mat *M = matrix_new_output((int)a.r, (int)a.c);
     if (!M) throw std::bad_alloc();
     if (a.r * a.c == 0) return M;
+    const size_t count = (size_t)a.r * (size_t)a.c;
+    double *stage = (double *)t_stage.get(sizeof(double) * count);
     if (std::is_same<T, double>::value) {
-        RSVD_CK(cudaMemcpy2DAsync(M->d, sizeof(double) * a.r, a.p, sizeof(T) * a.ld, sizeof(double) * a.r, a.c,
+        RSVD_CK(cudaMemcpy2DAsync(stage, sizeof(double) * a.r, a.p, sizeof(T) * a.ld, sizeof(double) * a.r, a.c,
                                   cudaMemcpyDeviceToHost, s));
+        RSVD_CK(cudaStreamSynchronize(s));
     } else {
         DMat<double> tmp(a.r, a.c, s, false);
         convert<T, double>(s, a, tmp.v);
-        RSVD_CK(cudaMemcpy2DAsync(M->d, sizeof(double) * a.r, tmp.v.p, sizeof(double) * tmp.v.ld,
+        RSVD_CK(cudaMemcpy2DAsync(stage, sizeof(double) * a.r, tmp.v.p, sizeof(double) * tmp.v.ld,
                                   sizeof(double) * a.r, a.c, cudaMemcpyDeviceToHost, s));
         RSVD_CK(cudaStreamSynchronize(s));
     }
-    RSVD_CK(cudaStreamSynchronize(s));
+    parallel_copy(M->d, stage, count);
     return M;
 }
 

@@ -262,7 +262,44 @@ __global__ void __launch_bounds__(NTHR, 1)
     tc_fence_after();
     const int row = m0 + warp * 32 + lane;
     double fro = 0.0;
-    if (ok) {
+    if (ok && EPI == EPI_UPDATE) {
+        // C may alias D: each 16-column group of C is loaded into registers before any of
+        // that group's stores, and the next group's loads are issued before this group is
+        // stored, so a thread keeps 16 loads in flight instead of one
+        const bool rv = row < P.M;
+        const bool want_fro = P.fro_part != nullptr;
+        float cnext[16];
+        auto load_c = [&](int c0, float (&cv)[16]) {
+#pragma unroll
+            for (int t = 0; t < 16; t++) {
+                const int col = n0 + c0 + t;
+                cv[t] = (rv && col < P.N) ? P.C[(long long)row + (long long)col * P.ldc] : 0.f;
+            }
+        };
+        load_c(0, cnext);
+        for (int c0 = 0; c0 < P.BN; c0 += 16) {
+            float cv[16], v[16];
+#pragma unroll
+            for (int t = 0; t < 16; t++) cv[t] = cnext[t];
+            if (nkb > 0) tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, v);
+            else {
+#pragma unroll
+                for (int t = 0; t < 16; t++) v[t] = 0.f;
+            }
+            if (c0 + 16 < P.BN) load_c(c0 + 16, cnext);
+            if (rv) {
+#pragma unroll
+                for (int t = 0; t < 16; t++) {
+                    const int col = n0 + c0 + t;
+                    if (col < P.N) {
+                        const float nv = cv[t] - P.alpha * v[t];
+                        P.D[(long long)row + (long long)col * P.ldd] = nv;
+                        if (want_fro) fro += (double)nv * (double)nv;
+                    }
+                }
+            }
+        }
+    } else if (ok) {
         for (int c0 = 0; c0 < P.BN; c0 += 16) {
             float v[16];
             if (nkb > 0) tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, v);
@@ -621,6 +658,16 @@ __global__ void split_tf32_kernel(const float *X, long long ldx, long long r, lo
 }
 }  // namespace
 
+namespace {
+__global__ void add2_kernel(float *D, long long ldd, const float *T1, const float *T2, long long ldt, int M, int N) {
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < (long long)M * N;
+         e += (long long)gridDim.x * blockDim.x) {
+        const long long j = e / M, i = e - j * M;
+        D[i + j * ldd] += T1[i + j * ldt] + T2[i + j * ldt];
+    }
+}
+}  // namespace
+
 void split_tf32(cudaStream_t s, const float *X, long long ldx, long long r, long long c, float *hi, float *lo,
                 long long ldo) {
     if (r * c == 0) return;
@@ -631,16 +678,26 @@ void split_tf32(cudaStream_t s, const float *X, long long ldx, long long r, long
 }
 
 // D (M x N) = A^T X with A K-major (K x M, lda) and X (K x N, ldx), both given split.
-// The leading hi^T hi product is split along K into chunks of ~2048 (FP32 accumulation in
-// TMEM within a chunk, FP64 across chunks), so its accumulation error does not grow with K.
+// All three products are split along K into chunks of ~2048 (FP32 accumulation in TMEM
+// within a chunk, FP64 across chunks), so neither the accumulation error nor the CTA count
+// is limited by a long K; the two correction terms go to temporaries and one elementwise
+// pass adds them.
 void tc_gemm_3xtf32(cudaStream_t s, const float *Ahi, const float *Alo, long long lda, const float *Xhi,
                     const float *Xlo, long long ldx, int M, int N, int K, float *D, long long ldd) {
     const int splits = std::max(1, std::min(32, K / 2048));
+    const long long ldt = ((long long)M + 31) / 32 * 32;
+    DBuf t1(sizeof(float) * (size_t)ldt * N, s), t2(sizeof(float) * (size_t)ldt * N, s);
     tc_gemm(s, tc::KIND_TF32, false, Ahi, lda, Xhi, ldx, M, N, K, 1.0f, D, ldd, tc::EPI_STORE, nullptr, 0, nullptr,
             splits);
-    // D = D - (-1) * (lo_A^T hi_X), then the hi_A^T lo_X term
-    tc_gemm(s, tc::KIND_TF32, false, Alo, lda, Xhi, ldx, M, N, K, -1.0f, D, ldd, tc::EPI_UPDATE, D, ldd, nullptr, 1);
-    tc_gemm(s, tc::KIND_TF32, false, Ahi, lda, Xlo, ldx, M, N, K, -1.0f, D, ldd, tc::EPI_UPDATE, D, ldd, nullptr, 1);
+    tc_gemm(s, tc::KIND_TF32, false, Alo, lda, Xhi, ldx, M, N, K, 1.0f, (float *)t1.get(), ldt, tc::EPI_STORE,
+            nullptr, 0, nullptr, splits);
+    tc_gemm(s, tc::KIND_TF32, false, Ahi, lda, Xlo, ldx, M, N, K, 1.0f, (float *)t2.get(), ldt, tc::EPI_STORE,
+            nullptr, 0, nullptr, splits);
+    const long long want = ((long long)M * N + 255) / 256, cap = (long long)std::max(1, ctx().sms) * 16;
+    add2_kernel<<<(unsigned)std::min(want, cap), 256, 0, s>>>(D, ldd, (const float *)t1.get(),
+                                                               (const float *)t2.get(), ldt, M, N);
+    RSVD_LAUNCH_CK();
+    ctx().launches++;
 }
 
 }  // namespace rsvd
