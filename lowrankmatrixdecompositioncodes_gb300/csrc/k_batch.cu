@@ -82,80 +82,139 @@ __device__ void gen_omega(float *Bsm, int n, int l, uint64_t seed, uint64_t offs
     }
 }
 
+// Register tiles of the two per-item products: thread t owns 4 consecutive rows (t / 16)
+// and the columns c = t % 16 + 16 u, u < 5 (l <= 80), so that one 16-byte load of A and five
+// broadcast loads of B feed 20 FMAs; the next chunk of A is prefetched into registers while
+// the current one is multiplied.
+constexpr int ATP = 68;          // pitch of a staged A chunk (64 values + 4, 16-byte rows)
+constexpr int CU = 5;            // column groups per thread: l <= 16 * CU
+
 // Y (m x l, ldy) = A (m x n) * B, B row-major in shared memory (B[j*l + c]).
-// 64-row tiles of A staged 32 columns at a time; thread -> (row, column group of 4).
+// Row tiles of 64; A chunks of 64 rows x 32 columns staged as At[jj][row] (pitch ATP).
 __device__ void gemm_A_B(const float *A, long long lda, int m, int n, const float *Bsm, int l, float *Y, long long ldy,
                          float *At) {
-    const int tid = threadIdx.x, row = tid & 63, grp = tid >> 6;   // 4 groups
-    constexpr int MAXC = 20;                                         // l <= 4 * 20 = 80
+    const int tid = threadIdx.x, rg = (tid >> 4) * 4, cg = tid & 15;
     for (int r0 = 0; r0 < m; r0 += 64) {
-        float acc[MAXC];
+        float acc[4][CU];
 #pragma unroll
-        for (int u = 0; u < MAXC; u++) acc[u] = 0.f;
+        for (int a = 0; a < 4; a++)
+#pragma unroll
+            for (int u = 0; u < CU; u++) acc[a][u] = 0.f;
+        float pre[8];
+        auto fetch = [&](int j0) {
+#pragma unroll
+            for (int t = 0; t < 8; t++) {
+                const int e = tid + BT * t, rr = e & 63, jj = e >> 6;
+                pre[t] = (r0 + rr < m && j0 + jj < n) ? A[(r0 + rr) + (long long)(j0 + jj) * lda] : 0.f;
+            }
+        };
+        fetch(0);
         for (int j0 = 0; j0 < n; j0 += 32) {
             __syncthreads();
-            for (int e = tid; e < 64 * 32; e += BT) {
-                const int rr = e & 63, jj = e >> 6;
-                At[jj * 64 + rr] = (r0 + rr < m && j0 + jj < n) ? A[(r0 + rr) + (long long)(j0 + jj) * lda] : 0.f;
+#pragma unroll
+            for (int t = 0; t < 8; t++) {
+                const int e = tid + BT * t;
+                At[(e >> 6) * ATP + (e & 63)] = pre[t];
             }
             __syncthreads();
+            if (j0 + 32 < n) fetch(j0 + 32);
             const int jn = min(32, n - j0);
             for (int jj = 0; jj < jn; jj++) {
-                const float a = At[jj * 64 + row];
+                const float4 a4 = *reinterpret_cast<const float4 *>(At + jj * ATP + rg);
+                const float av[4] = {a4.x, a4.y, a4.z, a4.w};
                 const float *b = Bsm + (size_t)(j0 + jj) * l;
+                float bv[CU];
 #pragma unroll
-                for (int u = 0; u < MAXC; u++) {
-                    const int c = grp + 4 * u;
-                    if (c < l) acc[u] = fmaf(a, b[c], acc[u]);
+                for (int u = 0; u < CU; u++) {
+                    const int c = cg + 16 * u;
+                    bv[u] = (c < l) ? b[c] : 0.f;
                 }
+#pragma unroll
+                for (int a = 0; a < 4; a++)
+#pragma unroll
+                    for (int u = 0; u < CU; u++) acc[a][u] = fmaf(av[a], bv[u], acc[a][u]);
             }
         }
-        if (r0 + row < m) {
 #pragma unroll
-            for (int u = 0; u < MAXC; u++) {
-                const int c = grp + 4 * u;
-                if (c < l) Y[(r0 + row) + (long long)c * ldy] = acc[u];
+        for (int a = 0; a < 4; a++) {
+            const int r = r0 + rg + a;
+            if (r < m) {
+#pragma unroll
+                for (int u = 0; u < CU; u++) {
+                    const int c = cg + 16 * u;
+                    if (c < l) Y[r + (long long)c * ldy] = acc[a][u];
+                }
             }
         }
     }
     __syncthreads();
 }
 
-// Z (n x l, ldz) = A^T (n x m) * Q (m x l, ldq, global).  32-column tiles of A; Q rows staged.
+// Z (n x l, ldz) = A^T (n x m) * Q (m x l, ldq, global).  Column tiles of 64 (thread: 4
+// columns of A); row chunks of 32 staged as At[ii][col] (pitch ATP) and Qs[ii][c].
 __device__ void gemm_At_Q(const float *A, long long lda, int m, int n, const float *Q, long long ldq, int l, float *Z,
                           long long ldz, float *At, float *Qs) {
-    const int tid = threadIdx.x, col = tid & 31, grp = tid >> 5;    // 8 groups
-    constexpr int MAXC = 10;                                          // l <= 8 * 10 = 80
-    for (int j0 = 0; j0 < n; j0 += 32) {
-        float acc[MAXC];
+    const int tid = threadIdx.x, jg = (tid >> 4) * 4, cg = tid & 15;
+    for (int j0 = 0; j0 < n; j0 += 64) {
+        float acc[4][CU];
 #pragma unroll
-        for (int u = 0; u < MAXC; u++) acc[u] = 0.f;
+        for (int a = 0; a < 4; a++)
+#pragma unroll
+            for (int u = 0; u < CU; u++) acc[a][u] = 0.f;
+        float pa[8], pq[10];
+        auto fetch = [&](int i0) {
+#pragma unroll
+            for (int t = 0; t < 8; t++) {
+                const int e = tid + BT * t, ii = e & 31, jj = e >> 5;
+                pa[t] = (i0 + ii < m && j0 + jj < n) ? A[(i0 + ii) + (long long)(j0 + jj) * lda] : 0.f;
+            }
+#pragma unroll
+            for (int t = 0; t < 10; t++) {
+                const int e = tid + BT * t, ii = e & 31, c = e >> 5;
+                pq[t] = (c < l && i0 + ii < m) ? Q[(i0 + ii) + (long long)c * ldq] : 0.f;
+            }
+        };
+        fetch(0);
         for (int i0 = 0; i0 < m; i0 += 32) {
             __syncthreads();
-            for (int e = tid; e < 32 * 32; e += BT) {
-                const int ii = e & 31, jj = e >> 5;
-                At[jj * 33 + ii] = (i0 + ii < m && j0 + jj < n) ? A[(i0 + ii) + (long long)(j0 + jj) * lda] : 0.f;
+#pragma unroll
+            for (int t = 0; t < 8; t++) {
+                const int e = tid + BT * t;
+                At[(e & 31) * ATP + (e >> 5)] = pa[t];
             }
-            for (int e = tid; e < 32 * l; e += BT) {
-                const int ii = e % 32, c = e / 32;
-                Qs[ii * l + c] = (i0 + ii < m) ? Q[(i0 + ii) + (long long)c * ldq] : 0.f;
+#pragma unroll
+            for (int t = 0; t < 10; t++) {
+                const int e = tid + BT * t, c = e >> 5;
+                if (c < l) Qs[(e & 31) * l + c] = pq[t];
             }
             __syncthreads();
-            for (int ii = 0; ii < 32; ii++) {
-                const float a = At[col * 33 + ii];
+            if (i0 + 32 < m) fetch(i0 + 32);
+            const int in = min(32, m - i0);
+            for (int ii = 0; ii < in; ii++) {
+                const float4 a4 = *reinterpret_cast<const float4 *>(At + ii * ATP + jg);
+                const float av[4] = {a4.x, a4.y, a4.z, a4.w};
                 const float *qr = Qs + ii * l;
+                float bv[CU];
 #pragma unroll
-                for (int u = 0; u < MAXC; u++) {
-                    const int c = grp + 8 * u;
-                    if (c < l) acc[u] = fmaf(a, qr[c], acc[u]);
+                for (int u = 0; u < CU; u++) {
+                    const int c = cg + 16 * u;
+                    bv[u] = (c < l) ? qr[c] : 0.f;
                 }
+#pragma unroll
+                for (int a = 0; a < 4; a++)
+#pragma unroll
+                    for (int u = 0; u < CU; u++) acc[a][u] = fmaf(av[a], bv[u], acc[a][u]);
             }
         }
-        if (j0 + col < n) {
 #pragma unroll
-            for (int u = 0; u < MAXC; u++) {
-                const int c = grp + 8 * u;
-                if (c < l) Z[(j0 + col) + (long long)c * ldz] = acc[u];
+        for (int a = 0; a < 4; a++) {
+            const int j = j0 + jg + a;
+            if (j < n) {
+#pragma unroll
+                for (int u = 0; u < CU; u++) {
+                    const int c = cg + 16 * u;
+                    if (c < l) Z[j + (long long)c * ldz] = acc[a][u];
+                }
             }
         }
     }
@@ -164,46 +223,53 @@ __device__ void gemm_At_Q(const float *A, long long lda, int m, int n, const flo
 
 // G (l x l, shared, ldg = l) = Y^T Y for Y (rows x l) in global; 32-row chunks staged.
 __device__ void gram_cta(const float *Y, long long ldy, int rows, int l, float *G, float *Ys) {
+    // upper 4 x 4 tiles of G, one per thread (l <= 80: at most 210 tiles); 32-row chunks of Y
+    // staged row-major (Ys[row * LP + col]) so a tile row is two 16-byte loads for 16 FMAs
     const int tid = threadIdx.x;
-    const int npairs = l * (l + 1) / 2;
-    constexpr int MAXP = 12;                                          // npairs <= 256 * 12
-    float acc[MAXP];
-    int pa[MAXP], pb[MAXP];
+    const int ng = (l + 3) / 4, LP = 4 * ng;
+    const int ntile = ng * (ng + 1) / 2;
+    const bool act = tid < ntile;
+    int gj = 0;
+    if (act)
+        while ((gj + 1) * (gj + 2) / 2 <= tid) gj++;
+    const int gi = act ? tid - gj * (gj + 1) / 2 : 0;
+    float acc[4][4];
 #pragma unroll
-    for (int u = 0; u < MAXP; u++) {
-        acc[u] = 0.f;
-        const int e = tid + BT * u;
-        int b = 0;
-        if (e < npairs) {
-            while ((b + 1) * (b + 2) / 2 <= e) b++;
-        }
-        pb[u] = b;
-        pa[u] = e - b * (b + 1) / 2;
-    }
+    for (int a = 0; a < 4; a++)
+#pragma unroll
+        for (int c = 0; c < 4; c++) acc[a][c] = 0.f;
     for (int r0 = 0; r0 < rows; r0 += 32) {
         __syncthreads();
-        for (int e = tid; e < 32 * l; e += BT) {
-            const int rr = e % 32, c = e / 32;
-            Ys[c * 33 + rr] = (r0 + rr < rows) ? Y[(r0 + rr) + (long long)c * ldy] : 0.f;
+        for (int e = tid; e < 32 * LP; e += BT) {
+            const int rr = e & 31, c = e >> 5;
+            Ys[rr * LP + c] = (r0 + rr < rows && c < l) ? Y[(r0 + rr) + (long long)c * ldy] : 0.f;
         }
         __syncthreads();
+        if (act) {
+            const int rn = min(32, rows - r0);
+            for (int rr = 0; rr < rn; rr++) {
+                const float4 x4 = *reinterpret_cast<const float4 *>(Ys + rr * LP + 4 * gi);
+                const float4 y4 = *reinterpret_cast<const float4 *>(Ys + rr * LP + 4 * gj);
+                const float xv[4] = {x4.x, x4.y, x4.z, x4.w}, yv[4] = {y4.x, y4.y, y4.z, y4.w};
 #pragma unroll
-        for (int u = 0; u < MAXP; u++) {
-            if (tid + BT * u < npairs) {
-                const float *ya = Ys + pa[u] * 33, *yb = Ys + pb[u] * 33;
-                float s = acc[u];
-#pragma unroll 8
-                for (int rr = 0; rr < 32; rr++) s = fmaf(ya[rr], yb[rr], s);
-                acc[u] = s;
+                for (int a = 0; a < 4; a++)
+#pragma unroll
+                    for (int c = 0; c < 4; c++) acc[a][c] = fmaf(xv[a], yv[c], acc[a][c]);
             }
         }
     }
+    if (act) {
 #pragma unroll
-    for (int u = 0; u < MAXP; u++)
-        if (tid + BT * u < npairs) {
-            G[pa[u] + pb[u] * l] = acc[u];
-            G[pb[u] + pa[u] * l] = acc[u];
-        }
+        for (int a = 0; a < 4; a++)
+#pragma unroll
+            for (int c = 0; c < 4; c++) {
+                const int i = 4 * gi + a, j = 4 * gj + c;
+                if (i < l && j < l) {
+                    G[i + j * l] = acc[a][c];
+                    G[j + i * l] = acc[a][c];
+                }
+            }
+    }
     __syncthreads();
 }
 
@@ -236,7 +302,7 @@ __device__ bool chol_cta(float *G, int l, int *bad) {
     return *bad == 0;
 }
 
-// X = R^-1 (upper, l x l, shared), one warp per column.
+// X = R^-1 (upper, l x l, shared, stored row-major: X[j * l + c]), one warp per column.
 __device__ void trinv_cta(const float *R, int l, float *X) {
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     for (int e = threadIdx.x; e < l * l; e += BT) X[e] = 0.f;
@@ -250,7 +316,7 @@ __device__ void trinv_cta(const float *R, int l, float *X) {
             float bj = (slot == 0) ? b[0] : (slot == 1 ? b[1] : b[2]);
             bj = __shfl_sync(0xffffffffu, bj, owner);
             const float xj = bj / R[j + j * l];
-            if (lane == 0) X[j + c * l] = xj;
+            if (lane == 0) X[j * l + c] = xj;                        // row-major: the B operand of the product
 #pragma unroll
             for (int t = 0; t < 3; t++) {
                 const int r = lane + 32 * t;
@@ -261,31 +327,15 @@ __device__ void trinv_cta(const float *R, int l, float *X) {
     __syncthreads();
 }
 
-// Y (rows x l, global) <- Y * X (X upper l x l in shared); one thread per row, in place.
-__device__ void apply_upper_cta(float *Y, long long ldy, int rows, int l, const float *X) {
-    constexpr int MAXL = 80;
-    for (int r = threadIdx.x; r < rows; r += BT) {
-        float y[MAXL];
-#pragma unroll
-        for (int c = 0; c < MAXL; c++) y[c] = (c < l) ? Y[r + (long long)c * ldy] : 0.f;
-        for (int c = l - 1; c >= 0; c--) {
-            float s = 0.f;
-#pragma unroll
-            for (int t = 0; t < MAXL; t++)
-                if (t <= c) s = fmaf(y[t], X[t + c * l], s);
-            Y[r + (long long)c * ldy] = s;
-        }
-    }
-    __syncthreads();
-}
-
 // CholeskyQR (passes 1 or 2) of Y (rows x l, global) in place; R (shared l x l) = R2 R1.
 // A pass whose Cholesky breaks down (Y too ill-conditioned for an FP32 Gram) is redone as
 // shifted CholeskyQR: the Gram's diagonal is raised by 8 l u trace(G), which keeps it
 // positive definite, and one extra plain pass restores the orthogonality (shifted
 // CholeskyQR3, Fukaya et al. 2020).
+// Y <- Y R^-1 is the tiled product gemm_A_B applied in place (each 64-row tile of Y is read
+// completely before it is written), with R^-1 row-major in X.
 __device__ bool cqr_cta(float *Y, long long ldy, int rows, int l, int passes, float *R, float *G, float *X, float *T,
-                        float *Ys, int *bad) {
+                        float *Ys, float *At, int *bad) {
     for (int e = threadIdx.x; e < l * l; e += BT) R[e] = ((e % l) == (e / l)) ? 1.f : 0.f;
     __syncthreads();
     __shared__ float trace_sh;
@@ -310,7 +360,7 @@ __device__ bool cqr_cta(float *Y, long long ldy, int rows, int l, int passes, fl
             passes++;
         }
         trinv_cta(G, l, X);
-        apply_upper_cta(Y, ldy, rows, l, X);
+        gemm_A_B(Y, ldy, rows, l, X, l, Y, ldy, At);
         // R <- G R  (both upper)
         for (int e = threadIdx.x; e < l * l; e += BT) {
             const int i = e % l, k = e / l;
@@ -327,7 +377,10 @@ __device__ bool cqr_cta(float *Y, long long ldy, int rows, int l, int passes, fl
 
 // One-sided Jacobi on W (l x l, shared), V accumulated; then sort descending.
 __device__ int jacobi_cta(float *W, float *V, int l, float *sv, int *rot) {
-    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+    // one-sided Jacobi, round-robin pairs; each pair is handled by a group of 8 lanes (32
+    // groups per CTA, so every pair of a round (l / 2 <= 36) runs at once for l <= 64)
+    const int tid = threadIdx.x, g8 = tid >> 3, gl = tid & 7;
+    const unsigned gmask = 0xffu << (tid & 24);                // the 8 lanes of this group
     for (int e = tid; e < l * l; e += BT) V[e] = ((e % l) == (e / l)) ? 1.f : 0.f;
     const int np = l + (l & 1);
     const float tol = 4.f * sqrtf((float)l) * 1.1920929e-7f;
@@ -336,26 +389,32 @@ __device__ int jacobi_cta(float *W, float *V, int l, float *sv, int *rot) {
         if (tid == 0) *rot = 0;
         __syncthreads();
         for (int r = 0; r < np - 1; r++) {
-            for (int pi = wid; pi < np / 2; pi += BT / 32) {
+            for (int pi = g8; pi < np / 2; pi += BT / 8) {
                 int p, q;
                 const int mm = np - 1;
                 if (pi == 0) { p = 0; q = (r % mm) + 1; }
                 else { p = ((r + pi) % mm) + 1; q = ((r - pi + mm) % mm) + 1; }
-                if (p >= l || q >= l) continue;
+                const bool valid = (p < l && q < l);
                 if (p > q) { const int t = p; p = q; q = t; }
-                float *wp = W + p * l, *wq = W + q * l;
                 float a = 0, b = 0, d = 0;
-                for (int i = lane; i < l; i += 32) {
-                    const float x = wp[i], y = wq[i];
-                    a = fmaf(x, x, a); b = fmaf(y, y, b); d = fmaf(x, y, d);
+                float *wp = W + p * l, *wq = W + q * l;
+                if (valid)
+                    for (int i = gl; i < l; i += 8) {
+                        const float x = wp[i], y = wq[i];
+                        a = fmaf(x, x, a); b = fmaf(y, y, b); d = fmaf(x, y, d);
+                    }
+#pragma unroll
+                for (int o = 4; o > 0; o >>= 1) {
+                    a += __shfl_xor_sync(gmask, a, o);
+                    b += __shfl_xor_sync(gmask, b, o);
+                    d += __shfl_xor_sync(gmask, d, o);
                 }
-                a = warp_sum(a); b = warp_sum(b); d = warp_sum(d);
-                if (d == 0.f || fabsf(d) <= tol * sqrtf(a * b)) continue;
+                if (!valid || d == 0.f || fabsf(d) <= tol * sqrtf(a * b)) continue;
                 const float zeta = (b - a) / (2.f * d);
                 const float t = copysignf(1.f, zeta) / (fabsf(zeta) + sqrtf(1.f + zeta * zeta));
                 const float cs = rsqrtf(1.f + t * t), sn = cs * t;
                 float *vp = V + p * l, *vq = V + q * l;
-                for (int i = lane; i < l; i += 32) {
+                for (int i = gl; i < l; i += 8) {
                     const float x = wp[i], y = wq[i];
                     wp[i] = cs * x - sn * y;
                     wq[i] = sn * x + cs * y;
@@ -363,7 +422,7 @@ __device__ int jacobi_cta(float *W, float *V, int l, float *sv, int *rot) {
                     vp[i] = cs * u - sn * v;
                     vq[i] = sn * u + cs * v;
                 }
-                if (lane == 0) *rot = 1;
+                if (gl == 0) *rot = 1;
             }
             __syncthreads();
         }
@@ -371,15 +430,17 @@ __device__ int jacobi_cta(float *W, float *V, int l, float *sv, int *rot) {
         __syncthreads();
         if (!any) break;
     }
+    const int lane = tid & 31, wid = tid >> 5;
     for (int c = wid; c < l; c += BT / 32) {
-        float s = 0.f;
-        for (int i = lane; i < l; i += 32) s = fmaf(W[i + c * l], W[i + c * l], s);
-        s = warp_sum(s);
-        if (lane == 0) sv[c] = sqrtf(s);
+        float s2 = 0.f;
+        for (int i = lane; i < l; i += 32) s2 = fmaf(W[i + c * l], W[i + c * l], s2);
+        s2 = warp_sum(s2);
+        if (lane == 0) sv[c] = sqrtf(s2);
     }
     __syncthreads();
     return sweep;
 }
+
 
 __global__ void __launch_bounds__(BT, 1)
     batch_rsvd_kernel(const BatchItem *items, int count, int *queue, float *work, long long slab, long long ldw,
@@ -397,7 +458,7 @@ __global__ void __launch_bounds__(BT, 1)
         const BatchItem B = items[it];
         const int m = B.m, n = B.n, l = B.l, k = B.k;
         // shared layout: [Bsm: n*l][At: 64*32]  (phase 1)  /  small l x l work areas (later)
-        float *Bsm = sm, *At = sm + (size_t)n * l;
+        float *Bsm = sm, *At = sm + ((size_t)n * l + 3) / 4 * 4;        // At: 16-byte aligned
         gen_omega(Bsm, n, l, seed, (uint64_t)B.index);
         __syncthreads();
         gemm_A_B(B.A, B.lda, m, n, Bsm, l, Yg, ldw, At);
@@ -405,24 +466,27 @@ __global__ void __launch_bounds__(BT, 1)
         const int L2 = l * l;
         float *R = sm, *G = R + L2, *X = G + L2, *T = X + L2, *Ys = T + L2, *W = Ys + 33 * 96, *Vs = W + L2;
         float *sv = Vs + L2, *Qs = sv + 96;
+        float *At2 = sm + ((size_t)(Qs + 32 * 96 - sm) + 3) / 4 * 4;   // A chunks of the A^T Q product
         bool ok = true;
         for (int j = 1; j < q && ok; j++) {                            // q-1 power rounds, s=1 schedule
-            if ((2 * j - 2) % s == 0) ok = cqr_cta(Yg, ldw, m, l, 1, R, G, X, T, Ys, &bad);
-            gemm_At_Q(B.A, B.lda, m, n, Yg, ldw, l, Zg, ldw, Qs + 32 * 96, Qs);
-            if ((2 * j - 1) % s == 0 && ok) ok = cqr_cta(Zg, ldw, n, l, 1, R, G, X, T, Ys, &bad);
+            if ((2 * j - 2) % s == 0) ok = cqr_cta(Yg, ldw, m, l, 1, R, G, X, T, Ys, At2, &bad);
+            gemm_At_Q(B.A, B.lda, m, n, Yg, ldw, l, Zg, ldw, At2, Qs);
+            if ((2 * j - 1) % s == 0 && ok) ok = cqr_cta(Zg, ldw, n, l, 1, R, G, X, T, Ys, At2, &bad);
             // Y = A Zo : stage Zo row-major in shared memory as the B operand
             for (int e = threadIdx.x; e < n * l; e += BT) Bsm[(e % n) * l + e / n] = Zg[(e % n) + (long long)(e / n) * ldw];
             __syncthreads();
             gemm_A_B(B.A, B.lda, m, n, Bsm, l, Yg, ldw, At);
         }
-        if (ok) ok = cqr_cta(Yg, ldw, m, l, 2, R, G, X, T, Ys, &bad);                // Q in Yg
-        if (ok) gemm_At_Q(B.A, B.lda, m, n, Yg, ldw, l, Zg, ldw, Qs + 32 * 96, Qs);  // Bt in Zg
-        if (ok) ok = cqr_cta(Zg, ldw, n, l, 2, R, G, X, T, Ys, &bad);                // Qh in Zg, Rh in R
+        if (ok) ok = cqr_cta(Yg, ldw, m, l, 2, R, G, X, T, Ys, At2, &bad);                // Q in Yg
+        if (ok) gemm_At_Q(B.A, B.lda, m, n, Yg, ldw, l, Zg, ldw, At2, Qs);  // Bt in Zg
+        if (ok) ok = cqr_cta(Zg, ldw, n, l, 2, R, G, X, T, Ys, At2, &bad);                // Qh in Zg, Rh in R
         if (!ok) {
             if (threadIdx.x == 0) atomicAdd(flag, 1);
             continue;
         }
-        for (int e = threadIdx.x; e < L2; e += BT) W[e] = R[e];
+        // Jacobi on Rh^T (rows of the triangular factor of a graded matrix are nearly
+        // orthogonal, so fewer sweeps): Rh^T = W diag(1/sv) ... i.e. Rh = Vs S (W / sv)^T
+        for (int e = threadIdx.x; e < L2; e += BT) W[e] = R[(e / l) + (e % l) * l];
         __syncthreads();
         jacobi_cta(W, Vs, l, sv, &rot);
         // order: rank of each column by descending sv
@@ -433,30 +497,21 @@ __global__ void __launch_bounds__(BT, 1)
             rank_of[c] = r;
         }
         __syncthreads();
-        // Rh = Uh S Vh^T with Uh = W / sv, Vh = Vs.  U = Q Vh(:, :k) ; V = Qh Uh(:, :k)
-        // stage the k selected columns (by rank) of Vh and Uh in shared memory (G and X areas)
+        // Rh = Uh S Vh^T with Uh = Vs, Vh = W / sv.  U = Q Vh(:, :k) ; V = Qh Uh(:, :k).
+        // The k selected columns (by rank) go row-major into T (Vh) and G (Uh), the B operands
+        // of the tiled product (rows t, columns r: B[t * k + r]).
         for (int e = threadIdx.x; e < L2; e += BT) {
             const int i = e % l, c = e / l, r = rank_of[c];
             if (r < k) {
-                G[i + r * l] = Vs[i + c * l];
-                X[i + r * l] = (sv[c] > 0.f) ? W[i + c * l] / sv[c] : 0.f;
+                T[i * k + r] = (sv[c] > 0.f) ? W[i + c * l] / sv[c] : 0.f;
+                G[i * k + r] = Vs[i + c * l];
             }
         }
-        __syncthreads();
         for (int c = threadIdx.x; c < l; c += BT)
             if (rank_of[c] < k) B.S[rank_of[c]] = (double)sv[c];
-        for (long long e = threadIdx.x; e < (long long)m * k; e += BT) {
-            const int i = (int)(e % m), c = (int)(e / m);
-            float acc = 0.f;
-            for (int t = 0; t < l; t++) acc = fmaf(Yg[i + (long long)t * ldw], G[t + c * l], acc);
-            B.U[i + (long long)c * B.ldu] = acc;
-        }
-        for (long long e = threadIdx.x; e < (long long)n * k; e += BT) {
-            const int i = (int)(e % n), c = (int)(e / n);
-            float acc = 0.f;
-            for (int t = 0; t < l; t++) acc = fmaf(Zg[i + (long long)t * ldw], X[t + c * l], acc);
-            B.V[i + (long long)c * B.ldv] = acc;
-        }
+        __syncthreads();
+        gemm_A_B(Yg, ldw, m, l, T, k, B.U, B.ldu, At2);
+        gemm_A_B(Zg, ldw, n, l, G, k, B.V, B.ldv, At2);
         __syncthreads();
     }
 }
@@ -465,9 +520,9 @@ __global__ void __launch_bounds__(BT, 1)
 
 // Shared memory and slab sizes for a batch whose largest matrix is (mmax x nmax), l <= lmax.
 size_t batch_smem_bytes(int nmax, int lmax) {
-    const size_t phase1 = (size_t)nmax * lmax + 64 * 32;
+    const size_t phase1 = (size_t)nmax * lmax + 3 + 32 * ATP;
     const size_t L2 = (size_t)lmax * lmax;
-    const size_t small = 4 * L2 + 33 * 96 + 2 * L2 + 96 + 32 * 96 + 32 * 33 + 64;
+    const size_t small = 4 * L2 + 33 * 96 + 2 * L2 + 96 + 32 * 96 + 3 + 32 * ATP + 64;
     return sizeof(float) * std::max(phase1, small) + 64;
 }
 
