@@ -50,6 +50,7 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-learned", action="store_true")
+    ap.add_argument("--no-batched", action="store_true")
     return ap.parse_args()
 
 
@@ -226,6 +227,76 @@ def learned_qb_leg(torch, eng, dev, steps=2):
     del At, Q, B
     torch.cuda.empty_cache()
     return out
+
+
+def batched_leg(torch, eng, dev, execs=5):
+    """Batched rSVD workload: 4096 FP32 matrices, m ~ U[64, 1024], n ~ U[32, 512] (seed 0),
+    s_i = 0.9^i with Haar factors, k = floor(min(m, n) / 8), p = 8, q = 1; one graph-captured
+    persistent launch per execute.  Residuals of four items are checked against the optimal
+    rank-k tail of their spectrum."""
+    import numpy as np
+    L = eng.lib
+    L.rsvdpack_batch_plan_create.restype = C.c_void_p
+    L.rsvdpack_batch_plan_create.argtypes = [C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int,
+                                             C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                             C.c_void_p, C.c_ulonglong]
+    L.rsvdpack_batch_plan_execute.restype = C.c_int
+    L.rsvdpack_batch_plan_execute.argtypes = [C.c_void_p]
+    L.rsvdpack_batch_plan_destroy.argtypes = [C.c_void_p]
+    cnt = 4096
+    g = np.random.default_rng(0)
+    ms, ns = g.integers(64, 1025, cnt), g.integers(32, 513, cnt)
+    ks = [max(1, int(min(a, b)) // 8) for a, b in zip(ms, ns)]
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(0)
+    dA, dU, dV, dS = [], [], [], []
+    for m, n, k in zip(ms, ns, ks):
+        r = int(min(m, n))
+        Uq, _ = torch.linalg.qr(torch.randn(int(m), r, device=dev, generator=gen))
+        Vq, _ = torch.linalg.qr(torch.randn(int(n), r, device=dev, generator=gen))
+        sv = 0.9 ** torch.arange(r, device=dev, dtype=torch.float32)
+        dA.append(((Uq * sv) @ Vq.T).T.contiguous())
+        dU.append(torch.zeros(k, int(m), device=dev))
+        dV.append(torch.zeros(k, int(n), device=dev))
+        dS.append(torch.zeros(k, device=dev, dtype=torch.float64))
+    arr = lambda vals, t: (t * cnt)(*vals)
+    ptr = lambda ts: (C.c_void_p * cnt)(*[t.data_ptr() for t in ts])
+    mi = arr([int(x) for x in ms], C.c_int)
+    ni = arr([int(x) for x in ns], C.c_int)
+    torch.cuda.synchronize()
+    plan = L.rsvdpack_batch_plan_create(cnt, mi, ni, arr(ks, C.c_int), 8, 1, 1, ptr(dA),
+                                        arr([int(x) for x in ms], C.c_longlong), ptr(dU),
+                                        arr([int(x) for x in ms], C.c_longlong), ptr(dS), ptr(dV),
+                                        arr([int(x) for x in ns], C.c_longlong), 7)
+    if not plan:
+        raise RuntimeError(f"batch plan failed: {eng.last_error()}")
+    stream = torch.cuda.ExternalStream(L.rsvdpack_stream())
+    try:
+        for _ in range(3):
+            if L.rsvdpack_batch_plan_execute(plan):
+                raise RuntimeError(eng.last_error())
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for _ in range(execs):
+            if L.rsvdpack_batch_plan_execute(plan):
+                raise RuntimeError(eng.last_error())
+        e1.record(stream)
+        e1.synchronize()
+        ms_exec = e0.elapsed_time(e1) / execs
+    finally:
+        L.rsvdpack_batch_plan_destroy(plan)
+    checks = []
+    for i in (0, 1, cnt // 2, cnt - 1):
+        A = dA[i].T.double()
+        res = float(torch.linalg.norm(A - (dU[i].T.double() * dS[i]) @ dV[i].double()) / torch.linalg.norm(A))
+        r = int(min(ms[i], ns[i]))
+        sv = 0.9 ** np.arange(r)
+        checks.append({"item": i, "rel_residual": res, "optimal": float(np.sqrt(np.sum(sv[ks[i]:] ** 2) / np.sum(sv ** 2)))})
+    nbytes = sum(int(a) * int(b) for a, b in zip(ms, ns)) * 4
+    return {"workload": "4096 matrices m~U[64,1024] n~U[32,512], s_i = 0.9^i, k = min(m,n)/8, p = 8, q = 1",
+            "ms_per_batch": ms_exec, "solves_per_s": cnt * 1000.0 / ms_exec, "bytes_of_A": nbytes,
+            "residual_checks": checks}
 
 
 def run_reference(args):
@@ -458,6 +529,12 @@ def run_ours(args):
         learned_leg = learned_qb_leg(torch, eng, dev)
         eng.set_precision(args.precision)
 
+    # ---------------- batched workload (extra measurement)
+    batched = None
+    if rank == 0 and not args.no_batched:
+        batched = batched_leg(torch, eng, dev)
+        eng.set_precision(args.precision)
+
     # ---------------- CPU baseline: the oracle on the host cores, one full solve
     cpu = None
     if rank == 0 and not args.no_cpu:
@@ -478,7 +555,8 @@ def run_ours(args):
                        "l2": "inputs larger than L2 (A = 512 MiB)", "parallelism": f"replicas x{world}"},
             "residual": {"rel_frobenius": res_mixed, "fp64_same_method": res_fp64,
                          "matched": (res_fp64 is None) or (res_mixed <= (1 + 1e-3) * res_fp64)},
-            "roofline": roof, "plain_gpu": plain, "learned_qb": learned_leg, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches, "clocks": clocks,
+            "roofline": roof, "plain_gpu": plain, "learned_qb": learned_leg, "batched": batched,
+            "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches, "clocks": clocks,
             "device": name,
         }
         print(json.dumps(line), flush=True)

@@ -718,6 +718,69 @@ int rsvdpack_dev_sketch(const void *dA, int dtype, long long lda, int m, int n, 
     return rsvdpack_last_error();
 }
 
+// ---- FP32-accurate tensor-core products (k_gemm_tc.cu: split_tf32, tc_gemm_3xtf32, tc_update_3xtf32)
+namespace {
+void split_operands(cudaStream_t st, const float *dA, long long lda, const float *dX, long long ldx, int M, int N,
+                    int K, DMat<float> &Ah, DMat<float> &Al, DMat<float> &Xh, DMat<float> &Xl) {
+    Ah = DMat<float>(K, M, st, false);
+    Al = DMat<float>(K, M, st, false);
+    Xh = DMat<float>(K, N, st, false);
+    Xl = DMat<float>(K, N, st, false);
+    split_tf32(st, dA, lda, K, M, Ah.v.p, Al.v.p, Ah.v.ld);
+    split_tf32(st, dX, ldx, K, N, Xh.v.p, Xl.v.p, Xh.v.ld);
+}
+}  // namespace
+
+int rsvdpack_dev_gemm_3xtf32(const float *dA, long long lda, const float *dX, long long ldx, int M, int N, int K,
+                             float *dD, long long ldd) {
+    guarded("rsvdpack_dev_gemm_3xtf32", [&] {
+        need(dA && dX && dD, "null device pointer");
+        need(M > 0 && N > 0 && K > 0, "bad sizes");
+        need(lda >= K && ldx >= K && ldd >= M, "bad leading dimension");
+        begin_call();
+        order_after_default_stream();
+        cudaStream_t st = ctx().stream;
+        DMat<float> Ah, Al, Xh, Xl;
+        split_operands(st, dA, lda, dX, ldx, M, N, K, Ah, Al, Xh, Xl);
+        tc_gemm_3xtf32(st, Ah.v.p, Al.v.p, Ah.v.ld, Xh.v.p, Xl.v.p, Xh.v.ld, M, N, K, dD, ldd);
+        RSVD_CK(cudaStreamSynchronize(st));
+        check_device_flags(ctx());
+        ctx().timing.kernel_launches = ctx().launches;
+    });
+    return rsvdpack_last_error();
+}
+
+int rsvdpack_dev_update_3xtf32(const float *dA, long long lda, const float *dX, long long ldx, int M, int N, int K,
+                               float *dC, long long ldc, double *fro2) {
+    guarded("rsvdpack_dev_update_3xtf32", [&] {
+        need(dA && dX && dC, "null device pointer");
+        need(M > 0 && N > 0 && K > 0, "bad sizes");
+        need(lda >= K && ldx >= K && ldc >= M, "bad leading dimension");
+        begin_call();
+        order_after_default_stream();
+        cudaStream_t st = ctx().stream;
+        DMat<float> Ah, Al, Xh, Xl;
+        split_operands(st, dA, lda, dX, ldx, M, N, K, Ah, Al, Xh, Xl);
+        // one sum of squares per CTA of the update grid (128-row tiles; one column tile up
+        // to 512 columns, else 256-column tiles)
+        const long long parts = ((long long)M + 127) / 128 * (N <= 512 ? 1 : ((long long)N + 255) / 256);
+        DBuf fp(sizeof(double) * (size_t)parts, st);
+        tc_update_3xtf32(st, Ah.v.p, Al.v.p, Ah.v.ld, Xh.v.p, Xl.v.p, Xh.v.ld, M, N, K, dC, ldc,
+                         fro2 ? (double *)fp.get() : nullptr);
+        std::vector<double> h(fro2 ? (size_t)parts : 0);
+        if (fro2) RSVD_CK(cudaMemcpyAsync(h.data(), fp.get(), sizeof(double) * h.size(), cudaMemcpyDeviceToHost, st));
+        RSVD_CK(cudaStreamSynchronize(st));
+        check_device_flags(ctx());
+        if (fro2) {
+            double acc = 0.0;
+            for (double v : h) acc += v;
+            *fro2 = acc;
+        }
+        ctx().timing.kernel_launches = ctx().launches;
+    });
+    return rsvdpack_last_error();
+}
+
 // ---- the learned proposal's network (k_mlp.cu): device pointers, engine stream, synchronous
 int rsvdpack_mlp_info(int *dims, int *nparams) {
     guarded("rsvdpack_mlp_info", [&] {

@@ -64,8 +64,25 @@ struct Bf16Cache {
     const void *src = nullptr;
     i64 r = 0, c = 0, ld = 0;
     DMat<__nv_bfloat16> m;
+    DMat<__nv_bfloat16> lo;      // second part of a two-part split (empty when not split)
+    bool split = false;
 };
 thread_local Bf16Cache t_bf16_a;
+
+// A = hi + lo (two BF16 parts), cached like to_bf16's copy; hi is the plain BF16 rounding,
+// so a cached split also serves to_bf16.
+void to_bf16_pair(cudaStream_t s, DM<float> X, DM<__nv_bfloat16> &hi, DM<__nv_bfloat16> &lo) {
+    if (!(t_bf16_a.split && t_bf16_a.src == X.p && t_bf16_a.r == X.r && t_bf16_a.c == X.c && t_bf16_a.ld == X.ld)) {
+        DMat<__nv_bfloat16> h(X.r, X.c, s, false), l(X.r, X.c, s, false);
+        split_bf16(s, X, h.v, l.v);
+        t_bf16_a.m = std::move(h);
+        t_bf16_a.lo = std::move(l);
+        t_bf16_a.split = true;
+        t_bf16_a.src = X.p; t_bf16_a.r = X.r; t_bf16_a.c = X.c; t_bf16_a.ld = X.ld;
+    }
+    hi = t_bf16_a.m.v;
+    lo = t_bf16_a.lo.v;
+}
 
 DM<__nv_bfloat16> to_bf16(cudaStream_t s, DM<float> X, DMat<__nv_bfloat16> &tmp, bool cache) {
     if (cache && t_bf16_a.src == X.p && t_bf16_a.r == X.r && t_bf16_a.c == X.c && t_bf16_a.ld == X.ld)
@@ -73,6 +90,7 @@ DM<__nv_bfloat16> to_bf16(cudaStream_t s, DM<float> X, DMat<__nv_bfloat16> &tmp,
     DMat<__nv_bfloat16> d(X.r, X.c, s, false);
     convert<float, __nv_bfloat16>(s, X, d.v);
     if (cache) {
+        t_bf16_a = Bf16Cache{};
         t_bf16_a.m = std::move(d);
         t_bf16_a.src = X.p; t_bf16_a.r = X.r; t_bf16_a.c = X.c; t_bf16_a.ld = X.ld;
         return t_bf16_a.m.v;
@@ -103,6 +121,16 @@ void prod(cudaStream_t s, bool ta, bool tb, T alpha, DM<T> A, DM<T> B, T beta, D
             if (prec == RSVD_PREC_TF32 && ta) {
                 tc_gemm(s, 0, false, A.p, A.ld, B.p, B.ld, (int)M, (int)N, (int)K, (float)alpha, (float *)C.p, C.ld,
                         0, nullptr, 0, nullptr, 0);
+            } else if (prec == RSVD_PREC_TF32 && !ta && ctx().ax_split && A.r * A.c >= B.r * B.c) {
+                // A X with A as hi + lo BF16 parts: two K segments (lo first) of one product
+                DMat<__nv_bfloat16> tb_tmp;
+                DM<__nv_bfloat16> Ah, Al;
+                to_bf16_pair(s, *(DM<float> *)&A, Ah, Al);
+                DM<__nv_bfloat16> Bb = to_bf16(s, *(DM<float> *)&B, tb_tmp, false);
+                const TcSeg g[2] = {{Al.p, Al.ld, Bb.p, Bb.ld, (int)K}, {Ah.p, Ah.ld, Bb.p, Bb.ld, (int)K}};
+                tc_gemm_segs(s, 1, true, 2, g, (int)M, (int)N, (float)alpha, (float *)C.p, C.ld, 0, nullptr, 0,
+                             nullptr, 0);
+                RSVD_CK(cudaStreamSynchronize(s));   // tb_tmp leaves scope
             } else {
                 // bf16 operands: the larger operand (normally A) is converted once per call
                 DMat<__nv_bfloat16> ta_tmp, tb_tmp;
@@ -434,25 +462,35 @@ static QBOut<T> qb_plain(DM<T> A, int kstep, int nstep, double TOL, int q, int s
 // ------------------------------------------------------------------ learned proposal
 // Fixed-precision QB (randQB_pb_new in TOL mode) with the block widths and power count set by
 // the learned network from a 32-column probe sketch:
-//   probe   Y0 = A Omega0 (n x 32, FP32 products), R0 = chol(Y0^T Y0); features = log10 of
-//           R0's diagonal relative to ||A||_F, the captured energy, log10 min(m, n),
+//   probe   Y0 = A Omega0 (n x 32, FP32 products), R0 from orth(Y0); features = log10 of
+//           R0's diagonal relative to ||A||_F, log10 of the energy the probe leaves (floored
+//           at 1e-5), log10 min(m, n),
 //           log10(m / n), log10(TOL / ||A||_F) (the training set's feature_vector);
 //   network 2 outputs = predicted log2(total width / 32) for q = 1, 2 (+ the calibrated
 //           margin); the q with the fewest passes x width is taken;
 //   blocks  the predicted width W is split into nb = ceil((2q+1) log10(||A||_F / TOL) / 2.5)
 //           blocks: a tensor-core (TF32 / BF16) sketch of the deflated matrix resolves ~2.5
-//           decades of its sketched spectrum sigma^(2q+1), so a block must not span more.  Per block: Y = A_res Omega, q power rounds, projection against the
-//           earlier blocks (twice), Q_j = orth(Y), B_j = Q_j^T A_res and A_res -= Q_j B_j by
-//           3xTF32 (FP32-accurate), ||A_res||_F from the update's epilogue.
+//           decades of its sketched spectrum sigma^(2q+1), so a block must not span more
+//           (a probe that already falls faster than that takes q = 0).  Per block:
+//           Y = A_res Omega, q power rounds, projection against the earlier blocks (twice),
+//           Q_j = orth(Y), B_j = Q_j^T A_res and A_res -= Q_j B_j by 3xTF32 (FP32-accurate;
+//           the long-K products accumulate in short chains, see tc_gemm_3xtf32),
+//           ||A_res||_F from the update's epilogue.
 //   judge   the loop stops when ||A_res||_F <= TOL (the reference's criterion, exact up to
 //           FP32 rounding); when the proposed width is used up first, it continues with
 //           blocks of the same width, i.e. the adaptive loop is the fallback.
 static constexpr int kProbe = 32, kFeat = 36;
-static constexpr int kTf32 = 0, kEpiUpdate = 1;                          // tc_gemm kind / epilogue codes
 
 static bool learned_qb(DM<float> A, double TOL, QBOut<float> &out, int *q_used) {
     Ctx &cx = ctx();
     cudaStream_t s = cx.stream;
+    // sketches of the deflated matrix read it as a two-part BF16 split in TF32 mode: one BF16
+    // copy (7 mantissa bits) stalls the blocks once ||A_res|| falls to ~3e-4 ||A||
+    struct AxSplit {
+        bool prev;
+        AxSplit() : prev(ctx().ax_split) { ctx().ax_split = true; }
+        ~AxSplit() { ctx().ax_split = prev; }
+    } ax_split_scope;
     const ProposalModel *pm = proposal_model();
     const i64 m = A.r, n = A.c, rmin = std::min(m, n);
     const double fro = frob_norm<float>(s, A);
@@ -463,11 +501,13 @@ static bool learned_qb(DM<float> A, double TOL, QBOut<float> &out, int *q_used) 
         DMat<float> Om0 = make_omega<float>(n, kProbe);
         DMat<float> Y0(m, kProbe, s, false);
         gemm<float>(s, false, false, 1.f, A, Om0.v, 0.f, Y0.v);
-        DMat<double> G0(kProbe, kProbe, s, false);
-        gram<float>(s, Y0.v, G0.v);
-        if (!cholesky_small<double>(s, G0.v, 0.0, cx.d_flags + FLAG_CHOL_BREAKDOWN)) return false;
+        // R0 of the probe by the engine's orthonormalisation (CholeskyQR2, Householder when a
+        // steep spectrum makes the 32-column probe too ill-conditioned for a Gram)
+        DMat<float> Q0(m, kProbe, s, false);
+        DMat<double> R0(kProbe, kProbe, s, true);
+        orth<float>(Y0.v, Q0.v, &R0.v, 2);
         std::vector<double> h((size_t)kProbe * kProbe);
-        RSVD_CK(cudaMemcpy2DAsync(h.data(), sizeof(double) * kProbe, G0.v.p, sizeof(double) * G0.v.ld,
+        RSVD_CK(cudaMemcpy2DAsync(h.data(), sizeof(double) * kProbe, R0.v.p, sizeof(double) * R0.v.ld,
                                   sizeof(double) * kProbe, kProbe, cudaMemcpyDeviceToHost, s));
         RSVD_CK(cudaStreamSynchronize(s));
         for (int j = 0; j < kProbe; j++) rdiag[j] = std::fabs(h[(size_t)j * kProbe + j]);
@@ -479,7 +519,7 @@ static bool learned_qb(DM<float> A, double TOL, QBOut<float> &out, int *q_used) 
         feat[j] = (float)std::log10(rel);
         energy += rel * rel;
     }
-    feat[kProbe] = (float)energy;
+    feat[kProbe] = (float)std::log10(std::max(1.0 - energy, 1e-5));
     feat[kProbe + 1] = (float)std::log10((double)rmin);
     feat[kProbe + 2] = (float)std::log10((double)m / (double)n);
     feat[kProbe + 3] = (float)std::log10(TOL / fro);
@@ -511,6 +551,11 @@ static bool learned_qb(DM<float> A, double TOL, QBOut<float> &out, int *q_used) 
     // ---- blocks on the deflated matrix
     // a TF32 / BF16 sketch resolves ~2.5 decades of the sketched spectrum sigma^(2q+1), and
     // the proposed width spans the log10(||A|| / TOL) decades of sigma that the tolerance needs
+    // a spectrum that already falls by more than the sketch can resolve (~2.5 decades of
+    // sigma^(2q+1)) across the probe's 32 columns gets no power rounds: they would only
+    // steepen what each block must resolve
+    const double probe_decades = std::log10(std::max(rdiag[0], 1e-300) / std::max(rdiag[kProbe - 1], 1e-300));
+    if ((2 * q + 1) * probe_decades > 2.5) q = 0;
     const double tol_rel = TOL / fro;
     const double decades = -std::log10(std::max(tol_rel, 1e-12));
     const int nb = std::max(1, (int)std::ceil((2 * q + 1) * decades / 2.5));
@@ -559,12 +604,8 @@ static bool learned_qb(DM<float> A, double TOL, QBOut<float> &out, int *q_used) 
                     split_tf32(s, P.v.p, P.v.ld, f, b, Ph.v.p, Pl.v.p, Ph.v.ld);
                     split_tf32(s, Qt.v.p, Qt.v.ld, f, m, Th.v.p, Tl.v.p, Th.v.ld);
                     // Yt (b x m) = Yt - P^T Q_f^T : A^T X form with A = P (K = f), X = Q_f^T (K = f)
-                    tc_gemm(s, kTf32, false, Ph.v.p, Ph.v.ld, Th.v.p, Th.v.ld, b, (int)m, f, 1.f, Yt.v.p,
-                            Yt.v.ld, kEpiUpdate, Yt.v.p, Yt.v.ld, nullptr, 1);
-                    tc_gemm(s, kTf32, false, Pl.v.p, Pl.v.ld, Th.v.p, Th.v.ld, b, (int)m, f, 1.f, Yt.v.p,
-                            Yt.v.ld, kEpiUpdate, Yt.v.p, Yt.v.ld, nullptr, 1);
-                    tc_gemm(s, kTf32, false, Ph.v.p, Ph.v.ld, Tl.v.p, Tl.v.ld, b, (int)m, f, 1.f, Yt.v.p,
-                            Yt.v.ld, kEpiUpdate, Yt.v.p, Yt.v.ld, nullptr, 1);
+                    tc_update_3xtf32(s, Ph.v.p, Pl.v.p, Ph.v.ld, Th.v.p, Tl.v.p, Th.v.ld, b, (int)m, f, Yt.v.p,
+                                     Yt.v.ld, nullptr);
                     RSVD_CK(cudaStreamSynchronize(s));
                 }
                 transpose<float>(s, Yt.v, Y.v);
@@ -586,17 +627,13 @@ static bool learned_qb(DM<float> A, double TOL, QBOut<float> &out, int *q_used) 
             transpose<float>(s, Bt.v, Bj);
             RSVD_CK(cudaStreamSynchronize(s));
         }
-        // A_res -= Q_j B_j (3xTF32, in place) with per-CTA sums of squares of the result
+        // A_res -= Q_j B_j (3xTF32, one in-place pass) with per-CTA sums of squares of the result
         {
             DMat<float> Th(b, m, s, false), Tl(b, m, s, false), Bh(b, n, s, false), Bl(b, n, s, false);
             split_tf32(s, Qtj.p, Qtj.ld, b, m, Th.v.p, Tl.v.p, Th.v.ld);
             split_tf32(s, Bj.p, Bj.ld, b, n, Bh.v.p, Bl.v.p, Bh.v.ld);
-            tc_gemm(s, kTf32, false, Th.v.p, Th.v.ld, Bh.v.p, Bh.v.ld, (int)m, (int)n, b, 1.f, Ar.v.p, Ar.v.ld,
-                    kEpiUpdate, Ar.v.p, Ar.v.ld, nullptr, 1);
-            tc_gemm(s, kTf32, false, Tl.v.p, Tl.v.ld, Bh.v.p, Bh.v.ld, (int)m, (int)n, b, 1.f, Ar.v.p, Ar.v.ld,
-                    kEpiUpdate, Ar.v.p, Ar.v.ld, nullptr, 1);
-            tc_gemm(s, kTf32, false, Th.v.p, Th.v.ld, Bl.v.p, Bl.v.ld, (int)m, (int)n, b, 1.f, Ar.v.p, Ar.v.ld,
-                    kEpiUpdate, Ar.v.p, Ar.v.ld, (double *)frob_part.get(), 1);
+            tc_update_3xtf32(s, Th.v.p, Tl.v.p, Th.v.ld, Bh.v.p, Bl.v.p, Bh.v.ld, (int)m, (int)n, b, Ar.v.p, Ar.v.ld,
+                             (double *)frob_part.get());
             release_operand_cache();                                     // A_res changed
             hpart.resize((size_t)(mt * ntl));
             RSVD_CK(cudaMemcpyAsync(hpart.data(), frob_part.get(), sizeof(double) * hpart.size(),

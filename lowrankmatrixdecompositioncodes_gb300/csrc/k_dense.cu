@@ -297,6 +297,39 @@ unsigned grid_for(i64 n) {
 }
 }  // namespace
 
+namespace {
+// Same 2-D layout as convert_kernel: hi = bf16(x), lo = bf16(x - hi).
+__global__ void split_bf16_kernel(const float *src, i64 lds, __nv_bfloat16 *hi, i64 ldh, __nv_bfloat16 *lo, i64 ldl,
+                                  i64 r, i64 c) {
+    const i64 i0 = (i64)blockIdx.x * 1024 + threadIdx.x;
+    for (i64 j = blockIdx.y; j < c; j += gridDim.y) {
+        float v[4];
+#pragma unroll
+        for (int t = 0; t < 4; t++) {
+            const i64 i = i0 + 256 * t;
+            v[t] = (i < r) ? src[i + j * lds] : 0.f;
+        }
+#pragma unroll
+        for (int t = 0; t < 4; t++) {
+            const i64 i = i0 + 256 * t;
+            if (i < r) {
+                const __nv_bfloat16 h = __float2bfloat16_rn(v[t]);
+                hi[i + j * ldh] = h;
+                lo[i + j * ldl] = __float2bfloat16_rn(v[t] - __bfloat162float(h));
+            }
+        }
+    }
+}
+}  // namespace
+
+void split_bf16(cudaStream_t s, DM<float> src, DM<__nv_bfloat16> hi, DM<__nv_bfloat16> lo) {
+    if (src.r * src.c == 0) return;
+    const dim3 grid((unsigned)((src.r + 1023) / 1024), (unsigned)std::min<i64>(src.c, 65535));
+    split_bf16_kernel<<<grid, 256, 0, s>>>(src.p, src.ld, hi.p, hi.ld, lo.p, lo.ld, src.r, src.c);
+    RSVD_LAUNCH_CK();
+    ctx().launches++;
+}
+
 template <typename Ts, typename Td>
 void convert(cudaStream_t s, DM<Ts> src, DM<Td> dst) {
     if (src.r * src.c == 0) return;

@@ -30,6 +30,8 @@ constexpr int KB = 128;          // bytes of K per pipeline stage (one 128B swiz
 constexpr int NTHR = 128;
 constexpr int A_BYTES = BM * KB; // 16 KB per stage for operand A
 constexpr int MAX_BN = 512;      // TMEM columns available to one CTA
+constexpr int MAX_SEG = 3;       // K segments per product (3xTF32 terms in one accumulation)
+constexpr int CW = 64;           // update epilogue: C columns per TMA chunk (128 x 64 FP32 = 32 KB)
 
 enum { KIND_TF32 = 0, KIND_BF16 = 1 };
 enum { EPI_STORE = 0, EPI_UPDATE = 1, EPI_PARTIAL = 2 };
@@ -44,7 +46,10 @@ struct Params {
     int BN;            // columns per CTA (multiple of 16, <= 512)
     int chunk_n0, chunk_n1;   // MMA N of the (up to) two column chunks (chunk_n1 may be 0)
     int kb_per_split;  // K blocks handled by one split
-    int num_kb;        // total K blocks
+    int num_kb;        // total K blocks (over all segments)
+    int nseg;          // K segments: segment s contracts maps.a[s] with maps.b[s] over seg_kb[s] blocks
+    int seg_kb[MAX_SEG];
+    int c_tma;         // EPI_UPDATE: C is TMA-loaded into the free stage buffers, D TMA-stored
     int stages;
     float alpha;
     double *fro_part;  // EPI_UPDATE: per-CTA sum of squares of the new D (or null)
@@ -84,6 +89,18 @@ __device__ bool mbar_wait(uint32_t bar, uint32_t parity, volatile int *abort_fla
         }
     }
     return true;
+}
+
+// Operand maps of the K segments, and the (unswizzled) C / D maps of the update epilogue.
+struct Maps {
+    CUtensorMap a[MAX_SEG], b[MAX_SEG], c, d;
+};
+
+__device__ __forceinline__ void tma_store_2d(const CUtensorMap *tm, uint32_t src, int c0, int c1) {
+    asm volatile("cp.async.bulk.tensor.2d.global.shared::cta.bulk_group [%0, {%2, %3}], [%1];" ::"l"(
+                     (unsigned long long)tm),
+                 "r"(src), "r"(c0), "r"(c1)
+                 : "memory");
 }
 
 __device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap *tm, uint32_t bar, int c0, int c1) {
@@ -147,7 +164,7 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
 
 template <int KIND, bool A_MN, int EPI>
 __global__ void __launch_bounds__(NTHR, 1)
-    tc_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, Params P) {
+    tc_gemm_kernel(const __grid_constant__ Maps maps, Params P) {
     extern __shared__ uint8_t smem_raw[];
     // 1024-byte alignment for the 128B-swizzled tiles
     const uint32_t raw = smem_u32(smem_raw);
@@ -158,7 +175,8 @@ __global__ void __launch_bounds__(NTHR, 1)
     const uint32_t stage_bytes = A_BYTES + b_bytes;
     uint64_t *bars = (uint64_t *)(sbase + (size_t)stages * stage_bytes);
     uint64_t *full = bars, *empty = bars + stages, *done = bars + 2 * stages;
-    uint32_t *tmem_holder = (uint32_t *)(done + 1);
+    uint64_t *cbar = done + 1;                       // update epilogue: one per C chunk (<= 4)
+    uint32_t *tmem_holder = (uint32_t *)(cbar + 4);
     volatile int *abort_flag = (volatile int *)(tmem_holder + 1);
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -177,6 +195,7 @@ __global__ void __launch_bounds__(NTHR, 1)
             mbar_init(smem_u32(&empty[s]), 1);
         }
         mbar_init(smem_u32(done), 1);
+        for (int c = 0; c < 4; c++) mbar_init(smem_u32(&cbar[c]), 1);
         *abort_flag = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
@@ -205,7 +224,15 @@ __global__ void __launch_bounds__(NTHR, 1)
             if (!mbar_wait(smem_u32(&empty[s]), ph ^ 1u, abort_flag, P.flag)) break;
             const uint32_t sa = base + (uint32_t)s * stage_bytes;
             const uint32_t sb = sa + A_BYTES;
-            const int kidx = (kb0 + i) * KE;
+            // segment of this K block, and the block's index within it
+            int seg = 0, kk = kb0 + i;
+            if (P.nseg > 1 && kk >= P.seg_kb[0]) {
+                kk -= P.seg_kb[0];
+                seg = 1;
+                if (P.nseg > 2 && kk >= P.seg_kb[1]) { kk -= P.seg_kb[1]; seg = 2; }
+            }
+            const CUtensorMap *tmA = &maps.a[seg], *tmB = &maps.b[seg];
+            const int kidx = kk * KE;
             uint32_t bytes = 0;
             int nbox_a = 0;
             if (A_MN) {
@@ -220,12 +247,12 @@ __global__ void __launch_bounds__(NTHR, 1)
             mbar_expect_tx(fb, bytes);
             if (A_MN) {
                 for (int j = 0; j < nbox_a; j++)
-                    tma_load_2d(sa + (uint32_t)j * (uint32_t)(KE * KB), &tmA, fb, m0 + j * ATOM_M, kidx);
+                    tma_load_2d(sa + (uint32_t)j * (uint32_t)(KE * KB), tmA, fb, m0 + j * ATOM_M, kidx);
             } else {
-                tma_load_2d(sa, &tmA, fb, kidx, m0);
+                tma_load_2d(sa, tmA, fb, kidx, m0);
             }
-            tma_load_2d(sb, &tmB, fb, kidx, n0);
-            if (P.chunk_n1 > 0) tma_load_2d(sb + (uint32_t)P.chunk_n0 * KB, &tmB, fb, kidx, n0 + P.chunk_n0);
+            tma_load_2d(sb, tmB, fb, kidx, n0);
+            if (P.chunk_n1 > 0) tma_load_2d(sb + (uint32_t)P.chunk_n0 * KB, tmB, fb, kidx, n0 + P.chunk_n0);
         }
     } else if (threadIdx.x == 32 && nkb > 0) {
         // ---------------- MMA issuer
@@ -262,7 +289,47 @@ __global__ void __launch_bounds__(NTHR, 1)
     tc_fence_after();
     const int row = m0 + warp * 32 + lane;
     double fro = 0.0;
-    if (ok && EPI == EPI_UPDATE) {
+    if (EPI == EPI_UPDATE && P.c_tma) {
+        // C tile -> the stage buffers (free once `done` has fired) by TMA, in 64-column chunks
+        // that all start at once; D = C - alpha * acc in place in shared memory, each chunk
+        // TMA-stored as soon as it is done.  Rows / columns outside the matrix are zero-filled
+        // on load, clipped on store and left out of the sum of squares.
+        ok = __syncthreads_and(ok) != 0;
+        const int nch = (P.BN + CW - 1) / CW;
+        float *sc = (float *)sbase;
+        if (ok && threadIdx.x == 0) {
+            for (int c = 0; c < nch; c++) {
+                const uint32_t cb = smem_u32(&cbar[c]);
+                mbar_expect_tx(cb, (uint32_t)(BM * CW * 4));
+                tma_load_2d(base + (uint32_t)(c * BM * CW * 4), &maps.c, cb, m0, n0 + c * CW);
+            }
+        }
+        const int r = warp * 32 + lane;
+        for (int c = 0; ok && c < nch; c++) {
+            const bool got = mbar_wait(smem_u32(&cbar[c]), 0u, abort_flag, P.flag);
+            if (!__syncthreads_and(got)) break;
+            float *tile = sc + (size_t)c * BM * CW;
+#pragma unroll 1
+            for (int cc = 0; cc < CW; cc += 16) {
+                float v[16];
+                tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(c * CW + cc), v);
+#pragma unroll
+                for (int t = 0; t < 16; t++) {
+                    float *e = tile + (size_t)(cc + t) * BM + r;
+                    const float nv = *e - P.alpha * v[t];
+                    *e = nv;
+                    if (row < P.M && n0 + c * CW + cc + t < P.N) fro += (double)nv * (double)nv;
+                }
+            }
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            __syncthreads();
+            if (threadIdx.x == 0) {
+                tma_store_2d(&maps.d, base + (uint32_t)(c * BM * CW * 4), m0, n0 + c * CW);
+                asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+            }
+        }
+        if (threadIdx.x == 0) asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");
+    } else if (ok && EPI == EPI_UPDATE) {
         // C may alias D: each 16-column group of C is loaded into registers before any of
         // that group's stores, and the next group's loads are issued before this group is
         // stored, so a thread keeps 16 loads in flight instead of one
@@ -338,15 +405,45 @@ __global__ void __launch_bounds__(NTHR, 1)
     }
 }
 
+// D = alpha * (sum of the split-K partial slabs), summed in FP64.  Each thread reduces four
+// consecutive rows of one column with 16-byte loads, four slabs per step (the slabs'
+// leading dimension ldp and stride are multiples of 4 floats; rows M..ldp-1 are read and
+// dropped).
 __global__ void splitk_reduce_kernel(const float *part, long long stride, int splits, int M, int N, long long ldp,
                                      float *D, long long ldd, float alpha) {
-    const long long total = (long long)M * N;
+    const long long mq = ((long long)M + 3) / 4, total = mq * N, s4 = stride / 4;
     for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total; e += (long long)gridDim.x * blockDim.x) {
-        const long long i = e % M, j = e / M;
-        double acc = 0.0;                        // FP64 sum of the FP32 partial sums
-        for (int z = 0; z < splits; z++) acc += (double)part[z * stride + i + j * ldp];
-        D[i + j * ldd] = (float)((double)alpha * acc);
+        const long long j = e / mq, i = (e - j * mq) * 4;
+        const float4 *p = (const float4 *)(part + i + j * ldp);
+        double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
+        int z = 0;
+        for (; z + 4 <= splits; z += 4) {
+            const float4 v0 = __ldcs(p + (long long)z * s4), v1 = __ldcs(p + (long long)(z + 1) * s4);
+            const float4 v2 = __ldcs(p + (long long)(z + 2) * s4), v3 = __ldcs(p + (long long)(z + 3) * s4);
+            a0 += ((double)v0.x + (double)v1.x) + ((double)v2.x + (double)v3.x);
+            a1 += ((double)v0.y + (double)v1.y) + ((double)v2.y + (double)v3.y);
+            a2 += ((double)v0.z + (double)v1.z) + ((double)v2.z + (double)v3.z);
+            a3 += ((double)v0.w + (double)v1.w) + ((double)v2.w + (double)v3.w);
+        }
+        for (; z < splits; z++) {
+            const float4 v = __ldcs(p + (long long)z * s4);
+            a0 += (double)v.x; a1 += (double)v.y; a2 += (double)v.z; a3 += (double)v.w;
+        }
+        float *d = D + i + j * ldd;
+        const double al = (double)alpha;
+        d[0] = (float)(al * a0);
+        if (i + 1 < M) d[1] = (float)(al * a1);
+        if (i + 2 < M) d[2] = (float)(al * a2);
+        if (i + 3 < M) d[3] = (float)(al * a3);
     }
+}
+
+static void splitk_reduce(cudaStream_t s, const float *part, long long stride, int splits, int M, int N,
+                          long long ldp, float *D, long long ldd, float alpha, int sms) {
+    const long long total = ((long long)M + 3) / 4 * N;
+    const unsigned g = (unsigned)std::max<long long>(1, std::min<long long>((total + 255) / 256, (long long)sms * 16));
+    splitk_reduce_kernel<<<g, 256, 0, s>>>(part, stride, splits, M, N, ldp, D, ldd, alpha);
+    RSVD_LAUNCH_CK();
 }
 
 // ------------------------------------------------------------------ host side
@@ -388,9 +485,25 @@ static CUtensorMap make_map(const void *ptr, int esz, long long e0, long long e1
     return m;
 }
 
+// Unswizzled FP32 map for the update epilogue's C / D tiles: dim0 = rows (contiguous), box
+// {BM, CW} (512-byte rows of the box, packed column after column in shared memory).
+static CUtensorMap make_map_tile(const void *ptr, long long e0, long long e1, long long stride_bytes) {
+    if (((uintptr_t)ptr & 15) || (stride_bytes & 15)) fail(RSVD_ERR_ARGUMENT, "tensor map: 16-byte alignment");
+    CUtensorMap m;
+    std::memset(&m, 0, sizeof m);
+    cuuint64_t dims[2] = {(cuuint64_t)e0, (cuuint64_t)e1};
+    cuuint64_t strides[1] = {(cuuint64_t)stride_bytes};
+    cuuint32_t box[2] = {(cuuint32_t)BM, (cuuint32_t)CW};
+    cuuint32_t es[2] = {1, 1};
+    CUresult r = encode_fn()(&m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<void *>(ptr), dims, strides, box, es,
+                             CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                             CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) fail(RSVD_ERR_CUDA, "cuTensorMapEncodeTiled failed (C/D tile)");
+    return m;
+}
+
 template <int KIND, bool A_MN, int EPI>
-static void launch(cudaStream_t s, dim3 grid, size_t smem, const CUtensorMap &ta, const CUtensorMap &tb,
-                   const Params &P) {
+static void launch(cudaStream_t s, dim3 grid, size_t smem, const Maps &maps, const Params &P) {
     auto k = tc_gemm_kernel<KIND, A_MN, EPI>;
     static bool attr_set = false;   // per instantiation
     if (!attr_set) {
@@ -402,7 +515,7 @@ static void launch(cudaStream_t s, dim3 grid, size_t smem, const CUtensorMap &ta
                                      232448 - (int)fa.sharedSizeBytes));
         attr_set = true;
     }
-    k<<<grid, NTHR, smem, s>>>(ta, tb, P);
+    k<<<grid, NTHR, smem, s>>>(maps, P);
     RSVD_LAUNCH_CK();
     ctx().launches++;
     ctx().timing.gemm_launches++;
@@ -410,15 +523,20 @@ static void launch(cudaStream_t s, dim3 grid, size_t smem, const CUtensorMap &ta
 
 }  // namespace tc
 
-// Public launcher (declared in rsvd_internal.h).
-// D (M x N, fp32, ldd) = alpha * op(A) X^T-contracted ... see rsvd_internal.h.
-void tc_gemm(cudaStream_t s, int kind, bool a_mn, const void *A, long long lda, const void *X, long long ldx,
-             int M, int N, int K, float alpha, float *D, long long ldd, int epi, const float *C, long long ldc,
-             double *fro_part, int splits_hint) {
+// Public launchers (declared in rsvd_internal.h).
+void tc_gemm_segs(cudaStream_t s, int kind, bool a_mn, int nseg, const TcSeg *seg, int M, int N, float alpha,
+                  float *D, long long ldd, int epi, const float *C, long long ldc, double *fro_part, int splits_hint) {
     using namespace tc;
     const int esz = (kind == KIND_TF32) ? 4 : 2;
     const int KE = KB / esz;
-    if (M <= 0 || N <= 0 || K <= 0) fail(RSVD_ERR_ARGUMENT, "tc_gemm: empty");
+    if (nseg < 1 || nseg > MAX_SEG) fail(RSVD_ERR_ARGUMENT, "tc_gemm: 1 to 3 K segments");
+    if (M <= 0 || N <= 0) fail(RSVD_ERR_ARGUMENT, "tc_gemm: empty");
+    int num_kb = 0, Ktot = 0;
+    for (int g = 0; g < nseg; g++) {
+        if (seg[g].K <= 0) fail(RSVD_ERR_ARGUMENT, "tc_gemm: empty K segment");
+        num_kb += (seg[g].K + KE - 1) / KE;
+        Ktot += seg[g].K;
+    }
     // kind::tf32 with an MN-major A operand produced wrong products on GB300; only the
     // K-major form is used with tf32 (MN-major operands go through kind::f16 / bf16).
     if (kind == KIND_TF32 && a_mn) fail(RSVD_ERR_ARGUMENT, "tc_gemm: tf32 needs a K-major A operand");
@@ -432,7 +550,6 @@ void tc_gemm(cudaStream_t s, int kind, bool a_mn, const void *A, long long lda, 
     else { BN = 256; c0 = 256; c1 = 0; }
     const int ntiles = (N + BN - 1) / BN;
     const int mtiles = (M + BM - 1) / BM;
-    const int num_kb = (K + KE - 1) / KE;
     // split-K so that the grid fills the GPU when row tiles are few
     int splits = 1;
     const int sms = std::max(1, ctx().sms);
@@ -466,10 +583,17 @@ void tc_gemm(cudaStream_t s, int kind, bool a_mn, const void *A, long long lda, 
     const size_t smem = (size_t)stages * stage_bytes + 1024 + 64 + 16 * stages;
 
     // tensor maps: A either MN-major (dim0 = M) or K-major (dim0 = K); X K-major (dim0 = K)
-    CUtensorMap ta = a_mn ? make_map(A, esz, M, K, lda * esz, KE, KE) : make_map(A, esz, K, M, lda * esz, KE, BM);
-    CUtensorMap tb = make_map(X, esz, K, N, ldx * esz, KE, c0);
+    Maps maps;
+    std::memset(&maps, 0, sizeof maps);
     Params P{};
-    P.M = M; P.N = N; P.K = K; P.BN = BN; P.chunk_n0 = c0; P.chunk_n1 = c1;
+    for (int g = 0; g < nseg; g++) {
+        const TcSeg &q = seg[g];
+        maps.a[g] = a_mn ? make_map(q.A, esz, M, q.K, q.lda * esz, KE, KE) : make_map(q.A, esz, q.K, M, q.lda * esz, KE, BM);
+        maps.b[g] = make_map(q.X, esz, q.K, N, q.ldx * esz, KE, c0);
+        P.seg_kb[g] = (q.K + KE - 1) / KE;
+    }
+    P.nseg = nseg;
+    P.M = M; P.N = N; P.K = Ktot; P.BN = BN; P.chunk_n0 = c0; P.chunk_n1 = c1;
     P.num_kb = num_kb; P.kb_per_split = kb_per_split; P.stages = stages; P.alpha = alpha;
     P.flag = ctx().d_flags + FLAG_TIMEOUT;
     P.fro_part = fro_part;
@@ -477,23 +601,35 @@ void tc_gemm(cudaStream_t s, int kind, bool a_mn, const void *A, long long lda, 
     dim3 grid(mtiles, ntiles, splits);
     if (epi == EPI_UPDATE) {
         P.D = D; P.ldd = ldd;
+        // C through shared memory by TMA when the tile fits in the stage buffers, the
+        // 64-column chunks stay inside this CTA's columns, and M is a multiple of 4 (the
+        // bulk store clipped a ragged row extent only at 16-byte granularity on GB300: with
+        // M = 257 it wrote rows 257..259)
+        const int nch = (BN + CW - 1) / CW;
+        P.c_tma = M % 4 == 0 && BN <= 256 && (ntiles == 1 || BN % CW == 0) &&
+                  (size_t)nch * BM * CW * 4 <= (size_t)stages * stage_bytes &&
+                  ((uintptr_t)C % 16 == 0) && ((uintptr_t)D % 16 == 0) && (ldc * 4) % 16 == 0 && (ldd * 4) % 16 == 0;
+        if (P.c_tma) {
+            maps.c = make_map_tile(C, M, N, ldc * 4);
+            maps.d = make_map_tile(D, M, N, ldd * 4);
+        }
         if (kind == KIND_TF32) {
-            if (a_mn) launch<KIND_TF32, true, EPI_UPDATE>(s, grid, smem, ta, tb, P);
-            else launch<KIND_TF32, false, EPI_UPDATE>(s, grid, smem, ta, tb, P);
+            if (a_mn) launch<KIND_TF32, true, EPI_UPDATE>(s, grid, smem, maps, P);
+            else launch<KIND_TF32, false, EPI_UPDATE>(s, grid, smem, maps, P);
         } else {
-            if (a_mn) launch<KIND_BF16, true, EPI_UPDATE>(s, grid, smem, ta, tb, P);
-            else launch<KIND_BF16, false, EPI_UPDATE>(s, grid, smem, ta, tb, P);
+            if (a_mn) launch<KIND_BF16, true, EPI_UPDATE>(s, grid, smem, maps, P);
+            else launch<KIND_BF16, false, EPI_UPDATE>(s, grid, smem, maps, P);
         }
         return;
     }
     if (splits == 1) {
         P.D = D; P.ldd = ldd;
         if (kind == KIND_TF32) {
-            if (a_mn) launch<KIND_TF32, true, EPI_STORE>(s, grid, smem, ta, tb, P);
-            else launch<KIND_TF32, false, EPI_STORE>(s, grid, smem, ta, tb, P);
+            if (a_mn) launch<KIND_TF32, true, EPI_STORE>(s, grid, smem, maps, P);
+            else launch<KIND_TF32, false, EPI_STORE>(s, grid, smem, maps, P);
         } else {
-            if (a_mn) launch<KIND_BF16, true, EPI_STORE>(s, grid, smem, ta, tb, P);
-            else launch<KIND_BF16, false, EPI_STORE>(s, grid, smem, ta, tb, P);
+            if (a_mn) launch<KIND_BF16, true, EPI_STORE>(s, grid, smem, maps, P);
+            else launch<KIND_BF16, false, EPI_STORE>(s, grid, smem, maps, P);
         }
         return;
     }
@@ -502,17 +638,22 @@ void tc_gemm(cudaStream_t s, int kind, bool a_mn, const void *A, long long lda, 
     DBuf part(sizeof(float) * (size_t)stride * splits, s);
     P.D = (float *)part.get(); P.ldd = ldp; P.part_stride = stride;
     if (kind == KIND_TF32) {
-        if (a_mn) launch<KIND_TF32, true, EPI_PARTIAL>(s, grid, smem, ta, tb, P);
-        else launch<KIND_TF32, false, EPI_PARTIAL>(s, grid, smem, ta, tb, P);
+        if (a_mn) launch<KIND_TF32, true, EPI_PARTIAL>(s, grid, smem, maps, P);
+        else launch<KIND_TF32, false, EPI_PARTIAL>(s, grid, smem, maps, P);
     } else {
-        if (a_mn) launch<KIND_BF16, true, EPI_PARTIAL>(s, grid, smem, ta, tb, P);
-        else launch<KIND_BF16, false, EPI_PARTIAL>(s, grid, smem, ta, tb, P);
+        if (a_mn) launch<KIND_BF16, true, EPI_PARTIAL>(s, grid, smem, maps, P);
+        else launch<KIND_BF16, false, EPI_PARTIAL>(s, grid, smem, maps, P);
     }
-    const long long total = (long long)M * N;
-    const unsigned g = (unsigned)std::min<long long>((total + 255) / 256, (long long)sms * 8);
-    splitk_reduce_kernel<<<g, 256, 0, s>>>((const float *)part.get(), stride, splits, M, N, ldp, D, ldd, alpha);
-    RSVD_LAUNCH_CK();
+    splitk_reduce(s, (const float *)part.get(), stride, splits, M, N, ldp, D, ldd, alpha, sms);
     ctx().launches++;
+}
+
+void tc_gemm(cudaStream_t s, int kind, bool a_mn, const void *A, long long lda, const void *X, long long ldx,
+             int M, int N, int K, float alpha, float *D, long long ldd, int epi, const float *C, long long ldc,
+             double *fro_part, int splits_hint) {
+    if (K <= 0) fail(RSVD_ERR_ARGUMENT, "tc_gemm: empty");
+    const TcSeg g{A, lda, X, ldx, K};
+    tc_gemm_segs(s, kind, a_mn, 1, &g, M, N, alpha, D, ldd, epi, C, ldc, fro_part, splits_hint);
 }
 
 // =====================================================================================
@@ -611,21 +752,21 @@ extern "C" int rsvdpack_dev_sketch_t_noalloc(const float *dA, long long lda, int
         const size_t stage_bytes = (size_t)A_BYTES + (size_t)BN * KB;
         const int stages = (int)std::min<size_t>(8, (220 * 1024) / stage_bytes);
         const size_t smem = (size_t)stages * stage_bytes + 1024 + 64 + 16 * stages;
-        CUtensorMap ta = make_map(dA, 4, K, M, lda * 4, KE, BM);
-        CUtensorMap tb = make_map(dX, 4, K, N, ldx * 4, KE, c0);
+        Maps maps;
+        std::memset(&maps, 0, sizeof maps);
+        maps.a[0] = make_map(dA, 4, K, M, lda * 4, KE, BM);
+        maps.b[0] = make_map(dX, 4, K, N, ldx * 4, KE, c0);
         int *flag = (int *)scratch;
         float *part = (float *)(scratch + NOALLOC_HEADER);
         Params P{};
         P.M = M; P.N = N; P.K = K; P.BN = BN; P.chunk_n0 = c0; P.chunk_n1 = c1;
         P.num_kb = num_kb; P.kb_per_split = kb_per_split; P.stages = stages; P.alpha = 1.0f;
+        P.nseg = 1; P.seg_kb[0] = num_kb;
         P.flag = flag; P.D = part; P.ldd = ldp; P.part_stride = stride;
         RSVD_CK(cudaMemsetAsync(flag, 0, sizeof(int), s));
-        tc_gemm_kernel<KIND_TF32, false, EPI_PARTIAL><<<dim3(mtiles, ntiles, splits), NTHR, smem, s>>>(ta, tb, P);
+        tc_gemm_kernel<KIND_TF32, false, EPI_PARTIAL><<<dim3(mtiles, ntiles, splits), NTHR, smem, s>>>(maps, P);
         RSVD_LAUNCH_CK();
-        const long long total = (long long)M * N;
-        const unsigned g = (unsigned)std::min<long long>((total + 255) / 256, (long long)std::max(1, sms) * 8);
-        splitk_reduce_kernel<<<g, 256, 0, s>>>(part, stride, splits, M, N, ldp, dY, ldy, 1.0f);
-        RSVD_LAUNCH_CK();
+        splitk_reduce(s, part, stride, splits, M, N, ldp, dY, ldy, 1.0f, sms);
         int h = 0;
         RSVD_CK(cudaMemcpyAsync(&h, flag, sizeof(int), cudaMemcpyDeviceToHost, s));
         RSVD_CK(cudaStreamSynchronize(s));
@@ -659,11 +800,11 @@ __global__ void split_tf32_kernel(const float *X, long long ldx, long long r, lo
 }  // namespace
 
 namespace {
-__global__ void add2_kernel(float *D, long long ldd, const float *T1, const float *T2, long long ldt, int M, int N) {
+__global__ void add_kernel(float *D, long long ldd, const float *T, long long ldt, int M, int N) {
     for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < (long long)M * N;
          e += (long long)gridDim.x * blockDim.x) {
         const long long j = e / M, i = e - j * M;
-        D[i + j * ldd] += T1[i + j * ldt] + T2[i + j * ldt];
+        D[i + j * ldd] += T[i + j * ldt];
     }
 }
 }  // namespace
@@ -678,26 +819,39 @@ void split_tf32(cudaStream_t s, const float *X, long long ldx, long long r, long
 }
 
 // D (M x N) = A^T X with A K-major (K x M, lda) and X (K x N, ldx), both given split.
-// All three products are split along K into chunks of ~2048 (FP32 accumulation in TMEM
-// within a chunk, FP64 across chunks), so neither the accumulation error nor the CTA count
-// is limited by a long K; the two correction terms go to temporaries and one elementwise
-// pass adds them.
+// The tensor core's FP32 accumulation truncates at every MMA step, so its error grows with
+// the number of steps in one accumulation chain, not with sqrt(K): a 2048-long chain of
+// the dominant hi x hi product already costs ~1e-5 relative.  That product is therefore
+// split along K into chains of ~256 (FP32 in TMEM within a chain, FP64 across chains,
+// ~1e-6 relative), its partial slabs capped at 1 GiB.  The two correction terms, 2^-11
+// smaller, are one two-segment product with chains of ~2048 into a temporary that one
+// elementwise pass adds.
 void tc_gemm_3xtf32(cudaStream_t s, const float *Ahi, const float *Alo, long long lda, const float *Xhi,
                     const float *Xlo, long long ldx, int M, int N, int K, float *D, long long ldd) {
-    const int splits = std::max(1, std::min(32, K / 2048));
     const long long ldt = ((long long)M + 31) / 32 * 32;
-    DBuf t1(sizeof(float) * (size_t)ldt * N, s), t2(sizeof(float) * (size_t)ldt * N, s);
+    const long long slab_cap = std::max(1ll, (1ll << 30) / (ldt * N * (long long)sizeof(float)));
+    const int splits_hh = (int)std::max(1ll, std::min({(K + 255) / 256ll, slab_cap, 128ll}));
+    const int splits = std::max(1, std::min(32, K / 1024));
+    DBuf t(sizeof(float) * (size_t)ldt * N, s);
     tc_gemm(s, tc::KIND_TF32, false, Ahi, lda, Xhi, ldx, M, N, K, 1.0f, D, ldd, tc::EPI_STORE, nullptr, 0, nullptr,
-            splits);
-    tc_gemm(s, tc::KIND_TF32, false, Alo, lda, Xhi, ldx, M, N, K, 1.0f, (float *)t1.get(), ldt, tc::EPI_STORE,
-            nullptr, 0, nullptr, splits);
-    tc_gemm(s, tc::KIND_TF32, false, Ahi, lda, Xlo, ldx, M, N, K, 1.0f, (float *)t2.get(), ldt, tc::EPI_STORE,
-            nullptr, 0, nullptr, splits);
+            splits_hh);
+    const TcSeg corr[2] = {{Alo, lda, Xhi, ldx, K}, {Ahi, lda, Xlo, ldx, K}};
+    tc_gemm_segs(s, tc::KIND_TF32, false, 2, corr, M, N, 1.0f, (float *)t.get(), ldt, tc::EPI_STORE, nullptr, 0,
+                 nullptr, splits);
     const long long want = ((long long)M * N + 255) / 256, cap = (long long)std::max(1, ctx().sms) * 16;
-    add2_kernel<<<(unsigned)std::min(want, cap), 256, 0, s>>>(D, ldd, (const float *)t1.get(),
-                                                               (const float *)t2.get(), ldt, M, N);
+    add_kernel<<<(unsigned)std::min(want, cap), 256, 0, s>>>(D, ldd, (const float *)t.get(), ldt, M, N);
     RSVD_LAUNCH_CK();
     ctx().launches++;
+}
+
+// C (M x N) -= A^T X from split operands, the three terms as one three-segment update
+// (lo x hi, hi x lo, then hi x hi: the small terms accumulate first).  fro_part: per-CTA
+// sums of squares of the new C (tc_gemm's update layout), or null.
+void tc_update_3xtf32(cudaStream_t s, const float *Ahi, const float *Alo, long long lda, const float *Xhi,
+                      const float *Xlo, long long ldx, int M, int N, int K, float *Cm, long long ldc,
+                      double *fro_part) {
+    const TcSeg g[3] = {{Alo, lda, Xhi, ldx, K}, {Ahi, lda, Xlo, ldx, K}, {Ahi, lda, Xhi, ldx, K}};
+    tc_gemm_segs(s, tc::KIND_TF32, false, 3, g, M, N, 1.0f, Cm, ldc, tc::EPI_UPDATE, Cm, ldc, fro_part, 1);
 }
 
 }  // namespace rsvd

@@ -91,6 +91,10 @@ struct Ctx {
     rsvdpack_opts opts{};
     rsvdpack_timing timing{};
     long long launches = 0;
+    // TF32 mode: products A X (A the MN-major operand, which kind::tf32 cannot read) take A
+    // as a two-part BF16 split (hi + lo, 16 mantissa bits) instead of one BF16 copy (7 bits).
+    // Set by the fixed-precision block loop, whose sketches must resolve the deflated matrix.
+    bool ax_split = false;
 };
 Ctx &ctx();                       // initialises the device on first use; throws RSVD_ERR_NO_DEVICE
 const rsvdpack_opts &global_opts();
@@ -118,6 +122,8 @@ void gemm(cudaStream_t s, bool ta, bool tb, T alpha, DM<T> A, DM<T> B, T beta, D
 
 template <typename Ts, typename Td>
 void convert(cudaStream_t s, DM<Ts> src, DM<Td> dst);      // dst = (Td)src, same shape
+// hi = bf16(x) (round to nearest), lo = bf16(x - hi): x = hi + lo to ~2^-16 relative.
+void split_bf16(cudaStream_t s, DM<float> src, DM<__nv_bfloat16> hi, DM<__nv_bfloat16> lo);
 template <typename T>
 void fill_zero(cudaStream_t s, DM<T> a);
 template <typename T>
@@ -185,12 +191,29 @@ namespace rsvd {
 void tc_gemm(cudaStream_t s, int kind, bool a_mn, const void *A, long long lda, const void *X, long long ldx,
              int M, int N, int K, float alpha, float *D, long long ldd, int epi, const float *C, long long ldc,
              double *fro_part, int splits_hint);
+// The same product with K split into up to 3 segments that accumulate into one result:
+// acc = sum_s Aop_s^T-contracted X_s (each segment its own operands, leading dimensions and
+// K; all share M, N and a_mn), in segment order.  Used for the three terms of a 3xTF32
+// product (small terms first), so that they make one pass over the output.
+struct TcSeg {
+    const void *A;
+    long long lda;
+    const void *X;
+    long long ldx;
+    int K;
+};
+void tc_gemm_segs(cudaStream_t s, int kind, bool a_mn, int nseg, const TcSeg *seg, int M, int N, float alpha,
+                  float *D, long long ldd, int epi, const float *C, long long ldc, double *fro_part, int splits_hint);
 // 3xTF32 (FP32-accurate) products on the tf32 pipe: split_tf32 writes hi = tf32(X) and
 // lo = X - hi; tc_gemm_3xtf32 computes D = A^T X (A K-major, K x M) from split operands.
 void split_tf32(cudaStream_t s, const float *X, long long ldx, long long r, long long c, float *hi, float *lo,
                 long long ldo);
 void tc_gemm_3xtf32(cudaStream_t s, const float *Ahi, const float *Alo, long long lda, const float *Xhi,
                     const float *Xlo, long long ldx, int M, int N, int K, float *D, long long ldd);
+// C (M x N) -= A^T X (3xTF32, one pass over C, in place); fro_part as for tc_gemm's update.
+void tc_update_3xtf32(cudaStream_t s, const float *Ahi, const float *Alo, long long lda, const float *Xhi,
+                      const float *Xlo, long long ldx, int M, int N, int K, float *Cm, long long ldc,
+                      double *fro_part);
 // ----------------------------------------------------------------- tiled triangular steps (k_chol.cu)
 // G (n x n, FP64, upper triangle read) -> R, G = R^T R (upper, zero below), compute type S.
 // dinv (optional): receives the inverses of R's 32 x 32 diagonal tiles (ceil(n/32) row-major

@@ -4,7 +4,8 @@ Each sample is a generated spectrum s (length r = min(m, n)), a tolerance TOL an
 outcome of runs of the method itself on it:
 
   features : the 32 R-diagonal magnitudes of a 32-column probe sketch Y0 = A Omega0 (relative
-             to ||A||_F, log10), the captured energy sum_j R_jj^2 / ||A||_F^2, log10 r,
+             to ||A||_F, log10), the energy the probe leaves, log10 max(1 - sum_j R_jj^2 /
+             ||A||_F^2, 1e-5) (floored where FP32 rounding would blur it), log10 r,
              log10(m / n) and log10 TOL.
   labels   : for q = 1 and q = 2 power iterations, the smallest sketch width l (a multiple
              of 32) at which the single-shot randomized range finder with l Gaussian
@@ -85,7 +86,7 @@ def feature_vector(rdiag: np.ndarray, fro: float, m: int, n: int, tol: float) ->
     rel = np.maximum(np.asarray(rdiag, dtype=np.float64) / fro, 1e-30)
     f = np.empty(N_FEATURES, dtype=np.float64)
     f[:PROBE] = np.log10(rel)
-    f[PROBE] = float(np.sum(rel * rel))
+    f[PROBE] = np.log10(max(1.0 - float(np.sum(rel * rel)), 1e-5))
     f[PROBE + 1] = np.log10(min(m, n))
     f[PROBE + 2] = np.log10(m / n)
     f[PROBE + 3] = np.log10(tol)
@@ -134,6 +135,17 @@ def sample(seed: int) -> tuple[np.ndarray, np.ndarray, np.ndarray]:
     return f, widths, reached
 
 
+def features_only(seed: int) -> np.ndarray:
+    """The feature vector of sample(seed), without the label runs (the probe draws its test
+    matrix before the labels do, so the stream is the same)."""
+    rng = np.random.default_rng(seed)
+    m = int(rng.integers(1024, 8193))
+    n = int(rng.integers(1024, 8193))
+    s, _ = spectrum(rng, min(m, n))
+    tol = float(10.0 ** rng.uniform(-6.0, -2.0))
+    return probe_features(s, m, n, tol, rng)
+
+
 def _work(args):
     lo, hi, base = args
     os.environ.setdefault("OPENBLAS_NUM_THREADS", "1")
@@ -167,7 +179,15 @@ def main():
     ap.add_argument("--count", type=int, default=20000)
     ap.add_argument("--seed", type=int, default=1_000_000)
     ap.add_argument("--procs", type=int, default=os.cpu_count() or 1)
+    ap.add_argument("--refeature", help="recompute the features of an existing set (labels kept)")
     a = ap.parse_args()
+    if a.refeature:
+        d = dict(np.load(a.refeature))
+        base = int(d["base_seed"])
+        d["features"] = np.stack([features_only(base + i) for i in range(len(d["features"]))]).astype(np.float32)
+        np.savez_compressed(a.out, **d)
+        print("refeatured", a.out)
+        return
     d = build(a.count, a.seed, a.procs)
     np.savez_compressed(a.out, **d)
     print("wrote", a.out, {k: v.shape for k, v in d.items() if hasattr(v, "shape")})

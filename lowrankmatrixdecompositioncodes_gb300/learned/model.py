@@ -2,11 +2,11 @@
 kernels (rsvdpack_mlp_train_step / rsvdpack_mlp_forward, csrc/k_mlp.cu), the weights file,
 and the decision rule.
 
-Model: features (dataset.feature_vector: the probe's R-diagonal, captured energy, log sizes,
-log TOL) -> predicted log2(width / 32) of the single-shot range finder for q = 1 and q = 2.
-A safety margin per output (the validation set's 95th percentile of target - prediction over
-runs that reached the tolerance) is added before the width is used, so that most proposals
-verify and the adaptive loop (the fallback) runs rarely.
+Model: features (dataset.feature_vector: the probe's R-diagonal, the energy it leaves, log
+sizes, log TOL) -> predicted log2(width / 32) of the single-shot range finder for q = 1 and q = 2.
+A margin per output (the validation set's 60th percentile of target - prediction over runs
+that reached the tolerance) is added before the width is used: an undersized proposal costs
+one more block of the adaptive continuation, an oversized one costs columns in every block.
 
 Weights file (little-endian): b"RSVDMLP1", int32 ndims, int32 dims[ndims], int32 nparams,
 int32 nnorm, float32 params[nparams], float32 norm[nnorm], float32 margin[dims[-1]].
@@ -106,7 +106,7 @@ class Trainer:
         return dP.cpu().numpy(), norm
 
 
-def calibrate_margin(pred: np.ndarray, T: np.ndarray, R: np.ndarray, quantile=0.95) -> np.ndarray:
+def calibrate_margin(pred: np.ndarray, T: np.ndarray, R: np.ndarray, quantile=0.6) -> np.ndarray:
     m = np.zeros(pred.shape[1], np.float32)
     for j in range(pred.shape[1]):
         ok = R[:, j] > 0

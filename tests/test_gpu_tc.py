@@ -87,3 +87,70 @@ def test_mixed_precision_rsvd_matches_fp64_error(engine, prec, k, p):
         res[mode] = np.linalg.norm(A - U @ S @ V.T) / np.linalg.norm(A)
     engine.set_precision("fp64")
     assert res[prec] <= res["fp64"] * (1 + 1e-3), res
+
+
+def _bind3(L):
+    L.rsvdpack_dev_gemm_3xtf32.restype = C.c_int
+    L.rsvdpack_dev_gemm_3xtf32.argtypes = [C.c_void_p, C.c_longlong, C.c_void_p, C.c_longlong, C.c_int, C.c_int,
+                                           C.c_int, C.c_void_p, C.c_longlong]
+    L.rsvdpack_dev_update_3xtf32.restype = C.c_int
+    L.rsvdpack_dev_update_3xtf32.argtypes = [C.c_void_p, C.c_longlong, C.c_void_p, C.c_longlong, C.c_int, C.c_int,
+                                             C.c_int, C.c_void_p, C.c_longlong, C.POINTER(C.c_double)]
+
+
+@pytest.mark.parametrize("M,N,K", [(1000, 300, 4096), (333, 130, 20000), (2048, 64, 777), (130, 520, 33)])
+def test_3xtf32_product_is_fp32_accurate(engine, M, N, K):
+    """D = A^T X from split operands: the error stays at FP32 level (~1e-6 of the product's
+    scale) even for long K, where one FP32-accumulated tensor-core chain would drift."""
+    _bind3(engine.lib)
+    g = torch.Generator(device="cuda")
+    g.manual_seed(M + N + K)
+    lda, ldx, ldd = (K + 3) // 4 * 4, (K + 3) // 4 * 4, (M + 3) // 4 * 4
+    A = colmajor(K, M, lda, g)
+    X = colmajor(K, N, ldx, g)
+    D = torch.full((N, ldd), float("nan"), device="cuda")
+    torch.cuda.synchronize()
+    rc = engine.lib.rsvdpack_dev_gemm_3xtf32(A.data_ptr(), lda, X.data_ptr(), ldx, M, N, K, D.data_ptr(), ldd)
+    assert rc == 0, engine.last_error()
+    ref = view(A, K).T @ view(X, K)
+    err = float((view(D, M) - ref).norm() / ref.norm())
+    assert err < 3e-6, err
+    if ldd > M:
+        assert torch.isnan(D[:, M:]).all()
+
+
+# (M, N, K, ldc pad): N > 512 tiles by 256 columns, N <= 256 is one tile with a ragged last
+# 64-column chunk (both through the TMA epilogue); 256 < N <= 512 is two MMA chunks, and an
+# odd ldc or M % 4 != 0 (padding rows right after row M) take the register epilogue; M not
+# a multiple of 128 leaves a ragged last row tile
+@pytest.mark.parametrize("M,N,K,pad", [(1000, 700, 96, 4), (300, 200, 64, 0), (257, 530, 40, 3), (300, 400, 50, 4),
+                                       (129, 1030, 288, 1), (4096, 2048, 256, 0), (260, 530, 40, 4),
+                                       (1000, 130, 33, 8)])
+def test_3xtf32_update_in_place(engine, M, N, K, pad):
+    """C -= A^T X in one pass (the blocked-QB deflation): C close to A^T X, so the result is
+    small against the terms; it must match FP64 to ~1e-6 of the terms' scale, leave padding
+    rows untouched, and report ||C||_F^2 of the result."""
+    _bind3(engine.lib)
+    g = torch.Generator(device="cuda")
+    g.manual_seed(M * 3 + N + K)
+    lda, ldx = (K + 3) // 4 * 4, (K + 3) // 4 * 4
+    ldc = M + pad if pad else M
+    A = colmajor(K, M, lda, g)
+    X = colmajor(K, N, ldx, g)
+    prod = view(A, K).T @ view(X, K)
+    Cm = torch.full((N, ldc), float("nan"), device="cuda")
+    small = 1e-3 * torch.randn(N, M, device="cuda", generator=g, dtype=torch.float64)
+    Cm[:, :M] = (prod.T + small).float()
+    C0 = view(Cm, M).clone()
+    fro2 = C.c_double(0.0)
+    torch.cuda.synchronize()
+    rc = engine.lib.rsvdpack_dev_update_3xtf32(A.data_ptr(), lda, X.data_ptr(), ldx, M, N, K, Cm.data_ptr(), ldc,
+                                               C.byref(fro2))
+    assert rc == 0, engine.last_error()
+    ref = C0 - prod
+    got = view(Cm, M)
+    err = float((got - ref).norm() / prod.norm())
+    assert err < 2e-6, err
+    assert abs(fro2.value - float((got * got).sum())) <= 1e-5 * float((got * got).sum())
+    if ldc > M:
+        assert torch.isnan(Cm[:, M:]).all()
