@@ -212,7 +212,7 @@ int rsvdpack_dev_sketch(const void *dA, int dtype, long long lda, int m, int n, 
 
 /* FP32-accurate tensor-core products (3xTF32): x = hi + lo with hi = x rounded to TF32; the
  * terms lo*hi, hi*lo and hi*hi accumulate on the tf32 pipe in FP32 (long K in chains of ~256,
- * summed in FP64).  FP32 device data, column-major: A is K x M (lda), X is K x N (ldx).
+ * summed with compensation).  FP32 device data, column-major: A is K x M (lda), X is K x N (ldx).
  * rsvdpack_dev_gemm_3xtf32:   D (M x N, ldd) = A^T X.
  * rsvdpack_dev_update_3xtf32: C (M x N, ldc) -= A^T X in place in one pass over C (the
  *   blocked-QB deflation A_res -= Q_j B_j with A = Q_j^T, X = B_j); fro2 (host, optional)

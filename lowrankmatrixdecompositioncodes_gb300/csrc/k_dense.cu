@@ -279,16 +279,30 @@ __global__ void sub_kernel(T *a, i64 lda, const T *b, i64 ldb, i64 r, i64 c) {
     }
 }
 template <typename T>
+// Sum of squares, 2-D like convert_kernel (blockIdx.x: 1024 rows, blockIdx.y strides the
+// columns).  Each thread sums its elements in T with Kahan compensation and converts once:
+// FP32 data costs no FP64 arithmetic per element (GB300's FP64 rate is a small fraction of
+// its FP32 rate), and the compensated FP32 sum keeps ~2^-24 relative accuracy.
 __global__ void sumsq_kernel(const T *a, i64 ld, i64 r, i64 c, double *partial) {
     __shared__ double sc[32];
-    double acc = 0.0;
-    for (i64 e = blockIdx.x * (i64)blockDim.x + threadIdx.x; e < r * c; e += (i64)gridDim.x * blockDim.x) {
-        const i64 i = e % r, j = e / r;
-        const double v = (double)a[i + j * ld];
-        acc = fma(v, v, acc);
+    const i64 i0 = (i64)blockIdx.x * 1024 + threadIdx.x;
+    T sum = T(0), comp = T(0);
+    for (i64 j = blockIdx.y; j < c; j += gridDim.y) {
+        const T *col = a + j * ld;
+#pragma unroll
+        for (int t = 0; t < 4; t++) {
+            const i64 i = i0 + 256 * t;
+            if (i < r) {
+                const T v = col[i];
+                const T y = v * v - comp;
+                const T tt = sum + y;
+                comp = (tt - sum) - y;
+                sum = tt;
+            }
+        }
     }
-    acc = block_sum(acc, sc);
-    if (threadIdx.x == 0) partial[blockIdx.x] = acc;
+    double acc = block_sum((double)sum - (double)comp, sc);
+    if (threadIdx.x == 0) partial[blockIdx.x + (i64)gridDim.x * blockIdx.y] = acc;
 }
 unsigned grid_for(i64 n) {
     i64 g = (n + 255) / 256;
@@ -386,9 +400,11 @@ void sub_inplace(cudaStream_t s, DM<T> a, DM<T> b) {
 template <typename T>
 double frob_norm(cudaStream_t s, DM<T> a) {
     if (a.r * a.c == 0) return 0.0;
-    const unsigned g = std::min<unsigned>(grid_for(a.r * a.c), 1024);
+    const unsigned gx = (unsigned)((a.r + 1023) / 1024);
+    const unsigned gy = (unsigned)std::max<i64>(1, std::min<i64>(a.c, std::max<i64>(1, (i64)std::max(1, ctx().sms) * 8 / gx)));
+    const unsigned g = gx * gy;
     DBuf part(sizeof(double) * g, s);
-    sumsq_kernel<T><<<g, 256, 0, s>>>(a.p, a.ld, a.r, a.c, (double *)part.get());
+    sumsq_kernel<T><<<dim3(gx, gy), 256, 0, s>>>(a.p, a.ld, a.r, a.c, (double *)part.get());
     RSVD_LAUNCH_CK();
     std::vector<double> h(g);
     RSVD_CK(cudaMemcpyAsync(h.data(), part.get(), sizeof(double) * g, cudaMemcpyDeviceToHost, s));

@@ -162,6 +162,18 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
     for (int i = 0; i < 16; i++) v[i] = __uint_as_float(r[i]);
 }
 
+// Kahan-compensated FP32 accumulation (the update epilogue's sum of squares; FP64 per
+// element would cost more than the epilogue itself on GB300).
+struct KahanF {
+    float s = 0.f, c = 0.f;
+    __device__ __forceinline__ void add(float x) {
+        const float y = x - c, t = s + y;
+        c = (t - s) - y;
+        s = t;
+    }
+    __device__ __forceinline__ double value() const { return (double)s - (double)c; }
+};
+
 template <int KIND, bool A_MN, int EPI>
 __global__ void __launch_bounds__(NTHR, 1)
     tc_gemm_kernel(const __grid_constant__ Maps maps, Params P) {
@@ -288,7 +300,7 @@ __global__ void __launch_bounds__(NTHR, 1)
     __syncwarp();
     tc_fence_after();
     const int row = m0 + warp * 32 + lane;
-    double fro = 0.0;
+    KahanF fro;
     if (EPI == EPI_UPDATE && P.c_tma) {
         // C tile -> the stage buffers (free once `done` has fired) by TMA, in 64-column chunks
         // that all start at once; D = C - alpha * acc in place in shared memory, each chunk
@@ -318,7 +330,7 @@ __global__ void __launch_bounds__(NTHR, 1)
                     float *e = tile + (size_t)(cc + t) * BM + r;
                     const float nv = *e - P.alpha * v[t];
                     *e = nv;
-                    if (row < P.M && n0 + c * CW + cc + t < P.N) fro += (double)nv * (double)nv;
+                    if (row < P.M && n0 + c * CW + cc + t < P.N) fro.add(nv * nv);
                 }
             }
             asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
@@ -361,7 +373,7 @@ __global__ void __launch_bounds__(NTHR, 1)
                     if (col < P.N) {
                         const float nv = cv[t] - P.alpha * v[t];
                         P.D[(long long)row + (long long)col * P.ldd] = nv;
-                        if (want_fro) fro += (double)nv * (double)nv;
+                        if (want_fro) fro.add(nv * nv);
                     }
                 }
             }
@@ -386,7 +398,7 @@ __global__ void __launch_bounds__(NTHR, 1)
                     } else {
                         const float nv = P.C[(long long)row + (long long)col * P.ldc] - P.alpha * v[t];
                         P.D[(long long)row + (long long)col * P.ldd] = nv;
-                        fro += (double)nv * (double)nv;
+                        fro.add(nv * nv);
                     }
                 }
             }
@@ -394,8 +406,8 @@ __global__ void __launch_bounds__(NTHR, 1)
     }
     if (EPI == EPI_UPDATE && P.fro_part) {
         __shared__ double red[32];
-        fro = block_sum(fro, red);
-        if (threadIdx.x == 0) P.fro_part[blockIdx.x + (long long)gridDim.x * blockIdx.y] = fro;
+        const double tot = block_sum(fro.value(), red);
+        if (threadIdx.x == 0) P.fro_part[blockIdx.x + (long long)gridDim.x * blockIdx.y] = tot;
     }
     tc_fence_before();
     __syncthreads();
@@ -405,36 +417,44 @@ __global__ void __launch_bounds__(NTHR, 1)
     }
 }
 
-// D = alpha * (sum of the split-K partial slabs), summed in FP64.  Each thread reduces four
-// consecutive rows of one column with 16-byte loads, four slabs per step (the slabs'
-// leading dimension ldp and stride are multiples of 4 floats; rows M..ldp-1 are read and
-// dropped).
+// D = alpha * (sum of the split-K partial slabs).  The slabs are summed in FP32 with
+// Neumaier's compensation (error ~2^-24 of the sum plus a second-order term), not in FP64:
+// FP64 adds and conversions, one of each per slab and element, made this pass FP64-bound
+// on GB300 (~1 TB/s).  Each thread reduces four consecutive rows of one column with 16-byte
+// loads, four slabs per step (the slabs' leading dimension ldp and stride are multiples of
+// 4 floats; rows M..ldp-1 are read and dropped).
+struct Neumaier {
+    float s = 0.f, c = 0.f;
+    __device__ __forceinline__ void add(float x) {
+        const float t = s + x;
+        c += (fabsf(s) >= fabsf(x)) ? ((s - t) + x) : ((x - t) + s);
+        s = t;
+    }
+};
 __global__ void splitk_reduce_kernel(const float *part, long long stride, int splits, int M, int N, long long ldp,
                                      float *D, long long ldd, float alpha) {
     const long long mq = ((long long)M + 3) / 4, total = mq * N, s4 = stride / 4;
     for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total; e += (long long)gridDim.x * blockDim.x) {
         const long long j = e / mq, i = (e - j * mq) * 4;
         const float4 *p = (const float4 *)(part + i + j * ldp);
-        double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
+        Neumaier a0, a1, a2, a3;
         int z = 0;
         for (; z + 4 <= splits; z += 4) {
-            const float4 v0 = __ldcs(p + (long long)z * s4), v1 = __ldcs(p + (long long)(z + 1) * s4);
-            const float4 v2 = __ldcs(p + (long long)(z + 2) * s4), v3 = __ldcs(p + (long long)(z + 3) * s4);
-            a0 += ((double)v0.x + (double)v1.x) + ((double)v2.x + (double)v3.x);
-            a1 += ((double)v0.y + (double)v1.y) + ((double)v2.y + (double)v3.y);
-            a2 += ((double)v0.z + (double)v1.z) + ((double)v2.z + (double)v3.z);
-            a3 += ((double)v0.w + (double)v1.w) + ((double)v2.w + (double)v3.w);
+            float4 v[4];
+#pragma unroll
+            for (int u = 0; u < 4; u++) v[u] = __ldcs(p + (long long)(z + u) * s4);
+#pragma unroll
+            for (int u = 0; u < 4; u++) { a0.add(v[u].x); a1.add(v[u].y); a2.add(v[u].z); a3.add(v[u].w); }
         }
         for (; z < splits; z++) {
             const float4 v = __ldcs(p + (long long)z * s4);
-            a0 += (double)v.x; a1 += (double)v.y; a2 += (double)v.z; a3 += (double)v.w;
+            a0.add(v.x); a1.add(v.y); a2.add(v.z); a3.add(v.w);
         }
         float *d = D + i + j * ldd;
-        const double al = (double)alpha;
-        d[0] = (float)(al * a0);
-        if (i + 1 < M) d[1] = (float)(al * a1);
-        if (i + 2 < M) d[2] = (float)(al * a2);
-        if (i + 3 < M) d[3] = (float)(al * a3);
+        d[0] = alpha * (a0.s + a0.c);
+        if (i + 1 < M) d[1] = alpha * (a1.s + a1.c);
+        if (i + 2 < M) d[2] = alpha * (a2.s + a2.c);
+        if (i + 3 < M) d[3] = alpha * (a3.s + a3.c);
     }
 }
 
@@ -822,7 +842,7 @@ void split_tf32(cudaStream_t s, const float *X, long long ldx, long long r, long
 // The tensor core's FP32 accumulation truncates at every MMA step, so its error grows with
 // the number of steps in one accumulation chain, not with sqrt(K): a 2048-long chain of
 // the dominant hi x hi product already costs ~1e-5 relative.  That product is therefore
-// split along K into chains of ~256 (FP32 in TMEM within a chain, FP64 across chains,
+// split along K into chains of ~256 (FP32 in TMEM within a chain, compensated FP32 across chains,
 // ~1e-6 relative), its partial slabs capped at 1 GiB.  The two correction terms, 2^-11
 // smaller, are one two-segment product with chains of ~2048 into a temporary that one
 // elementwise pass adds.
