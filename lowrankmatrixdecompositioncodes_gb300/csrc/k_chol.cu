@@ -116,14 +116,23 @@ __device__ __noinline__ bool factor_diag_warp(S *D, S *Di, const S *diag0, S rel
 #pragma unroll
     for (int i = 0; i < 32; i++) c[i] = (i <= lane) ? D[i * TP + lane] : S(0);
     bool bad = false;
+    S own_inv = S(1);                                   // 1 / R(lane, lane)
 #pragma unroll
     for (int j = 0; j < 32; j++) {
         const S d = __shfl_sync(FULL, c[j], j);
         const bool ok = (d > S(0)) && isfinite(d) && (d > rel_tol * diag0[j]);
         bad |= !ok;
-        const S p = ok ? sqrt(d) : S(1);
-        const S inv = S(1) / p;
-        if (lane == j) c[j] = p;
+        S p, inv;
+        if constexpr (sizeof(S) == 4) {
+            // FP32: one correctly rounded rsqrt instead of the square-root and division
+            // sequences on this one-warp critical path; sqrt(d) = d * rsqrt(d) (1 ulp)
+            inv = ok ? __frsqrt_rn(d) : S(1);
+            p = ok ? d * inv : S(1);
+        } else {
+            p = ok ? sqrt(d) : S(1);
+            inv = S(1) / p;
+        }
+        if (lane == j) { c[j] = p; own_inv = inv; }
         else if (lane > j) c[j] *= inv;                 // lane t now holds R(j, t)
 #pragma unroll
         for (int i = j + 1; i < 32; i++) {
@@ -140,11 +149,20 @@ __device__ __noinline__ bool factor_diag_warp(S *D, S *Di, const S *diag0, S rel
     S x[32];
 #pragma unroll
     for (int i = 31; i >= 0; i--) {
-        S acc = S(0);
+        S acc0 = S(0), acc1 = S(0);                     // two chains: half the FMA latency
 #pragma unroll
-        for (int k = i + 1; k < 32; k++) acc = fma(D[i * TP + k], x[k], acc);
-        const S rii = D[i * TP + i];
-        x[i] = (i == lane) ? S(1) / rii : ((i < lane) ? -acc / rii : S(0));
+        for (int k = i + 1; k < 32; k += 2) {
+            acc0 = fma(D[i * TP + k], x[k], acc0);
+            if (k + 1 < 32) acc1 = fma(D[i * TP + k + 1], x[k + 1], acc1);
+        }
+        const S acc = acc0 + acc1;
+        if constexpr (sizeof(S) == 4) {
+            const S inv_i = __shfl_sync(FULL, own_inv, i);
+            x[i] = (i == lane) ? inv_i : ((i < lane) ? -acc * inv_i : S(0));
+        } else {
+            const S rii = D[i * TP + i];
+            x[i] = (i == lane) ? S(1) / rii : ((i < lane) ? -acc / rii : S(0));
+        }
     }
 #pragma unroll
     for (int i = 0; i < 32; i++) Di[i * TP + lane] = x[i];
@@ -271,8 +289,9 @@ __device__ __forceinline__ void cp_async_wait_all() {
     asm volatile("cp.async.wait_group 0;\n" ::: "memory");
 }
 
-__global__ void __launch_bounds__(256) chol_tiles_f32_kernel(float *Gt, int n, int nb, double rel_tol, float *dinv,
-                                                             double *Rout, long long ldr, int *flag) {
+constexpr int CHOL_F32_THREADS = 512;
+__global__ void __launch_bounds__(CHOL_F32_THREADS) chol_tiles_f32_kernel(float *Gt, int n, int nb, double rel_tol,
+                                                                          float *dinv, int *flag) {
     extern __shared__ __align__(16) unsigned char shraw[];
     float *T = (float *)shraw;
     const int ntile = tix(0, nb);
@@ -303,13 +322,16 @@ __global__ void __launch_bounds__(256) chol_tiles_f32_kernel(float *Gt, int n, i
         *reinterpret_cast<float4 *>(Gt + (size_t)t * TB * TB + r * TB + q * 4) =
             *reinterpret_cast<const float4 *>(T + (size_t)t * TE + r * TP + q * 4);
     }
-    if (Rout) {
-        // column k by one warp, rows by lanes (coalesced)
-        const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
-        for (int k = wid; k < n; k += nw)
-            for (int i = lane; i < n; i += 32)
-                Rout[i + (long long)k * ldr] =
-                    (i <= k) ? (double)T[(size_t)tix(i >> 5, k >> 5) * TE + (i & 31) * TP + (k & 31)] : 0.0;
+}
+
+// R as FP64, column-major, zero below, from the packed FP32 tiles: a separate grid-wide pass,
+// because FP64 conversions from one SM (FP64 units are few on GB300) cost ~20 us at n = 272.
+__global__ void tiles_to_fp64_kernel(const float *Gt, int n, double *R, long long ldr) {
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < (long long)n * n;
+         e += (long long)gridDim.x * blockDim.x) {
+        const int k = (int)(e / n), i = (int)(e - (long long)k * n);
+        R[i + (long long)k * ldr] =
+            (i <= k) ? (double)Gt[(size_t)tix(i >> 5, k >> 5) * TB * TB + (i & 31) * TB + (k & 31)] : 0.0;
     }
 }
 
@@ -732,10 +754,16 @@ bool chol_tiles_f32(cudaStream_t s, float *Gt, int n, double rel_tol, int *d_fla
     RSVD_CK(cudaMemsetAsync(d_flag, 0, sizeof(int), s));
     const size_t smem = sizeof(float) * ((size_t)(tix(0, nb) + 1) * TE + (size_t)nb * TB);
     RSVD_CK(cudaFuncSetAttribute(chol_tiles_f32_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    chol_tiles_f32_kernel<<<1, 256, smem, s>>>(Gt, n, nb, rel_tol, dinv, Rout ? Rout->p : nullptr,
-                                               Rout ? Rout->ld : 0, d_flag);
+    chol_tiles_f32_kernel<<<1, CHOL_F32_THREADS, smem, s>>>(Gt, n, nb, rel_tol, dinv, d_flag);
     RSVD_LAUNCH_CK();
     ctx().launches++;
+    if (Rout) {
+        const long long nn = (long long)n * n;
+        tiles_to_fp64_kernel<<<(unsigned)std::min<long long>((nn + 255) / 256, (long long)std::max(1, ctx().sms) * 4),
+                               256, 0, s>>>(Gt, n, Rout->p, Rout->ld);
+        RSVD_LAUNCH_CK();
+        ctx().launches++;
+    }
     int h = 0;
     RSVD_CK(cudaMemcpyAsync(&h, d_flag, sizeof(int), cudaMemcpyDeviceToHost, s));
     RSVD_CK(cudaStreamSynchronize(s));

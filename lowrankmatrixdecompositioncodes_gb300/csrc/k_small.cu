@@ -198,39 +198,82 @@ __global__ void __launch_bounds__(1024) jacobi_cluster_kernel(const double *G, l
     cluster.sync();   // no CTA leaves while a peer may still write into its shared memory
 }
 
-// Block-cyclic one-sided Jacobi on a cluster of 8 CTAs.  The n columns of W and V are
-// cut into 16 blocks of bs columns.  CTA i holds the blocks at tournament positions i
-// (slot 0) and 15-i (slot 1), whole columns (all n rows) of W and V, in shared memory.
+// Jacobi rotation (cs, sn) zeroing w_p.w_q = d, |w_p|^2 = a, |w_q|^2 = b (Rutishauser's
+// formulas); FP32 with correctly rounded reciprocal / rsqrt intrinsics instead of the
+// division and square-root sequences.
+__device__ __forceinline__ void jrot(float a, float b, float d, float &cs, float &sn) {
+    const float zeta = (b - a) * __frcp_rn(2.f * d);
+    const float t = copysignf(__frcp_rn(fabsf(zeta) + __fsqrt_rn(fmaf(zeta, zeta, 1.f))), zeta);
+    cs = __frsqrt_rn(fmaf(t, t, 1.f));
+    sn = cs * t;
+}
+__device__ __forceinline__ void jrot(double a, double b, double d, double &cs, double &sn) {
+    const double zeta = (b - a) / (2.0 * d);
+    const double t = copysign(1.0, zeta) / (fabs(zeta) + sqrt(1.0 + zeta * zeta));
+    cs = 1.0 / sqrt(1.0 + t * t);
+    sn = cs * t;
+}
+__device__ __forceinline__ uint32_t smem_addr(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+// Block-cyclic one-sided Jacobi on a cluster of CLN CTAs (8, or 16 where the GPU can
+// co-schedule a non-portable cluster of 16).  The n columns of W and V are cut into
+// NBLK = 2 CLN blocks of bs columns.  CTA i holds the blocks at tournament positions i
+// (slot 0) and NBLK-1-i (slot 1), whole columns (all n rows) of W and V, in shared memory.
 // A super-round orthogonalises every pair among the CTA's 2*bs columns (one cyclic inner
-// sweep, block barriers only); then positions 1..15 rotate by one (position 0 stays) and
-// every block moves to its next holder through distributed shared memory, followed by
-// one cluster barrier.  15 super-rounds meet every pair of blocks once: one outer sweep.
-// Outer sweeps repeat until no CTA rotated anything during a whole sweep.
+// sweep, block barriers only); then positions 1..NBLK-1 rotate by one (position 0 stays)
+// and every block moves to its next holder as one bulk asynchronous copy into the holder's
+// shared memory (completing on the holder's mbarrier, waited with a bound), followed by one
+// cluster barrier.  NBLK-1 super-rounds meet every pair of blocks once: one outer sweep.
+// Outer sweeps repeat until no CTA rotated anything during a whole sweep, or (FP32) until
+// the largest |cos| = |w_p.w_q| / (|w_p||w_q|) seen in a sweep is below sqrt(tol): Jacobi
+// converges quadratically, so the next sweep would find every pair below tol.
+// One warp per pair (blockDim = 32 bs; FP64: at most 16 warps, so that the register-held
+// chunks fit): a lane keeps its 16-byte chunks of w_p and w_q in registers between the dot
+// products and the rotation (MAXIT chunks: ldr <= 32 MAXIT VW).
 // Shared memory per CTA: 2 buffers x 2 slots x bs x ldr x 2 (W, V) x sizeof(S).
-template <typename S>
-__global__ void __launch_bounds__(1024) jacobi_block_cluster_kernel(const double *G, long long ldg, int n, int bs,
+template <typename S, int CLN>
+__global__ void __launch_bounds__(sizeof(S) == 4 ? 1024 : 512) jacobi_block_cluster_kernel(const double *G, long long ldg, int n, int bs,
                                                                     int ldr, S tol, int max_sweeps, S *Wout, S *Vout,
                                                                     long long ldo, int *sweeps_out, int *flag) {
     namespace cg = cooperative_groups;
     cg::cluster_group cluster = cg::this_cluster();
     const int rank = (int)cluster.block_rank();
-    constexpr int CLN = 8, NBLK = 16;
+    constexpr int NBLK = 2 * CLN;
+    constexpr int VW = 16 / sizeof(S);
+    constexpr int MAXIT = sizeof(S) == 4 ? 4 : 8;
+    using V16 = typename std::conditional<sizeof(S) == 4, float4, double2>::type;
     extern __shared__ __align__(16) unsigned char shraw[];
     const size_t slot_elems = (size_t)bs * ldr * 2;          // W columns then V columns
     S *buf = (S *)shraw;                                      // [2 buffers][2 slots][slot_elems]
     __shared__ int blk[2][2];                                 // block id held in [buffer][slot]
     __shared__ int rot_count;
     __shared__ int sweep_rot[CLN];
+    __shared__ unsigned char ftab[64][32][2];                 // full-round pairs (p < q), nloc <= 64
+    __shared__ __align__(8) unsigned long long inbar;         // incoming block copies
+    __shared__ unsigned int sweep_max;                        // largest cos^2 of the sweep (float bits)
+    __shared__ unsigned int cl_max[CLN];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
     auto slot_ptr = [&](S *base, int b, int sl) { return base + ((size_t)b * 2 + sl) * slot_elems; };
     auto col_w = [&](S *sp, int j) { return sp + (size_t)j * ldr; };
     auto col_v = [&](S *sp, int j) { return sp + (size_t)(bs + j) * ldr; };
+    const int nloc = 2 * bs;                 // local columns (even)
 
-    // initial placement: slot 0 <- block rank, slot 1 <- block 15 - rank
+    // initial placement: slot 0 <- block rank, slot 1 <- block NBLK-1-rank; pair table
     if (threadIdx.x == 0) {
         blk[0][0] = rank;
         blk[0][1] = NBLK - 1 - rank;
         rot_count = 0;
+        sweep_max = 0u;
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&inbar)) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    for (int e = threadIdx.x; e < (nloc - 1) * bs; e += blockDim.x) {
+        const int r = e / bs, pi = e % bs;
+        int p, q;
+        rr_pair2(nloc, r, pi, p, q);
+        if (p > q) { const int t = p; p = q; q = t; }
+        ftab[r][pi][0] = (unsigned char)p;
+        ftab[r][pi][1] = (unsigned char)q;
     }
     for (int sl = 0; sl < 2; sl++) {
         const int b = (sl == 0) ? rank : NBLK - 1 - rank;
@@ -245,7 +288,9 @@ __global__ void __launch_bounds__(1024) jacobi_block_cluster_kernel(const double
     }
     cluster.sync();
     int cur = 0, sweep = 0;
-    const int nloc = 2 * bs;                 // local columns (even)
+    uint32_t mphase = 0;
+    const int nvec = ldr / VW;               // columns are zero beyond n up to ldr (a multiple of 4)
+    const uint32_t slot_bytes = (uint32_t)(slot_elems * sizeof(S));
     for (; sweep < max_sweeps; sweep++) {
         for (int sr = 0; sr < NBLK - 1; sr++) {
             S *s0 = slot_ptr(buf, cur, 0), *s1 = slot_ptr(buf, cur, 1);
@@ -256,66 +301,71 @@ __global__ void __launch_bounds__(1024) jacobi_block_cluster_kernel(const double
             const bool full = (sr == 0);
             const int nrounds = full ? nloc - 1 : bs;
             for (int r = 0; r < nrounds; r++) {
-                for (int pi = wid; pi < (full ? nloc / 2 : bs); pi += nw) {
+                for (int pi = wid; pi < bs; pi += nw) {
                     int p, q;
                     if (full) {
-                        rr_pair2(nloc, r, pi, p, q);
-                        if (p > q) { const int t = p; p = q; q = t; }
+                        p = ftab[r][pi][0];
+                        q = ftab[r][pi][1];
                     } else {
                         p = pi;
-                        q = bs + (pi + r) % bs;
+                        const int t = pi + r;
+                        q = bs + (t >= bs ? t - bs : t);
                     }
                     // skip padding columns beyond n
                     const int gp = (p < bs) ? b0 * bs + p : b1 * bs + (p - bs);
                     const int gq = (q < bs) ? b0 * bs + q : b1 * bs + (q - bs);
                     if (gp >= n || gq >= n) continue;
-                    S *wp = (p < bs) ? col_w(s0, p) : col_w(s1, p - bs);
-                    S *wq = (q < bs) ? col_w(s0, q) : col_w(s1, q - bs);
-                    // columns are zero beyond n up to ldr (a multiple of 4), so whole
-                    // 16-byte vectors can be processed: VW elements per lane per access
-                    constexpr int VW = 16 / sizeof(S);
-                    using V16 = typename std::conditional<sizeof(S) == 4, float4, double2>::type;
-                    const int nvec = ldr / VW;
+                    V16 *wp = reinterpret_cast<V16 *>((p < bs) ? col_w(s0, p) : col_w(s1, p - bs));
+                    V16 *wq = reinterpret_cast<V16 *>((q < bs) ? col_w(s0, q) : col_w(s1, q - bs));
+                    V16 xr[MAXIT], yr[MAXIT];
                     S a = 0, b = 0, d = 0;
-                    for (int iv = lane; iv < nvec; iv += 32) {
-                        const V16 xv = reinterpret_cast<const V16 *>(wp)[iv];
-                        const V16 yv = reinterpret_cast<const V16 *>(wq)[iv];
-                        const S *x = reinterpret_cast<const S *>(&xv), *y = reinterpret_cast<const S *>(&yv);
 #pragma unroll
-                        for (int e = 0; e < VW; e++) {
-                            a = fma(x[e], x[e], a); b = fma(y[e], y[e], b); d = fma(x[e], y[e], d);
+                    for (int it = 0; it < MAXIT; it++) {
+                        const int iv = lane + 32 * it;
+                        if (iv < nvec) {
+                            xr[it] = wp[iv];
+                            yr[it] = wq[iv];
+                            const S *x = reinterpret_cast<const S *>(&xr[it]), *y = reinterpret_cast<const S *>(&yr[it]);
+#pragma unroll
+                            for (int e = 0; e < VW; e++) {
+                                a = fma(x[e], x[e], a); b = fma(y[e], y[e], b); d = fma(x[e], y[e], d);
+                            }
                         }
                     }
                     a = warp_sum_t(a); b = warp_sum_t(b); d = warp_sum_t(d);
-                    if (d == S(0) || fabs(d) <= tol * sqrt(a * b)) continue;
-                    const S zeta = (b - a) / (S(2) * d);
-                    const S t = copysign(S(1), zeta) / (fabs(zeta) + sqrt(S(1) + zeta * zeta));
-                    const S cs = S(1) / sqrt(S(1) + t * t), sn = cs * t;
-                    S *vp = (p < bs) ? col_v(s0, p) : col_v(s1, p - bs);
-                    S *vq = (q < bs) ? col_v(s0, q) : col_v(s1, q - bs);
-                    for (int iv = lane; iv < nvec; iv += 32) {
-                        V16 xv = reinterpret_cast<V16 *>(wp)[iv], yv = reinterpret_cast<V16 *>(wq)[iv];
-                        V16 uv = reinterpret_cast<V16 *>(vp)[iv], vv = reinterpret_cast<V16 *>(vq)[iv];
-                        S *x = reinterpret_cast<S *>(&xv), *y = reinterpret_cast<S *>(&yv);
-                        S *u = reinterpret_cast<S *>(&uv), *v = reinterpret_cast<S *>(&vv);
+                    const S ab = a * b, dd = d * d;
+                    if (lane == 0 && ab > S(0)) atomicMax(&sweep_max, __float_as_uint((float)(dd / ab)));
+                    if (d == S(0) || dd <= tol * tol * ab) continue;
+                    S cs, sn;
+                    jrot(a, b, d, cs, sn);
+                    V16 *vp = reinterpret_cast<V16 *>((p < bs) ? col_v(s0, p) : col_v(s1, p - bs));
+                    V16 *vq = reinterpret_cast<V16 *>((q < bs) ? col_v(s0, q) : col_v(s1, q - bs));
 #pragma unroll
-                        for (int e = 0; e < VW; e++) {
-                            const S x0 = x[e], y0 = y[e], u0 = u[e], v0 = v[e];
-                            x[e] = cs * x0 - sn * y0;
-                            y[e] = sn * x0 + cs * y0;
-                            u[e] = cs * u0 - sn * v0;
-                            v[e] = sn * u0 + cs * v0;
+                    for (int it = 0; it < MAXIT; it++) {
+                        const int iv = lane + 32 * it;
+                        if (iv < nvec) {
+                            V16 uv = vp[iv], vv = vq[iv];
+                            S *x = reinterpret_cast<S *>(&xr[it]), *y = reinterpret_cast<S *>(&yr[it]);
+                            S *u = reinterpret_cast<S *>(&uv), *v = reinterpret_cast<S *>(&vv);
+#pragma unroll
+                            for (int e = 0; e < VW; e++) {
+                                const S x0 = x[e], y0 = y[e], u0 = u[e], v0 = v[e];
+                                x[e] = cs * x0 - sn * y0;
+                                y[e] = sn * x0 + cs * y0;
+                                u[e] = cs * u0 - sn * v0;
+                                v[e] = sn * u0 + cs * v0;
+                            }
+                            wp[iv] = xr[it];
+                            wq[iv] = yr[it];
+                            vp[iv] = uv;
+                            vq[iv] = vv;
                         }
-                        reinterpret_cast<V16 *>(wp)[iv] = xv;
-                        reinterpret_cast<V16 *>(wq)[iv] = yv;
-                        reinterpret_cast<V16 *>(vp)[iv] = uv;
-                        reinterpret_cast<V16 *>(vq)[iv] = vv;
                     }
                     if (lane == 0) atomicAdd(&rot_count, 1);
                 }
                 __syncthreads();
             }
-            // ---- move blocks to their next holders (positions 1..15 rotate by one)
+            // ---- move blocks to their next holders (positions 1..NBLK-1 rotate by one)
             const int nxt = cur ^ 1;
             int dst0, dsl0, dst1, dsl1;       // destination (cta, slot) of local slots 0 and 1
             if (rank == 0) { dst0 = 0; dsl0 = 0; }
@@ -323,35 +373,67 @@ __global__ void __launch_bounds__(1024) jacobi_block_cluster_kernel(const double
             else { dst0 = CLN - 1; dsl0 = 1; }
             if (rank == 0) { dst1 = 1; dsl1 = 0; }
             else { dst1 = rank - 1; dsl1 = 1; }
-            for (int sl = 0; sl < 2; sl++) {
-                const int dc = sl ? dst1 : dst0, ds = sl ? dsl1 : dsl0;
-                S *src = slot_ptr(buf, cur, sl);
-                S *dst = cluster.map_shared_rank(slot_ptr(buf, nxt, ds), dc);
-                const size_t nvec = slot_elems * sizeof(S) / 16;
-                const float4 *s4 = (const float4 *)src;
-                float4 *d4 = (float4 *)dst;
-                for (size_t e = threadIdx.x; e < nvec; e += blockDim.x) d4[e] = s4[e];
-                if (threadIdx.x == 0) {
+            // the rounds' generic-proxy writes of the outgoing slots, then the copies
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            __syncthreads();
+            if (threadIdx.x == 0) {
+                asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(&inbar)),
+                             "r"(2u * slot_bytes)
+                             : "memory");
+                for (int sl = 0; sl < 2; sl++) {
+                    const int dc = sl ? dst1 : dst0, ds = sl ? dsl1 : dsl0;
+                    uint32_t rdst, rbar;
+                    asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(rdst) : "r"(smem_addr(slot_ptr(buf, nxt, ds))), "r"(dc));
+                    asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(rbar) : "r"(smem_addr(&inbar)), "r"(dc));
+                    asm volatile(
+                        "cp.async.bulk.shared::cluster.shared::cta.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(rdst),
+                        "r"(smem_addr(slot_ptr(buf, cur, sl))), "r"(slot_bytes), "r"(rbar)
+                        : "memory");
                     int *rb = cluster.map_shared_rank(&blk[nxt][ds], dc);
                     *rb = sl ? b1 : b0;
                 }
             }
+            // both incoming slots (bounded wait: ~1 s of SM cycles, then the error flag)
+            {
+                uint32_t ok = 0;
+                const long long t0 = clock64();
+                while (true) {
+                    asm volatile(
+                        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+                        "selp.u32 %0, 1, 0, p;\n\t}\n"
+                        : "=r"(ok)
+                        : "r"(smem_addr(&inbar)), "r"(mphase)
+                        : "memory");
+                    if (ok) break;
+                    if (clock64() - t0 > (1ll << 31)) { atomicExch(flag, 1); break; }
+                }
+                mphase ^= 1u;
+            }
             cluster.sync();
             cur = nxt;
         }
-        // ---- did any CTA rotate during this sweep?
+        // ---- did any CTA rotate during this sweep, and how large was the largest cosine?
         if (threadIdx.x < CLN) {
             int *dstf = cluster.map_shared_rank(&sweep_rot[rank], (unsigned)threadIdx.x);
             *dstf = rot_count;
+            unsigned int *dstm = cluster.map_shared_rank(&cl_max[rank], (unsigned)threadIdx.x);
+            *dstm = sweep_max;
         }
         cluster.sync();
         int total = 0;
+        float cmax = 0.f;
 #pragma unroll
-        for (int c = 0; c < CLN; c++) total += sweep_rot[c];
+        for (int c = 0; c < CLN; c++) {
+            total += sweep_rot[c];
+            cmax = fmaxf(cmax, __uint_as_float(cl_max[c]));
+        }
         __syncthreads();
-        if (threadIdx.x == 0) rot_count = 0;
+        if (threadIdx.x == 0) { rot_count = 0; sweep_max = 0u; }
         cluster.sync();
         if (total == 0) break;
+        // FP32 only: |cos| < sqrt(tol) (cos^2 < tol).  FP64 keeps the plain criterion, so that
+        // its factors match the reference's to the last sweep.
+        if (sizeof(S) == 4 && (double)cmax < (double)tol) { sweep++; break; }
     }
     // ---- write the columns this CTA holds
     for (int sl = 0; sl < 2; sl++) {
@@ -447,26 +529,49 @@ int jacobi_small(cudaStream_t s, DM<double> G, DM<double> U, DM<double> V, doubl
     const int rows_per = (n + CL - 1) / CL;
     const int npairs = (n + (n & 1)) / 2;
     const size_t csmem = sizeof(S) * ((size_t)2 * n * rows_per + (size_t)2 * CL * 3 * npairs);
-    const int bs = (n + 15) / 16, ldr = (n + 3) / 4 * 4;
-    const size_t bsmem = sizeof(S) * (size_t)4 * bs * ldr * 2;
+    const int ldr = (n + 3) / 4 * 4;
+    constexpr int VW = 16 / sizeof(S), MAXIT = sizeof(S) == 4 ? 4 : 8;
+    // block-cyclic cluster kernel: 16 CTAs where a non-portable cluster of 16 can be
+    // scheduled and each CTA still gets >= 5 columns per slot, else 8
+    bool launched = false;
+    int variant = 0;                         // cluster size of the block-cyclic kernel that ran
     cudaLaunchAttribute cattr[1];
     cattr[0].id = cudaLaunchAttributeClusterDimension;
-    cattr[0].val.clusterDim.x = CL;
+    cattr[0].val.clusterDim.x = 8;
     cattr[0].val.clusterDim.y = 1;
     cattr[0].val.clusterDim.z = 1;
-    if (bsmem <= 220 * 1024 && n >= 64) {
-        auto kern = jacobi_block_cluster_kernel<S>;
+    for (int cl : {16, 8}) {
+        if (launched || n < 64 || ldr / VW > 32 * MAXIT) break;
+        const int nblk = 2 * cl, bs = (n + nblk - 1) / nblk;
+        if (cl == 16 && bs < 5) continue;
+        if (bs > 32 || 2 * bs > 64) continue;
+        const size_t bsmem = sizeof(S) * (size_t)4 * bs * ldr * 2;
+        if (bsmem > 200 * 1024) continue;
+        auto kern = (cl == 16) ? jacobi_block_cluster_kernel<S, 16> : jacobi_block_cluster_kernel<S, 8>;
+        if (cl == 16 && cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess) {
+            cudaGetLastError();
+            continue;
+        }
         RSVD_CK(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bsmem));
         cudaLaunchConfig_t cfg = {};
-        cfg.gridDim = dim3(CL);
-        cfg.blockDim = dim3(1024);
+        cfg.gridDim = dim3(cl);
+        cfg.blockDim = dim3(32 * std::min(bs, sizeof(S) == 4 ? 32 : 16));
         cfg.dynamicSmemBytes = bsmem;
         cfg.stream = s;
+        cattr[0].val.clusterDim.x = cl;
         cfg.attrs = cattr;
         cfg.numAttrs = 1;
+        int nclusters = 0;
+        if (cudaOccupancyMaxActiveClusters(&nclusters, (void *)kern, &cfg) != cudaSuccess || nclusters < 1) {
+            cudaGetLastError();
+            continue;
+        }
         RSVD_CK(cudaLaunchKernelEx(&cfg, kern, (const double *)G.p, (long long)G.ld, n, bs, ldr, tol, 40, W, Vacc,
                                    (long long)ld, d_sweeps, d_flag));
-    } else if (csmem <= 200 * 1024 && n >= 64) {
+        launched = true;
+        variant = cl;
+    }
+    if (!launched && csmem <= 200 * 1024 && n >= 64) {
         auto kern = jacobi_cluster_kernel<S, CL>;
         RSVD_CK(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)csmem));
         cudaLaunchConfig_t cfg = {};
@@ -483,7 +588,7 @@ int jacobi_small(cudaStream_t s, DM<double> G, DM<double> U, DM<double> V, doubl
         cfg.numAttrs = 1;
         RSVD_CK(cudaLaunchKernelEx(&cfg, kern, (const double *)G.p, (long long)G.ld, n, rows_per, tol, 40, W, Vacc,
                                    (long long)ld, d_sweeps, d_flag));
-    } else {
+    } else if (!launched) {
         load_kernel_t<S><<<gfor((long long)n * n), 256, 0, s>>>(G.p, G.ld, W, ld, n, 0);
         load_kernel_t<S><<<gfor((long long)n * n), 256, 0, s>>>(G.p, G.ld, Vacc, ld, n, 1);
         jacobi_kernel_t<S><<<1, 1024, 0, s>>>(W, ld, Vacc, ld, n, tol, 40, d_sweeps, d_flag);
@@ -497,7 +602,9 @@ int jacobi_small(cudaStream_t s, DM<double> G, DM<double> U, DM<double> V, doubl
     int sweeps = 0;
     RSVD_CK(cudaMemcpyAsync(&sweeps, d_sweeps, sizeof(int), cudaMemcpyDeviceToHost, s));
     RSVD_CK(cudaStreamSynchronize(s));
-    if (ctx().opts.verbose) std::fprintf(stderr, "rsvdpack: jacobi n=%d (%s) sweeps=%d\n", n, sizeof(S) == 4 ? "fp32" : "fp64", sweeps);
+    if (ctx().opts.verbose)
+        std::fprintf(stderr, "rsvdpack: jacobi n=%d (%s) sweeps=%d cluster=%d\n", n, sizeof(S) == 4 ? "fp32" : "fp64",
+                     sweeps, variant);
     return sweeps;
 }
 template int jacobi_small<double>(cudaStream_t, DM<double>, DM<double>, DM<double>, double *, int *);

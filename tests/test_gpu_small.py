@@ -52,7 +52,7 @@ def test_small_cholesky_reports_breakdown(engine):
 
 
 @pytest.mark.parametrize("fp32", [0, 1])
-@pytest.mark.parametrize("n", [7, 40, 64, 110, 200, 272])
+@pytest.mark.parametrize("n", [7, 40, 64, 110, 200, 272, 300, 400])
 def test_small_svd(engine, n, fp32):
     _bind(engine.lib)
     g = np.random.default_rng(100 + n)
