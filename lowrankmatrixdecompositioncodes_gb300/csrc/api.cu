@@ -55,6 +55,14 @@ template <typename T>
 DMat<T> upload(const mat *M) {
     cudaStream_t s = ctx().stream;
     const i64 m = M->nrows, n = M->ncols;
+    if (ctx().pageable_access) {
+        // the conversion kernel reads the caller's (pageable) host matrix over NVLink-C2C:
+        // one pass at the link's bandwidth, no staging copy and no FP64 device temporary
+        DMat<T> A(m, n, s, false);
+        convert<double, T>(s, DM<double>{M->d, m, n, m}, A.v);
+        RSVD_CK(cudaStreamSynchronize(s));     // the caller may reuse M->d on return
+        return A;
+    }
     if (std::is_same<T, double>::value) {
         DMat<T> A(m, n, s, false);
         RSVD_CK(cudaMemcpy2DAsync(A.v.p, sizeof(T) * A.v.ld, M->d, sizeof(double) * m, sizeof(double) * m, n,
@@ -151,6 +159,58 @@ mat *download(DM<T> a) {
     return M;
 }
 
+// An output of known size, allocated and pre-faulted by a host thread while the device
+// works, then filled by the device: with pageable access the conversion kernel writes FP64
+// straight into the caller-visible host buffer (its pages already present, so no faults from
+// the device side); otherwise through the pinned stage as in download().
+struct OutputPrefetch {
+    mat *M = nullptr;
+    std::thread th;
+    OutputPrefetch(int r, int c) {
+        th = std::thread([this, r, c] {
+            M = matrix_new_output(r, c);
+            if (!M) return;
+            volatile char *b = (volatile char *)M->d;
+            const size_t bytes = sizeof(double) * (size_t)r * (size_t)c;
+            for (size_t off = 0; off < bytes; off += 4096) b[off] = 0;
+        });
+    }
+    ~OutputPrefetch() {
+        if (th.joinable()) th.join();
+        if (M) matrix_delete(M);                 // not taken: an exception unwound the call
+    }
+    template <typename T>
+    mat *fill(DM<T> a) {
+        th.join();
+        if (!M) throw std::bad_alloc();
+        mat *out = M;
+        M = nullptr;
+        cudaStream_t s = ctx().stream;
+        if (a.r * a.c == 0) return out;
+        if (ctx().pageable_access) {
+            convert<T, double>(s, a, DM<double>{out->d, a.r, a.c, a.r});
+            RSVD_CK(cudaStreamSynchronize(s));
+            return out;
+        }
+        const size_t count = (size_t)a.r * (size_t)a.c;
+        double *stage = (double *)t_stage.get(sizeof(double) * count);
+        DMat<double> tmp;
+        const double *src = (const double *)a.p;
+        long long lds = a.ld;
+        if (!std::is_same<T, double>::value) {
+            tmp = DMat<double>(a.r, a.c, s, false);
+            convert<T, double>(s, a, tmp.v);
+            src = tmp.v.p;
+            lds = tmp.v.ld;
+        }
+        RSVD_CK(cudaMemcpy2DAsync(stage, sizeof(double) * a.r, src, sizeof(double) * lds, sizeof(double) * a.r, a.c,
+                                  cudaMemcpyDeviceToHost, s));
+        RSVD_CK(cudaStreamSynchronize(s));
+        parallel_copy(out->d, stage, count);
+        return out;
+    }
+};
+
 mat *diag_mat(const std::vector<double> &d) {
     const int k = (int)d.size();
     mat *S = matrix_new(k, k);
@@ -198,11 +258,14 @@ void svd_outputs(SvdOut<T> &r, mat **U, mat **S, mat **V) {
 template <typename T>
 void run_fixed_rank(mat *M, int k, int p, int vnum, int q, int s, mat **U, mat **S, mat **V) {
     auto t0 = Clock::now();
+    OutputPrefetch pu(M->nrows, k), pv(M->ncols, k);          // U: m x k, V: n x k
     DMat<T> A = upload<T>(M);
     ctx().timing.upload_ms = ms_since(t0);
     SvdOut<T> r = svd_fixed_rank<T>(A.v, k, p, vnum, q, s);
     auto t1 = Clock::now();
-    svd_outputs<T>(r, U, S, V);
+    *U = pu.fill<T>(r.U.v);
+    *V = pv.fill<T>(r.V.v);
+    *S = diag_mat(r.S);
     ctx().timing.download_ms = ms_since(t1);
     end_call(t0);
 }

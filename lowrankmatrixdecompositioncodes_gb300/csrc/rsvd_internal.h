@@ -95,6 +95,9 @@ struct Ctx {
     // as a two-part BF16 split (hi + lo, 16 mantissa bits) instead of one BF16 copy (7 bits).
     // Set by the fixed-precision block loop, whose sketches must resolve the deflated matrix.
     bool ax_split = false;
+    // kernels may read pageable host memory directly (cudaDevAttrPageableMemoryAccess: GB300
+    // with a Grace host, over NVLink-C2C)
+    bool pageable_access = false;
 };
 Ctx &ctx();                       // initialises the device on first use; throws RSVD_ERR_NO_DEVICE
 const rsvdpack_opts &global_opts();

@@ -135,6 +135,12 @@ Ctx &ctx() {
     h.c.sms = prop.multiProcessorCount;
     h.c.cc_major = prop.major;
     h.c.cc_minor = prop.minor;
+    int pma = 0;
+    if (cudaDeviceGetAttribute(&pma, cudaDevAttrPageableMemoryAccess, dev) != cudaSuccess) {
+        cudaGetLastError();
+        pma = 0;
+    }
+    h.c.pageable_access = pma != 0;
     RSVD_CK(cudaStreamCreateWithFlags(&h.c.stream, cudaStreamNonBlocking));
     cudaMemPool_t pool;
     RSVD_CK(cudaDeviceGetDefaultMemPool(&pool, dev));
