@@ -227,12 +227,12 @@ __device__ __forceinline__ uint32_t smem_addr(const void *p) { return (uint32_t)
 // Outer sweeps repeat until no CTA rotated anything during a whole sweep, or (FP32) until
 // the largest |cos| = |w_p.w_q| / (|w_p||w_q|) seen in a sweep is below sqrt(tol): Jacobi
 // converges quadratically, so the next sweep would find every pair below tol.
-// One warp per pair (blockDim = 32 bs; FP64: at most 16 warps, so that the register-held
-// chunks fit): a lane keeps its 16-byte chunks of w_p and w_q in registers between the dot
-// products and the rotation (MAXIT chunks: ldr <= 32 MAXIT VW).
+// One warp per pair (blockDim = 32 bs, at most 16 warps so that the register-held chunks
+// fit): a lane keeps its 16-byte chunks of w_p and w_q in registers between the dot
+// products and the rotation (MAXIT chunks: ldr <= 32 MAXIT VW); FP32 uses packed FFMA2.
 // Shared memory per CTA: 2 buffers x 2 slots x bs x ldr x 2 (W, V) x sizeof(S).
 template <typename S, int CLN>
-__global__ void __launch_bounds__(sizeof(S) == 4 ? 1024 : 512) jacobi_block_cluster_kernel(const double *G, long long ldg, int n, int bs,
+__global__ void __launch_bounds__(512, 1) jacobi_block_cluster_kernel(const double *G, long long ldg, int n, int bs,
                                                                     int ldr, S tol, int max_sweeps, S *Wout, S *Vout,
                                                                     long long ldo, int *sweeps_out, int *flag) {
     namespace cg = cooperative_groups;
@@ -319,16 +319,35 @@ __global__ void __launch_bounds__(sizeof(S) == 4 ? 1024 : 512) jacobi_block_clus
                     V16 *wq = reinterpret_cast<V16 *>((q < bs) ? col_w(s0, q) : col_w(s1, q - bs));
                     V16 xr[MAXIT], yr[MAXIT];
                     S a = 0, b = 0, d = 0;
+                    if constexpr (sizeof(S) == 4) {
+                        // packed FP32 pairs (FFMA2): half the FMA instructions
+                        float2 a2 = make_float2(0.f, 0.f), b2 = a2, d2 = a2;
 #pragma unroll
-                    for (int it = 0; it < MAXIT; it++) {
-                        const int iv = lane + 32 * it;
-                        if (iv < nvec) {
-                            xr[it] = wp[iv];
-                            yr[it] = wq[iv];
-                            const S *x = reinterpret_cast<const S *>(&xr[it]), *y = reinterpret_cast<const S *>(&yr[it]);
+                        for (int it = 0; it < MAXIT; it++) {
+                            const int iv = lane + 32 * it;
+                            if (iv < nvec) {
+                                xr[it] = wp[iv];
+                                yr[it] = wq[iv];
+                                const float2 x0 = make_float2(xr[it].x, xr[it].y), x1 = make_float2(xr[it].z, xr[it].w);
+                                const float2 y0 = make_float2(yr[it].x, yr[it].y), y1 = make_float2(yr[it].z, yr[it].w);
+                                a2 = __ffma2_rn(x0, x0, a2); a2 = __ffma2_rn(x1, x1, a2);
+                                b2 = __ffma2_rn(y0, y0, b2); b2 = __ffma2_rn(y1, y1, b2);
+                                d2 = __ffma2_rn(x0, y0, d2); d2 = __ffma2_rn(x1, y1, d2);
+                            }
+                        }
+                        a = a2.x + a2.y; b = b2.x + b2.y; d = d2.x + d2.y;
+                    } else {
 #pragma unroll
-                            for (int e = 0; e < VW; e++) {
-                                a = fma(x[e], x[e], a); b = fma(y[e], y[e], b); d = fma(x[e], y[e], d);
+                        for (int it = 0; it < MAXIT; it++) {
+                            const int iv = lane + 32 * it;
+                            if (iv < nvec) {
+                                xr[it] = wp[iv];
+                                yr[it] = wq[iv];
+                                const S *x = reinterpret_cast<const S *>(&xr[it]), *y = reinterpret_cast<const S *>(&yr[it]);
+#pragma unroll
+                                for (int e = 0; e < VW; e++) {
+                                    a = fma(x[e], x[e], a); b = fma(y[e], y[e], b); d = fma(x[e], y[e], d);
+                                }
                             }
                         }
                     }
@@ -345,15 +364,31 @@ __global__ void __launch_bounds__(sizeof(S) == 4 ? 1024 : 512) jacobi_block_clus
                         const int iv = lane + 32 * it;
                         if (iv < nvec) {
                             V16 uv = vp[iv], vv = vq[iv];
-                            S *x = reinterpret_cast<S *>(&xr[it]), *y = reinterpret_cast<S *>(&yr[it]);
-                            S *u = reinterpret_cast<S *>(&uv), *v = reinterpret_cast<S *>(&vv);
+                            if constexpr (sizeof(S) == 4) {
+                                // (x, y) <- (cs x - sn y, sn x + cs y) on packed pairs
+                                const float2 c2 = make_float2(cs, cs), s2 = make_float2(sn, sn);
+                                const float2 ns2 = make_float2(-sn, -sn);
+                                auto rot = [&](float &p0, float &p1, float &q0, float &q1) {
+                                    const float2 pp = make_float2(p0, p1), qq = make_float2(q0, q1);
+                                    const float2 np = __ffma2_rn(c2, pp, __fmul2_rn(ns2, qq));
+                                    const float2 nq = __ffma2_rn(s2, pp, __fmul2_rn(c2, qq));
+                                    p0 = np.x; p1 = np.y; q0 = nq.x; q1 = nq.y;
+                                };
+                                rot(xr[it].x, xr[it].y, yr[it].x, yr[it].y);
+                                rot(xr[it].z, xr[it].w, yr[it].z, yr[it].w);
+                                rot(uv.x, uv.y, vv.x, vv.y);
+                                rot(uv.z, uv.w, vv.z, vv.w);
+                            } else {
+                                S *x = reinterpret_cast<S *>(&xr[it]), *y = reinterpret_cast<S *>(&yr[it]);
+                                S *u = reinterpret_cast<S *>(&uv), *v = reinterpret_cast<S *>(&vv);
 #pragma unroll
-                            for (int e = 0; e < VW; e++) {
-                                const S x0 = x[e], y0 = y[e], u0 = u[e], v0 = v[e];
-                                x[e] = cs * x0 - sn * y0;
-                                y[e] = sn * x0 + cs * y0;
-                                u[e] = cs * u0 - sn * v0;
-                                v[e] = sn * u0 + cs * v0;
+                                for (int e = 0; e < VW; e++) {
+                                    const S x0 = x[e], y0 = y[e], u0 = u[e], v0 = v[e];
+                                    x[e] = cs * x0 - sn * y0;
+                                    y[e] = sn * x0 + cs * y0;
+                                    u[e] = cs * u0 - sn * v0;
+                                    v[e] = sn * u0 + cs * v0;
+                                }
                             }
                             wp[iv] = xr[it];
                             wq[iv] = yr[it];
@@ -555,7 +590,7 @@ int jacobi_small(cudaStream_t s, DM<double> G, DM<double> U, DM<double> V, doubl
         RSVD_CK(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bsmem));
         cudaLaunchConfig_t cfg = {};
         cfg.gridDim = dim3(cl);
-        cfg.blockDim = dim3(32 * std::min(bs, sizeof(S) == 4 ? 32 : 16));
+        cfg.blockDim = dim3(32 * std::min(bs, 16));
         cfg.dynamicSmemBytes = bsmem;
         cfg.stream = s;
         cattr[0].val.clusterDim.x = cl;
