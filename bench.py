@@ -51,6 +51,8 @@ def parse():
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-learned", action="store_true")
     ap.add_argument("--no-batched", action="store_true")
+    # bracket one leg's timed region with cudaProfilerStart/Stop (ncu --profile-from-start off)
+    ap.add_argument("--profile-leg", choices=["solve", "learned", "batched"], default=None)
     return ap.parse_args()
 
 
@@ -163,7 +165,7 @@ def cpu_solve_seconds(A_host, threads, repeats=1):
 WEIGHTS = os.path.join(ROOT, "lowrankmatrixdecompositioncodes_gb300", "learned", "proposal_mlp.bin")
 
 
-def learned_qb_leg(torch, eng, dev, steps=2):
+def learned_qb_leg(torch, eng, dev, steps=2, profile=False):
     """Fixed-precision blocked QB on the 32768 x 16384 FP32 workload (s_i = exp(-i/200), Haar
     factors; generated at rank 6000, where s_i is below 1e-13), TOL = 1e-5 ||A||_F: the plain
     FP32 adaptive loop (randQB_pb_new semantics, kstep = 128, q = 1) against the learned
@@ -202,11 +204,16 @@ def learned_qb_leg(torch, eng, dev, steps=2):
         for i in range(steps + 1):
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             torch.cuda.synchronize()
+            prof = profile and learned and i == steps
+            if prof:
+                torch.cuda.cudart().cudaProfilerStart()
             e0.record(stream)
             rc = L.rsvdpack_dev_qb(At.data_ptr(), 1, m, m, n, 128, 0, tol_rel * fro, 1, 1, Q.data_ptr(), m,
                                    B.data_ptr(), cap, cap, C.byref(fr))
             e1.record(stream)
             e1.synchronize()
+            if prof:
+                torch.cuda.cudart().cudaProfilerStop()
             if rc:
                 raise RuntimeError(f"QB failed: {eng.last_error()}")
             if i > 0:
@@ -229,7 +236,7 @@ def learned_qb_leg(torch, eng, dev, steps=2):
     return out
 
 
-def batched_leg(torch, eng, dev, execs=5):
+def batched_leg(torch, eng, dev, execs=5, profile=False):
     """Batched rSVD workload: 4096 FP32 matrices, m ~ U[64, 1024], n ~ U[32, 512] (seed 0),
     s_i = 0.9^i with Haar factors, k = floor(min(m, n) / 8), p = 8, q = 1; one graph-captured
     persistent launch per execute.  Residuals of four items are checked against the optimal
@@ -284,6 +291,13 @@ def batched_leg(torch, eng, dev, execs=5):
         e1.record(stream)
         e1.synchronize()
         ms_exec = e0.elapsed_time(e1) / execs
+        if profile:
+            torch.cuda.synchronize()
+            torch.cuda.cudart().cudaProfilerStart()
+            if L.rsvdpack_batch_plan_execute(plan):
+                raise RuntimeError(eng.last_error())
+            torch.cuda.synchronize()
+            torch.cuda.cudart().cudaProfilerStop()
     finally:
         L.rsvdpack_batch_plan_destroy(plan)
     checks = []
@@ -422,13 +436,22 @@ def run_ours(args):
     launches = 0
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     torch.cuda.synchronize()
+    if args.profile_leg == "solve":
+        torch.cuda.cudart().cudaProfilerStart()
     ev0.record(stream)
+    phase_sum = {"products": 0.0, "orthonormalisation": 0.0, "lxl_svd": 0.0}
     for _ in range(args.steps):
         solve()
-        launches += eng.last_timing().kernel_launches
+        tm = eng.last_timing()
+        launches += tm.kernel_launches
+        phase_sum["products"] += tm.sketch_ms
+        phase_sum["orthonormalisation"] += tm.orth_ms
+        phase_sum["lxl_svd"] += tm.small_ms
     ev1.record(stream)
     ev1.synchronize()
     torch.cuda.synchronize()
+    if args.profile_leg == "solve":
+        torch.cuda.cudart().cudaProfilerStop()
     clocks = sampler.stop()
     ms = ev0.elapsed_time(ev1) / args.steps
     if world > 1:
@@ -436,6 +459,9 @@ def run_ours(args):
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         ms = float(t.item())
     value = world * 1000.0 / ms
+    # device time per solve by phase (CUDA events inside the engine, same timed solves)
+    phases = {kk: v / args.steps for kk, v in phase_sum.items()}
+    phases["other"] = max(0.0, ms - sum(phases.values()))
 
     # ---------------- dominant kernel: the sketch product, timed alone.  The engine times
     # each product with CUDA events on its own stream (rsvdpack_last_timing().sketch_ms).
@@ -476,7 +502,8 @@ def run_ours(args):
     roof = {"bound": "hbm", "achieved": gbs, "peak": hbm_peak, "unit": "GB/s", "frac": gbs / hbm_peak,
             "traffic": TC_TRAFFIC_PER_LAUNCH if mixed else None, "peak_kind": peak_kind,
             "kernel": "sketch product " + ("(tcgen05, one A*X and one A^T*X launch)" if mixed else "(CUDA-core GEMM)"),
-            "tflops": 2.0 * m * n * l * len(forms) / tot_ms / 1e9, "tensor_peak_tflops": tc_peak, "forms": forms}
+            "tflops": 2.0 * m * n * l * len(forms) / tot_ms / 1e9, "tensor_peak_tflops": tc_peak, "forms": forms,
+            "solve_phases_ms": phases}
 
     # ---------------- the plain FP32 GPU form of the same method (CUDA-core GEMMs, no
     # tensor cores), same matrix and sizes: the comparison point for the mixed modes
@@ -526,13 +553,13 @@ def run_ours(args):
     learned_leg = None
     if rank == 0 and not args.no_learned and os.path.exists(WEIGHTS):
         eng.load_proposal_model(WEIGHTS)
-        learned_leg = learned_qb_leg(torch, eng, dev)
+        learned_leg = learned_qb_leg(torch, eng, dev, profile=(args.profile_leg == "learned"))
         eng.set_precision(args.precision)
 
     # ---------------- batched workload (extra measurement)
     batched = None
     if rank == 0 and not args.no_batched:
-        batched = batched_leg(torch, eng, dev)
+        batched = batched_leg(torch, eng, dev, profile=(args.profile_leg == "batched"))
         eng.set_precision(args.precision)
 
     # ---------------- CPU baseline: the oracle on the host cores, one full solve

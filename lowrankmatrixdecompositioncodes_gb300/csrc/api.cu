@@ -229,6 +229,7 @@ void begin_call() {
     c.opts = global_opts();
     std::memset(&c.timing, 0, sizeof c.timing);
     c.launches = 0;
+    phase_reset();
 }
 
 // Device entry points read caller memory: order the engine stream (non-blocking) after
@@ -243,6 +244,7 @@ void order_after_default_stream() {
 void end_call(Clock::time_point t0) {
     Ctx &c = ctx();
     release_operand_cache();
+    phase_collect();
     check_device_flags(c);
     c.timing.total_ms = ms_since(t0);
     c.timing.kernel_launches = c.launches;

@@ -111,6 +111,7 @@ void release_operand_cache() { t_bf16_a = Bf16Cache{}; }
 // Deflation updates (beta != 0) and small products stay on the CUDA cores in FP32.
 template <typename T>
 void prod(cudaStream_t s, bool ta, bool tb, T alpha, DM<T> A, DM<T> B, T beta, DM<T> C) {
+    PhaseTimer pt(&ctx().timing.sketch_ms);
     if (std::is_same<T, float>::value && !tb && beta == T(0)) {
         const int prec = ctx().opts.precision;
         const i64 M = ta ? A.c : A.r, K = ta ? A.r : A.c, N = B.c;
@@ -252,6 +253,7 @@ static bool chol_pass_tc(cudaStream_t s, DM<float> Y, DM<float> Q, DM<double> *R
 template <typename T>
 void orth(DM<T> Y, DM<T> Q, DM<double> *R, int passes) {
     Ctx &cx = ctx();
+    PhaseTimer pt(&cx.timing.orth_ms);
     cudaStream_t s = cx.stream;
     const i64 c = Y.c;
     if (Y.r < c) fail(RSVD_ERR_ARGUMENT, "orth: more columns than rows");

@@ -548,6 +548,7 @@ template bool cholesky_small<float>(cudaStream_t, DM<double>, double, int *);
 
 template <typename S>
 int jacobi_small(cudaStream_t s, DM<double> G, DM<double> U, DM<double> V, double *d_sv, int *d_flag) {
+    PhaseTimer pt(&ctx().timing.small_ms);
     const int n = (int)G.r;
     if (G.r != G.c) fail(RSVD_ERR_ARGUMENT, "jacobi: not square");
     if (n == 0) return 0;

@@ -98,8 +98,27 @@ struct Ctx {
     // kernels may read pageable host memory directly (cudaDevAttrPageableMemoryAccess: GB300
     // with a Grace host, over NVLink-C2C)
     bool pageable_access = false;
+    // device-time phase marks of the current call (PhaseTimer), resolved by phase_collect()
+    struct PhaseMark {
+        cudaEvent_t a, b;
+        double *acc;
+    };
+    std::vector<PhaseMark> marks;
+    std::vector<cudaEvent_t> ev_pool;
+    size_t ev_used = 0;
 };
 Ctx &ctx();                       // initialises the device on first use; throws RSVD_ERR_NO_DEVICE
+
+// Device time of a region on the engine stream, added to *acc (a rsvdpack_timing field) when
+// the call ends: two pooled events per region, no synchronisation inside the region.
+struct PhaseTimer {
+    cudaEvent_t b = nullptr;
+    double *acc;
+    explicit PhaseTimer(double *acc_ms);
+    ~PhaseTimer();
+};
+void phase_reset();                // start of a call
+void phase_collect();              // end of a call: waits for the stream, resolves the marks
 const rsvdpack_opts &global_opts();
 
 // The learned proposal's network (host copy; null when none is installed).

@@ -152,6 +152,46 @@ Ctx &ctx() {
     return h.c;
 }
 
+namespace {
+cudaEvent_t pooled_event(Ctx &c) {
+    if (c.ev_used == c.ev_pool.size()) {
+        cudaEvent_t e;
+        RSVD_CK(cudaEventCreate(&e));
+        c.ev_pool.push_back(e);
+    }
+    return c.ev_pool[c.ev_used++];
+}
+}  // namespace
+
+PhaseTimer::PhaseTimer(double *acc_ms) : acc(acc_ms) {
+    Ctx &c = ctx();
+    cudaEvent_t a = pooled_event(c);
+    b = pooled_event(c);
+    RSVD_CK(cudaEventRecord(a, c.stream));
+    c.marks.push_back({a, b, acc});
+}
+PhaseTimer::~PhaseTimer() {
+    Ctx &c = ctx();
+    cudaEventRecord(b, c.stream);           // no throw from a destructor; errors surface later
+}
+void phase_reset() {
+    Ctx &c = ctx();
+    c.marks.clear();
+    c.ev_used = 0;
+}
+void phase_collect() {
+    Ctx &c = ctx();
+    if (c.marks.empty()) return;
+    RSVD_CK(cudaStreamSynchronize(c.stream));
+    for (auto &mk : c.marks) {
+        float ms = 0.f;
+        if (cudaEventElapsedTime(&ms, mk.a, mk.b) == cudaSuccess) *mk.acc += ms;
+        else cudaGetLastError();
+    }
+    c.marks.clear();
+    c.ev_used = 0;
+}
+
 void check_device_flags(Ctx &c) {
     int f[FLAG_COUNT];
     RSVD_CK(cudaMemcpyAsync(f, c.d_flags, sizeof f, cudaMemcpyDeviceToHost, c.stream));
