@@ -200,15 +200,18 @@ __device__ void load_tile_g(S *T, const double *G, long long ldg, int n, int I, 
 
 // The J loop of the one-CTA factorisation over tiles resident in shared memory (T: packed
 // upper tiles, Dw: scratch tile, diag0: original diagonal).  *bad is set on breakdown.
+// Lookahead: while warps 1.. apply step J's trailing update, warp 0 updates the next
+// diagonal tile first and factors it, so the one-warp diagonal step (the sequential part)
+// overlaps the trailing update instead of following it.
 template <typename S>
 __device__ void chol_steps(S *T, S *Dw, const S *diag0, int nb, double rel_tol, S *dinv, int *bad) {
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    if (wid == 0) {
+        const bool ok = factor_diag_warp<S>(T, Dw, diag0, (S)rel_tol);
+        if (!ok && lane == 0) *bad = 1;
+    }
+    __syncthreads();
     for (int J = 0; J < nb; J++) {
-        if (wid == 0) {
-            const bool ok = factor_diag_warp<S>(T + (size_t)tix(J, J) * TE, Dw, diag0 + J * TB, (S)rel_tol);
-            if (!ok && lane == 0) *bad = 1;
-        }
-        __syncthreads();
         if (*bad) break;
         // panel R_JK = R_JJ^-T G_JK (in place; R_JJ^-1 upper: only k <= r contributes)
         for (int K = J + 1 + wid; K < nb; K += nw) {
@@ -221,16 +224,30 @@ __device__ void chol_steps(S *T, S *Dw, const S *diag0, int nb, double rel_tol, 
         }
         for (int e = threadIdx.x; e < TB * TB; e += blockDim.x) dinv[(size_t)J * TB * TB + e] = Dw[(e >> 5) * TP + (e & 31)];
         __syncthreads();
-        // trailing update G_IK -= R_JI^T R_JK, J < I <= K
+        // trailing update G_IK -= R_JI^T R_JK, J < I <= K: tile (J+1, J+1) (t = 0) and the
+        // next diagonal factorisation on warp 0, the other tiles on warps 1..
         const int nt = nb - J - 1;
-        for (int t = wid; t < nt * (nt + 1) / 2; t += nw) {
-            int Ip, Kp;
-            untix(t, Ip, Kp);
-            const int I = J + 1 + Ip, K = J + 1 + Kp;
-            S acc[4][8];
-            zero_acc(acc);
-            tile_tn<S>(T + (size_t)tix(J, I) * TE, T + (size_t)tix(J, K) * TE, 0, TB, acc);
-            put_acc<S>(T + (size_t)tix(I, K) * TE, acc, true);
+        if (nt > 0) {
+            if (wid == 0) {
+                S acc[4][8];
+                zero_acc(acc);
+                tile_tn<S>(T + (size_t)tix(J, J + 1) * TE, T + (size_t)tix(J, J + 1) * TE, 0, TB, acc);
+                put_acc<S>(T + (size_t)tix(J + 1, J + 1) * TE, acc, true);
+                __syncwarp();
+                const bool ok = factor_diag_warp<S>(T + (size_t)tix(J + 1, J + 1) * TE, Dw, diag0 + (J + 1) * TB,
+                                                    (S)rel_tol);
+                if (!ok && lane == 0) *bad = 1;
+            } else {
+                for (int t = wid; t < nt * (nt + 1) / 2; t += nw - 1) {
+                    int Ip, Kp;
+                    untix(t, Ip, Kp);
+                    const int I = J + 1 + Ip, K = J + 1 + Kp;
+                    S acc[4][8];
+                    zero_acc(acc);
+                    tile_tn<S>(T + (size_t)tix(J, I) * TE, T + (size_t)tix(J, K) * TE, 0, TB, acc);
+                    put_acc<S>(T + (size_t)tix(I, K) * TE, acc, true);
+                }
+            }
         }
         __syncthreads();
     }

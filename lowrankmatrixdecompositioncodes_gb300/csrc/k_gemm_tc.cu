@@ -458,9 +458,39 @@ __global__ void splitk_reduce_kernel(const float *part, long long stride, int sp
     }
 }
 
-static void splitk_reduce(cudaStream_t s, const float *part, long long stride, int splits, int M, int N,
-                          long long ldp, float *D, long long ldd, float alpha, int sms) {
+// First pass for small outputs with many slabs: slab g*G <- sum of slabs g*G .. g*G+G-1
+// (compensated), in place (group g reads and writes only its own slabs).
+__global__ void splitk_group_kernel(float *part, long long stride, int splits, int G, int M, int N, long long ldp) {
+    const long long mq = ((long long)M + 3) / 4, per = mq * N, s4 = stride / 4;
+    const int ng = (splits + G - 1) / G;
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < per * ng;
+         e += (long long)gridDim.x * blockDim.x) {
+        const long long g = e / per, r = e - g * per;
+        const long long j = r / mq, i = (r - j * mq) * 4;
+        float4 *p = (float4 *)(part + i + j * ldp);
+        Neumaier a0, a1, a2, a3;
+        const int z0 = (int)g * G, z1 = min(splits, z0 + G);
+        for (int z = z0; z < z1; z++) {
+            const float4 v = __ldcs(p + (long long)z * s4);
+            a0.add(v.x); a1.add(v.y); a2.add(v.z); a3.add(v.w);
+        }
+        p[(long long)z0 * s4] = make_float4(a0.s + a0.c, a1.s + a1.c, a2.s + a2.c, a3.s + a3.c);
+    }
+}
+
+static void splitk_reduce(cudaStream_t s, float *part, long long stride, int splits, int M, int N, long long ldp,
+                          float *D, long long ldd, float alpha, int sms) {
     const long long total = ((long long)M + 3) / 4 * N;
+    if (splits >= 16 && total < (long long)sms * 512) {
+        // too few outputs to spread over the GPU: sum groups of 8 slabs in parallel first
+        constexpr int G = 8;
+        const long long work = total * ((splits + G - 1) / G);
+        const unsigned g1 = (unsigned)std::max<long long>(1, std::min<long long>((work + 255) / 256, (long long)sms * 16));
+        splitk_group_kernel<<<g1, 256, 0, s>>>(part, stride, splits, G, M, N, ldp);
+        RSVD_LAUNCH_CK();
+        stride *= G;
+        splits = (splits + G - 1) / G;
+    }
     const unsigned g = (unsigned)std::max<long long>(1, std::min<long long>((total + 255) / 256, (long long)sms * 16));
     splitk_reduce_kernel<<<g, 256, 0, s>>>(part, stride, splits, M, N, ldp, D, ldd, alpha);
     RSVD_LAUNCH_CK();
@@ -664,7 +694,7 @@ void tc_gemm_segs(cudaStream_t s, int kind, bool a_mn, int nseg, const TcSeg *se
         if (a_mn) launch<KIND_BF16, true, EPI_PARTIAL>(s, grid, smem, maps, P);
         else launch<KIND_BF16, false, EPI_PARTIAL>(s, grid, smem, maps, P);
     }
-    splitk_reduce(s, (const float *)part.get(), stride, splits, M, N, ldp, D, ldd, alpha, sms);
+    splitk_reduce(s, (float *)part.get(), stride, splits, M, N, ldp, D, ldd, alpha, sms);
     ctx().launches++;
 }
 
@@ -851,7 +881,12 @@ void tc_gemm_3xtf32(cudaStream_t s, const float *Ahi, const float *Alo, long lon
     const long long ldt = ((long long)M + 31) / 32 * 32;
     const long long slab_cap = std::max(1ll, (1ll << 30) / (ldt * N * (long long)sizeof(float)));
     const int splits_hh = (int)std::max(1ll, std::min({(K + 255) / 256ll, slab_cap, 128ll}));
-    const int splits = std::max(1, std::min(32, K / 1024));
+    // corrections: chains of ~1024 where the output has many tiles; where it has few (a Gram,
+    // M = N = l), enough splits to fill two waves of the GPU, up to the hi x hi split count
+    const long long tiles = ((long long)M + 127) / 128 * (N <= 512 ? 1 : ((long long)N + 255) / 256);
+    const long long fill = (2ll * std::max(1, ctx().sms) + tiles - 1) / tiles;
+    const int splits = (int)std::max<long long>(1, std::max<long long>(std::min(32, K / 1024),
+                                                                        std::min<long long>(splits_hh, fill)));
     DBuf t(sizeof(float) * (size_t)ldt * N, s);
     tc_gemm(s, tc::KIND_TF32, false, Ahi, lda, Xhi, ldx, M, N, K, 1.0f, D, ldd, tc::EPI_STORE, nullptr, 0, nullptr,
             splits_hh);
