@@ -525,6 +525,28 @@ def run_ours(args):
         plain = {"precision": "fp32", "value": 1000.0 / ms_plain, "ms_per_step": ms_plain,
                  "rel_frobenius": res_plain, "speedup_of_value": ms_plain / ms}
 
+    # ---------------- the same solve in BF16 mode (both product forms on the BF16 copy of A),
+    # with its own matched-error check against the same FP64 residual
+    bf16_leg = None
+    if args.precision == "tf32" and not args.no_plain:
+        eng.set_precision("bf16")
+        L.rsvdpack_reset_omega_counter()
+        solve()
+        res_bf16 = residual()
+        for _ in range(2):
+            solve()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for _ in range(5):
+            solve()
+        e1.record(stream)
+        e1.synchronize()
+        ms_bf16 = e0.elapsed_time(e1) / 5
+        eng.set_precision(args.precision)
+        bf16_leg = {"value": 1000.0 / ms_bf16, "ms_per_step": ms_bf16, "rel_frobenius": res_bf16,
+                    "matched": (res_fp64 is None) or (res_bf16 <= (1 + 1e-3) * res_fp64)}
+
     # ---------------- end to end through the reference C API, pinned host FP64 A
     e2e = None
     if not args.no_e2e:
@@ -582,7 +604,7 @@ def run_ours(args):
                        "l2": "inputs larger than L2 (A = 512 MiB)", "parallelism": f"replicas x{world}"},
             "residual": {"rel_frobenius": res_mixed, "fp64_same_method": res_fp64,
                          "matched": (res_fp64 is None) or (res_mixed <= (1 + 1e-3) * res_fp64)},
-            "roofline": roof, "plain_gpu": plain, "learned_qb": learned_leg, "batched": batched,
+            "roofline": roof, "plain_gpu": plain, "bf16": bf16_leg, "learned_qb": learned_leg, "batched": batched,
             "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches, "clocks": clocks,
             "device": name,
         }

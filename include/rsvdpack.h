@@ -95,6 +95,13 @@ void pivoted_QR_of_specified_rank_or_prec(mat *M, int k, double TOL, int *frank,
 void id_decomp_fixed_rank_or_prec(mat *M, int k, double TOL, int *frank, vec **I, mat **T);
 /* :76 randomized column ID (row sketch (k+p) x n, q power rounds) */
 void id_rand_decomp_fixed_rank(mat *M, int k, int p, int q, int s, vec **I, mat **T);
+/* decompositions from a given QB (Q m x l, B l x n; the QB split of the oneAPI variant,
+ * oneapi_code/rank_revealing_algorithms_one_api.h:6,10, with this header's int dimensions):
+ * low_rank_svd_rand_decomp_fromQB: U (m x l), S (l x l, descending), V (n x l) from the SVD of
+ * B B^T, V = B^T Uhat S^-1; id_rand_decomp_fromQB: column ID of B with k = Q->ncols,
+ * I (0-based pivots of B, as doubles) and T = R11^-1 R12 (k x (n - k)).  FP64. */
+void low_rank_svd_rand_decomp_fromQB(mat *Q, mat *B, mat **U, mat **S, mat **V);
+void id_rand_decomp_fromQB(mat *Q, mat *B, vec **I, mat **T);
 /* :79 blocked randomized column ID */
 void id_blockrand_decomp_fixed_rank_or_prec(mat *M, int k, int p, double TOL, int kstep,
                                             int q, int s, int *frank, vec **I, mat **T);

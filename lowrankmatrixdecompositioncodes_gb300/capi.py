@@ -57,6 +57,9 @@ _ALGOS = {
     "cur_rand_decomp_fixed_rank": [PMat, _I, _I, _I, _I, _PPM, _PPM, _PPM],
     "cur_blockrand_decomp_fixed_rank_or_prec":
         [PMat, _I, _I, _D, _I, _I, _I, _PI, _PPM, _PPM, _PPM],
+    # the QB split of the oneAPI variant (oneapi_code/rank_revealing_algorithms_one_api.h:6,10)
+    "low_rank_svd_rand_decomp_fromQB": [PMat, PMat, _PPM, _PPM, _PPM],
+    "id_rand_decomp_fromQB": [PMat, PMat, _PPV, _PPM],
 }
 
 
@@ -217,6 +220,26 @@ class RsvdLibrary:
         finally:
             self.lib.matrix_delete(M)
         return self.from_mat(Q), self.from_mat(B), fr.value
+
+    def low_rank_svd_rand_decomp_fromQB(self, Qm, Bm):
+        Q, B = self.to_mat(Qm), self.to_mat(Bm)
+        U, S, V = PMat(), PMat(), PMat()
+        try:
+            self.lib.low_rank_svd_rand_decomp_fromQB(Q, B, C.byref(U), C.byref(S), C.byref(V))
+        finally:
+            self.lib.matrix_delete(Q)
+            self.lib.matrix_delete(B)
+        return self.from_mat(U), self.from_mat(S), self.from_mat(V)
+
+    def id_rand_decomp_fromQB(self, Qm, Bm):
+        Q, B = self.to_mat(Qm), self.to_mat(Bm)
+        I, T = PVec(), PMat()
+        try:
+            self.lib.id_rand_decomp_fromQB(Q, B, C.byref(I), C.byref(T))
+        finally:
+            self.lib.matrix_delete(Q)
+            self.lib.matrix_delete(B)
+        return self.from_vec(I), self.from_mat(T)
 
     def pivotedQR_mkl(self, A):
         M = self.to_mat(A)

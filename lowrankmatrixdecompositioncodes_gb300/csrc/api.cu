@@ -585,6 +585,38 @@ void id_blockrand_decomp_fixed_rank_or_prec(mat *M, int k, int p, double TOL, in
     });
 }
 
+void low_rank_svd_rand_decomp_fromQB(mat *Q, mat *B, mat **U, mat **S, mat **V) {
+    *U = *S = *V = nullptr;
+    guarded("low_rank_svd_rand_decomp_fromQB", [&] {
+        check_mat(Q);
+        check_mat(B);
+        need(Q->ncols == B->nrows, "Q must have as many columns as B has rows");
+        begin_call();
+        auto t0 = Clock::now();
+        DMat<double> dQ = upload<double>(Q), dB = upload<double>(B);
+        SvdOut<double> r = svd_from_qb(dQ.v, dB.v);
+        svd_outputs<double>(r, U, S, V);
+        end_call(t0);
+    });
+}
+
+void id_rand_decomp_fromQB(mat *Q, mat *B, vec **I, mat **T) {
+    *I = nullptr;
+    *T = nullptr;
+    guarded("id_rand_decomp_fromQB", [&] {
+        check_mat(Q);
+        check_mat(B);
+        need(Q->ncols <= std::min(B->nrows, B->ncols), "Q->ncols must not exceed min(B rows, B cols)");
+        begin_call();
+        auto t0 = Clock::now();
+        DMat<double> dB = upload<double>(B);
+        IdOut r = id_from_qb(dB.v, Q->ncols);
+        *I = index_vec(r.I);
+        *T = download<double>(r.T.v);
+        end_call(t0);
+    });
+}
+
 static void two_sided_outputs(TwoSidedOut &r, vec **Icol, vec **Irow, mat **T, mat **S) {
     *Icol = index_vec(r.Icol);
     *Irow = index_vec(r.Irow);

@@ -835,6 +835,61 @@ IdOut id_blockrand(DM<double> A, int k, int p, double TOL, int kstep, int q, int
     return out;
 }
 
+// ------------------------------------------------------------------ decompositions from a given QB
+// (oneapi_code/rank_revealing_algorithms_one_api.c:244-300) BB^T = B B^T, its SVD by the
+// engine's one-sided Jacobi (BB^T is symmetric PSD: singular values = eigenvalues, descending),
+// S = sqrt, U = Q Uhat, V = B^T Uhat S^-1, all l = Q.c columns; FP64 throughout.
+SvdOut<double> svd_from_qb(DM<double> Q, DM<double> B) {
+    Ctx &cx = ctx();
+    cudaStream_t s = cx.stream;
+    const i64 m = Q.r, l = Q.c, n = B.c;
+    DMat<double> Bt(n, l, s, false);
+    transpose<double>(s, B, Bt.v);
+    DMat<double> BBt(l, l, s, false), Uh(l, l, s, false), Vh(l, l, s, false);
+    gram<double>(s, Bt.v, BBt.v);                                          // B B^T = Bt^T Bt
+    DBuf svb(sizeof(double) * l, s);
+    jacobi_small<double>(s, BBt.v, Uh.v, Vh.v, (double *)svb.get(), cx.d_flags + FLAG_JACOBI_NOCONV);
+    std::vector<double> sv((size_t)l);
+    RSVD_CK(cudaMemcpyAsync(sv.data(), svb.get(), sizeof(double) * l, cudaMemcpyDeviceToHost, s));
+    RSVD_CK(cudaStreamSynchronize(s));
+    SvdOut<double> out;
+    out.S.resize((size_t)l);
+    std::vector<int> all((size_t)l);
+    std::vector<double> inv((size_t)l);
+    for (i64 j = 0; j < l; j++) {
+        out.S[j] = std::sqrt(std::max(sv[j], 0.0));
+        all[j] = (int)j;
+        inv[j] = 1.0 / out.S[j];                                           // 1/0 -> inf, as the reference
+    }
+    out.U = DMat<double>(m, l, s, false);
+    out.V = DMat<double>(n, l, s, false);
+    gemm<double>(s, false, false, 1.0, Q, Uh.v, 0.0, out.U.v);
+    DMat<double> Us(l, l, s, false);
+    select_cols<double, double>(s, Uh.v, all, &inv, Us.v);
+    gemm<double>(s, false, false, 1.0, Bt.v, Us.v, 0.0, out.V.v);
+    RSVD_CK(cudaStreamSynchronize(s));
+    return out;
+}
+
+// (oneapi_code/rank_revealing_algorithms_one_api.c:421-447) column-pivoted QR of B (LAPACK
+// dgeqp3 pivoting), T = triu(R(:, 1:k))^-1 R(:, k+1:n) with k = Q.c.
+IdOut id_from_qb(DM<double> B, int k) {
+    Ctx &cx = ctx();
+    cudaStream_t s = cx.stream;
+    const i64 lb = B.r, n = B.c;
+    if (k > std::min(lb, n)) fail(RSVD_ERR_ARGUMENT, "id_rand_decomp_fromQB: Q has more columns than B's rank bound");
+    DMat<double> W(lb, n, s, false);
+    copy_dm<double>(s, B, W.v);
+    DBuf taub(sizeof(double) * std::max<i64>(1, std::min(lb, n)), s), jb(sizeof(int) * std::max<i64>(1, n), s);
+    pivqr_lapack(s, W.v, (double *)taub.get(), (int *)jb.get());
+    IdOut out;
+    out.frank = k;
+    out.I = download_ints(s, (const int *)jb.get(), n);
+    out.T = interp_coeffs(W.v.sub(0, 0, k, n), k);
+    RSVD_CK(cudaStreamSynchronize(s));
+    return out;
+}
+
 namespace {
 __global__ void build_v_kernel(const double *T, i64 ldt, const int *inv, int k, i64 n, double *V, i64 ldv) {
     // V(i,:) = row inv[i] of [I_k ; T^T]

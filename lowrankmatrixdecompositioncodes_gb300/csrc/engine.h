@@ -75,6 +75,8 @@ IdOut id_det(DM<double> A, int k, double TOL);
 IdOut id_rand(DM<double> A, int k, int p, int q, int s);
 IdOut id_blockrand(DM<double> A, int k, int p, double TOL, int kstep, int q, int s);
 TwoSidedOut id_two_sided(DM<double> A, IdOut col);
+SvdOut<double> svd_from_qb(DM<double> Q, DM<double> B);
+IdOut id_from_qb(DM<double> B, int k);
 CurOut cur_from_two_sided(DM<double> A, int k, const TwoSidedOut &ts);
 
 }  // namespace rsvd

@@ -582,6 +582,38 @@ void id_blockrand_decomp_fixed_rank_or_prec(mat *M, int k, int p, double TOL, in
     matrix_delete(Q); matrix_delete(B); matrix_delete(Qk); matrix_delete(Rk);
 }
 
+/* ===================== decompositions from a given QB (oneapi_code variant) ===================== */
+/* oneapi_code/rank_revealing_algorithms_one_api.c:244-300: BBt = B B^T; [Uhat, St, ~] = svd(BBt)
+   (descending); S = sqrt(diag(St)) for all l = Q->ncols columns; U = Q Uhat; V = B^T Uhat S^-1. */
+void low_rank_svd_rand_decomp_fromQB(mat *Q, mat *B, mat **U, mat **S, mat **V)
+{
+    int m = Q->nrows, n = B->ncols, l = Q->ncols;
+    mat *BBt = matrix_new(l, l), *Uhat = matrix_new(l, l), *St = matrix_new(l, l), *Vt = matrix_new(l, l);
+    gemm_nt(B, B, BBt);
+    svd_small(BBt, Uhat, St, Vt);
+    *U = matrix_new(m, l);
+    *S = matrix_new(l, l);
+    *V = matrix_new(n, l);
+    for (int i = 0; i < l; i++) AT(*S, i, i) = sqrt(AT(St, i, i));
+    gemm_nn(Q, Uhat, *U);
+    mat *US = matrix_new(l, l);                     /* Uhat S^-1 (1/0 -> inf as in the reference) */
+    for (int j = 0; j < l; j++)
+        for (int i = 0; i < l; i++) AT(US, i, j) = AT(Uhat, i, j) / AT(*S, j, j);
+    gemm_tn(B, US, *V);
+    matrix_delete(BBt); matrix_delete(Uhat); matrix_delete(St); matrix_delete(Vt); matrix_delete(US);
+}
+
+/* oneapi_code/rank_revealing_algorithms_one_api.c:421-447: k = Q->ncols; [~, Rk, I] = pivotedQR(B);
+   T = triu(Rk(:, 1:k))^-1 Rk(:, k+1:n). */
+void id_rand_decomp_fromQB(mat *Q, mat *B, vec **I, mat **T)
+{
+    int k = Q->ncols;
+    mat *Qk, *Rk;
+    pivotedQR_mkl(B, &Qk, &Rk, I);
+    *T = interp_coeffs(Rk, k);
+    matrix_delete(Qk); matrix_delete(Rk);
+}
+
 /* MIt = M(:,Icol(1:r))^T, then a full-rank deterministic row ID of it (RRA:2042-2051) */
 static void row_id_of_selected_columns(mat *M, vec *Icol, int r, vec **Irow, mat **S)
 {

@@ -45,6 +45,8 @@ void pivoted_QR_of_specified_rank_or_prec(mat *M, int k, double TOL, int *frank,
                                           mat **Qk, mat **Rk, vec **I);
 void id_decomp_fixed_rank_or_prec(mat *M, int k, double TOL, int *frank, vec **I, mat **T);
 void id_rand_decomp_fixed_rank(mat *M, int k, int p, int q, int s, vec **I, mat **T);
+void low_rank_svd_rand_decomp_fromQB(mat *Q, mat *B, mat **U, mat **S, mat **V);
+void id_rand_decomp_fromQB(mat *Q, mat *B, vec **I, mat **T);
 void id_blockrand_decomp_fixed_rank_or_prec(mat *M, int k, int p, double TOL, int kstep,
                                             int q, int s, int *frank, vec **I, mat **T);
 void id_two_sided_decomp_fixed_rank_or_prec(mat *M, int k, double TOL, int *frank,
