@@ -87,12 +87,16 @@ __device__ void gen_omega(float *Bsm, int n, int l, uint64_t seed, uint64_t offs
 // broadcast loads of B feed 20 FMAs; the next chunk of A is prefetched into registers while
 // the current one is multiplied.
 constexpr int ATP = 68;          // pitch of a staged A chunk (64 values + 4, 16-byte rows)
-constexpr int CU = 5;            // column groups per thread: l <= 16 * CU
+constexpr int CU_MAX = 5;        // column groups per thread: l <= 16 * CU_MAX
+// The products are instantiated for CU = 1..5 column groups and each call takes the
+// smallest CU with 16 * CU >= its width (l, or k for the output products): at the batch's
+// mean width (~37) the fixed CU = 5 spent 40% of its FMAs on zero padding.
 
 // Y (m x l, ldy) = A (m x n) * B, B row-major in shared memory (B[j*l + c]).
 // Row tiles of 64; A chunks of 64 rows x 32 columns staged as At[jj][row] (pitch ATP).
-__device__ void gemm_A_B(const float *A, long long lda, int m, int n, const float *Bsm, int l, float *Y, long long ldy,
-                         float *At) {
+template <int CU>
+__device__ void gemm_A_B_t(const float *A, long long lda, int m, int n, const float *Bsm, int l, float *Y,
+                           long long ldy, float *At) {
     const int tid = threadIdx.x, rg = (tid >> 4) * 4, cg = tid & 15;
     for (int r0 = 0; r0 < m; r0 += 64) {
         float acc[4][CU];
@@ -152,8 +156,9 @@ __device__ void gemm_A_B(const float *A, long long lda, int m, int n, const floa
 
 // Z (n x l, ldz) = A^T (n x m) * Q (m x l, ldq, global).  Column tiles of 64 (thread: 4
 // columns of A); row chunks of 32 staged as At[ii][col] (pitch ATP) and Qs[ii][c].
-__device__ void gemm_At_Q(const float *A, long long lda, int m, int n, const float *Q, long long ldq, int l, float *Z,
-                          long long ldz, float *At, float *Qs) {
+template <int CU>
+__device__ void gemm_At_Q_t(const float *A, long long lda, int m, int n, const float *Q, long long ldq, int l,
+                            float *Z, long long ldz, float *At, float *Qs) {
     const int tid = threadIdx.x, jg = (tid >> 4) * 4, cg = tid & 15;
     for (int j0 = 0; j0 < n; j0 += 64) {
         float acc[4][CU];
@@ -161,7 +166,7 @@ __device__ void gemm_At_Q(const float *A, long long lda, int m, int n, const flo
         for (int a = 0; a < 4; a++)
 #pragma unroll
             for (int u = 0; u < CU; u++) acc[a][u] = 0.f;
-        float pa[8], pq[10];
+        float pa[8], pq[2 * CU];          // Q: 32 rows x 16 CU columns over BT threads
         auto fetch = [&](int i0) {
 #pragma unroll
             for (int t = 0; t < 8; t++) {
@@ -169,7 +174,7 @@ __device__ void gemm_At_Q(const float *A, long long lda, int m, int n, const flo
                 pa[t] = (i0 + ii < m && j0 + jj < n) ? A[(i0 + ii) + (long long)(j0 + jj) * lda] : 0.f;
             }
 #pragma unroll
-            for (int t = 0; t < 10; t++) {
+            for (int t = 0; t < 2 * CU; t++) {
                 const int e = tid + BT * t, ii = e & 31, c = e >> 5;
                 pq[t] = (c < l && i0 + ii < m) ? Q[(i0 + ii) + (long long)c * ldq] : 0.f;
             }
@@ -183,7 +188,7 @@ __device__ void gemm_At_Q(const float *A, long long lda, int m, int n, const flo
                 At[(e & 31) * ATP + (e >> 5)] = pa[t];
             }
 #pragma unroll
-            for (int t = 0; t < 10; t++) {
+            for (int t = 0; t < 2 * CU; t++) {
                 const int e = tid + BT * t, c = e >> 5;
                 if (c < l) Qs[(e & 31) * l + c] = pq[t];
             }
@@ -219,6 +224,27 @@ __device__ void gemm_At_Q(const float *A, long long lda, int m, int n, const flo
         }
     }
     __syncthreads();
+}
+
+__device__ __forceinline__ void gemm_A_B(const float *A, long long lda, int m, int n, const float *Bsm, int l,
+                                         float *Y, long long ldy, float *At) {
+    switch ((l + 15) / 16) {
+        case 1: gemm_A_B_t<1>(A, lda, m, n, Bsm, l, Y, ldy, At); break;
+        case 2: gemm_A_B_t<2>(A, lda, m, n, Bsm, l, Y, ldy, At); break;
+        case 3: gemm_A_B_t<3>(A, lda, m, n, Bsm, l, Y, ldy, At); break;
+        case 4: gemm_A_B_t<4>(A, lda, m, n, Bsm, l, Y, ldy, At); break;
+        default: gemm_A_B_t<CU_MAX>(A, lda, m, n, Bsm, l, Y, ldy, At); break;
+    }
+}
+__device__ __forceinline__ void gemm_At_Q(const float *A, long long lda, int m, int n, const float *Q, long long ldq,
+                                          int l, float *Z, long long ldz, float *At, float *Qs) {
+    switch ((l + 15) / 16) {
+        case 1: gemm_At_Q_t<1>(A, lda, m, n, Q, ldq, l, Z, ldz, At, Qs); break;
+        case 2: gemm_At_Q_t<2>(A, lda, m, n, Q, ldq, l, Z, ldz, At, Qs); break;
+        case 3: gemm_At_Q_t<3>(A, lda, m, n, Q, ldq, l, Z, ldz, At, Qs); break;
+        case 4: gemm_At_Q_t<4>(A, lda, m, n, Q, ldq, l, Z, ldz, At, Qs); break;
+        default: gemm_At_Q_t<CU_MAX>(A, lda, m, n, Q, ldq, l, Z, ldz, At, Qs); break;
+    }
 }
 
 // G (l x l, shared, ldg = l) = Y^T Y for Y (rows x l) in global; 32-row chunks staged.
