@@ -66,13 +66,32 @@ struct Bf16Cache {
     DMat<__nv_bfloat16> m;
     DMat<__nv_bfloat16> lo;      // second part of a two-part split (empty when not split)
     bool split = false;
+    bool borrowed = false;       // vh / vl: a caller-owned pair (borrow_operand_pair)
+    DM<__nv_bfloat16> vh, vl;
 };
 thread_local Bf16Cache t_bf16_a;
+
+// Serve X's two-part BF16 split from caller-owned buffers (kept current by the caller)
+// until release_operand_cache().
+void borrow_operand_pair(DM<float> X, DM<__nv_bfloat16> hi, DM<__nv_bfloat16> lo) {
+    t_bf16_a = Bf16Cache{};
+    t_bf16_a.src = X.p; t_bf16_a.r = X.r; t_bf16_a.c = X.c; t_bf16_a.ld = X.ld;
+    t_bf16_a.split = true;
+    t_bf16_a.borrowed = true;
+    t_bf16_a.vh = hi;
+    t_bf16_a.vl = lo;
+}
 
 // A = hi + lo (two BF16 parts), cached like to_bf16's copy; hi is the plain BF16 rounding,
 // so a cached split also serves to_bf16.
 void to_bf16_pair(cudaStream_t s, DM<float> X, DM<__nv_bfloat16> &hi, DM<__nv_bfloat16> &lo) {
-    if (!(t_bf16_a.split && t_bf16_a.src == X.p && t_bf16_a.r == X.r && t_bf16_a.c == X.c && t_bf16_a.ld == X.ld)) {
+    const bool hit = t_bf16_a.split && t_bf16_a.src == X.p && t_bf16_a.r == X.r && t_bf16_a.c == X.c && t_bf16_a.ld == X.ld;
+    if (hit && t_bf16_a.borrowed) {
+        hi = t_bf16_a.vh;
+        lo = t_bf16_a.vl;
+        return;
+    }
+    if (!hit) {
         DMat<__nv_bfloat16> h(X.r, X.c, s, false), l(X.r, X.c, s, false);
         split_bf16(s, X, h.v, l.v);
         t_bf16_a.m = std::move(h);
@@ -86,7 +105,7 @@ void to_bf16_pair(cudaStream_t s, DM<float> X, DM<__nv_bfloat16> &hi, DM<__nv_bf
 
 DM<__nv_bfloat16> to_bf16(cudaStream_t s, DM<float> X, DMat<__nv_bfloat16> &tmp, bool cache) {
     if (cache && t_bf16_a.src == X.p && t_bf16_a.r == X.r && t_bf16_a.c == X.c && t_bf16_a.ld == X.ld)
-        return t_bf16_a.m.v;
+        return t_bf16_a.borrowed ? t_bf16_a.vh : t_bf16_a.m.v;
     DMat<__nv_bfloat16> d(X.r, X.c, s, false);
     convert<float, __nv_bfloat16>(s, X, d.v);
     if (cache) {
@@ -464,7 +483,7 @@ static QBOut<T> qb_plain(DM<T> A, int kstep, int nstep, double TOL, int q, int s
 // ------------------------------------------------------------------ learned proposal
 // Fixed-precision QB (randQB_pb_new in TOL mode) with the block widths and power count set by
 // the learned network from a 32-column probe sketch:
-//   probe   Y0 = A Omega0 (n x 32, FP32 products), R0 from orth(Y0); features = log10 of
+//   probe   Y0 = A Omega0 (m x 32, tensor cores), R0 from orth(Y0); features = log10 of
 //           R0's diagonal relative to ||A||_F, log10 of the energy the probe leaves (floored
 //           at 1e-5), log10 min(m, n),
 //           log10(m / n), log10(TOL / ||A||_F) (the training set's feature_vector);
@@ -502,7 +521,10 @@ static bool learned_qb(DM<float> A, double TOL, QBOut<float> &out, int *q_used) 
     {
         DMat<float> Om0 = make_omega<float>(n, kProbe);
         DMat<float> Y0(m, kProbe, s, false);
-        gemm<float>(s, false, false, 1.f, A, Om0.v, 0.f, Y0.v);
+        // tensor cores, A read as the two-part BF16 split (~2^-16): the features are log10
+        // magnitudes, far coarser than that
+        prod<float>(s, false, false, 1.f, A, Om0.v, 0.f, Y0.v);
+        release_operand_cache();                                           // A is not A_res
         // R0 of the probe by the engine's orthonormalisation (CholeskyQR2, Householder when a
         // steep spectrum makes the 32-column probe too ill-conditioned for a Gram)
         DMat<float> Q0(m, kProbe, s, false);
@@ -566,6 +588,19 @@ static bool learned_qb(DM<float> A, double TOL, QBOut<float> &out, int *q_used) 
     DMat<float> Ar(m, n, s, false);                                    // the residual A - Q B
     copy_dm<float>(s, A, Ar.v);
     DMat<float> Qall(m, rmin, s, false), Qt(rmin, m, s, false), Ball(rmin, n, s, false);
+    // operands kept split: A_res as TF32 hi / lo (B_j = Q_j^T A_res) and as BF16 hi / lo (the
+    // sketches; the operand cache serves the pair under A_res's address), both rewritten by
+    // the deflation's epilogue; Q_f and Q_f^T as TF32 hi / lo, extended block by block
+    DMat<float> Arh(m, n, s, false), Arl(m, n, s, false);
+    split_tf32(s, Ar.v.p, Ar.v.ld, m, n, Arh.v.p, Arl.v.p, Arh.v.ld);
+    DMat<__nv_bfloat16> Abh_own(m, n, s, false), Abl_own(m, n, s, false);
+    split_bf16(s, Ar.v, Abh_own.v, Abl_own.v);
+    borrow_operand_pair(Ar.v, Abh_own.v, Abl_own.v);
+    struct DropBorrowed {                                              // also on an exception
+        ~DropBorrowed() { release_operand_cache(); }
+    } drop_borrowed;
+    const DM<__nv_bfloat16> Abh = Abh_own.v, Abl = Abl_own.v;
+    DMat<float> Qah(m, rmin, s, false), Qal(m, rmin, s, false), Qth(rmin, m, s, false), Qtl(rmin, m, s, false);
     // tc_gemm's grid for an m x n update: 128-row tiles; one column tile up to 512 columns,
     // else 256-column tiles (one sum of squares per CTA)
     const i64 mt = (m + 127) / 128, ntl = (n <= 512) ? 1 : (n + 255) / 256;
@@ -594,21 +629,17 @@ static bool learned_qb(DM<float> A, double TOL, QBOut<float> &out, int *q_used) 
             for (int pass = 0; pass < 2; pass++) {
                 DMat<float> P(f, b, s, false), Yt(b, m, s, false);
                 {
-                    DMat<float> Qh(m, f, s, false), Ql(m, f, s, false), Yh(m, b, s, false), Yl(m, b, s, false);
-                    split_tf32(s, Qall.v.p, Qall.v.ld, m, f, Qh.v.p, Ql.v.p, Qh.v.ld);
+                    DMat<float> Yh(m, b, s, false), Yl(m, b, s, false);
                     split_tf32(s, Yo.v.p, Yo.v.ld, m, b, Yh.v.p, Yl.v.p, Yh.v.ld);
-                    tc_gemm_3xtf32(s, Qh.v.p, Ql.v.p, Qh.v.ld, Yh.v.p, Yl.v.p, Yh.v.ld, f, b, (int)m, P.v.p, P.v.ld);
-                    RSVD_CK(cudaStreamSynchronize(s));
+                    tc_gemm_3xtf32(s, Qah.v.p, Qal.v.p, Qah.v.ld, Yh.v.p, Yl.v.p, Yh.v.ld, f, b, (int)m, P.v.p, P.v.ld);
                 }
                 transpose<float>(s, Yo.v, Yt.v);
                 {
-                    DMat<float> Ph(f, b, s, false), Pl(f, b, s, false), Th(f, m, s, false), Tl(f, m, s, false);
+                    DMat<float> Ph(f, b, s, false), Pl(f, b, s, false);
                     split_tf32(s, P.v.p, P.v.ld, f, b, Ph.v.p, Pl.v.p, Ph.v.ld);
-                    split_tf32(s, Qt.v.p, Qt.v.ld, f, m, Th.v.p, Tl.v.p, Th.v.ld);
                     // Yt (b x m) = Yt - P^T Q_f^T : A^T X form with A = P (K = f), X = Q_f^T (K = f)
-                    tc_update_3xtf32(s, Ph.v.p, Pl.v.p, Ph.v.ld, Th.v.p, Tl.v.p, Th.v.ld, b, (int)m, f, Yt.v.p,
+                    tc_update_3xtf32(s, Ph.v.p, Pl.v.p, Ph.v.ld, Qth.v.p, Qtl.v.p, Qth.v.ld, b, (int)m, f, Yt.v.p,
                                      Yt.v.ld, nullptr);
-                    RSVD_CK(cudaStreamSynchronize(s));
                 }
                 transpose<float>(s, Yt.v, Y.v);
                 orth<float>(Y.v, Yo.v, nullptr, pass == 0 ? 1 : 2);
@@ -618,25 +649,24 @@ static bool learned_qb(DM<float> A, double TOL, QBOut<float> &out, int *q_used) 
         copy_dm<float>(s, Yo.v, Qj);
         DM<float> Qtj = Qt.v.sub(f, 0, b, m);
         transpose<float>(s, Qj, Qtj);
+        split_tf32(s, Qj.p, Qj.ld, m, b, Qah.v.p + (size_t)f * Qah.v.ld, Qal.v.p + (size_t)f * Qal.v.ld, Qah.v.ld);
+        split_tf32(s, Qtj.p, Qtj.ld, b, m, Qth.v.p + f, Qtl.v.p + f, Qth.v.ld);
         // B_j (b x n) = Q_j^T A_res, as B_j^T = A_res^T Q_j (3xTF32)
         DM<float> Bj = Ball.v.sub(f, 0, b, n);
         {
-            DMat<float> Ah(m, n, s, false), Al(m, n, s, false), Qh(m, b, s, false), Ql(m, b, s, false);
-            split_tf32(s, Ar.v.p, Ar.v.ld, m, n, Ah.v.p, Al.v.p, Ah.v.ld);
-            split_tf32(s, Qj.p, Qj.ld, m, b, Qh.v.p, Ql.v.p, Qh.v.ld);
             DMat<float> Bt(n, b, s, false);
-            tc_gemm_3xtf32(s, Ah.v.p, Al.v.p, Ah.v.ld, Qh.v.p, Ql.v.p, Qh.v.ld, (int)n, b, (int)m, Bt.v.p, Bt.v.ld);
+            tc_gemm_3xtf32(s, Arh.v.p, Arl.v.p, Arh.v.ld, Qah.v.p + (size_t)f * Qah.v.ld,
+                           Qal.v.p + (size_t)f * Qal.v.ld, Qah.v.ld, (int)n, b, (int)m, Bt.v.p, Bt.v.ld);
             transpose<float>(s, Bt.v, Bj);
-            RSVD_CK(cudaStreamSynchronize(s));
         }
         // A_res -= Q_j B_j (3xTF32, one in-place pass) with per-CTA sums of squares of the result
         {
             DMat<float> Th(b, m, s, false), Tl(b, m, s, false), Bh(b, n, s, false), Bl(b, n, s, false);
             split_tf32(s, Qtj.p, Qtj.ld, b, m, Th.v.p, Tl.v.p, Th.v.ld);
             split_tf32(s, Bj.p, Bj.ld, b, n, Bh.v.p, Bl.v.p, Bh.v.ld);
+            const TcSplitOut so{Arh.v.p, Arl.v.p, Arh.v.ld, Abh.p, Abl.p, Abh.ld};
             tc_update_3xtf32(s, Th.v.p, Tl.v.p, Th.v.ld, Bh.v.p, Bl.v.p, Bh.v.ld, (int)m, (int)n, b, Ar.v.p, Ar.v.ld,
-                             (double *)frob_part.get());
-            release_operand_cache();                                     // A_res changed
+                             (double *)frob_part.get(), &so);                // also rewrites the splits of A_res
             hpart.resize((size_t)(mt * ntl));
             RSVD_CK(cudaMemcpyAsync(hpart.data(), frob_part.get(), sizeof(double) * hpart.size(),
                                     cudaMemcpyDeviceToHost, s));
@@ -651,6 +681,8 @@ static bool learned_qb(DM<float> A, double TOL, QBOut<float> &out, int *q_used) 
             std::fprintf(stderr, "rsvdpack: learned QB block %d width %d rank %d residual %.3e (TOL %.3e)\n", blocks,
                          b, f, res, TOL);
     }
+    release_operand_cache();                                           // A_res (and its BF16 pair) go away
+    RSVD_CK(cudaStreamSynchronize(s));
     out.Q = std::move(Qall);
     out.B = std::move(Ball);
     out.Q.v.c = f;

@@ -50,6 +50,11 @@ struct Params {
     int nseg;          // K segments: segment s contracts maps.a[s] with maps.b[s] over seg_kb[s] blocks
     int seg_kb[MAX_SEG];
     int c_tma;         // EPI_UPDATE: C is TMA-loaded into the free stage buffers, D TMA-stored
+    // EPI_UPDATE with c_tma (optional, null = none): the new D also split as TF32 hi / lo
+    // (hi = D rounded to TF32, lo = D - hi; ld lds) and as BF16 hi / lo (ld ldb)
+    float *Shi, *Slo;
+    __nv_bfloat16 *Bhi, *Blo;
+    long long lds, ldb;
     int stages;
     float alpha;
     double *fro_part;  // EPI_UPDATE: per-CTA sum of squares of the new D (or null)
@@ -330,7 +335,19 @@ __global__ void __launch_bounds__(NTHR, 1)
                     float *e = tile + (size_t)(cc + t) * BM + r;
                     const float nv = *e - P.alpha * v[t];
                     *e = nv;
-                    if (row < P.M && n0 + c * CW + cc + t < P.N) fro.add(nv * nv);
+                    const int col = n0 + c * CW + cc + t;
+                    if (row < P.M && col < P.N) {
+                        fro.add(nv * nv);
+                        if (P.Shi) {
+                            // the next products' operands, written while the value is in hand
+                            const float h = __uint_as_float((__float_as_uint(nv) + 0x1000u) & 0xFFFFE000u);
+                            P.Shi[(long long)row + (long long)col * P.lds] = h;
+                            P.Slo[(long long)row + (long long)col * P.lds] = nv - h;
+                            const __nv_bfloat16 bh = __float2bfloat16_rn(nv);
+                            P.Bhi[(long long)row + (long long)col * P.ldb] = bh;
+                            P.Blo[(long long)row + (long long)col * P.ldb] = __float2bfloat16_rn(nv - __bfloat162float(bh));
+                        }
+                    }
                 }
             }
             asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
@@ -575,7 +592,8 @@ static void launch(cudaStream_t s, dim3 grid, size_t smem, const Maps &maps, con
 
 // Public launchers (declared in rsvd_internal.h).
 void tc_gemm_segs(cudaStream_t s, int kind, bool a_mn, int nseg, const TcSeg *seg, int M, int N, float alpha,
-                  float *D, long long ldd, int epi, const float *C, long long ldc, double *fro_part, int splits_hint) {
+                  float *D, long long ldd, int epi, const float *C, long long ldc, double *fro_part, int splits_hint,
+                  const TcSplitOut *so) {
     using namespace tc;
     const int esz = (kind == KIND_TF32) ? 4 : 2;
     const int KE = KB / esz;
@@ -662,6 +680,10 @@ void tc_gemm_segs(cudaStream_t s, int kind, bool a_mn, int nseg, const TcSeg *se
         if (P.c_tma) {
             maps.c = make_map_tile(C, M, N, ldc * 4);
             maps.d = make_map_tile(D, M, N, ldd * 4);
+            if (so) {
+                P.Shi = so->hi; P.Slo = so->lo; P.lds = so->ld;
+                P.Bhi = so->bhi; P.Blo = so->blo; P.ldb = so->ldb;
+            }
         }
         if (kind == KIND_TF32) {
             if (a_mn) launch<KIND_TF32, true, EPI_UPDATE>(s, grid, smem, maps, P);
@@ -669,6 +691,12 @@ void tc_gemm_segs(cudaStream_t s, int kind, bool a_mn, int nseg, const TcSeg *se
         } else {
             if (a_mn) launch<KIND_BF16, true, EPI_UPDATE>(s, grid, smem, maps, P);
             else launch<KIND_BF16, false, EPI_UPDATE>(s, grid, smem, maps, P);
+        }
+        if (so && !P.c_tma) {
+            // the register epilogue does not write the splits: separate passes
+            split_tf32(s, D, ldd, M, N, so->hi, so->lo, so->ld);
+            split_bf16(s, DM<float>{D, M, N, ldd}, DM<__nv_bfloat16>{so->bhi, M, N, so->ldb},
+                       DM<__nv_bfloat16>{so->blo, M, N, so->ldb});
         }
         return;
     }
@@ -703,7 +731,7 @@ void tc_gemm(cudaStream_t s, int kind, bool a_mn, const void *A, long long lda, 
              double *fro_part, int splits_hint) {
     if (K <= 0) fail(RSVD_ERR_ARGUMENT, "tc_gemm: empty");
     const TcSeg g{A, lda, X, ldx, K};
-    tc_gemm_segs(s, kind, a_mn, 1, &g, M, N, alpha, D, ldd, epi, C, ldc, fro_part, splits_hint);
+    tc_gemm_segs(s, kind, a_mn, 1, &g, M, N, alpha, D, ldd, epi, C, ldc, fro_part, splits_hint, nullptr);
 }
 
 // =====================================================================================
@@ -904,9 +932,9 @@ void tc_gemm_3xtf32(cudaStream_t s, const float *Ahi, const float *Alo, long lon
 // sums of squares of the new C (tc_gemm's update layout), or null.
 void tc_update_3xtf32(cudaStream_t s, const float *Ahi, const float *Alo, long long lda, const float *Xhi,
                       const float *Xlo, long long ldx, int M, int N, int K, float *Cm, long long ldc,
-                      double *fro_part) {
+                      double *fro_part, const TcSplitOut *so) {
     const TcSeg g[3] = {{Alo, lda, Xhi, ldx, K}, {Ahi, lda, Xlo, ldx, K}, {Ahi, lda, Xhi, ldx, K}};
-    tc_gemm_segs(s, tc::KIND_TF32, false, 3, g, M, N, 1.0f, Cm, ldc, tc::EPI_UPDATE, Cm, ldc, fro_part, 1);
+    tc_gemm_segs(s, tc::KIND_TF32, false, 3, g, M, N, 1.0f, Cm, ldc, tc::EPI_UPDATE, Cm, ldc, fro_part, 1, so);
 }
 
 }  // namespace rsvd

@@ -224,8 +224,19 @@ struct TcSeg {
     long long ldx;
     int K;
 };
+// Optional extra outputs of an update (epi 1): the new D split as TF32 hi / lo (hi = D
+// rounded to TF32, lo = D - hi) and as BF16 hi / lo -- the operands the next 3xTF32 and
+// two-part BF16 products read -- written by the epilogue (or by separate passes when the
+// update cannot use the TMA epilogue).
+struct TcSplitOut {
+    float *hi, *lo;
+    long long ld;
+    __nv_bfloat16 *bhi, *blo;
+    long long ldb;
+};
 void tc_gemm_segs(cudaStream_t s, int kind, bool a_mn, int nseg, const TcSeg *seg, int M, int N, float alpha,
-                  float *D, long long ldd, int epi, const float *C, long long ldc, double *fro_part, int splits_hint);
+                  float *D, long long ldd, int epi, const float *C, long long ldc, double *fro_part, int splits_hint,
+                  const TcSplitOut *so = nullptr);
 // 3xTF32 (FP32-accurate) products on the tf32 pipe: split_tf32 writes hi = tf32(X) and
 // lo = X - hi; tc_gemm_3xtf32 computes D = A^T X (A K-major, K x M) from split operands.
 void split_tf32(cudaStream_t s, const float *X, long long ldx, long long r, long long c, float *hi, float *lo,
@@ -235,7 +246,7 @@ void tc_gemm_3xtf32(cudaStream_t s, const float *Ahi, const float *Alo, long lon
 // C (M x N) -= A^T X (3xTF32, one pass over C, in place); fro_part as for tc_gemm's update.
 void tc_update_3xtf32(cudaStream_t s, const float *Ahi, const float *Alo, long long lda, const float *Xhi,
                       const float *Xlo, long long ldx, int M, int N, int K, float *Cm, long long ldc,
-                      double *fro_part);
+                      double *fro_part, const TcSplitOut *so = nullptr);
 // ----------------------------------------------------------------- tiled triangular steps (k_chol.cu)
 // G (n x n, FP64, upper triangle read) -> R, G = R^T R (upper, zero below), compute type S.
 // dinv (optional): receives the inverses of R's 32 x 32 diagonal tiles (ceil(n/32) row-major
