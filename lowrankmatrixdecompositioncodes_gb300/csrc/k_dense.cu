@@ -133,11 +133,13 @@ __global__ void __launch_bounds__(256) sgemm_128x64_kernel(i64 M, i64 N, i64 K, 
             Bs[idx & 15][idx >> 4] = rb[e];
         }
     };
-    float acc[8][4];
+    // accumulators as row pairs (rows x, x+1 of column y) for packed FP32 FMAs (FFMA2):
+    // the A operand pairs come straight from the float4 loads, only B is broadcast
+    float2 acc2[4][4];
 #pragma unroll
-    for (int a = 0; a < 8; a++)
+    for (int a = 0; a < 4; a++)
 #pragma unroll
-        for (int b = 0; b < 4; b++) acc[a][b] = 0.f;
+        for (int b = 0; b < 4; b++) acc2[a][b] = make_float2(0.f, 0.f);
     load(0);
     for (i64 k0 = 0; k0 < K; k0 += 16) {
         store();
@@ -148,15 +150,25 @@ __global__ void __launch_bounds__(256) sgemm_128x64_kernel(i64 M, i64 N, i64 K, 
             const float4 a0 = *reinterpret_cast<const float4 *>(&As[kk][ty * 4]);
             const float4 a1 = *reinterpret_cast<const float4 *>(&As[kk][64 + ty * 4]);
             const float4 b0 = *reinterpret_cast<const float4 *>(&Bs[kk][tx * 4]);
-            const float av[8] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w};
-            const float bv[4] = {b0.x, b0.y, b0.z, b0.w};
+            const float2 ap[4] = {make_float2(a0.x, a0.y), make_float2(a0.z, a0.w), make_float2(a1.x, a1.y),
+                                  make_float2(a1.z, a1.w)};
+            const float2 bp[4] = {make_float2(b0.x, b0.x), make_float2(b0.y, b0.y), make_float2(b0.z, b0.z),
+                                  make_float2(b0.w, b0.w)};
 #pragma unroll
-            for (int x = 0; x < 8; x++)
+            for (int x = 0; x < 4; x++)
 #pragma unroll
-                for (int y = 0; y < 4; y++) acc[x][y] = fmaf(av[x], bv[y], acc[x][y]);
+                for (int y = 0; y < 4; y++) acc2[x][y] = __ffma2_rn(ap[x], bp[y], acc2[x][y]);
         }
         __syncthreads();
     }
+    float acc[8][4];
+#pragma unroll
+    for (int x = 0; x < 4; x++)
+#pragma unroll
+        for (int y = 0; y < 4; y++) {
+            acc[2 * x][y] = acc2[x][y].x;
+            acc[2 * x + 1][y] = acc2[x][y].y;
+        }
 #pragma unroll
     for (int x = 0; x < 8; x++) {
         const i64 gi = m0 + (x < 4 ? ty * 4 + x : 64 + ty * 4 + (x - 4));
