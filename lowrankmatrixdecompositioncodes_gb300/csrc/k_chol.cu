@@ -69,20 +69,50 @@ __device__ __forceinline__ void zero_acc(S (&acc)[4][8]) {
 }
 
 // acc(r, c) += sum_{k0 <= k < k1} P[k][r] Q[k][c]     (P^T Q, row-major tiles of pitch TP)
+// FP32: packed pairs of adjacent columns (FFMA2), P's value broadcast; same rounding as fma.
 template <typename S>
 __device__ __forceinline__ void tile_tn(const S *P, const S *Q, int k0, int k1, S (&acc)[4][8]) {
     const int r0 = lane_r0(), c0 = lane_c0();
-    for (int k = k0; k < k1; k++) {
-        S p[4], q[8], q2[4];
-        ld4<S>(P + k * TP + r0, p);
-        ld4<S>(Q + k * TP + c0, *reinterpret_cast<S(*)[4]>(q));
-        ld4<S>(Q + k * TP + c0 + 4, q2);
-#pragma unroll
-        for (int b = 0; b < 4; b++) q[4 + b] = q2[b];
+    if constexpr (sizeof(S) == 4) {
+        float2 acc2[4][4];
 #pragma unroll
         for (int a = 0; a < 4; a++)
 #pragma unroll
-            for (int b = 0; b < 8; b++) acc[a][b] = fma(p[a], q[b], acc[a][b]);
+            for (int b = 0; b < 4; b++) acc2[a][b] = make_float2(acc[a][2 * b], acc[a][2 * b + 1]);
+        for (int k = k0; k < k1; k++) {
+            const float4 p4 = *reinterpret_cast<const float4 *>(P + k * TP + r0);
+            const float4 qa = *reinterpret_cast<const float4 *>(Q + k * TP + c0);
+            const float4 qb = *reinterpret_cast<const float4 *>(Q + k * TP + c0 + 4);
+            const float pv[4] = {p4.x, p4.y, p4.z, p4.w};
+            const float2 qp[4] = {make_float2(qa.x, qa.y), make_float2(qa.z, qa.w), make_float2(qb.x, qb.y),
+                                  make_float2(qb.z, qb.w)};
+#pragma unroll
+            for (int a = 0; a < 4; a++) {
+                const float2 pp = make_float2(pv[a], pv[a]);
+#pragma unroll
+                for (int b = 0; b < 4; b++) acc2[a][b] = __ffma2_rn(pp, qp[b], acc2[a][b]);
+            }
+        }
+#pragma unroll
+        for (int a = 0; a < 4; a++)
+#pragma unroll
+            for (int b = 0; b < 4; b++) {
+                acc[a][2 * b] = acc2[a][b].x;
+                acc[a][2 * b + 1] = acc2[a][b].y;
+            }
+    } else {
+        for (int k = k0; k < k1; k++) {
+            S p[4], q[8], q2[4];
+            ld4<S>(P + k * TP + r0, p);
+            ld4<S>(Q + k * TP + c0, *reinterpret_cast<S(*)[4]>(q));
+            ld4<S>(Q + k * TP + c0 + 4, q2);
+#pragma unroll
+            for (int b = 0; b < 4; b++) q[4 + b] = q2[b];
+#pragma unroll
+            for (int a = 0; a < 4; a++)
+#pragma unroll
+                for (int b = 0; b < 8; b++) acc[a][b] = fma(p[a], q[b], acc[a][b]);
+        }
     }
 }
 
