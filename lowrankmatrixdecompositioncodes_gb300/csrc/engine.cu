@@ -497,7 +497,7 @@ static QBOut<T> qb_plain(DM<T> A, int kstep, int nstep, double TOL, int q, int s
 //           Q_j = orth(Y), B_j = Q_j^T A_res and A_res -= Q_j B_j by 3xTF32 (FP32-accurate;
 //           the long-K products accumulate in short chains, see tc_gemm_3xtf32),
 //           ||A_res||_F from the update's epilogue.
-//   judge   the loop stops when ||A_res||_F <= TOL (the reference's criterion, exact up to
+//   check   the loop stops when ||A_res||_F <= TOL (the reference's criterion, exact up to
 //           FP32 rounding); when the proposed width is used up first, it continues with
 //           blocks of the same width, i.e. the adaptive loop is the fallback.
 static constexpr int kProbe = 32, kFeat = 36;

@@ -7,6 +7,11 @@ GB and the operands larger than L2 (129 MB), so DRAM counters stay meaningful.
   gemm3x   D (16384 x 256) = A^T X, K = 16384   (B = Q^T A of the block loop, rsvdpack_dev_gemm_3xtf32)
   solve    one fixed-rank TF32 solve, 16384 x 8192, k = 256, p = 16, q = 2 (the Jacobi SVD,
            Cholesky and product kernels of the headline workload)
+  pivot    pivotedQR_mkl of a 520 x 10000 FP64 matrix through the C API (the row sketch of the
+           two-sided ID / CUR workload: the column-norm, pivot-select and reflector-apply
+           sweeps)
+  norm     the Frobenius-norm sweep of the plain FP32 blocked QB (rsvdpack_dev_qb, TOL mode,
+           one block) on a 32768 x 16384 FP32 matrix (2 GiB)
 
     python -m lowrankmatrixdecompositioncodes_gb300.prof_cases update
 """
@@ -100,7 +105,42 @@ def case_solve(torch, eng):
     _run(torch, call)
 
 
-CASES = {"update": case_update, "gemm3x": case_gemm3x, "solve": case_solve}
+def case_pivot(torch, eng):
+    import numpy as np
+    eng.set_precision("fp64")
+    A = np.random.default_rng(2).standard_normal((520, 10000))
+
+    def call():
+        eng.pivotedQR_mkl(A)
+        eng.check()
+    _run(torch, call, warm=1)
+
+
+def case_norm(torch, eng):
+    L = eng.lib
+    L.rsvdpack_dev_qb.restype = C.c_int
+    L.rsvdpack_dev_qb.argtypes = [C.c_void_p, C.c_int, C.c_longlong, C.c_int, C.c_int, C.c_int, C.c_int, C.c_double,
+                                  C.c_int, C.c_int, C.c_void_p, C.c_longlong, C.c_void_p, C.c_longlong, C.c_int,
+                                  C.POINTER(C.c_int)]
+    eng.set_precision("fp32")
+    eng.set_learned(False)
+    m, n, cap = 32768, 16384, 64
+    g = torch.Generator(device="cuda")
+    g.manual_seed(3)
+    At = torch.randn(n, m, device="cuda", generator=g)
+    Q = torch.empty(cap, m, device="cuda")
+    B = torch.empty(n, cap, device="cuda")
+    tol = 0.999 * float(torch.linalg.norm(At.double()))           # stops after the first block
+    fr = C.c_int(0)
+
+    def call():
+        if L.rsvdpack_dev_qb(At.data_ptr(), 1, m, m, n, 64, 0, tol, 1, 1, Q.data_ptr(), m, B.data_ptr(), cap, cap,
+                             C.byref(fr)):
+            raise RuntimeError(eng.last_error())
+    _run(torch, call)
+
+
+CASES = {"update": case_update, "gemm3x": case_gemm3x, "solve": case_solve, "pivot": case_pivot, "norm": case_norm}
 
 
 def main(argv=None):
