@@ -56,6 +56,17 @@ def parse():
     return ap.parse_args()
 
 
+def job_throughput(ms_local, world, torch, device):
+    """Whole-job solves/s from this rank's ms per solve: the slowest rank's time (MAX over
+    ranks; every rank runs the same per-rank work, so the job rate is world / slowest)."""
+    ms = float(ms_local)
+    if world > 1:
+        t = torch.tensor([ms], device=device, dtype=torch.float64)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    return ms, world * 1000.0 / ms
+
+
 def dist_env():
     return (int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)),
             int(os.environ.get("LOCAL_RANK", 0)))
@@ -453,12 +464,7 @@ def run_ours(args):
     if args.profile_leg == "solve":
         torch.cuda.cudart().cudaProfilerStop()
     clocks = sampler.stop()
-    ms = ev0.elapsed_time(ev1) / args.steps
-    if world > 1:
-        t = torch.tensor([ms], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
-    value = world * 1000.0 / ms
+    ms, value = job_throughput(ev0.elapsed_time(ev1) / args.steps, world, torch, dev)
     # device time per solve by phase (CUDA events inside the engine, same timed solves)
     phases = {kk: v / args.steps for kk, v in phase_sum.items()}
     phases["other"] = max(0.0, ms - sum(phases.values()))
