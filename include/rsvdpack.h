@@ -34,29 +34,43 @@ extern "C" {
 
 /* ============================== Part 1: reference API ============================== */
 
-/* matrix_vector_functions_intel_mkl.h:18-27 (LP64 int dimensions, column-major) */
+/* Index type of Part 1.  The default library, librsvdpack.so, has the LP64 int dimensions of
+ * multi_core_mkl_code; librsvdpack64.so, built from the same sources with RSVDPACK_INDEX64, has
+ * the int64_t dimensions of multi_core_mkl_code_64bit (matrix_vector_functions_intel_mkl.h:20-28
+ * and every dimension, rank and step argument of its rank_revealing_algorithms_intel_mkl.h), for
+ * matrices of more than 2^31 entries.  Define RSVDPACK_INDEX64 before including this header to
+ * compile against the 64-bit library.  Part 2 keeps int in both libraries. */
+#ifdef RSVDPACK_INDEX64
+typedef int64_t rsvd_int;
+#else
+typedef int rsvd_int;
+#endif
+
+/* matrix_vector_functions_intel_mkl.h:18-27 (rsvd_int dimensions, column-major) */
 typedef struct {
-    int nrows, ncols;
+    rsvd_int nrows, ncols;
     double *d;
 } mat;
 
 typedef struct {
-    int nrows;
+    rsvd_int nrows;
     double *d;
 } vec;
 
 /* ---- storage and element access: matrix_vector_functions_intel_mkl.h:31-58 ---- */
-mat *matrix_new(int nrows, int ncols);
-vec *vector_new(int nrows);
+mat *matrix_new(rsvd_int nrows, rsvd_int ncols);
+vec *vector_new(rsvd_int nrows);
 void matrix_delete(mat *M);
 void vector_delete(vec *v);
-void matrix_set_element(mat *M, int row_num, int col_num, double val);
-double matrix_get_element(mat *M, int row_num, int col_num);
-void vector_set_element(vec *v, int row_num, double val);
-double vector_get_element(vec *v, int row_num);
+void matrix_set_element(mat *M, rsvd_int row_num, rsvd_int col_num, double val);
+double matrix_get_element(mat *M, rsvd_int row_num, rsvd_int col_num);
+void vector_set_element(vec *v, rsvd_int row_num, double val);
+double vector_get_element(vec *v, rsvd_int row_num);
 
-/* ---- binary matrix files: matrix_vector_functions_intel_mkl.h:60-64 (format: int32 m,
- *      int32 n, then m*n doubles in row-major order; matrix_vector_functions_intel_mkl.c:77-133) ---- */
+/* ---- binary matrix files: matrix_vector_functions_intel_mkl.h:60-64 (format: m and n as
+ *      rsvd_int -- int32 in librsvdpack.so, int64 in librsvdpack64.so as in
+ *      multi_core_mkl_code_64bit/matrix_vector_functions_intel_mkl.c:86-87 -- then m*n doubles in
+ *      row-major order; matrix_vector_functions_intel_mkl.c:77-133) ---- */
 mat *matrix_load_from_binary_file(char *fname);
 void matrix_write_to_binary_file(mat *M, char *fname);
 
@@ -77,61 +91,61 @@ double get_seconds_frac(struct timeval start_timeval, struct timeval end_timeval
 /* :5  fixed-rank randomized SVD.  q means q-1 rounds of (M M^T); vnum 1 (or >2): QR of
  *     B^T route, singular values descending; vnum 2: eig(B B^T) route, ascending.
  *     U m x k, S k x k dense diagonal, V n x k.  frank is not written (as in the reference). */
-void low_rank_svd_rand_decomp_fixed_rank(mat *M, int k, int p, int vnum, int q, int s,
-                                         int *frank, mat **U, mat **S, mat **V);
+void low_rank_svd_rand_decomp_fixed_rank(mat *M, rsvd_int k, rsvd_int p, rsvd_int vnum, rsvd_int q, rsvd_int s,
+                                         rsvd_int *frank, mat **U, mat **S, mat **V);
 /* :7  blocked randomized SVD (rank k, or absolute Frobenius tolerance TOL when k <= 0) */
-void low_rank_svd_blockrand_decomp_fixed_rank_or_prec(mat *M, int k, int p, double TOL,
-                                                      int vnum, int kstep, int q, int s,
-                                                      int *frank, mat **U, mat **S, mat **V);
+void low_rank_svd_blockrand_decomp_fixed_rank_or_prec(mat *M, rsvd_int k, rsvd_int p, double TOL,
+                                                      rsvd_int vnum, rsvd_int kstep, rsvd_int q, rsvd_int s,
+                                                      rsvd_int *frank, mat **U, mat **S, mat **V);
 /* :67 blocked randomized QB (nstep <= 0 selects the TOL mode) */
-void randQB_pb_new(mat *M, int kstep, int nstep, double TOL, int q, int s, int *frank,
+void randQB_pb_new(mat *M, rsvd_int kstep, rsvd_int nstep, double TOL, rsvd_int q, rsvd_int s, rsvd_int *frank,
                    mat **Q, mat **B);
 /* :43 full column-pivoted QR, M(:,I) = Q R (LAPACK dgeqp3 pivoting, all columns free) */
 void pivotedQR_mkl(mat *M, mat **Q, mat **R, vec **I);
 /* :52 partial pivoted Householder QR of rank k, or of precision TOL when k <= 0 */
-void pivoted_QR_of_specified_rank_or_prec(mat *M, int k, double TOL, int *frank,
+void pivoted_QR_of_specified_rank_or_prec(mat *M, rsvd_int k, double TOL, rsvd_int *frank,
                                           mat **Qk, mat **Rk, vec **I);
 /* :73 column ID, T = Rk1^-1 Rk2 */
-void id_decomp_fixed_rank_or_prec(mat *M, int k, double TOL, int *frank, vec **I, mat **T);
+void id_decomp_fixed_rank_or_prec(mat *M, rsvd_int k, double TOL, rsvd_int *frank, vec **I, mat **T);
 /* :76 randomized column ID (row sketch (k+p) x n, q power rounds) */
-void id_rand_decomp_fixed_rank(mat *M, int k, int p, int q, int s, vec **I, mat **T);
+void id_rand_decomp_fixed_rank(mat *M, rsvd_int k, rsvd_int p, rsvd_int q, rsvd_int s, vec **I, mat **T);
 /* decompositions from a given QB (Q m x l, B l x n; the QB split of the oneAPI variant,
- * oneapi_code/rank_revealing_algorithms_one_api.h:6,10, with this header's int dimensions):
+ * oneapi_code/rank_revealing_algorithms_one_api.h:6,10, with this header's rsvd_int dimensions):
  * low_rank_svd_rand_decomp_fromQB: U (m x l), S (l x l, descending), V (n x l) from the SVD of
  * B B^T, V = B^T Uhat S^-1; id_rand_decomp_fromQB: column ID of B with k = Q->ncols,
  * I (0-based pivots of B, as doubles) and T = R11^-1 R12 (k x (n - k)).  FP64. */
 void low_rank_svd_rand_decomp_fromQB(mat *Q, mat *B, mat **U, mat **S, mat **V);
 void id_rand_decomp_fromQB(mat *Q, mat *B, vec **I, mat **T);
 /* :79 blocked randomized column ID */
-void id_blockrand_decomp_fixed_rank_or_prec(mat *M, int k, int p, double TOL, int kstep,
-                                            int q, int s, int *frank, vec **I, mat **T);
+void id_blockrand_decomp_fixed_rank_or_prec(mat *M, rsvd_int k, rsvd_int p, double TOL, rsvd_int kstep,
+                                            rsvd_int q, rsvd_int s, rsvd_int *frank, vec **I, mat **T);
 /* :84 two-sided ID */
-void id_two_sided_decomp_fixed_rank_or_prec(mat *M, int k, double TOL, int *frank,
+void id_two_sided_decomp_fixed_rank_or_prec(mat *M, rsvd_int k, double TOL, rsvd_int *frank,
                                             vec **Icol, vec **Irow, mat **T, mat **S);
 /* :87 randomized two-sided ID.  The reference header names the parameters (k,l,p,s);
  *     the definition (rank_revealing_algorithms_intel_mkl.c:2060) uses (k,p,q,s). */
-void id_two_sided_rand_decomp_fixed_rank(mat *M, int k, int p, int q, int s,
+void id_two_sided_rand_decomp_fixed_rank(mat *M, rsvd_int k, rsvd_int p, rsvd_int q, rsvd_int s,
                                          vec **Icol, vec **Irow, mat **T, mat **S);
 /* :90 blocked randomized two-sided ID */
-void id_two_sided_blockrand_decomp_fixed_rank_or_prec(mat *M, int k, int p, double TOL,
-                                                      int kstep, int q, int s, int *frank,
+void id_two_sided_blockrand_decomp_fixed_rank_or_prec(mat *M, rsvd_int k, rsvd_int p, double TOL,
+                                                      rsvd_int kstep, rsvd_int q, rsvd_int s, rsvd_int *frank,
                                                       vec **Icol, vec **Irow, mat **T, mat **S);
 /* :95 CUR */
-void cur_decomp_fixed_rank_or_prec(mat *M, int k, double TOL, int *frank,
+void cur_decomp_fixed_rank_or_prec(mat *M, rsvd_int k, double TOL, rsvd_int *frank,
                                    mat **C, mat **U, mat **R);
 /* :98 randomized CUR */
-void cur_rand_decomp_fixed_rank(mat *M, int k, int p, int q, int s, mat **C, mat **U, mat **R);
+void cur_rand_decomp_fixed_rank(mat *M, rsvd_int k, rsvd_int p, rsvd_int q, rsvd_int s, mat **C, mat **U, mat **R);
 /* :101 blocked randomized CUR */
-void cur_blockrand_decomp_fixed_rank_or_prec(mat *M, int k, int p, double TOL, int kstep,
-                                             int q, int s, int *frank,
+void cur_blockrand_decomp_fixed_rank_or_prec(mat *M, rsvd_int k, rsvd_int p, double TOL, rsvd_int kstep,
+                                             rsvd_int q, rsvd_int s, rsvd_int *frank,
                                              mat **C, mat **U, mat **R);
 /* :105-120 approximation reports (print norms and percent error, as the reference does).
  * use_pivoted_QR_decomp_for_approximation frees Qk and Rk, as the reference does. */
 void use_low_rank_svd_for_approximation(mat *M, mat *U, mat *S, mat *V);
 void use_pivoted_QR_decomp_for_approximation(mat *M, mat *Qk, mat *Rk, vec *I);
 void use_QB_decomp_for_approximation(mat *M, mat *Q, mat *B);
-void use_id_decomp_for_approximation(mat *M, mat *T, vec *I, int k);
-void use_id_two_sided_decomp_for_approximation(mat *M, mat *T, mat *S, vec *Icol, vec *Irow, int k);
+void use_id_decomp_for_approximation(mat *M, mat *T, vec *I, rsvd_int k);
+void use_id_two_sided_decomp_for_approximation(mat *M, mat *T, mat *S, vec *Icol, vec *Irow, rsvd_int k);
 void use_cur_decomp_for_approximation(mat *M, mat *C, mat *U, mat *R);
 
 /* ============================== Part 2: extensions ============================== */

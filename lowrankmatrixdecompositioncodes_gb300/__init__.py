@@ -5,7 +5,8 @@ sm_103a (see ``include/rsvdpack.h``).  This package only locates, builds and bin
 ``load_engine()`` returns a :class:`capi.RsvdLibrary` over the engine with the
 reference's API names.  There is no CPU fallback: if the library is missing,
 ``load_engine()`` raises; if no GB300 is visible, every decomposition call reports
-``RSVD_ERR_NO_DEVICE`` through ``rsvdpack_last_error()``.
+``RSVD_ERR_NO_DEVICE`` through ``rsvdpack_last_error()``.  ``load_engine64()`` binds
+``librsvdpack64.so``, the same engine behind the reference API with int64_t dimensions.
 """
 from __future__ import annotations
 
@@ -16,6 +17,7 @@ from .capi import RsvdLibrary
 
 PKG_DIR = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(PKG_DIR, "librsvdpack.so")
+LIB64_PATH = os.path.join(PKG_DIR, "librsvdpack64.so")
 
 PREC = {"fp64": 0, "fp32": 1, "tf32": 2, "bf16": 3}
 
@@ -35,8 +37,8 @@ class RsvdTiming(C.Structure):
 class EngineLibrary(RsvdLibrary):
     """RsvdLibrary plus the engine's extension entry points (include/rsvdpack.h Part 2)."""
 
-    def __init__(self, path: str = LIB_PATH):
-        super().__init__(path)
+    def __init__(self, path: str = LIB_PATH, index64: bool = False):
+        super().__init__(path, index64=index64)
         L = self.lib
         L.rsvdpack_last_error.restype = C.c_int
         L.rsvdpack_last_error_string.restype = C.c_char_p
@@ -93,6 +95,7 @@ class EngineLibrary(RsvdLibrary):
 
 
 _ENGINE = None
+_ENGINE64 = None
 
 
 def build(verbose: bool = False) -> str:
@@ -108,6 +111,16 @@ def load_engine() -> EngineLibrary:
             build()
         _ENGINE = EngineLibrary(LIB_PATH)
     return _ENGINE
+
+
+def load_engine64() -> EngineLibrary:
+    """Load librsvdpack64.so, the int64_t-dimension form of the reference API."""
+    global _ENGINE64
+    if _ENGINE64 is None:
+        if not os.path.exists(LIB64_PATH):
+            build()
+        _ENGINE64 = EngineLibrary(LIB64_PATH, index64=True)
+    return _ENGINE64
 
 
 def engine_available() -> bool:

@@ -3,6 +3,9 @@
 Each translation unit in csrc/ is compiled in parallel into _build/, then linked into
 lowrankmatrixdecompositioncodes_gb300/librsvdpack.so (static CUDA runtime, no libcuda
 link-time dependency: the driver API is reached through cudaGetDriverEntryPoint).
+api.cu, the reference API layer, is compiled a second time with RSVDPACK_INDEX64 and linked
+with the same engine objects into librsvdpack64.so: the reference API with int64_t
+dimensions (multi_core_mkl_code_64bit), over the same kernels.
 Incremental: a unit is rebuilt when it or any header in csrc/ or include/ is newer
 than its object file.
 """
@@ -20,6 +23,8 @@ ROOT = os.path.dirname(PKG)
 CSRC = os.path.join(PKG, "csrc")
 BUILD = os.path.join(ROOT, "_build")
 LIB = os.path.join(PKG, "librsvdpack.so")
+LIB64 = os.path.join(PKG, "librsvdpack64.so")
+INDEX64_UNIT = "api.cu"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -51,15 +56,22 @@ def build(verbose: bool = False, jobs: int | None = None) -> str:
     hdr_t = _newest_header()
     todo = []
     objs = []
+    objs64 = []
     for s in srcs:
-        o = os.path.join(BUILD, os.path.basename(s) + ".o")
-        objs.append(o)
-        if not os.path.exists(o) or os.path.getmtime(o) < max(os.path.getmtime(s), hdr_t):
-            todo.append((s, o))
+        units = [(os.path.join(BUILD, os.path.basename(s) + ".o"), ())]
+        if os.path.basename(s) == INDEX64_UNIT:
+            units.append((os.path.join(BUILD, os.path.basename(s) + ".i64.o"), ("-DRSVDPACK_INDEX64",)))
+        for o, extra in units:
+            if not extra:
+                objs.append(o)
+            if extra or os.path.basename(s) != INDEX64_UNIT:
+                objs64.append(o)
+            if not os.path.exists(o) or os.path.getmtime(o) < max(os.path.getmtime(s), hdr_t):
+                todo.append((s, o, extra))
 
-    def compile_one(so):
-        s, o = so
-        cmd = [nvcc, *_flags(), "-c", s, "-o", o]
+    def compile_one(soe):
+        s, o, extra = soe
+        cmd = [nvcc, *_flags(extra), "-c", s, "-o", o]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"nvcc failed for {os.path.basename(s)}:\n{r.stderr}")
@@ -72,13 +84,14 @@ def build(verbose: bool = False, jobs: int | None = None) -> str:
             for s in ex.map(compile_one, todo):
                 if verbose:
                     print("compiled", os.path.basename(s))
-    if todo or not os.path.exists(LIB):
-        tmp = LIB + ".tmp"
-        cmd = [nvcc, *ARCH, "-shared", "-o", tmp, *objs, "-Xlinker", "-Bsymbolic", "-Xlinker", "--no-undefined"]
-        r = subprocess.run(cmd, capture_output=True, text=True)
-        if r.returncode != 0:
-            raise RuntimeError(f"link failed:\n{r.stderr}")
-        os.replace(tmp, LIB)
+    for lib, lobjs in ((LIB, objs), (LIB64, objs64)):
+        if todo or not os.path.exists(lib):
+            tmp = lib + ".tmp"
+            cmd = [nvcc, *ARCH, "-shared", "-o", tmp, *lobjs, "-Xlinker", "-Bsymbolic", "-Xlinker", "--no-undefined"]
+            r = subprocess.run(cmd, capture_output=True, text=True)
+            if r.returncode != 0:
+                raise RuntimeError(f"link of {os.path.basename(lib)} failed:\n{r.stderr}")
+            os.replace(tmp, lib)
     return LIB
 
 

@@ -12,6 +12,10 @@ singular-value order as the reference gives it).
 Ownership follows the reference: inputs are borrowed, outputs are allocated by the
 callee with ``matrix_new``/``vector_new`` and released here with
 ``matrix_delete``/``vector_delete`` after copying into numpy.
+
+``RsvdLibrary(path, index64=True)`` binds the int64_t-dimension form of the same API
+(multi_core_mkl_code_64bit/matrix_vector_functions_intel_mkl.h:20-28 and
+rank_revealing_algorithms_intel_mkl.h), which librsvdpack64.so exports.
 """
 from __future__ import annotations
 
@@ -29,38 +33,49 @@ class Vec(C.Structure):
     _fields_ = [("nrows", C.c_int), ("d", C.POINTER(C.c_double))]
 
 
+class Mat64(C.Structure):
+    _fields_ = [("nrows", C.c_int64), ("ncols", C.c_int64), ("d", C.POINTER(C.c_double))]
+
+
+class Vec64(C.Structure):
+    _fields_ = [("nrows", C.c_int64), ("d", C.POINTER(C.c_double))]
+
+
 PMat = C.POINTER(Mat)
 PVec = C.POINTER(Vec)
 OMEGA_FN = C.CFUNCTYPE(None, C.c_void_p, C.c_int, C.c_int, C.c_int, C.POINTER(C.c_double))
 
-_I, _D = C.c_int, C.c_double
-_PI = C.POINTER(C.c_int)
-_PPM = C.POINTER(PMat)
-_PPV = C.POINTER(PVec)
+_D = C.c_double
 
-# name -> argtypes for the reference API (rank_revealing_algorithms_intel_mkl.h:3-110)
-_ALGOS = {
-    "low_rank_svd_rand_decomp_fixed_rank": [PMat, _I, _I, _I, _I, _I, _PI, _PPM, _PPM, _PPM],
-    "low_rank_svd_blockrand_decomp_fixed_rank_or_prec":
-        [PMat, _I, _I, _D, _I, _I, _I, _I, _PI, _PPM, _PPM, _PPM],
-    "randQB_pb_new": [PMat, _I, _I, _D, _I, _I, _PI, _PPM, _PPM],
-    "pivotedQR_mkl": [PMat, _PPM, _PPM, _PPV],
-    "pivoted_QR_of_specified_rank_or_prec": [PMat, _I, _D, _PI, _PPM, _PPM, _PPV],
-    "id_decomp_fixed_rank_or_prec": [PMat, _I, _D, _PI, _PPV, _PPM],
-    "id_rand_decomp_fixed_rank": [PMat, _I, _I, _I, _I, _PPV, _PPM],
-    "id_blockrand_decomp_fixed_rank_or_prec": [PMat, _I, _I, _D, _I, _I, _I, _PI, _PPV, _PPM],
-    "id_two_sided_decomp_fixed_rank_or_prec": [PMat, _I, _D, _PI, _PPV, _PPV, _PPM, _PPM],
-    "id_two_sided_rand_decomp_fixed_rank": [PMat, _I, _I, _I, _I, _PPV, _PPV, _PPM, _PPM],
-    "id_two_sided_blockrand_decomp_fixed_rank_or_prec":
-        [PMat, _I, _I, _D, _I, _I, _I, _PI, _PPV, _PPV, _PPM, _PPM],
-    "cur_decomp_fixed_rank_or_prec": [PMat, _I, _D, _PI, _PPM, _PPM, _PPM],
-    "cur_rand_decomp_fixed_rank": [PMat, _I, _I, _I, _I, _PPM, _PPM, _PPM],
-    "cur_blockrand_decomp_fixed_rank_or_prec":
-        [PMat, _I, _I, _D, _I, _I, _I, _PI, _PPM, _PPM, _PPM],
-    # the QB split of the oneAPI variant (oneapi_code/rank_revealing_algorithms_one_api.h:6,10)
-    "low_rank_svd_rand_decomp_fromQB": [PMat, PMat, _PPM, _PPM, _PPM],
-    "id_rand_decomp_fromQB": [PMat, PMat, _PPV, _PPM],
-}
+
+def _algos(_I, PMat, PVec):
+    """name -> argtypes for the reference API (rank_revealing_algorithms_intel_mkl.h:3-110),
+    with index type _I (c_int, or c_int64 for the 64-bit form)."""
+    _PI = C.POINTER(_I)
+    _PPM = C.POINTER(PMat)
+    _PPV = C.POINTER(PVec)
+    return {
+        "low_rank_svd_rand_decomp_fixed_rank": [PMat, _I, _I, _I, _I, _I, _PI, _PPM, _PPM, _PPM],
+        "low_rank_svd_blockrand_decomp_fixed_rank_or_prec":
+            [PMat, _I, _I, _D, _I, _I, _I, _I, _PI, _PPM, _PPM, _PPM],
+        "randQB_pb_new": [PMat, _I, _I, _D, _I, _I, _PI, _PPM, _PPM],
+        "pivotedQR_mkl": [PMat, _PPM, _PPM, _PPV],
+        "pivoted_QR_of_specified_rank_or_prec": [PMat, _I, _D, _PI, _PPM, _PPM, _PPV],
+        "id_decomp_fixed_rank_or_prec": [PMat, _I, _D, _PI, _PPV, _PPM],
+        "id_rand_decomp_fixed_rank": [PMat, _I, _I, _I, _I, _PPV, _PPM],
+        "id_blockrand_decomp_fixed_rank_or_prec": [PMat, _I, _I, _D, _I, _I, _I, _PI, _PPV, _PPM],
+        "id_two_sided_decomp_fixed_rank_or_prec": [PMat, _I, _D, _PI, _PPV, _PPV, _PPM, _PPM],
+        "id_two_sided_rand_decomp_fixed_rank": [PMat, _I, _I, _I, _I, _PPV, _PPV, _PPM, _PPM],
+        "id_two_sided_blockrand_decomp_fixed_rank_or_prec":
+            [PMat, _I, _I, _D, _I, _I, _I, _PI, _PPV, _PPV, _PPM, _PPM],
+        "cur_decomp_fixed_rank_or_prec": [PMat, _I, _D, _PI, _PPM, _PPM, _PPM],
+        "cur_rand_decomp_fixed_rank": [PMat, _I, _I, _I, _I, _PPM, _PPM, _PPM],
+        "cur_blockrand_decomp_fixed_rank_or_prec":
+            [PMat, _I, _I, _D, _I, _I, _I, _PI, _PPM, _PPM, _PPM],
+        # the QB split of the oneAPI variant (oneapi_code/rank_revealing_algorithms_one_api.h:6,10)
+        "low_rank_svd_rand_decomp_fromQB": [PMat, PMat, _PPM, _PPM, _PPM],
+        "id_rand_decomp_fromQB": [PMat, PMat, _PPV, _PPM],
+    }
 
 
 class SeededOmega:
@@ -95,11 +110,22 @@ class ListOmega:
         return a
 
 
-class RsvdLibrary:
-    """Binds one shared library exporting the reference C API."""
+_ALGOS = _algos(C.c_int, PMat, PVec)
 
-    def __init__(self, path: str):
+
+class RsvdLibrary:
+    """Binds one shared library exporting the reference C API: LP64 int dimensions, or
+    int64_t dimensions with ``index64=True``."""
+
+    def __init__(self, path: str, index64: bool = False):
         self.path = str(path)
+        self.index64 = bool(index64)
+        self.Int = C.c_int64 if self.index64 else C.c_int
+        self.Mat = Mat64 if self.index64 else Mat
+        self.Vec = Vec64 if self.index64 else Vec
+        self.PMat = C.POINTER(self.Mat)
+        self.PVec = C.POINTER(self.Vec)
+        PMat, PVec, _I = self.PMat, self.PVec, self.Int
         self.lib = C.CDLL(self.path)
         L = self.lib
         L.matrix_new.restype = PMat
@@ -114,7 +140,7 @@ class RsvdLibrary:
         L.get_matrix_frobenius_norm.argtypes = [PMat]
         L.get_percent_error_between_two_mats.restype = _D
         L.get_percent_error_between_two_mats.argtypes = [PMat, PMat]
-        for name, args in _ALGOS.items():
+        for name, args in _algos(_I, PMat, PVec).items():
             f = getattr(L, name, None)
             if f is not None:
                 f.argtypes = args
@@ -131,7 +157,7 @@ class RsvdLibrary:
     def has(self, name: str) -> bool:
         return hasattr(self.lib, name)
 
-    def to_mat(self, A) -> PMat:
+    def to_mat(self, A):
         A = np.asarray(A, dtype=np.float64)
         if A.ndim != 2:
             raise ValueError("matrix must be 2-D")
@@ -142,7 +168,7 @@ class RsvdLibrary:
             buf[:] = A.ravel(order="F")
         return pM
 
-    def from_mat(self, pM: PMat, free: bool = True) -> np.ndarray:
+    def from_mat(self, pM, free: bool = True) -> np.ndarray:
         m, n = pM.contents.nrows, pM.contents.ncols
         if m * n:
             out = np.ctypeslib.as_array(pM.contents.d, shape=(m * n,)).copy()
@@ -153,7 +179,7 @@ class RsvdLibrary:
             self.lib.matrix_delete(pM)
         return out
 
-    def from_vec(self, pv: PVec, free: bool = True) -> np.ndarray:
+    def from_vec(self, pv, free: bool = True) -> np.ndarray:
         n = pv.contents.nrows
         out = np.ctypeslib.as_array(pv.contents.d, shape=(n,)).copy() if n else np.zeros(0)
         if free:
@@ -181,9 +207,9 @@ class RsvdLibrary:
         return int(self.lib.rsvdpack_omega_calls())
 
     def _call(self, name, M, *scalars, nm=0, nv=0, frank=False):
-        pm = [PMat() for _ in range(nm)]
-        pv = [PVec() for _ in range(nv)]
-        fr = C.c_int(-1)
+        pm = [self.PMat() for _ in range(nm)]
+        pv = [self.PVec() for _ in range(nv)]
+        fr = self.Int(-1)
         args = [M, *scalars]
         if frank:
             args.append(C.byref(fr))
@@ -192,7 +218,7 @@ class RsvdLibrary:
     # ------------------------------------------------------------ algorithms
     def low_rank_svd_rand_decomp_fixed_rank(self, A, k, p, vnum, q, s):
         M = self.to_mat(A)
-        U, S, V, fr = PMat(), PMat(), PMat(), C.c_int(-1)
+        U, S, V, fr = self.PMat(), self.PMat(), self.PMat(), self.Int(-1)
         try:
             self.lib.low_rank_svd_rand_decomp_fixed_rank(
                 M, k, p, vnum, q, s, C.byref(fr), C.byref(U), C.byref(S), C.byref(V))
@@ -202,7 +228,7 @@ class RsvdLibrary:
 
     def low_rank_svd_blockrand_decomp_fixed_rank_or_prec(self, A, k, p, TOL, vnum, kstep, q, s):
         M = self.to_mat(A)
-        U, S, V, fr = PMat(), PMat(), PMat(), C.c_int(-1)
+        U, S, V, fr = self.PMat(), self.PMat(), self.PMat(), self.Int(-1)
         try:
             self.lib.low_rank_svd_blockrand_decomp_fixed_rank_or_prec(
                 M, k, p, float(TOL), vnum, kstep, q, s, C.byref(fr),
@@ -213,7 +239,7 @@ class RsvdLibrary:
 
     def randQB_pb_new(self, A, kstep, nstep, TOL, q, s):
         M = self.to_mat(A)
-        Q, B, fr = PMat(), PMat(), C.c_int(-1)
+        Q, B, fr = self.PMat(), self.PMat(), self.Int(-1)
         try:
             self.lib.randQB_pb_new(M, kstep, nstep, float(TOL), q, s, C.byref(fr),
                                    C.byref(Q), C.byref(B))
@@ -223,7 +249,7 @@ class RsvdLibrary:
 
     def low_rank_svd_rand_decomp_fromQB(self, Qm, Bm):
         Q, B = self.to_mat(Qm), self.to_mat(Bm)
-        U, S, V = PMat(), PMat(), PMat()
+        U, S, V = self.PMat(), self.PMat(), self.PMat()
         try:
             self.lib.low_rank_svd_rand_decomp_fromQB(Q, B, C.byref(U), C.byref(S), C.byref(V))
         finally:
@@ -233,7 +259,7 @@ class RsvdLibrary:
 
     def id_rand_decomp_fromQB(self, Qm, Bm):
         Q, B = self.to_mat(Qm), self.to_mat(Bm)
-        I, T = PVec(), PMat()
+        I, T = self.PVec(), self.PMat()
         try:
             self.lib.id_rand_decomp_fromQB(Q, B, C.byref(I), C.byref(T))
         finally:
@@ -243,7 +269,7 @@ class RsvdLibrary:
 
     def pivotedQR_mkl(self, A):
         M = self.to_mat(A)
-        Q, R, I = PMat(), PMat(), PVec()
+        Q, R, I = self.PMat(), self.PMat(), self.PVec()
         try:
             self.lib.pivotedQR_mkl(M, C.byref(Q), C.byref(R), C.byref(I))
         finally:
@@ -252,7 +278,7 @@ class RsvdLibrary:
 
     def pivoted_QR_of_specified_rank_or_prec(self, A, k, TOL):
         M = self.to_mat(A)
-        Q, R, I, fr = PMat(), PMat(), PVec(), C.c_int(-1)
+        Q, R, I, fr = self.PMat(), self.PMat(), self.PVec(), self.Int(-1)
         try:
             self.lib.pivoted_QR_of_specified_rank_or_prec(
                 M, k, float(TOL), C.byref(fr), C.byref(Q), C.byref(R), C.byref(I))
@@ -262,7 +288,7 @@ class RsvdLibrary:
 
     def id_decomp_fixed_rank_or_prec(self, A, k, TOL):
         M = self.to_mat(A)
-        I, T, fr = PVec(), PMat(), C.c_int(-1)
+        I, T, fr = self.PVec(), self.PMat(), self.Int(-1)
         try:
             self.lib.id_decomp_fixed_rank_or_prec(M, k, float(TOL), C.byref(fr),
                                                   C.byref(I), C.byref(T))
@@ -272,7 +298,7 @@ class RsvdLibrary:
 
     def id_rand_decomp_fixed_rank(self, A, k, p, q, s):
         M = self.to_mat(A)
-        I, T = PVec(), PMat()
+        I, T = self.PVec(), self.PMat()
         try:
             self.lib.id_rand_decomp_fixed_rank(M, k, p, q, s, C.byref(I), C.byref(T))
         finally:
@@ -281,7 +307,7 @@ class RsvdLibrary:
 
     def id_blockrand_decomp_fixed_rank_or_prec(self, A, k, p, TOL, kstep, q, s):
         M = self.to_mat(A)
-        I, T, fr = PVec(), PMat(), C.c_int(-1)
+        I, T, fr = self.PVec(), self.PMat(), self.Int(-1)
         try:
             self.lib.id_blockrand_decomp_fixed_rank_or_prec(
                 M, k, p, float(TOL), kstep, q, s, C.byref(fr), C.byref(I), C.byref(T))
@@ -291,7 +317,7 @@ class RsvdLibrary:
 
     def id_two_sided_decomp_fixed_rank_or_prec(self, A, k, TOL):
         M = self.to_mat(A)
-        Ic, Ir, T, S, fr = PVec(), PVec(), PMat(), PMat(), C.c_int(-1)
+        Ic, Ir, T, S, fr = self.PVec(), self.PVec(), self.PMat(), self.PMat(), self.Int(-1)
         try:
             self.lib.id_two_sided_decomp_fixed_rank_or_prec(
                 M, k, float(TOL), C.byref(fr), C.byref(Ic), C.byref(Ir), C.byref(T), C.byref(S))
@@ -302,7 +328,7 @@ class RsvdLibrary:
 
     def id_two_sided_rand_decomp_fixed_rank(self, A, k, p, q, s):
         M = self.to_mat(A)
-        Ic, Ir, T, S = PVec(), PVec(), PMat(), PMat()
+        Ic, Ir, T, S = self.PVec(), self.PVec(), self.PMat(), self.PMat()
         try:
             self.lib.id_two_sided_rand_decomp_fixed_rank(
                 M, k, p, q, s, C.byref(Ic), C.byref(Ir), C.byref(T), C.byref(S))
@@ -312,7 +338,7 @@ class RsvdLibrary:
 
     def id_two_sided_blockrand_decomp_fixed_rank_or_prec(self, A, k, p, TOL, kstep, q, s):
         M = self.to_mat(A)
-        Ic, Ir, T, S, fr = PVec(), PVec(), PMat(), PMat(), C.c_int(-1)
+        Ic, Ir, T, S, fr = self.PVec(), self.PVec(), self.PMat(), self.PMat(), self.Int(-1)
         try:
             self.lib.id_two_sided_blockrand_decomp_fixed_rank_or_prec(
                 M, k, p, float(TOL), kstep, q, s, C.byref(fr), C.byref(Ic), C.byref(Ir),
@@ -324,7 +350,7 @@ class RsvdLibrary:
 
     def cur_decomp_fixed_rank_or_prec(self, A, k, TOL):
         M = self.to_mat(A)
-        Cm, U, R, fr = PMat(), PMat(), PMat(), C.c_int(-1)
+        Cm, U, R, fr = self.PMat(), self.PMat(), self.PMat(), self.Int(-1)
         try:
             self.lib.cur_decomp_fixed_rank_or_prec(M, k, float(TOL), C.byref(fr),
                                                    C.byref(Cm), C.byref(U), C.byref(R))
@@ -334,7 +360,7 @@ class RsvdLibrary:
 
     def cur_rand_decomp_fixed_rank(self, A, k, p, q, s):
         M = self.to_mat(A)
-        Cm, U, R = PMat(), PMat(), PMat()
+        Cm, U, R = self.PMat(), self.PMat(), self.PMat()
         try:
             self.lib.cur_rand_decomp_fixed_rank(M, k, p, q, s, C.byref(Cm), C.byref(U),
                                                 C.byref(R))
@@ -344,7 +370,7 @@ class RsvdLibrary:
 
     def cur_blockrand_decomp_fixed_rank_or_prec(self, A, k, p, TOL, kstep, q, s):
         M = self.to_mat(A)
-        Cm, U, R, fr = PMat(), PMat(), PMat(), C.c_int(-1)
+        Cm, U, R, fr = self.PMat(), self.PMat(), self.PMat(), self.Int(-1)
         try:
             self.lib.cur_blockrand_decomp_fixed_rank_or_prec(
                 M, k, p, float(TOL), kstep, q, s, C.byref(fr), C.byref(Cm), C.byref(U),

@@ -8,6 +8,7 @@
 #include "k_common.cuh"
 
 #include <chrono>
+#include <climits>
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
@@ -43,9 +44,19 @@ void need(bool ok, const char *what) {
     if (!ok) fail(RSVD_ERR_ARGUMENT, what);
 }
 
+// The engine's dimensions are int (offsets and element counts are 64-bit throughout), so the
+// 64-bit-index library takes any matrix whose rows and columns each fit an int: m * n may
+// exceed 2^31.
 void check_mat(const mat *M) {
     need(M != nullptr && M->d != nullptr, "null matrix");
     need(M->nrows > 0 && M->ncols > 0, "empty matrix");
+    need((long long)M->nrows <= INT_MAX && (long long)M->ncols <= INT_MAX, "dimension above 2^31 - 1");
+}
+
+// Rank, oversampling, power and step arguments of the 64-bit-index library: each must fit an int.
+template <typename... Ts>
+void need_int(Ts... v) {
+    need(((v >= (rsvd_int)INT_MIN && v <= (rsvd_int)INT_MAX) && ...), "argument outside the int range");
 }
 
 // Working precision of the tall products for this call.
@@ -81,8 +92,8 @@ DMat<T> upload(const mat *M) {
 // An output matrix the engine overwrites entirely: same ownership as matrix_new (freed
 // with matrix_delete / free), but for large sizes 2 MB aligned with a transparent-huge-page
 // hint and not zeroed, so that filling it costs a few page faults instead of one per 4 KB.
-mat *matrix_new_output(int nrows, int ncols) {
-    const size_t bytes = sizeof(double) * (size_t)std::max(nrows, 0) * (size_t)std::max(ncols, 0);
+mat *matrix_new_output(rsvd_int nrows, rsvd_int ncols) {
+    const size_t bytes = sizeof(double) * (size_t)std::max<rsvd_int>(nrows, 0) * (size_t)std::max<rsvd_int>(ncols, 0);
     if (bytes < ((size_t)4 << 20)) return matrix_new(nrows, ncols);
     mat *M = (mat *)std::malloc(sizeof(mat));
     if (!M) return nullptr;
@@ -139,7 +150,7 @@ void parallel_copy(double *dst, const double *src, size_t count) {
 template <typename T>
 mat *download(DM<T> a) {
     cudaStream_t s = ctx().stream;
-    mat *M = matrix_new_output((int)a.r, (int)a.c);
+    mat *M = matrix_new_output((rsvd_int)a.r, (rsvd_int)a.c);
     if (!M) throw std::bad_alloc();
     if (a.r * a.c == 0) return M;
     const size_t count = (size_t)a.r * (size_t)a.c;
@@ -166,7 +177,7 @@ mat *download(DM<T> a) {
 struct OutputPrefetch {
     mat *M = nullptr;
     std::thread th;
-    OutputPrefetch(int r, int c) {
+    OutputPrefetch(i64 r, i64 c) {
         th = std::thread([this, r, c] {
             M = matrix_new_output(r, c);
             if (!M) return;
@@ -219,7 +230,7 @@ mat *diag_mat(const std::vector<double> &d) {
 }
 
 vec *index_vec(const std::vector<int> &I) {
-    vec *v = vector_new((int)I.size());
+    vec *v = vector_new((rsvd_int)I.size());
     for (size_t i = 0; i < I.size(); i++) v->d[i] = (double)I[i];
     return v;
 }
@@ -273,7 +284,7 @@ void run_fixed_rank(mat *M, int k, int p, int vnum, int q, int s, mat **U, mat *
 }
 
 template <typename T>
-void run_blockrand(mat *M, int k, int p, double TOL, int vnum, int kstep, int q, int s, int *frank, mat **U,
+void run_blockrand(mat *M, int k, int p, double TOL, int vnum, int kstep, int q, int s, rsvd_int *frank, mat **U,
                    mat **S, mat **V) {
     auto t0 = Clock::now();
     DMat<T> A = upload<T>(M);
@@ -285,7 +296,7 @@ void run_blockrand(mat *M, int k, int p, double TOL, int vnum, int kstep, int q,
 }
 
 template <typename T>
-void run_qb(mat *M, int kstep, int nstep, double TOL, int q, int s, int *frank, mat **Q, mat **B) {
+void run_qb(mat *M, int kstep, int nstep, double TOL, int q, int s, rsvd_int *frank, mat **Q, mat **B) {
     auto t0 = Clock::now();
     DMat<T> A = upload<T>(M);
     QBOut<T> r = qb_blocked<T>(A.v, kstep, nstep, TOL, q, s);
@@ -300,7 +311,7 @@ void run_qb(mat *M, int kstep, int nstep, double TOL, int q, int s, int *frank, 
 extern "C" {
 
 // ============================================================ storage (MVF:8-63)
-mat *matrix_new(int nrows, int ncols) {
+mat *matrix_new(rsvd_int nrows, rsvd_int ncols) {
     mat *M = (mat *)std::malloc(sizeof(mat));
     if (!M) return nullptr;
     M->nrows = nrows;
@@ -310,7 +321,7 @@ mat *matrix_new(int nrows, int ncols) {
     return M;
 }
 
-vec *vector_new(int nrows) {
+vec *vector_new(rsvd_int nrows) {
     vec *v = (vec *)std::malloc(sizeof(vec));
     if (!v) return nullptr;
     v->nrows = nrows;
@@ -330,34 +341,35 @@ void vector_delete(vec *v) {
     std::free(v);
 }
 
-void matrix_set_element(mat *M, int i, int j, double val) { M->d[(size_t)j * M->nrows + i] = val; }
-double matrix_get_element(mat *M, int i, int j) { return M->d[(size_t)j * M->nrows + i]; }
-void vector_set_element(vec *v, int i, double val) { v->d[i] = val; }
-double vector_get_element(vec *v, int i) { return v->d[i]; }
+void matrix_set_element(mat *M, rsvd_int i, rsvd_int j, double val) { M->d[(size_t)j * M->nrows + i] = val; }
+double matrix_get_element(mat *M, rsvd_int i, rsvd_int j) { return M->d[(size_t)j * M->nrows + i]; }
+void vector_set_element(vec *v, rsvd_int i, double val) { v->d[i] = val; }
+double vector_get_element(vec *v, rsvd_int i) { return v->d[i]; }
 
-// int32 m, int32 n, then m*n doubles in row-major order (MVF:77-133)
+// m, n as rsvd_int (int32; int64 in the 64-bit-index library, as the reference's 64-bit
+// variant writes them), then m*n doubles in row-major order (MVF:77-133)
 mat *matrix_load_from_binary_file(char *fname) {
     FILE *fp = std::fopen(fname, "rb");
     if (!fp) {
         set_error(RSVD_ERR_ARGUMENT, std::string("cannot open ") + fname);
         return nullptr;
     }
-    int hdr[2] = {0, 0};
-    if (std::fread(hdr, sizeof(int), 2, fp) != 2 || hdr[0] <= 0 || hdr[1] <= 0) {
+    rsvd_int hdr[2] = {0, 0};
+    if (std::fread(hdr, sizeof(rsvd_int), 2, fp) != 2 || hdr[0] <= 0 || hdr[1] <= 0) {
         std::fclose(fp);
         set_error(RSVD_ERR_ARGUMENT, "bad matrix file header");
         return nullptr;
     }
     mat *M = matrix_new(hdr[0], hdr[1]);
     std::vector<double> row((size_t)hdr[1]);
-    for (int i = 0; i < hdr[0]; i++) {
+    for (rsvd_int i = 0; i < hdr[0]; i++) {
         if (std::fread(row.data(), sizeof(double), (size_t)hdr[1], fp) != (size_t)hdr[1]) {
             std::fclose(fp);
             matrix_delete(M);
             set_error(RSVD_ERR_ARGUMENT, "truncated matrix file");
             return nullptr;
         }
-        for (int j = 0; j < hdr[1]; j++) M->d[(size_t)j * hdr[0] + i] = row[(size_t)j];
+        for (rsvd_int j = 0; j < hdr[1]; j++) M->d[(size_t)j * hdr[0] + i] = row[(size_t)j];
     }
     std::fclose(fp);
     return M;
@@ -369,11 +381,11 @@ void matrix_write_to_binary_file(mat *M, char *fname) {
         set_error(RSVD_ERR_ARGUMENT, std::string("cannot open ") + fname);
         return;
     }
-    const int hdr[2] = {M->nrows, M->ncols};
-    std::fwrite(hdr, sizeof(int), 2, fp);
+    const rsvd_int hdr[2] = {M->nrows, M->ncols};
+    std::fwrite(hdr, sizeof(rsvd_int), 2, fp);
     std::vector<double> row((size_t)M->ncols);
-    for (int i = 0; i < M->nrows; i++) {
-        for (int j = 0; j < M->ncols; j++) row[(size_t)j] = M->d[(size_t)j * M->nrows + i];
+    for (rsvd_int i = 0; i < M->nrows; i++) {
+        for (rsvd_int j = 0; j < M->ncols; j++) row[(size_t)j] = M->d[(size_t)j * M->nrows + i];
         std::fwrite(row.data(), sizeof(double), (size_t)M->ncols, fp);
     }
     std::fclose(fp);
@@ -384,8 +396,8 @@ void matrix_copy(mat *D, mat *S) {
 }
 
 void matrix_build_transpose(mat *Mt, mat *M) {
-    for (int j = 0; j < M->ncols; j++)
-        for (int i = 0; i < M->nrows; i++) Mt->d[(size_t)i * Mt->nrows + j] = M->d[(size_t)j * M->nrows + i];
+    for (rsvd_int j = 0; j < M->ncols; j++)
+        for (rsvd_int i = 0; i < M->nrows; i++) Mt->d[(size_t)i * Mt->nrows + j] = M->d[(size_t)j * M->nrows + i];
 }
 
 double get_matrix_frobenius_norm(mat *M) {
@@ -456,12 +468,13 @@ void form_cur_product_matrix(mat *C, mat *U, mat *R, mat *P) {
 }
 
 // ============================================================ decompositions
-void low_rank_svd_rand_decomp_fixed_rank(mat *M, int k, int p, int vnum, int q, int s, int *frank, mat **U,
+void low_rank_svd_rand_decomp_fixed_rank(mat *M, rsvd_int k, rsvd_int p, rsvd_int vnum, rsvd_int q, rsvd_int s, rsvd_int *frank, mat **U,
                                          mat **S, mat **V) {
     (void)frank;   // not written by the reference (RRA:73-234)
     *U = *S = *V = nullptr;
     guarded("low_rank_svd_rand_decomp_fixed_rank", [&] {
         check_mat(M);
+        need_int(k, p, vnum, q, s);
         need(k >= 1 && p >= 0, "need k >= 1 and p >= 0");
         need(k + p <= std::min(M->nrows, M->ncols), "k + p exceeds min(m, n)");
         need(q < 2 || s >= 1, "s must be >= 1 when q >= 2");
@@ -471,11 +484,12 @@ void low_rank_svd_rand_decomp_fixed_rank(mat *M, int k, int p, int vnum, int q, 
     });
 }
 
-void low_rank_svd_blockrand_decomp_fixed_rank_or_prec(mat *M, int k, int p, double TOL, int vnum, int kstep, int q,
-                                                      int s, int *frank, mat **U, mat **S, mat **V) {
+void low_rank_svd_blockrand_decomp_fixed_rank_or_prec(mat *M, rsvd_int k, rsvd_int p, double TOL, rsvd_int vnum, rsvd_int kstep, rsvd_int q,
+                                                      rsvd_int s, rsvd_int *frank, mat **U, mat **S, mat **V) {
     *U = *S = *V = nullptr;
     guarded("low_rank_svd_blockrand_decomp_fixed_rank_or_prec", [&] {
         check_mat(M);
+        need_int(k, p, vnum, kstep, q, s);
         need(kstep >= 1 && p >= 0, "need kstep >= 1 and p >= 0");
         need(q < 1 || s >= 1, "s must be >= 1");
         begin_call();
@@ -484,10 +498,11 @@ void low_rank_svd_blockrand_decomp_fixed_rank_or_prec(mat *M, int k, int p, doub
     });
 }
 
-void randQB_pb_new(mat *M, int kstep, int nstep, double TOL, int q, int s, int *frank, mat **Q, mat **B) {
+void randQB_pb_new(mat *M, rsvd_int kstep, rsvd_int nstep, double TOL, rsvd_int q, rsvd_int s, rsvd_int *frank, mat **Q, mat **B) {
     *Q = *B = nullptr;
     guarded("randQB_pb_new", [&] {
         check_mat(M);
+        need_int(kstep, nstep, q, s);
         need(kstep >= 1, "need kstep >= 1");
         need(q < 1 || s >= 1, "s must be >= 1");
         need((long long)kstep * nstep <= (long long)std::min(M->nrows, M->ncols) || kstep > std::min(M->nrows, M->ncols) / 2,
@@ -514,11 +529,12 @@ void pivotedQR_mkl(mat *M, mat **Q, mat **R, vec **I) {
     });
 }
 
-void pivoted_QR_of_specified_rank_or_prec(mat *M, int k, double TOL, int *frank, mat **Qk, mat **Rk, vec **I) {
+void pivoted_QR_of_specified_rank_or_prec(mat *M, rsvd_int k, double TOL, rsvd_int *frank, mat **Qk, mat **Rk, vec **I) {
     *Qk = *Rk = nullptr;
     *I = nullptr;
     guarded("pivoted_QR_of_specified_rank_or_prec", [&] {
         check_mat(M);
+        need_int(k);
         need(k <= std::min(M->nrows, M->ncols), "k exceeds min(m, n)");
         begin_call();
         auto t0 = Clock::now();
@@ -532,11 +548,12 @@ void pivoted_QR_of_specified_rank_or_prec(mat *M, int k, double TOL, int *frank,
     });
 }
 
-void id_decomp_fixed_rank_or_prec(mat *M, int k, double TOL, int *frank, vec **I, mat **T) {
+void id_decomp_fixed_rank_or_prec(mat *M, rsvd_int k, double TOL, rsvd_int *frank, vec **I, mat **T) {
     *I = nullptr;
     *T = nullptr;
     guarded("id_decomp_fixed_rank_or_prec", [&] {
         check_mat(M);
+        need_int(k);
         need(k <= std::min(M->nrows, M->ncols), "k exceeds min(m, n)");
         begin_call();
         auto t0 = Clock::now();
@@ -549,11 +566,12 @@ void id_decomp_fixed_rank_or_prec(mat *M, int k, double TOL, int *frank, vec **I
     });
 }
 
-void id_rand_decomp_fixed_rank(mat *M, int k, int p, int q, int s, vec **I, mat **T) {
+void id_rand_decomp_fixed_rank(mat *M, rsvd_int k, rsvd_int p, rsvd_int q, rsvd_int s, vec **I, mat **T) {
     *I = nullptr;
     *T = nullptr;
     guarded("id_rand_decomp_fixed_rank", [&] {
         check_mat(M);
+        need_int(k, p, q, s);
         need(k >= 1 && p >= 0 && k + p <= std::min(M->nrows, M->ncols), "need 1 <= k, k + p <= min(m, n)");
         need(q < 1 || s >= 1, "s must be >= 1");
         begin_call();
@@ -566,12 +584,13 @@ void id_rand_decomp_fixed_rank(mat *M, int k, int p, int q, int s, vec **I, mat 
     });
 }
 
-void id_blockrand_decomp_fixed_rank_or_prec(mat *M, int k, int p, double TOL, int kstep, int q, int s, int *frank,
+void id_blockrand_decomp_fixed_rank_or_prec(mat *M, rsvd_int k, rsvd_int p, double TOL, rsvd_int kstep, rsvd_int q, rsvd_int s, rsvd_int *frank,
                                             vec **I, mat **T) {
     *I = nullptr;
     *T = nullptr;
     guarded("id_blockrand_decomp_fixed_rank_or_prec", [&] {
         check_mat(M);
+        need_int(k, p, kstep, q, s);
         need(kstep >= 1, "need kstep >= 1");
         need(q < 1 || s >= 1, "s must be >= 1");
         begin_call();
@@ -624,12 +643,13 @@ static void two_sided_outputs(TwoSidedOut &r, vec **Icol, vec **Irow, mat **T, m
     *S = download<double>(r.S.v);
 }
 
-void id_two_sided_decomp_fixed_rank_or_prec(mat *M, int k, double TOL, int *frank, vec **Icol, vec **Irow, mat **T,
+void id_two_sided_decomp_fixed_rank_or_prec(mat *M, rsvd_int k, double TOL, rsvd_int *frank, vec **Icol, vec **Irow, mat **T,
                                             mat **S) {
     *Icol = *Irow = nullptr;
     *T = *S = nullptr;
     guarded("id_two_sided_decomp_fixed_rank_or_prec", [&] {
         check_mat(M);
+        need_int(k);
         need(k <= std::min(M->nrows, M->ncols), "k exceeds min(m, n)");
         begin_call();
         auto t0 = Clock::now();
@@ -641,12 +661,13 @@ void id_two_sided_decomp_fixed_rank_or_prec(mat *M, int k, double TOL, int *fran
     });
 }
 
-void id_two_sided_rand_decomp_fixed_rank(mat *M, int k, int p, int q, int s, vec **Icol, vec **Irow, mat **T,
+void id_two_sided_rand_decomp_fixed_rank(mat *M, rsvd_int k, rsvd_int p, rsvd_int q, rsvd_int s, vec **Icol, vec **Irow, mat **T,
                                          mat **S) {
     *Icol = *Irow = nullptr;
     *T = *S = nullptr;
     guarded("id_two_sided_rand_decomp_fixed_rank", [&] {
         check_mat(M);
+        need_int(k, p, q, s);
         need(k >= 1 && p >= 0 && k + p <= std::min(M->nrows, M->ncols), "need 1 <= k, k + p <= min(m, n)");
         need(q < 1 || s >= 1, "s must be >= 1");
         begin_call();
@@ -658,12 +679,13 @@ void id_two_sided_rand_decomp_fixed_rank(mat *M, int k, int p, int q, int s, vec
     });
 }
 
-void id_two_sided_blockrand_decomp_fixed_rank_or_prec(mat *M, int k, int p, double TOL, int kstep, int q, int s,
-                                                      int *frank, vec **Icol, vec **Irow, mat **T, mat **S) {
+void id_two_sided_blockrand_decomp_fixed_rank_or_prec(mat *M, rsvd_int k, rsvd_int p, double TOL, rsvd_int kstep, rsvd_int q, rsvd_int s,
+                                                      rsvd_int *frank, vec **Icol, vec **Irow, mat **T, mat **S) {
     *Icol = *Irow = nullptr;
     *T = *S = nullptr;
     guarded("id_two_sided_blockrand_decomp_fixed_rank_or_prec", [&] {
         check_mat(M);
+        need_int(k, p, kstep, q, s);
         need(kstep >= 1, "need kstep >= 1");
         need(q < 1 || s >= 1, "s must be >= 1");
         begin_call();
@@ -682,10 +704,11 @@ static void cur_outputs(CurOut &r, mat **C, mat **U, mat **R) {
     *R = download<double>(r.R.v);
 }
 
-void cur_decomp_fixed_rank_or_prec(mat *M, int k, double TOL, int *frank, mat **C, mat **U, mat **R) {
+void cur_decomp_fixed_rank_or_prec(mat *M, rsvd_int k, double TOL, rsvd_int *frank, mat **C, mat **U, mat **R) {
     *C = *U = *R = nullptr;
     guarded("cur_decomp_fixed_rank_or_prec", [&] {
         check_mat(M);
+        need_int(k);
         need(k <= std::min(M->nrows, M->ncols), "k exceeds min(m, n)");
         begin_call();
         auto t0 = Clock::now();
@@ -698,10 +721,11 @@ void cur_decomp_fixed_rank_or_prec(mat *M, int k, double TOL, int *frank, mat **
     });
 }
 
-void cur_rand_decomp_fixed_rank(mat *M, int k, int p, int q, int s, mat **C, mat **U, mat **R) {
+void cur_rand_decomp_fixed_rank(mat *M, rsvd_int k, rsvd_int p, rsvd_int q, rsvd_int s, mat **C, mat **U, mat **R) {
     *C = *U = *R = nullptr;
     guarded("cur_rand_decomp_fixed_rank", [&] {
         check_mat(M);
+        need_int(k, p, q, s);
         need(k >= 1 && p >= 0 && k + p <= std::min(M->nrows, M->ncols), "need 1 <= k, k + p <= min(m, n)");
         need(q < 1 || s >= 1, "s must be >= 1");
         begin_call();
@@ -714,11 +738,12 @@ void cur_rand_decomp_fixed_rank(mat *M, int k, int p, int q, int s, mat **C, mat
     });
 }
 
-void cur_blockrand_decomp_fixed_rank_or_prec(mat *M, int k, int p, double TOL, int kstep, int q, int s, int *frank,
+void cur_blockrand_decomp_fixed_rank_or_prec(mat *M, rsvd_int k, rsvd_int p, double TOL, rsvd_int kstep, rsvd_int q, rsvd_int s, rsvd_int *frank,
                                              mat **C, mat **U, mat **R) {
     *C = *U = *R = nullptr;
     guarded("cur_blockrand_decomp_fixed_rank_or_prec", [&] {
         check_mat(M);
+        need_int(k, p, kstep, q, s);
         need(kstep >= 1, "need kstep >= 1");
         need(q < 1 || s >= 1, "s must be >= 1");
         begin_call();
@@ -1046,12 +1071,12 @@ void use_low_rank_svd_for_approximation(mat *M, mat *U, mat *S, mat *V) {
 }
 
 void use_pivoted_QR_decomp_for_approximation(mat *M, mat *Qk, mat *Rk, vec *I) {
-    const int m = M->nrows, n = M->ncols;
+    const rsvd_int m = M->nrows, n = M->ncols;
     mat *QR = matrix_new(m, n), *QRPt = matrix_new(m, n);
     matrix_matrix_mult(Qk, Rk, QR);
     // (Qk Rk) P^T : column j of the product goes back to column I[j]
-    for (int j = 0; j < n; j++)
-        std::memcpy(QRPt->d + (size_t)((int)I->d[j]) * m, QR->d + (size_t)j * m, sizeof(double) * m);
+    for (rsvd_int j = 0; j < n; j++)
+        std::memcpy(QRPt->d + (size_t)((rsvd_int)I->d[j]) * m, QR->d + (size_t)j * m, sizeof(double) * m);
     std::printf("percent_error between M and QkRkPt = %f\n", get_percent_error_between_two_mats(M, QRPt));
     matrix_delete(Qk);
     matrix_delete(Rk);
@@ -1069,24 +1094,24 @@ void use_QB_decomp_for_approximation(mat *M, mat *Q, mat *B) {
 }
 
 // V = [I_k; T^T](Iinv,:) ; MA = M(:,I(1:k)) V^T
-static mat *id_basis(mat *T, vec *I, int k) {
-    const int n = I->nrows;
-    std::vector<int> inv((size_t)n);
-    for (int j = 0; j < n; j++) inv[(size_t)((int)I->d[j])] = j;
+static mat *id_basis(mat *T, vec *I, rsvd_int k) {
+    const rsvd_int n = I->nrows;
+    std::vector<rsvd_int> inv((size_t)n);
+    for (rsvd_int j = 0; j < n; j++) inv[(size_t)((rsvd_int)I->d[j])] = j;
     mat *V = matrix_new(n, k);
-    for (int i = 0; i < n; i++) {
-        const int r = inv[(size_t)i];
-        for (int c = 0; c < k; c++)
+    for (rsvd_int i = 0; i < n; i++) {
+        const rsvd_int r = inv[(size_t)i];
+        for (rsvd_int c = 0; c < k; c++)
             V->d[(size_t)c * n + i] = (r < k) ? (r == c ? 1.0 : 0.0) : T->d[(size_t)(r - k) * T->nrows + c];
     }
     return V;
 }
 
-void use_id_decomp_for_approximation(mat *M, mat *T, vec *I, int k) {
-    const int m = M->nrows, n = M->ncols;
+void use_id_decomp_for_approximation(mat *M, mat *T, vec *I, rsvd_int k) {
+    const rsvd_int m = M->nrows, n = M->ncols;
     mat *V = id_basis(T, I, k);
     mat *MI = matrix_new(m, k);
-    for (int c = 0; c < k; c++) std::memcpy(MI->d + (size_t)c * m, M->d + (size_t)((int)I->d[c]) * m, sizeof(double) * m);
+    for (rsvd_int c = 0; c < k; c++) std::memcpy(MI->d + (size_t)c * m, M->d + (size_t)((rsvd_int)I->d[c]) * m, sizeof(double) * m);
     mat *MA = matrix_new(m, n);
     matrix_matrix_transpose_mult(MI, V, MA);
     std::printf("norm(M,fro) = %f\n", get_matrix_frobenius_norm(M));
@@ -1097,14 +1122,14 @@ void use_id_decomp_for_approximation(mat *M, mat *T, vec *I, int k) {
     matrix_delete(MA);
 }
 
-void use_id_two_sided_decomp_for_approximation(mat *M, mat *T, mat *S, vec *Icol, vec *Irow, int k) {
-    const int m = M->nrows, n = M->ncols;
+void use_id_two_sided_decomp_for_approximation(mat *M, mat *T, mat *S, vec *Icol, vec *Irow, rsvd_int k) {
+    const rsvd_int m = M->nrows, n = M->ncols;
     mat *V = id_basis(T, Icol, k);
     mat *Uu = id_basis(S, Irow, k);
     mat *MIJ = matrix_new(k, k);
-    for (int c = 0; c < k; c++)
-        for (int r = 0; r < k; r++)
-            MIJ->d[(size_t)c * k + r] = M->d[(size_t)((int)Icol->d[c]) * m + (size_t)((int)Irow->d[r])];
+    for (rsvd_int c = 0; c < k; c++)
+        for (rsvd_int r = 0; r < k; r++)
+            MIJ->d[(size_t)c * k + r] = M->d[(size_t)((rsvd_int)Icol->d[c]) * m + (size_t)((rsvd_int)Irow->d[r])];
     mat *UM = matrix_new(m, k), *MA = matrix_new(m, n);
     matrix_matrix_mult(Uu, MIJ, UM);
     matrix_matrix_transpose_mult(UM, V, MA);
