@@ -150,7 +150,7 @@ void prod(cudaStream_t s, bool ta, bool tb, T alpha, DM<T> A, DM<T> B, T beta, D
                 const TcSeg g[2] = {{Al.p, Al.ld, Bb.p, Bb.ld, (int)K}, {Ah.p, Ah.ld, Bb.p, Bb.ld, (int)K}};
                 tc_gemm_segs(s, 1, true, 2, g, (int)M, (int)N, (float)alpha, (float *)C.p, C.ld, 0, nullptr, 0,
                              nullptr, 0);
-                RSVD_CK(cudaStreamSynchronize(s));   // tb_tmp leaves scope
+                // tb_tmp is a stream-ordered buffer: freed after the product, no host wait
             } else {
                 // bf16 operands: the larger operand (normally A) is converted once per call
                 DMat<__nv_bfloat16> ta_tmp, tb_tmp;
@@ -159,7 +159,7 @@ void prod(cudaStream_t s, bool ta, bool tb, T alpha, DM<T> A, DM<T> B, T beta, D
                 DM<__nv_bfloat16> Bb = to_bf16(s, *(DM<float> *)&B, tb_tmp, !a_big);
                 tc_gemm(s, 1, !ta, Ab.p, Ab.ld, Bb.p, Bb.ld, (int)M, (int)N, (int)K, (float)alpha, (float *)C.p, C.ld,
                         0, nullptr, 0, nullptr, 0);
-                RSVD_CK(cudaStreamSynchronize(s));   // temporaries leave scope
+                // the temporaries are stream-ordered buffers: freed after the product, no host wait
             }
             if (t_bf16_a.src == (const void *)C.p) release_operand_cache();   // C was overwritten
             return;
@@ -366,23 +366,24 @@ static SvdOut<T> svd_from_q(DM<T> A, DM<T> Q, int k, int vnum) {
         {
             DMat<double> RhT(l, l, s, false);
             transpose<double>(s, Rh.v, RhT.v);
-            jacobi_small<T>(s, RhT.v, Vh.v, Uh.v, (double *)svb.get(), cx.d_flags + FLAG_JACOBI_NOCONV);
+            jacobi_small<T>(s, RhT.v, Vh.v, Uh.v, (double *)svb.get(), cx.d_flags + FLAG_JACOBI_NOCONV, false);
         }
-        RSVD_CK(cudaMemcpyAsync(sv.data(), svb.get(), sizeof(double) * l, cudaMemcpyDeviceToHost, s));
-        std::vector<int> first((size_t)k);
-        for (int j = 0; j < k; j++) first[j] = j;
+        // the leading k singular pairs: column prefixes of Vh, Uh in the working precision
         DMat<T> Vk(l, k, s, false), Uk(l, k, s, false);
-        select_cols<double, T>(s, Vh.v, first, nullptr, Vk.v);
-        select_cols<double, T>(s, Uh.v, first, nullptr, Uk.v);
+        convert<double, T>(s, Vh.v.cols(0, k), Vk.v);
+        convert<double, T>(s, Uh.v.cols(0, k), Uk.v);
         // factor formation stays in the working precision (never rounded to bf16)
         gemm<T>(s, false, false, T(1), Q, Vk.v, T(0), out.U.v);
         gemm<T>(s, false, false, T(1), Qh.v, Uk.v, T(0), out.V.v);
+        // the one host wait of this step: singular values into pageable memory
+        RSVD_CK(cudaMemcpyAsync(sv.data(), svb.get(), sizeof(double) * l, cudaMemcpyDeviceToHost, s));
+        RSVD_CK(cudaStreamSynchronize(s));
         out.S.assign(sv.begin(), sv.begin() + k);
     } else {
         // eig(B B^T) ascending, keep the last k; U = Q Uh; V = B^T Uh S^-1   (RRA:176-224)
         DMat<double> BBt(l, l, s, false);
         gram<T>(s, Bt.v, BBt.v);                                         // B B^T = Bt^T Bt
-        jacobi_small<T>(s, BBt.v, Uh.v, Vh.v, (double *)svb.get(), cx.d_flags + FLAG_JACOBI_NOCONV);
+        jacobi_small<T>(s, BBt.v, Uh.v, Vh.v, (double *)svb.get(), cx.d_flags + FLAG_JACOBI_NOCONV, false);
         RSVD_CK(cudaMemcpyAsync(sv.data(), svb.get(), sizeof(double) * l, cudaMemcpyDeviceToHost, s));
         RSVD_CK(cudaStreamSynchronize(s));
         // ascending order position i in [0,k) <- descending position k-1-i
@@ -880,7 +881,7 @@ SvdOut<double> svd_from_qb(DM<double> Q, DM<double> B) {
     DMat<double> BBt(l, l, s, false), Uh(l, l, s, false), Vh(l, l, s, false);
     gram<double>(s, Bt.v, BBt.v);                                          // B B^T = Bt^T Bt
     DBuf svb(sizeof(double) * l, s);
-    jacobi_small<double>(s, BBt.v, Uh.v, Vh.v, (double *)svb.get(), cx.d_flags + FLAG_JACOBI_NOCONV);
+    jacobi_small<double>(s, BBt.v, Uh.v, Vh.v, (double *)svb.get(), cx.d_flags + FLAG_JACOBI_NOCONV, false);
     std::vector<double> sv((size_t)l);
     RSVD_CK(cudaMemcpyAsync(sv.data(), svb.get(), sizeof(double) * l, cudaMemcpyDeviceToHost, s));
     RSVD_CK(cudaStreamSynchronize(s));

@@ -547,7 +547,8 @@ template bool cholesky_small<double>(cudaStream_t, DM<double>, double, int *);
 template bool cholesky_small<float>(cudaStream_t, DM<double>, double, int *);
 
 template <typename S>
-int jacobi_small(cudaStream_t s, DM<double> G, DM<double> U, DM<double> V, double *d_sv, int *d_flag) {
+int jacobi_small(cudaStream_t s, DM<double> G, DM<double> U, DM<double> V, double *d_sv, int *d_flag,
+                 bool want_sweeps) {
     PhaseTimer pt(&ctx().timing.small_ms);
     const int n = (int)G.r;
     if (G.r != G.c) fail(RSVD_ERR_ARGUMENT, "jacobi: not square");
@@ -635,6 +636,8 @@ int jacobi_small(cudaStream_t s, DM<double> G, DM<double> U, DM<double> V, doubl
                                                                  d_sv);
     RSVD_LAUNCH_CK();
     ctx().launches += 6;
+    // the buffers above are stream-ordered: without a count to report, nothing waits here
+    if (!want_sweeps && !ctx().opts.verbose) return 0;
     int sweeps = 0;
     RSVD_CK(cudaMemcpyAsync(&sweeps, d_sweeps, sizeof(int), cudaMemcpyDeviceToHost, s));
     RSVD_CK(cudaStreamSynchronize(s));
@@ -643,7 +646,7 @@ int jacobi_small(cudaStream_t s, DM<double> G, DM<double> U, DM<double> V, doubl
                      sweeps, variant);
     return sweeps;
 }
-template int jacobi_small<double>(cudaStream_t, DM<double>, DM<double>, DM<double>, double *, int *);
-template int jacobi_small<float>(cudaStream_t, DM<double>, DM<double>, DM<double>, double *, int *);
+template int jacobi_small<double>(cudaStream_t, DM<double>, DM<double>, DM<double>, double *, int *, bool);
+template int jacobi_small<float>(cudaStream_t, DM<double>, DM<double>, DM<double>, double *, int *, bool);
 
 }  // namespace rsvd

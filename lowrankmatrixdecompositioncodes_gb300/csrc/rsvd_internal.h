@@ -285,5 +285,7 @@ namespace rsvd {
 template <typename S>
 bool cholesky_small(cudaStream_t s, DM<double> G, double rel_tol, int *d_flag);
 template <typename S>
-int jacobi_small(cudaStream_t s, DM<double> G, DM<double> U, DM<double> V, double *d_sv, int *d_flag);
+// Returns the sweep count when want_sweeps (a host read of the count, i.e. a stream sync), else 0.
+int jacobi_small(cudaStream_t s, DM<double> G, DM<double> U, DM<double> V, double *d_sv, int *d_flag,
+                 bool want_sweeps = true);
 }  // namespace rsvd
