@@ -576,6 +576,33 @@ def run_ours(args):
         e2e = {"value": world / sec, "unit": "solves/s", "h2d_bytes_per_step": m * n * 8,
                "d2h_bytes_per_step": 8 * (m * k + n * k + k), "ms_per_step": 1000 * sec}
         del A_pin
+        # the same call through the float-data ABI of the oneAPI variant (librsvdpack_f32.so,
+        # a float host matrix, the same precision mode): half the bytes over the host link
+        from lowrankmatrixdecompositioncodes_gb300 import load_engine_f32
+        from lowrankmatrixdecompositioncodes_gb300.capi import MatF32
+        ef = load_engine_f32()
+        ef.set_precision(args.precision)
+        ef.set_use_provider(False)
+        A_f = torch.empty(n, m, dtype=torch.float32, pin_memory=True)
+        A_f.copy_(At.cpu())
+        Mf = MatF32(m, n, C.cast(C.c_void_p(A_f.data_ptr()), C.POINTER(C.c_float)))
+        t_f = []
+        for i in range(args.warmup + args.steps):
+            Uo, So, Vo, fr = ef.PMat(), ef.PMat(), ef.PMat(), C.c_int64(0)
+            t0 = time.perf_counter()
+            ef.lib.low_rank_svd_rand_decomp_fixed_rank(C.byref(Mf), k, P, VNUM, Q, S_ORTH, C.byref(fr), C.byref(Uo),
+                                                       C.byref(So), C.byref(Vo))
+            t1 = time.perf_counter()
+            ef.check()
+            for x in (Uo, So, Vo):
+                ef.lib.matrix_delete(x)
+            if i >= args.warmup:
+                t_f.append(t1 - t0)
+        sec_f = sum(t_f) / len(t_f)
+        e2e["float_abi"] = {"value": world / sec_f, "unit": "solves/s", "h2d_bytes_per_step": m * n * 4,
+                            "d2h_bytes_per_step": 4 * (m * k + n * k + k), "ms_per_step": 1000 * sec_f,
+                            "library": "librsvdpack_f32.so (oneAPI variant ABI: float data, int64_t dims)"}
+        del A_f
 
     # ---------------- learned fixed-precision QB against the plain loop (extra measurement)
     learned_leg = None

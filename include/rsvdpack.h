@@ -6,10 +6,10 @@
  * function names, argument meanings, output shapes and ownership rules.
  *   - mat / vec and their helpers: multi_core_mkl_code/matrix_vector_functions_intel_mkl.h
  *   - decompositions:             multi_core_mkl_code/rank_revealing_algorithms_intel_mkl.h
- * Matrices are column-major doubles on the host (ld = nrows).  Inputs are
+ * Matrices are column-major on the host (ld = nrows; double, or float in librsvdpack_f32.so).  Inputs are
  * borrowed and never modified; outputs are allocated by the callee with
  * matrix_new / vector_new (calloc) and freed by the caller with
- * matrix_delete / vector_delete.  Index vectors hold 0-based integers as doubles.
+ * matrix_delete / vector_delete.  Index vectors hold 0-based integers as rsvd_real values.
  * All calls are synchronous: device work is finished when they return.
  * Calls are re-entrant per host thread (each thread owns a CUDA stream).
  *
@@ -34,27 +34,39 @@ extern "C" {
 
 /* ============================== Part 1: reference API ============================== */
 
-/* Index type of Part 1.  The default library, librsvdpack.so, has the LP64 int dimensions of
- * multi_core_mkl_code; librsvdpack64.so, built from the same sources with RSVDPACK_INDEX64, has
- * the int64_t dimensions of multi_core_mkl_code_64bit (matrix_vector_functions_intel_mkl.h:20-28
- * and every dimension, rank and step argument of its rank_revealing_algorithms_intel_mkl.h), for
- * matrices of more than 2^31 entries.  Define RSVDPACK_INDEX64 before including this header to
- * compile against the 64-bit library.  Part 2 keeps int in both libraries. */
-#ifdef RSVDPACK_INDEX64
+/* Index and element types of Part 1, one library per variant of the reference, all three built
+ * from the same sources over the same engine:
+ *   librsvdpack.so      int dimensions, double data: multi_core_mkl_code (the default);
+ *   librsvdpack64.so    int64_t dimensions, double data (RSVDPACK_INDEX64):
+ *                       multi_core_mkl_code_64bit/matrix_vector_functions_intel_mkl.h:20-28 and every
+ *                       dimension, rank and step argument of its rank_revealing_algorithms_intel_mkl.h,
+ *                       for matrices of more than 2^31 entries;
+ *   librsvdpack_f32.so  int64_t dimensions, float data and float TOL (RSVDPACK_REAL32):
+ *                       oneapi_code/matrix_vector_functions_one_api.h:19-32 and
+ *                       rank_revealing_algorithms_one_api.h; its default precision mode is
+ *                       RSVD_PREC_FP32 (the oneAPI variant computes in single precision).
+ * Define RSVDPACK_INDEX64 or RSVDPACK_REAL32 before including this header to compile against the
+ * matching library.  Part 2 is the same in all three (int sizes, typed device pointers). */
+#if defined(RSVDPACK_REAL32)
 typedef int64_t rsvd_int;
+typedef float rsvd_real;
+#elif defined(RSVDPACK_INDEX64)
+typedef int64_t rsvd_int;
+typedef double rsvd_real;
 #else
 typedef int rsvd_int;
+typedef double rsvd_real;
 #endif
 
-/* matrix_vector_functions_intel_mkl.h:18-27 (rsvd_int dimensions, column-major) */
+/* matrix_vector_functions_intel_mkl.h:18-27 (rsvd_int dimensions, rsvd_real data, column-major) */
 typedef struct {
     rsvd_int nrows, ncols;
-    double *d;
+    rsvd_real *d;
 } mat;
 
 typedef struct {
     rsvd_int nrows;
-    double *d;
+    rsvd_real *d;
 } vec;
 
 /* ---- storage and element access: matrix_vector_functions_intel_mkl.h:31-58 ---- */
@@ -62,14 +74,15 @@ mat *matrix_new(rsvd_int nrows, rsvd_int ncols);
 vec *vector_new(rsvd_int nrows);
 void matrix_delete(mat *M);
 void vector_delete(vec *v);
-void matrix_set_element(mat *M, rsvd_int row_num, rsvd_int col_num, double val);
-double matrix_get_element(mat *M, rsvd_int row_num, rsvd_int col_num);
-void vector_set_element(vec *v, rsvd_int row_num, double val);
-double vector_get_element(vec *v, rsvd_int row_num);
+void matrix_set_element(mat *M, rsvd_int row_num, rsvd_int col_num, rsvd_real val);
+rsvd_real matrix_get_element(mat *M, rsvd_int row_num, rsvd_int col_num);
+void vector_set_element(vec *v, rsvd_int row_num, rsvd_real val);
+rsvd_real vector_get_element(vec *v, rsvd_int row_num);
 
 /* ---- binary matrix files: matrix_vector_functions_intel_mkl.h:60-64 (format: m and n as
- *      rsvd_int -- int32 in librsvdpack.so, int64 in librsvdpack64.so as in
- *      multi_core_mkl_code_64bit/matrix_vector_functions_intel_mkl.c:86-87 -- then m*n doubles in
+ *      rsvd_int -- int32 in librsvdpack.so, int64 in librsvdpack64.so and librsvdpack_f32.so as in
+ *      multi_core_mkl_code_64bit/matrix_vector_functions_intel_mkl.c:86-87 and
+ *      oneapi_code/matrix_vector_functions_one_api.c:79-80 -- then m*n rsvd_real values in
  *      row-major order; matrix_vector_functions_intel_mkl.c:77-133) ---- */
 mat *matrix_load_from_binary_file(char *fname);
 void matrix_write_to_binary_file(mat *M, char *fname);
@@ -77,12 +90,19 @@ void matrix_write_to_binary_file(mat *M, char *fname);
 /* ---- helpers callers use around the decompositions ---- */
 void matrix_copy(mat *D, mat *S);                                 /* :92-94 */
 void matrix_build_transpose(mat *Mt, mat *M);                     /* :100-101 */
-double get_matrix_frobenius_norm(mat *M);                         /* :116-117 */
-double get_percent_error_between_two_mats(mat *A, mat *B);        /* :288-289 */
+rsvd_real get_matrix_frobenius_norm(mat *M);                      /* :116-117 */
+rsvd_real get_percent_error_between_two_mats(mat *A, mat *B);     /* :288-289 */
+rsvd_real vector_get2norm(vec *v);                                /* :83 */
+void initialize_diagonal_matrix(mat *D, vec *data);               /* :199: D(i,i) = data(i) */
 void initialize_random_matrix(mat *M);                            /* :128-129 */
 void matrix_matrix_mult(mat *A, mat *B, mat *C);                  /* :132-133 */
 void matrix_transpose_matrix_mult(mat *A, mat *B, mat *C);        /* :136-137 */
 void matrix_matrix_transpose_mult(mat *A, mat *B, mat *C);        /* :140-141 */
+/* :333, :338 Householder QR with LAPACK's reflector signs (dgeqrf + dorgqr), m >= n: M = Q R with
+ * Q (m x n, caller-allocated) and, for compact_QR_factorization, R (n x n, caller-allocated; its
+ * upper triangle is written, as the reference writes it). */
+void compact_QR_factorization(mat *M, mat *Q, mat *R);
+void QR_factorization_getQ(mat *M, mat *Q);
 void form_svd_product_matrix(mat *U, mat *S, mat *V, mat *P);     /* :343-344 */
 void form_cur_product_matrix(mat *C, mat *U, mat *R, mat *P);     /* :346-347 */
 double get_seconds_frac(struct timeval start_timeval, struct timeval end_timeval); /* :359-360 */
@@ -94,19 +114,26 @@ double get_seconds_frac(struct timeval start_timeval, struct timeval end_timeval
 void low_rank_svd_rand_decomp_fixed_rank(mat *M, rsvd_int k, rsvd_int p, rsvd_int vnum, rsvd_int q, rsvd_int s,
                                          rsvd_int *frank, mat **U, mat **S, mat **V);
 /* :7  blocked randomized SVD (rank k, or absolute Frobenius tolerance TOL when k <= 0) */
-void low_rank_svd_blockrand_decomp_fixed_rank_or_prec(mat *M, rsvd_int k, rsvd_int p, double TOL,
+void low_rank_svd_blockrand_decomp_fixed_rank_or_prec(mat *M, rsvd_int k, rsvd_int p, rsvd_real TOL,
                                                       rsvd_int vnum, rsvd_int kstep, rsvd_int q, rsvd_int s,
                                                       rsvd_int *frank, mat **U, mat **S, mat **V);
 /* :67 blocked randomized QB (nstep <= 0 selects the TOL mode) */
-void randQB_pb_new(mat *M, rsvd_int kstep, rsvd_int nstep, double TOL, rsvd_int q, rsvd_int s, rsvd_int *frank,
+void randQB_pb_new(mat *M, rsvd_int kstep, rsvd_int nstep, rsvd_real TOL, rsvd_int q, rsvd_int s, rsvd_int *frank,
                    mat **Q, mat **B);
+/* oneapi_code/rank_revealing_algorithms_one_api.h:13-14: randQB_pb2 is randQB_pb_new (the same
+ * algorithm, one_api.c:605-815); :57 randQB_pb: nstep blocks of kstep, q power rounds, every block
+ * after the first re-orthogonalised against the earlier ones (rank_revealing_algorithms_intel_mkl.c
+ * :1425-1570), Q m x (kstep nstep), B (kstep nstep) x n. */
+void randQB_pb2(mat *M, rsvd_int kstep, rsvd_int nstep, rsvd_real TOL, rsvd_int q, rsvd_int s, rsvd_int *frank,
+                mat **Q, mat **B);
+void randQB_pb(mat *M, rsvd_int kstep, rsvd_int nstep, rsvd_int q, rsvd_int s, mat **Q, mat **B);
 /* :43 full column-pivoted QR, M(:,I) = Q R (LAPACK dgeqp3 pivoting, all columns free) */
 void pivotedQR_mkl(mat *M, mat **Q, mat **R, vec **I);
 /* :52 partial pivoted Householder QR of rank k, or of precision TOL when k <= 0 */
-void pivoted_QR_of_specified_rank_or_prec(mat *M, rsvd_int k, double TOL, rsvd_int *frank,
+void pivoted_QR_of_specified_rank_or_prec(mat *M, rsvd_int k, rsvd_real TOL, rsvd_int *frank,
                                           mat **Qk, mat **Rk, vec **I);
 /* :73 column ID, T = Rk1^-1 Rk2 */
-void id_decomp_fixed_rank_or_prec(mat *M, rsvd_int k, double TOL, rsvd_int *frank, vec **I, mat **T);
+void id_decomp_fixed_rank_or_prec(mat *M, rsvd_int k, rsvd_real TOL, rsvd_int *frank, vec **I, mat **T);
 /* :76 randomized column ID (row sketch (k+p) x n, q power rounds) */
 void id_rand_decomp_fixed_rank(mat *M, rsvd_int k, rsvd_int p, rsvd_int q, rsvd_int s, vec **I, mat **T);
 /* decompositions from a given QB (Q m x l, B l x n; the QB split of the oneAPI variant,
@@ -117,26 +144,26 @@ void id_rand_decomp_fixed_rank(mat *M, rsvd_int k, rsvd_int p, rsvd_int q, rsvd_
 void low_rank_svd_rand_decomp_fromQB(mat *Q, mat *B, mat **U, mat **S, mat **V);
 void id_rand_decomp_fromQB(mat *Q, mat *B, vec **I, mat **T);
 /* :79 blocked randomized column ID */
-void id_blockrand_decomp_fixed_rank_or_prec(mat *M, rsvd_int k, rsvd_int p, double TOL, rsvd_int kstep,
+void id_blockrand_decomp_fixed_rank_or_prec(mat *M, rsvd_int k, rsvd_int p, rsvd_real TOL, rsvd_int kstep,
                                             rsvd_int q, rsvd_int s, rsvd_int *frank, vec **I, mat **T);
 /* :84 two-sided ID */
-void id_two_sided_decomp_fixed_rank_or_prec(mat *M, rsvd_int k, double TOL, rsvd_int *frank,
+void id_two_sided_decomp_fixed_rank_or_prec(mat *M, rsvd_int k, rsvd_real TOL, rsvd_int *frank,
                                             vec **Icol, vec **Irow, mat **T, mat **S);
 /* :87 randomized two-sided ID.  The reference header names the parameters (k,l,p,s);
  *     the definition (rank_revealing_algorithms_intel_mkl.c:2060) uses (k,p,q,s). */
 void id_two_sided_rand_decomp_fixed_rank(mat *M, rsvd_int k, rsvd_int p, rsvd_int q, rsvd_int s,
                                          vec **Icol, vec **Irow, mat **T, mat **S);
 /* :90 blocked randomized two-sided ID */
-void id_two_sided_blockrand_decomp_fixed_rank_or_prec(mat *M, rsvd_int k, rsvd_int p, double TOL,
+void id_two_sided_blockrand_decomp_fixed_rank_or_prec(mat *M, rsvd_int k, rsvd_int p, rsvd_real TOL,
                                                       rsvd_int kstep, rsvd_int q, rsvd_int s, rsvd_int *frank,
                                                       vec **Icol, vec **Irow, mat **T, mat **S);
 /* :95 CUR */
-void cur_decomp_fixed_rank_or_prec(mat *M, rsvd_int k, double TOL, rsvd_int *frank,
+void cur_decomp_fixed_rank_or_prec(mat *M, rsvd_int k, rsvd_real TOL, rsvd_int *frank,
                                    mat **C, mat **U, mat **R);
 /* :98 randomized CUR */
 void cur_rand_decomp_fixed_rank(mat *M, rsvd_int k, rsvd_int p, rsvd_int q, rsvd_int s, mat **C, mat **U, mat **R);
 /* :101 blocked randomized CUR */
-void cur_blockrand_decomp_fixed_rank_or_prec(mat *M, rsvd_int k, rsvd_int p, double TOL, rsvd_int kstep,
+void cur_blockrand_decomp_fixed_rank_or_prec(mat *M, rsvd_int k, rsvd_int p, rsvd_real TOL, rsvd_int kstep,
                                              rsvd_int q, rsvd_int s, rsvd_int *frank,
                                              mat **C, mat **U, mat **R);
 /* :105-120 approximation reports (print norms and percent error, as the reference does).

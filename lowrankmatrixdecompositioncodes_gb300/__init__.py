@@ -6,7 +6,8 @@ sm_103a (see ``include/rsvdpack.h``).  This package only locates, builds and bin
 reference's API names.  There is no CPU fallback: if the library is missing,
 ``load_engine()`` raises; if no GB300 is visible, every decomposition call reports
 ``RSVD_ERR_NO_DEVICE`` through ``rsvdpack_last_error()``.  ``load_engine64()`` binds
-``librsvdpack64.so``, the same engine behind the reference API with int64_t dimensions.
+``librsvdpack64.so``, the same engine behind the reference API with int64_t dimensions;
+``load_engine_f32()`` binds ``librsvdpack_f32.so``, the oneAPI variant's float-data API.
 """
 from __future__ import annotations
 
@@ -18,6 +19,7 @@ from .capi import RsvdLibrary
 PKG_DIR = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(PKG_DIR, "librsvdpack.so")
 LIB64_PATH = os.path.join(PKG_DIR, "librsvdpack64.so")
+LIBF32_PATH = os.path.join(PKG_DIR, "librsvdpack_f32.so")
 
 PREC = {"fp64": 0, "fp32": 1, "tf32": 2, "bf16": 3}
 
@@ -37,8 +39,8 @@ class RsvdTiming(C.Structure):
 class EngineLibrary(RsvdLibrary):
     """RsvdLibrary plus the engine's extension entry points (include/rsvdpack.h Part 2)."""
 
-    def __init__(self, path: str = LIB_PATH, index64: bool = False):
-        super().__init__(path, index64=index64)
+    def __init__(self, path: str = LIB_PATH, index64: bool = False, real32: bool = False):
+        super().__init__(path, index64=index64, real32=real32)
         L = self.lib
         L.rsvdpack_last_error.restype = C.c_int
         L.rsvdpack_last_error_string.restype = C.c_char_p
@@ -96,6 +98,7 @@ class EngineLibrary(RsvdLibrary):
 
 _ENGINE = None
 _ENGINE64 = None
+_ENGINE_F32 = None
 
 
 def build(verbose: bool = False) -> str:
@@ -121,6 +124,16 @@ def load_engine64() -> EngineLibrary:
             build()
         _ENGINE64 = EngineLibrary(LIB64_PATH, index64=True)
     return _ENGINE64
+
+
+def load_engine_f32() -> EngineLibrary:
+    """Load librsvdpack_f32.so, the float-data (oneAPI variant) form of the reference API."""
+    global _ENGINE_F32
+    if _ENGINE_F32 is None:
+        if not os.path.exists(LIBF32_PATH):
+            build()
+        _ENGINE_F32 = EngineLibrary(LIBF32_PATH, real32=True)
+    return _ENGINE_F32
 
 
 def engine_available() -> bool:

@@ -3,9 +3,10 @@
 Each translation unit in csrc/ is compiled in parallel into _build/, then linked into
 lowrankmatrixdecompositioncodes_gb300/librsvdpack.so (static CUDA runtime, no libcuda
 link-time dependency: the driver API is reached through cudaGetDriverEntryPoint).
-api.cu, the reference API layer, is compiled a second time with RSVDPACK_INDEX64 and linked
-with the same engine objects into librsvdpack64.so: the reference API with int64_t
-dimensions (multi_core_mkl_code_64bit), over the same kernels.
+api.cu, the reference API layer, is compiled twice more and linked with the same engine
+objects: with RSVDPACK_INDEX64 into librsvdpack64.so (int64_t dimensions, as
+multi_core_mkl_code_64bit) and with RSVDPACK_REAL32 into librsvdpack_f32.so (float data and
+int64_t dimensions, as oneapi_code), over the same kernels.
 Incremental: a unit is rebuilt when it or any header in csrc/ or include/ is newer
 than its object file.
 """
@@ -24,7 +25,10 @@ CSRC = os.path.join(PKG, "csrc")
 BUILD = os.path.join(ROOT, "_build")
 LIB = os.path.join(PKG, "librsvdpack.so")
 LIB64 = os.path.join(PKG, "librsvdpack64.so")
-INDEX64_UNIT = "api.cu"
+LIBF32 = os.path.join(PKG, "librsvdpack_f32.so")
+API_UNIT = "api.cu"
+# library -> (object suffix, defines) of its API unit; the other units are shared
+VARIANTS = {LIB: ("", ()), LIB64: (".i64", ("-DRSVDPACK_INDEX64",)), LIBF32: (".f32", ("-DRSVDPACK_REAL32",))}
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -55,17 +59,19 @@ def build(verbose: bool = False, jobs: int | None = None) -> str:
     srcs = sorted(glob.glob(os.path.join(CSRC, "*.cu")))
     hdr_t = _newest_header()
     todo = []
-    objs = []
-    objs64 = []
+    shared = []
+    api_objs = {}
     for s in srcs:
-        units = [(os.path.join(BUILD, os.path.basename(s) + ".o"), ())]
-        if os.path.basename(s) == INDEX64_UNIT:
-            units.append((os.path.join(BUILD, os.path.basename(s) + ".i64.o"), ("-DRSVDPACK_INDEX64",)))
-        for o, extra in units:
-            if not extra:
-                objs.append(o)
-            if extra or os.path.basename(s) != INDEX64_UNIT:
-                objs64.append(o)
+        base = os.path.basename(s)
+        if base == API_UNIT:
+            units = [(lib, os.path.join(BUILD, base + suf + ".o"), extra) for lib, (suf, extra) in VARIANTS.items()]
+        else:
+            units = [(None, os.path.join(BUILD, base + ".o"), ())]
+        for lib, o, extra in units:
+            if lib is None:
+                shared.append(o)
+            else:
+                api_objs[lib] = o
             if not os.path.exists(o) or os.path.getmtime(o) < max(os.path.getmtime(s), hdr_t):
                 todo.append((s, o, extra))
 
@@ -84,7 +90,8 @@ def build(verbose: bool = False, jobs: int | None = None) -> str:
             for s in ex.map(compile_one, todo):
                 if verbose:
                     print("compiled", os.path.basename(s))
-    for lib, lobjs in ((LIB, objs), (LIB64, objs64)):
+    for lib in VARIANTS:
+        lobjs = shared + [api_objs[lib]]
         if todo or not os.path.exists(lib):
             tmp = lib + ".tmp"
             cmd = [nvcc, *ARCH, "-shared", "-o", tmp, *lobjs, "-Xlinker", "-Bsymbolic", "-Xlinker", "--no-undefined"]

@@ -15,7 +15,10 @@ callee with ``matrix_new``/``vector_new`` and released here with
 
 ``RsvdLibrary(path, index64=True)`` binds the int64_t-dimension form of the same API
 (multi_core_mkl_code_64bit/matrix_vector_functions_intel_mkl.h:20-28 and
-rank_revealing_algorithms_intel_mkl.h), which librsvdpack64.so exports.
+rank_revealing_algorithms_intel_mkl.h), which librsvdpack64.so exports;
+``RsvdLibrary(path, real32=True)`` the float-data, int64_t-dimension form of the oneAPI variant
+(oneapi_code/matrix_vector_functions_one_api.h:19-32, float TOL), which librsvdpack_f32.so
+exports: numpy inputs are rounded to float32 and outputs come back as float32.
 """
 from __future__ import annotations
 
@@ -41,16 +44,22 @@ class Vec64(C.Structure):
     _fields_ = [("nrows", C.c_int64), ("d", C.POINTER(C.c_double))]
 
 
+class MatF32(C.Structure):
+    _fields_ = [("nrows", C.c_int64), ("ncols", C.c_int64), ("d", C.POINTER(C.c_float))]
+
+
+class VecF32(C.Structure):
+    _fields_ = [("nrows", C.c_int64), ("d", C.POINTER(C.c_float))]
+
+
 PMat = C.POINTER(Mat)
 PVec = C.POINTER(Vec)
 OMEGA_FN = C.CFUNCTYPE(None, C.c_void_p, C.c_int, C.c_int, C.c_int, C.POINTER(C.c_double))
 
-_D = C.c_double
-
-
-def _algos(_I, PMat, PVec):
+def _algos(_I, PMat, PVec, _D=C.c_double):
     """name -> argtypes for the reference API (rank_revealing_algorithms_intel_mkl.h:3-110),
-    with index type _I (c_int, or c_int64 for the 64-bit form)."""
+    with index type _I (c_int, or c_int64 for the 64-bit forms) and TOL type _D (c_double, or
+    c_float for the oneAPI form)."""
     _PI = C.POINTER(_I)
     _PPM = C.POINTER(PMat)
     _PPV = C.POINTER(PVec)
@@ -59,6 +68,8 @@ def _algos(_I, PMat, PVec):
         "low_rank_svd_blockrand_decomp_fixed_rank_or_prec":
             [PMat, _I, _I, _D, _I, _I, _I, _I, _PI, _PPM, _PPM, _PPM],
         "randQB_pb_new": [PMat, _I, _I, _D, _I, _I, _PI, _PPM, _PPM],
+        "randQB_pb2": [PMat, _I, _I, _D, _I, _I, _PI, _PPM, _PPM],
+        "randQB_pb": [PMat, _I, _I, _I, _I, _PPM, _PPM],
         "pivotedQR_mkl": [PMat, _PPM, _PPM, _PPV],
         "pivoted_QR_of_specified_rank_or_prec": [PMat, _I, _D, _PI, _PPM, _PPM, _PPV],
         "id_decomp_fixed_rank_or_prec": [PMat, _I, _D, _PI, _PPV, _PPM],
@@ -117,15 +128,21 @@ class RsvdLibrary:
     """Binds one shared library exporting the reference C API: LP64 int dimensions, or
     int64_t dimensions with ``index64=True``."""
 
-    def __init__(self, path: str, index64: bool = False):
+    def __init__(self, path: str, index64: bool = False, real32: bool = False):
         self.path = str(path)
-        self.index64 = bool(index64)
+        self.real32 = bool(real32)
+        self.index64 = bool(index64) or self.real32
         self.Int = C.c_int64 if self.index64 else C.c_int
-        self.Mat = Mat64 if self.index64 else Mat
-        self.Vec = Vec64 if self.index64 else Vec
+        self.Real = C.c_float if self.real32 else C.c_double
+        self.dtype = np.float32 if self.real32 else np.float64
+        if self.real32:
+            self.Mat, self.Vec = MatF32, VecF32
+        else:
+            self.Mat = Mat64 if self.index64 else Mat
+            self.Vec = Vec64 if self.index64 else Vec
         self.PMat = C.POINTER(self.Mat)
         self.PVec = C.POINTER(self.Vec)
-        PMat, PVec, _I = self.PMat, self.PVec, self.Int
+        PMat, PVec, _I, _D = self.PMat, self.PVec, self.Int, self.Real
         self.lib = C.CDLL(self.path)
         L = self.lib
         L.matrix_new.restype = PMat
@@ -140,7 +157,7 @@ class RsvdLibrary:
         L.get_matrix_frobenius_norm.argtypes = [PMat]
         L.get_percent_error_between_two_mats.restype = _D
         L.get_percent_error_between_two_mats.argtypes = [PMat, PMat]
-        for name, args in _algos(_I, PMat, PVec).items():
+        for name, args in _algos(_I, PMat, PVec, _D).items():
             f = getattr(L, name, None)
             if f is not None:
                 f.argtypes = args
@@ -158,7 +175,7 @@ class RsvdLibrary:
         return hasattr(self.lib, name)
 
     def to_mat(self, A):
-        A = np.asarray(A, dtype=np.float64)
+        A = np.asarray(A, dtype=self.dtype)
         if A.ndim != 2:
             raise ValueError("matrix must be 2-D")
         m, n = A.shape
@@ -246,6 +263,24 @@ class RsvdLibrary:
         finally:
             self.lib.matrix_delete(M)
         return self.from_mat(Q), self.from_mat(B), fr.value
+
+    def randQB_pb2(self, A, kstep, nstep, TOL, q, s):
+        M = self.to_mat(A)
+        Q, B, fr = self.PMat(), self.PMat(), self.Int(-1)
+        try:
+            self.lib.randQB_pb2(M, kstep, nstep, float(TOL), q, s, C.byref(fr), C.byref(Q), C.byref(B))
+        finally:
+            self.lib.matrix_delete(M)
+        return self.from_mat(Q), self.from_mat(B), fr.value
+
+    def randQB_pb(self, A, kstep, nstep, q, s):
+        M = self.to_mat(A)
+        Q, B = self.PMat(), self.PMat()
+        try:
+            self.lib.randQB_pb(M, kstep, nstep, q, s, C.byref(Q), C.byref(B))
+        finally:
+            self.lib.matrix_delete(M)
+        return self.from_mat(Q), self.from_mat(B)
 
     def low_rank_svd_rand_decomp_fromQB(self, Qm, Bm):
         Q, B = self.to_mat(Qm), self.to_mat(Bm)

@@ -19,6 +19,21 @@
 
 using namespace rsvd;
 
+// Host element type of this build's mat / vec: double, or float in the oneAPI-variant library.
+using real = rsvd_real;
+
+namespace rsvd {
+// Default precision mode of this library's reference API (read once by the option setup):
+// FP64 for the double-data libraries (the reference's arithmetic), FP32 for the float-data one.
+int api_default_precision() {
+#ifdef RSVDPACK_REAL32
+    return RSVD_PREC_FP32;
+#else
+    return RSVD_PREC_FP64;
+#endif
+}
+}  // namespace rsvd
+
 namespace {
 
 using Clock = std::chrono::steady_clock;
@@ -68,23 +83,23 @@ DMat<T> upload(const mat *M) {
     const i64 m = M->nrows, n = M->ncols;
     if (ctx().pageable_access) {
         // the conversion kernel reads the caller's (pageable) host matrix over NVLink-C2C:
-        // one pass at the link's bandwidth, no staging copy and no FP64 device temporary
+        // one pass at the link's bandwidth, no staging copy and no device temporary
         DMat<T> A(m, n, s, false);
-        convert<double, T>(s, DM<double>{M->d, m, n, m}, A.v);
+        convert<real, T>(s, DM<real>{M->d, m, n, m}, A.v);
         RSVD_CK(cudaStreamSynchronize(s));     // the caller may reuse M->d on return
         return A;
     }
-    if (std::is_same<T, double>::value) {
+    if (std::is_same<T, real>::value) {
         DMat<T> A(m, n, s, false);
-        RSVD_CK(cudaMemcpy2DAsync(A.v.p, sizeof(T) * A.v.ld, M->d, sizeof(double) * m, sizeof(double) * m, n,
+        RSVD_CK(cudaMemcpy2DAsync(A.v.p, sizeof(T) * A.v.ld, M->d, sizeof(real) * m, sizeof(real) * m, n,
                                   cudaMemcpyHostToDevice, s));
         return A;
     }
-    DMat<double> tmp(m, n, s, false);
-    RSVD_CK(cudaMemcpy2DAsync(tmp.v.p, sizeof(double) * tmp.v.ld, M->d, sizeof(double) * m, sizeof(double) * m, n,
+    DMat<real> tmp(m, n, s, false);
+    RSVD_CK(cudaMemcpy2DAsync(tmp.v.p, sizeof(real) * tmp.v.ld, M->d, sizeof(real) * m, sizeof(real) * m, n,
                               cudaMemcpyHostToDevice, s));
     DMat<T> A(m, n, s, false);
-    convert<double, T>(s, tmp.v, A.v);
+    convert<real, T>(s, tmp.v, A.v);
     RSVD_CK(cudaStreamSynchronize(s));
     return A;
 }
@@ -93,7 +108,7 @@ DMat<T> upload(const mat *M) {
 // with matrix_delete / free), but for large sizes 2 MB aligned with a transparent-huge-page
 // hint and not zeroed, so that filling it costs a few page faults instead of one per 4 KB.
 mat *matrix_new_output(rsvd_int nrows, rsvd_int ncols) {
-    const size_t bytes = sizeof(double) * (size_t)std::max<rsvd_int>(nrows, 0) * (size_t)std::max<rsvd_int>(ncols, 0);
+    const size_t bytes = sizeof(real) * (size_t)std::max<rsvd_int>(nrows, 0) * (size_t)std::max<rsvd_int>(ncols, 0);
     if (bytes < ((size_t)4 << 20)) return matrix_new(nrows, ncols);
     mat *M = (mat *)std::malloc(sizeof(mat));
     if (!M) return nullptr;
@@ -106,7 +121,7 @@ mat *matrix_new_output(rsvd_int nrows, rsvd_int ncols) {
     madvise(p, (bytes + align - 1) / align * align, MADV_HUGEPAGE);
     M->nrows = nrows;
     M->ncols = ncols;
-    M->d = (double *)p;
+    M->d = (real *)p;
     return M;
 }
 
@@ -131,8 +146,8 @@ struct PinnedStage {
 thread_local PinnedStage t_stage;
 
 // Host copy from the pinned stage into the (pageable) output, split over a few threads.
-void parallel_copy(double *dst, const double *src, size_t count) {
-    const size_t bytes = count * sizeof(double);
+void parallel_copy(real *dst, const real *src, size_t count) {
+    const size_t bytes = count * sizeof(real);
     const int nt = bytes < ((size_t)8 << 20) ? 1 : 8;
     if (nt == 1) {
         std::memcpy(dst, src, bytes);
@@ -142,7 +157,7 @@ void parallel_copy(double *dst, const double *src, size_t count) {
     const size_t per = (count + nt - 1) / nt;
     for (int t = 0; t < nt; t++) {
         const size_t a = std::min(count, (size_t)t * per), b = std::min(count, a + per);
-        if (a < b) th.emplace_back([=] { std::memcpy(dst + a, src + a, (b - a) * sizeof(double)); });
+        if (a < b) th.emplace_back([=] { std::memcpy(dst + a, src + a, (b - a) * sizeof(real)); });
     }
     for (auto &x : th) x.join();
 }
@@ -154,16 +169,16 @@ mat *download(DM<T> a) {
     if (!M) throw std::bad_alloc();
     if (a.r * a.c == 0) return M;
     const size_t count = (size_t)a.r * (size_t)a.c;
-    double *stage = (double *)t_stage.get(sizeof(double) * count);
-    if (std::is_same<T, double>::value) {
-        RSVD_CK(cudaMemcpy2DAsync(stage, sizeof(double) * a.r, a.p, sizeof(T) * a.ld, sizeof(double) * a.r, a.c,
+    real *stage = (real *)t_stage.get(sizeof(real) * count);
+    if (std::is_same<T, real>::value) {
+        RSVD_CK(cudaMemcpy2DAsync(stage, sizeof(real) * a.r, a.p, sizeof(T) * a.ld, sizeof(real) * a.r, a.c,
                                   cudaMemcpyDeviceToHost, s));
         RSVD_CK(cudaStreamSynchronize(s));
     } else {
-        DMat<double> tmp(a.r, a.c, s, false);
-        convert<T, double>(s, a, tmp.v);
-        RSVD_CK(cudaMemcpy2DAsync(stage, sizeof(double) * a.r, tmp.v.p, sizeof(double) * tmp.v.ld,
-                                  sizeof(double) * a.r, a.c, cudaMemcpyDeviceToHost, s));
+        DMat<real> tmp(a.r, a.c, s, false);
+        convert<T, real>(s, a, tmp.v);
+        RSVD_CK(cudaMemcpy2DAsync(stage, sizeof(real) * a.r, tmp.v.p, sizeof(real) * tmp.v.ld,
+                                  sizeof(real) * a.r, a.c, cudaMemcpyDeviceToHost, s));
         RSVD_CK(cudaStreamSynchronize(s));
     }
     parallel_copy(M->d, stage, count);
@@ -182,7 +197,7 @@ struct OutputPrefetch {
             M = matrix_new_output(r, c);
             if (!M) return;
             volatile char *b = (volatile char *)M->d;
-            const size_t bytes = sizeof(double) * (size_t)r * (size_t)c;
+            const size_t bytes = sizeof(real) * (size_t)r * (size_t)c;
             for (size_t off = 0; off < bytes; off += 4096) b[off] = 0;
         });
     }
@@ -199,22 +214,22 @@ struct OutputPrefetch {
         cudaStream_t s = ctx().stream;
         if (a.r * a.c == 0) return out;
         if (ctx().pageable_access) {
-            convert<T, double>(s, a, DM<double>{out->d, a.r, a.c, a.r});
+            convert<T, real>(s, a, DM<real>{out->d, a.r, a.c, a.r});
             RSVD_CK(cudaStreamSynchronize(s));
             return out;
         }
         const size_t count = (size_t)a.r * (size_t)a.c;
-        double *stage = (double *)t_stage.get(sizeof(double) * count);
-        DMat<double> tmp;
-        const double *src = (const double *)a.p;
+        real *stage = (real *)t_stage.get(sizeof(real) * count);
+        DMat<real> tmp;
+        const real *src = (const real *)a.p;
         long long lds = a.ld;
-        if (!std::is_same<T, double>::value) {
-            tmp = DMat<double>(a.r, a.c, s, false);
-            convert<T, double>(s, a, tmp.v);
+        if (!std::is_same<T, real>::value) {
+            tmp = DMat<real>(a.r, a.c, s, false);
+            convert<T, real>(s, a, tmp.v);
             src = tmp.v.p;
             lds = tmp.v.ld;
         }
-        RSVD_CK(cudaMemcpy2DAsync(stage, sizeof(double) * a.r, src, sizeof(double) * lds, sizeof(double) * a.r, a.c,
+        RSVD_CK(cudaMemcpy2DAsync(stage, sizeof(real) * a.r, src, sizeof(real) * lds, sizeof(real) * a.r, a.c,
                                   cudaMemcpyDeviceToHost, s));
         RSVD_CK(cudaStreamSynchronize(s));
         parallel_copy(out->d, stage, count);
@@ -225,13 +240,13 @@ struct OutputPrefetch {
 mat *diag_mat(const std::vector<double> &d) {
     const int k = (int)d.size();
     mat *S = matrix_new(k, k);
-    for (int i = 0; i < k; i++) S->d[(size_t)i * k + i] = d[(size_t)i];
+    for (int i = 0; i < k; i++) S->d[(size_t)i * k + i] = (real)d[(size_t)i];
     return S;
 }
 
 vec *index_vec(const std::vector<int> &I) {
     vec *v = vector_new((rsvd_int)I.size());
-    for (size_t i = 0; i < I.size(); i++) v->d[i] = (double)I[i];
+    for (size_t i = 0; i < I.size(); i++) v->d[i] = (real)I[i];
     return v;
 }
 
@@ -296,10 +311,11 @@ void run_blockrand(mat *M, int k, int p, double TOL, int vnum, int kstep, int q,
 }
 
 template <typename T>
-void run_qb(mat *M, int kstep, int nstep, double TOL, int q, int s, rsvd_int *frank, mat **Q, mat **B) {
+void run_qb(mat *M, int kstep, int nstep, double TOL, int q, int s, rsvd_int *frank, mat **Q, mat **B,
+            QbRule rule = QB_PB_NEW) {
     auto t0 = Clock::now();
     DMat<T> A = upload<T>(M);
-    QBOut<T> r = qb_blocked<T>(A.v, kstep, nstep, TOL, q, s);
+    QBOut<T> r = qb_blocked<T>(A.v, kstep, nstep, TOL, q, s, rule);
     *Q = download<T>(r.Q.v);
     *B = download<T>(r.B.v);
     if (frank) *frank = r.frank;
@@ -317,7 +333,7 @@ mat *matrix_new(rsvd_int nrows, rsvd_int ncols) {
     M->nrows = nrows;
     M->ncols = ncols;
     const size_t n = (size_t)(nrows > 0 ? nrows : 0) * (size_t)(ncols > 0 ? ncols : 0);
-    M->d = (double *)std::calloc(n ? n : 1, sizeof(double));
+    M->d = (real *)std::calloc(n ? n : 1, sizeof(real));
     return M;
 }
 
@@ -325,7 +341,7 @@ vec *vector_new(rsvd_int nrows) {
     vec *v = (vec *)std::malloc(sizeof(vec));
     if (!v) return nullptr;
     v->nrows = nrows;
-    v->d = (double *)std::calloc(nrows > 0 ? (size_t)nrows : 1, sizeof(double));
+    v->d = (real *)std::calloc(nrows > 0 ? (size_t)nrows : 1, sizeof(real));
     return v;
 }
 
@@ -341,13 +357,14 @@ void vector_delete(vec *v) {
     std::free(v);
 }
 
-void matrix_set_element(mat *M, rsvd_int i, rsvd_int j, double val) { M->d[(size_t)j * M->nrows + i] = val; }
-double matrix_get_element(mat *M, rsvd_int i, rsvd_int j) { return M->d[(size_t)j * M->nrows + i]; }
-void vector_set_element(vec *v, rsvd_int i, double val) { v->d[i] = val; }
-double vector_get_element(vec *v, rsvd_int i) { return v->d[i]; }
+void matrix_set_element(mat *M, rsvd_int i, rsvd_int j, real val) { M->d[(size_t)j * M->nrows + i] = val; }
+real matrix_get_element(mat *M, rsvd_int i, rsvd_int j) { return M->d[(size_t)j * M->nrows + i]; }
+void vector_set_element(vec *v, rsvd_int i, real val) { v->d[i] = val; }
+real vector_get_element(vec *v, rsvd_int i) { return v->d[i]; }
 
-// m, n as rsvd_int (int32; int64 in the 64-bit-index library, as the reference's 64-bit
-// variant writes them), then m*n doubles in row-major order (MVF:77-133)
+// m, n as rsvd_int (int32; int64 in the 64-bit-index and float libraries, as the reference's
+// 64-bit and oneAPI variants write them), then m*n values of the element type in row-major order
+// (MVF:77-133; oneapi_code/matrix_vector_functions_one_api.c:71-130)
 mat *matrix_load_from_binary_file(char *fname) {
     FILE *fp = std::fopen(fname, "rb");
     if (!fp) {
@@ -361,9 +378,9 @@ mat *matrix_load_from_binary_file(char *fname) {
         return nullptr;
     }
     mat *M = matrix_new(hdr[0], hdr[1]);
-    std::vector<double> row((size_t)hdr[1]);
+    std::vector<real> row((size_t)hdr[1]);
     for (rsvd_int i = 0; i < hdr[0]; i++) {
-        if (std::fread(row.data(), sizeof(double), (size_t)hdr[1], fp) != (size_t)hdr[1]) {
+        if (std::fread(row.data(), sizeof(real), (size_t)hdr[1], fp) != (size_t)hdr[1]) {
             std::fclose(fp);
             matrix_delete(M);
             set_error(RSVD_ERR_ARGUMENT, "truncated matrix file");
@@ -383,16 +400,16 @@ void matrix_write_to_binary_file(mat *M, char *fname) {
     }
     const rsvd_int hdr[2] = {M->nrows, M->ncols};
     std::fwrite(hdr, sizeof(rsvd_int), 2, fp);
-    std::vector<double> row((size_t)M->ncols);
+    std::vector<real> row((size_t)M->ncols);
     for (rsvd_int i = 0; i < M->nrows; i++) {
         for (rsvd_int j = 0; j < M->ncols; j++) row[(size_t)j] = M->d[(size_t)j * M->nrows + i];
-        std::fwrite(row.data(), sizeof(double), (size_t)M->ncols, fp);
+        std::fwrite(row.data(), sizeof(real), (size_t)M->ncols, fp);
     }
     std::fclose(fp);
 }
 
 void matrix_copy(mat *D, mat *S) {
-    std::memcpy(D->d, S->d, sizeof(double) * (size_t)S->nrows * (size_t)S->ncols);
+    std::memcpy(D->d, S->d, sizeof(real) * (size_t)S->nrows * (size_t)S->ncols);
 }
 
 void matrix_build_transpose(mat *Mt, mat *M) {
@@ -400,21 +417,35 @@ void matrix_build_transpose(mat *Mt, mat *M) {
         for (rsvd_int i = 0; i < M->nrows; i++) Mt->d[(size_t)i * Mt->nrows + j] = M->d[(size_t)j * M->nrows + i];
 }
 
-double get_matrix_frobenius_norm(mat *M) {
+// host reductions accumulate in double for either element type
+real get_matrix_frobenius_norm(mat *M) {
     double acc = 0.0;
     const size_t n = (size_t)M->nrows * (size_t)M->ncols;
-    for (size_t i = 0; i < n; i++) acc += M->d[i] * M->d[i];
-    return std::sqrt(acc);
+    for (size_t i = 0; i < n; i++) acc += (double)M->d[i] * (double)M->d[i];
+    return (real)std::sqrt(acc);
 }
 
-double get_percent_error_between_two_mats(mat *A, mat *B) {
-    double num = 0.0;
+real get_percent_error_between_two_mats(mat *A, mat *B) {
+    double num = 0.0, den = 0.0;
     const size_t n = (size_t)A->nrows * (size_t)A->ncols;
     for (size_t i = 0; i < n; i++) {
-        const double d = A->d[i] - B->d[i];
+        const double d = (double)A->d[i] - (double)B->d[i];
         num += d * d;
+        den += (double)A->d[i] * (double)A->d[i];
     }
-    return 100.0 * std::sqrt(num) / get_matrix_frobenius_norm(A);
+    return (real)(100.0 * std::sqrt(num) / std::sqrt(den));
+}
+
+// MVF:299-311
+real vector_get2norm(vec *v) {
+    double acc = 0.0;
+    for (rsvd_int i = 0; i < v->nrows; i++) acc += (double)v->d[i] * (double)v->d[i];
+    return (real)std::sqrt(acc);
+}
+
+// MVF:490-499: D(i,i) = data(i) for the rows of D; the rest of D is left as it is
+void initialize_diagonal_matrix(mat *D, vec *data) {
+    for (rsvd_int i = 0; i < D->nrows; i++) D->d[(size_t)i * D->nrows + i] = data->d[i];
 }
 
 double get_seconds_frac(struct timeval start_timeval, struct timeval end_timeval) {
@@ -429,7 +460,7 @@ void initialize_random_matrix(mat *M) {
         begin_call();
         DMat<double> Om = make_omega<double>(M->nrows, M->ncols);
         mat *tmp = download<double>(Om.v);
-        std::memcpy(M->d, tmp->d, sizeof(double) * (size_t)M->nrows * (size_t)M->ncols);
+        std::memcpy(M->d, tmp->d, sizeof(real) * (size_t)M->nrows * (size_t)M->ncols);
         matrix_delete(tmp);
     });
 }
@@ -442,7 +473,7 @@ static void host_gemm(const char *fn, bool ta, bool tb, mat *A, mat *B, mat *C) 
         DMat<double> dC(C->nrows, C->ncols, ctx().stream, false);
         gemm<double>(ctx().stream, ta, tb, 1.0, dA.v, dB.v, 0.0, dC.v);
         mat *r = download<double>(dC.v);
-        std::memcpy(C->d, r->d, sizeof(double) * (size_t)C->nrows * (size_t)C->ncols);
+        std::memcpy(C->d, r->d, sizeof(real) * (size_t)C->nrows * (size_t)C->ncols);
         matrix_delete(r);
     });
 }
@@ -484,7 +515,7 @@ void low_rank_svd_rand_decomp_fixed_rank(mat *M, rsvd_int k, rsvd_int p, rsvd_in
     });
 }
 
-void low_rank_svd_blockrand_decomp_fixed_rank_or_prec(mat *M, rsvd_int k, rsvd_int p, double TOL, rsvd_int vnum, rsvd_int kstep, rsvd_int q,
+void low_rank_svd_blockrand_decomp_fixed_rank_or_prec(mat *M, rsvd_int k, rsvd_int p, real TOL, rsvd_int vnum, rsvd_int kstep, rsvd_int q,
                                                       rsvd_int s, rsvd_int *frank, mat **U, mat **S, mat **V) {
     *U = *S = *V = nullptr;
     guarded("low_rank_svd_blockrand_decomp_fixed_rank_or_prec", [&] {
@@ -498,9 +529,10 @@ void low_rank_svd_blockrand_decomp_fixed_rank_or_prec(mat *M, rsvd_int k, rsvd_i
     });
 }
 
-void randQB_pb_new(mat *M, rsvd_int kstep, rsvd_int nstep, double TOL, rsvd_int q, rsvd_int s, rsvd_int *frank, mat **Q, mat **B) {
+static void qb_pb_new(const char *fn, mat *M, rsvd_int kstep, rsvd_int nstep, real TOL, rsvd_int q, rsvd_int s,
+                      rsvd_int *frank, mat **Q, mat **B) {
     *Q = *B = nullptr;
-    guarded("randQB_pb_new", [&] {
+    guarded(fn, [&] {
         check_mat(M);
         need_int(kstep, nstep, q, s);
         need(kstep >= 1, "need kstep >= 1");
@@ -512,6 +544,64 @@ void randQB_pb_new(mat *M, rsvd_int kstep, rsvd_int nstep, double TOL, rsvd_int 
         else run_qb<double>(M, kstep, nstep, TOL, q, s, frank, Q, B);
     });
 }
+
+void randQB_pb_new(mat *M, rsvd_int kstep, rsvd_int nstep, real TOL, rsvd_int q, rsvd_int s, rsvd_int *frank, mat **Q,
+                   mat **B) {
+    qb_pb_new("randQB_pb_new", M, kstep, nstep, TOL, q, s, frank, Q, B);
+}
+
+// oneapi_code/rank_revealing_algorithms_one_api.c:605-815: the randQB_pb_new algorithm
+void randQB_pb2(mat *M, rsvd_int kstep, rsvd_int nstep, real TOL, rsvd_int q, rsvd_int s, rsvd_int *frank, mat **Q,
+                mat **B) {
+    qb_pb_new("randQB_pb2", M, kstep, nstep, TOL, q, s, frank, Q, B);
+}
+
+// RRA:1425-1570 (one_api.c:451-600): nstep blocks, no TOL mode, no kstep rule, every block
+// after the first re-orthogonalised
+void randQB_pb(mat *M, rsvd_int kstep, rsvd_int nstep, rsvd_int q, rsvd_int s, mat **Q, mat **B) {
+    *Q = *B = nullptr;
+    guarded("randQB_pb", [&] {
+        check_mat(M);
+        need_int(kstep, nstep, q, s);
+        need(kstep >= 1 && nstep >= 1, "need kstep >= 1 and nstep >= 1");
+        need(q < 1 || s >= 1, "s must be >= 1");
+        need((long long)kstep * nstep <= (long long)std::min(M->nrows, M->ncols), "kstep * nstep exceeds min(m, n)");
+        begin_call();
+        if (use_fp32_path()) run_qb<float>(M, kstep, nstep, 0.0, q, s, nullptr, Q, B, QB_PB);
+        else run_qb<double>(M, kstep, nstep, 0.0, q, s, nullptr, Q, B, QB_PB);
+    });
+}
+
+// MVF:1214-1263: Householder QR with LAPACK's reflectors (FP64 on the device); Q m x n, and R
+// n x n whose upper triangle is written
+static void host_qr(const char *fn, mat *M, mat *Q, mat *R) {
+    guarded(fn, [&] {
+        check_mat(M);
+        need(Q != nullptr && Q->d != nullptr, "null Q");
+        need(M->nrows >= M->ncols, "QR needs rows >= columns");
+        need(Q->nrows == M->nrows && Q->ncols == M->ncols, "Q must be m x n");
+        if (R) need(R->d != nullptr && R->nrows == M->ncols && R->ncols == M->ncols, "R must be n x n");
+        begin_call();
+        auto t0 = Clock::now();
+        DMat<double> W = upload<double>(M);
+        const i64 n = M->ncols;
+        DMat<double> dQ(M->nrows, n, ctx().stream, false), dR(n, n, ctx().stream, true);
+        householder_qr<double>(ctx().stream, W.v, dQ.v, dR.v);
+        mat *hq = download<double>(dQ.v);
+        std::memcpy(Q->d, hq->d, sizeof(real) * (size_t)M->nrows * (size_t)n);
+        matrix_delete(hq);
+        if (R) {
+            mat *hr = download<double>(dR.v);
+            for (i64 j = 0; j < n; j++)
+                for (i64 i = 0; i <= j; i++) R->d[(size_t)j * n + i] = hr->d[(size_t)j * n + i];
+            matrix_delete(hr);
+        }
+        end_call(t0);
+    });
+}
+
+void compact_QR_factorization(mat *M, mat *Q, mat *R) { host_qr("compact_QR_factorization", M, Q, R); }
+void QR_factorization_getQ(mat *M, mat *Q) { host_qr("QR_factorization_getQ", M, Q, nullptr); }
 
 void pivotedQR_mkl(mat *M, mat **Q, mat **R, vec **I) {
     *Q = *R = nullptr;
@@ -529,7 +619,7 @@ void pivotedQR_mkl(mat *M, mat **Q, mat **R, vec **I) {
     });
 }
 
-void pivoted_QR_of_specified_rank_or_prec(mat *M, rsvd_int k, double TOL, rsvd_int *frank, mat **Qk, mat **Rk, vec **I) {
+void pivoted_QR_of_specified_rank_or_prec(mat *M, rsvd_int k, real TOL, rsvd_int *frank, mat **Qk, mat **Rk, vec **I) {
     *Qk = *Rk = nullptr;
     *I = nullptr;
     guarded("pivoted_QR_of_specified_rank_or_prec", [&] {
@@ -548,7 +638,7 @@ void pivoted_QR_of_specified_rank_or_prec(mat *M, rsvd_int k, double TOL, rsvd_i
     });
 }
 
-void id_decomp_fixed_rank_or_prec(mat *M, rsvd_int k, double TOL, rsvd_int *frank, vec **I, mat **T) {
+void id_decomp_fixed_rank_or_prec(mat *M, rsvd_int k, real TOL, rsvd_int *frank, vec **I, mat **T) {
     *I = nullptr;
     *T = nullptr;
     guarded("id_decomp_fixed_rank_or_prec", [&] {
@@ -584,7 +674,7 @@ void id_rand_decomp_fixed_rank(mat *M, rsvd_int k, rsvd_int p, rsvd_int q, rsvd_
     });
 }
 
-void id_blockrand_decomp_fixed_rank_or_prec(mat *M, rsvd_int k, rsvd_int p, double TOL, rsvd_int kstep, rsvd_int q, rsvd_int s, rsvd_int *frank,
+void id_blockrand_decomp_fixed_rank_or_prec(mat *M, rsvd_int k, rsvd_int p, real TOL, rsvd_int kstep, rsvd_int q, rsvd_int s, rsvd_int *frank,
                                             vec **I, mat **T) {
     *I = nullptr;
     *T = nullptr;
@@ -643,7 +733,7 @@ static void two_sided_outputs(TwoSidedOut &r, vec **Icol, vec **Irow, mat **T, m
     *S = download<double>(r.S.v);
 }
 
-void id_two_sided_decomp_fixed_rank_or_prec(mat *M, rsvd_int k, double TOL, rsvd_int *frank, vec **Icol, vec **Irow, mat **T,
+void id_two_sided_decomp_fixed_rank_or_prec(mat *M, rsvd_int k, real TOL, rsvd_int *frank, vec **Icol, vec **Irow, mat **T,
                                             mat **S) {
     *Icol = *Irow = nullptr;
     *T = *S = nullptr;
@@ -679,7 +769,7 @@ void id_two_sided_rand_decomp_fixed_rank(mat *M, rsvd_int k, rsvd_int p, rsvd_in
     });
 }
 
-void id_two_sided_blockrand_decomp_fixed_rank_or_prec(mat *M, rsvd_int k, rsvd_int p, double TOL, rsvd_int kstep, rsvd_int q, rsvd_int s,
+void id_two_sided_blockrand_decomp_fixed_rank_or_prec(mat *M, rsvd_int k, rsvd_int p, real TOL, rsvd_int kstep, rsvd_int q, rsvd_int s,
                                                       rsvd_int *frank, vec **Icol, vec **Irow, mat **T, mat **S) {
     *Icol = *Irow = nullptr;
     *T = *S = nullptr;
@@ -704,7 +794,7 @@ static void cur_outputs(CurOut &r, mat **C, mat **U, mat **R) {
     *R = download<double>(r.R.v);
 }
 
-void cur_decomp_fixed_rank_or_prec(mat *M, rsvd_int k, double TOL, rsvd_int *frank, mat **C, mat **U, mat **R) {
+void cur_decomp_fixed_rank_or_prec(mat *M, rsvd_int k, real TOL, rsvd_int *frank, mat **C, mat **U, mat **R) {
     *C = *U = *R = nullptr;
     guarded("cur_decomp_fixed_rank_or_prec", [&] {
         check_mat(M);
@@ -738,7 +828,7 @@ void cur_rand_decomp_fixed_rank(mat *M, rsvd_int k, rsvd_int p, rsvd_int q, rsvd
     });
 }
 
-void cur_blockrand_decomp_fixed_rank_or_prec(mat *M, rsvd_int k, rsvd_int p, double TOL, rsvd_int kstep, rsvd_int q, rsvd_int s, rsvd_int *frank,
+void cur_blockrand_decomp_fixed_rank_or_prec(mat *M, rsvd_int k, rsvd_int p, real TOL, rsvd_int kstep, rsvd_int q, rsvd_int s, rsvd_int *frank,
                                              mat **C, mat **U, mat **R) {
     *C = *U = *R = nullptr;
     guarded("cur_blockrand_decomp_fixed_rank_or_prec", [&] {
@@ -1076,7 +1166,7 @@ void use_pivoted_QR_decomp_for_approximation(mat *M, mat *Qk, mat *Rk, vec *I) {
     matrix_matrix_mult(Qk, Rk, QR);
     // (Qk Rk) P^T : column j of the product goes back to column I[j]
     for (rsvd_int j = 0; j < n; j++)
-        std::memcpy(QRPt->d + (size_t)((rsvd_int)I->d[j]) * m, QR->d + (size_t)j * m, sizeof(double) * m);
+        std::memcpy(QRPt->d + (size_t)((rsvd_int)I->d[j]) * m, QR->d + (size_t)j * m, sizeof(real) * m);
     std::printf("percent_error between M and QkRkPt = %f\n", get_percent_error_between_two_mats(M, QRPt));
     matrix_delete(Qk);
     matrix_delete(Rk);
@@ -1111,7 +1201,7 @@ void use_id_decomp_for_approximation(mat *M, mat *T, vec *I, rsvd_int k) {
     const rsvd_int m = M->nrows, n = M->ncols;
     mat *V = id_basis(T, I, k);
     mat *MI = matrix_new(m, k);
-    for (rsvd_int c = 0; c < k; c++) std::memcpy(MI->d + (size_t)c * m, M->d + (size_t)((rsvd_int)I->d[c]) * m, sizeof(double) * m);
+    for (rsvd_int c = 0; c < k; c++) std::memcpy(MI->d + (size_t)c * m, M->d + (size_t)((rsvd_int)I->d[c]) * m, sizeof(real) * m);
     mat *MA = matrix_new(m, n);
     matrix_matrix_transpose_mult(MI, V, MA);
     std::printf("norm(M,fro) = %f\n", get_matrix_frobenius_norm(M));

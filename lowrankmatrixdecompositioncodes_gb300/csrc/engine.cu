@@ -430,13 +430,13 @@ template SvdOut<float> svd_fixed_rank<float>(DM<float>, int, int, int, int, int)
 
 // ------------------------------------------------------------------ blocked QB (RRA:1576-1801)
 template <typename T>
-static QBOut<T> qb_plain(DM<T> A, int kstep, int nstep, double TOL, int q, int s_) {
+static QBOut<T> qb_plain(DM<T> A, int kstep, int nstep, double TOL, int q, int s_, QbRule rule) {
     Ctx &cx = ctx();
     cudaStream_t s = cx.stream;
     const i64 m = A.r, n = A.c, mn = std::min(m, n);
-    if (kstep > (int)(mn / 2)) kstep = (int)mn / 10;                      // RRA:1589-1592
+    if (rule == QB_PB_NEW && kstep > (int)(mn / 2)) kstep = (int)mn / 10;   // RRA:1589-1592
     if (kstep <= 0) fail(RSVD_ERR_ARGUMENT, "randQB_pb_new: block size collapses to zero");
-    const bool tol_mode = nstep <= 0;
+    const bool tol_mode = rule == QB_PB_NEW && nstep <= 0;
     if (tol_mode) nstep = (int)(mn / kstep);
     const i64 l = (i64)kstep * nstep;
     DMat<T> Om = make_omega<T>(n, l);
@@ -458,7 +458,7 @@ static QBOut<T> qb_plain(DM<T> A, int kstep, int nstep, double TOL, int q, int s
             else prod<T>(s, false, false, T(1), Aw.v, AtQp.v, T(0), Yp.v);
         }
         orth<T>(Yp.v, Qp.v, nullptr, 2);
-        if (step > 0 && step % 2 == 0) {                                  // RRA:1703-1732
+        if (step > 0 && (rule == QB_PB || step % 2 == 0)) {               // RRA:1703-1732, RRA:1500
             DM<T> Qj = out.Q.v.cols(0, c0);
             DMat<T> QjtQp(c0, kstep, s, false);
             prod<T>(s, true, false, T(1), Qj, Qp.v, T(0), QjtQp.v);
@@ -694,11 +694,11 @@ static bool learned_qb(DM<float> A, double TOL, QBOut<float> &out, int *q_used) 
 }
 
 template <typename T>
-QBOut<T> qb_blocked(DM<T> A, int kstep, int nstep, double TOL, int q, int s_) {
+QBOut<T> qb_blocked(DM<T> A, int kstep, int nstep, double TOL, int q, int s_, QbRule rule) {
     Ctx &cx = ctx();
     cx.timing.learned_path = 0;
     if constexpr (std::is_same<T, float>::value) {
-        if (nstep <= 0 && cx.opts.learned && proposal_model() != nullptr) {
+        if (rule == QB_PB_NEW && nstep <= 0 && cx.opts.learned && proposal_model() != nullptr) {
             QBOut<float> out;
             int q_used = 0;
             if (learned_qb(A, TOL, out, &q_used)) {
@@ -708,10 +708,10 @@ QBOut<T> qb_blocked(DM<T> A, int kstep, int nstep, double TOL, int q, int s_) {
             cx.timing.learned_path = 2;                                   // fell back
         }
     }
-    return qb_plain<T>(A, kstep, nstep, TOL, q, s_);
+    return qb_plain<T>(A, kstep, nstep, TOL, q, s_, rule);
 }
-template QBOut<double> qb_blocked<double>(DM<double>, int, int, double, int, int);
-template QBOut<float> qb_blocked<float>(DM<float>, int, int, double, int, int);
+template QBOut<double> qb_blocked<double>(DM<double>, int, int, double, int, int, QbRule);
+template QBOut<float> qb_blocked<float>(DM<float>, int, int, double, int, int, QbRule);
 
 // ------------------------------------------------------------------ blocked rSVD (RRA:239-381)
 template <typename T>

@@ -66,8 +66,13 @@ template <typename T>
 SvdOut<T> svd_fixed_rank(DM<T> A, int k, int p, int vnum, int q, int s);
 template <typename T>
 SvdOut<T> svd_blockrand(DM<T> A, int k, int p, double TOL, int vnum, int kstep, int q, int s, int *frank);
+// Blocked QB rules: randQB_pb_new / randQB_pb2 (RRA:1576-1801, oneapi_code
+// rank_revealing_algorithms_one_api.c:605-815: kstep above min(m,n)/2 shrinks to min(m,n)/10,
+// nstep <= 0 selects the TOL mode, re-orthogonalisation on even steps) or randQB_pb (RRA:1425-1570,
+// one_api.c:451-600: fixed rank, no kstep rule, re-orthogonalisation on every step after the first).
+enum QbRule { QB_PB_NEW = 0, QB_PB = 1 };
 template <typename T>
-QBOut<T> qb_blocked(DM<T> A, int kstep, int nstep, double TOL, int q, int s);
+QBOut<T> qb_blocked(DM<T> A, int kstep, int nstep, double TOL, int q, int s, QbRule rule = QB_PB_NEW);
 
 PivQROut pivoted_qr_full(DM<double> A);
 PivQROut pivoted_qr_partial(DM<double> A, int k, double TOL);

@@ -175,6 +175,9 @@ void trsm_left_upper(cudaStream_t s, DM<double> R, DM<double> B, DM<double> X);
 // One-sided Jacobi SVD of square G (n x n, FP64): G = U diag(sv) V^T, sorted descending.
 // G is overwritten.  U, V: n x n.  Returns the sweep count.
 int jacobi_svd(cudaStream_t s, DM<double> G, DM<double> U, DM<double> V, double *d_sv, int *d_flag);
+// Default precision mode of the reference API of this library (defined by its api.cu build).
+int api_default_precision();
+
 // Householder QR of a tall matrix: Q (r x c) explicit, R (c x c) upper.  FP64/FP32 tall data.
 template <typename T>
 void householder_qr(cudaStream_t s, DM<T> Y, DM<T> Q, DM<double> R);

@@ -40,7 +40,7 @@ rsvdpack_opts g_opts;
 void init_opts_locked() {
     if (g_opts_init) return;
     std::memset(&g_opts, 0, sizeof g_opts);
-    g_opts.precision = RSVD_PREC_FP64;
+    g_opts.precision = api_default_precision();   // FP64; FP32 in the float-data library
     g_opts.use_provider = 1;
     g_opts.seed = 0x5EED5EEDull;
     g_opts.verbose = 0;

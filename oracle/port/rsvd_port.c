@@ -330,13 +330,16 @@ void low_rank_svd_rand_decomp_fixed_rank(mat *M, int k, int p, int vnum, int q, 
     matrix_delete(Yo); matrix_delete(Zo); matrix_delete(Q);
 }
 
-/* ===================== blocked randQB (RRA:1576-1801) ===================== */
-void randQB_pb_new(mat *M, int kstep, int nstep, double TOL, int q, int s, int *frank,
-                   mat **Q, mat **B)
+/* ===================== blocked randQB (RRA:1576-1801; randQB_pb RRA:1425-1570) =====================
+ * every_step = 0: randQB_pb_new (kstep rule, TOL mode when nstep <= 0, re-orthogonalisation on even
+ * steps); every_step = 1: randQB_pb (fixed rank, no kstep rule, re-orthogonalisation on every step
+ * after the first, RRA:1500). */
+static void qb_blocked_port(mat *M, int kstep, int nstep, double TOL, int q, int s, int *frank,
+                            mat **Q, mat **B, int every_step)
 {
     int m = M->nrows, n = M->ncols;
-    if (kstep > (int)(MIN(m, n) / 2)) kstep = (int)MIN(m, n) / 10;     /* RRA:1589-1592 */
-    int tol_mode = (nstep <= 0);
+    if (!every_step && kstep > (int)(MIN(m, n) / 2)) kstep = (int)MIN(m, n) / 10;   /* RRA:1589-1592 */
+    int tol_mode = !every_step && (nstep <= 0);
     if (tol_mode) nstep = (int)(MIN(m, n) / kstep);                    /* RRA:1595-1602 */
     int l = kstep * nstep;
     mat *Om = matrix_new(n, l);
@@ -355,10 +358,14 @@ void randQB_pb_new(mat *M, int kstep, int nstep, double TOL, int q, int s, int *
         for (int j = 1; j <= q; j++) {
             if ((2 * j - 2) % s == 0) {
                 orth_q(Yp, Qp);
-                gemm_tn(Qp, A, QptA);
-                mat *t = transpose(QptA);
-                memcpy(AtQp->d, t->d, nel(t) * sizeof(double));
-                matrix_delete(t);
+                if (every_step) {
+                    gemm_tn(A, Qp, AtQp);                                  /* RRA:1475 */
+                } else {
+                    gemm_tn(Qp, A, QptA);
+                    mat *t = transpose(QptA);
+                    memcpy(AtQp->d, t->d, nel(t) * sizeof(double));
+                    matrix_delete(t);
+                }
             } else {
                 gemm_tn(A, Yp, AtQp);
             }
@@ -366,8 +373,9 @@ void randQB_pb_new(mat *M, int kstep, int nstep, double TOL, int q, int s, int *
             else gemm_nn(A, AtQp, Yp);
         }
         orth_q(Yp, Qp);
-        /* RRA:1703-1732: re-orthogonalise against earlier blocks on even steps only */
-        if (step > 0 && step % 2 == 0) {
+        /* RRA:1703-1732: re-orthogonalise against earlier blocks on even steps only
+         * (randQB_pb: every step, RRA:1500-1524) */
+        if (step > 0 && (every_step || step % 2 == 0)) {
             int c = step * kstep;
             mat *Qj = cols(*Q, 0, c), *QjtQp = matrix_new(c, kstep), *QjQjtQp = matrix_new(m, kstep);
             gemm_tn(Qj, Qp, QjtQp);
@@ -393,6 +401,18 @@ void randQB_pb_new(mat *M, int kstep, int nstep, double TOL, int q, int s, int *
     matrix_delete(A); matrix_delete(Om); matrix_delete(Yp); matrix_delete(Qp);
     matrix_delete(Bp); matrix_delete(QpBp); matrix_delete(AtQp); matrix_delete(AtQp2);
     matrix_delete(QptA);
+}
+
+void randQB_pb_new(mat *M, int kstep, int nstep, double TOL, int q, int s, int *frank,
+                   mat **Q, mat **B)
+{
+    qb_blocked_port(M, kstep, nstep, TOL, q, s, frank, Q, B, 0);
+}
+
+void randQB_pb(mat *M, int kstep, int nstep, int q, int s, mat **Q, mat **B)
+{
+    int frank = 0;
+    qb_blocked_port(M, kstep, nstep, 0.0, q, s, &frank, Q, B, 1);
 }
 
 /* ===================== blocked rSVD (RRA:239-381) ===================== */

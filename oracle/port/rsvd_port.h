@@ -40,6 +40,7 @@ void low_rank_svd_blockrand_decomp_fixed_rank_or_prec(mat *M, int k, int p, doub
                                                       int *frank, mat **U, mat **S, mat **V);
 void randQB_pb_new(mat *M, int kstep, int nstep, double TOL, int q, int s, int *frank,
                    mat **Q, mat **B);
+void randQB_pb(mat *M, int kstep, int nstep, int q, int s, mat **Q, mat **B);
 void pivotedQR_mkl(mat *M, mat **Q, mat **R, vec **I);
 void pivoted_QR_of_specified_rank_or_prec(mat *M, int k, double TOL, int *frank,
                                           mat **Qk, mat **Rk, vec **I);

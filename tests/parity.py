@@ -16,6 +16,8 @@ KINDS = {
     "low_rank_svd_rand_decomp_fixed_rank": ("cols", "f", "cols"),
     "low_rank_svd_blockrand_decomp_fixed_rank_or_prec": ("cols", "f", "cols", "int"),
     "randQB_pb_new": ("cols", "rows", "int"),
+    "randQB_pb2": ("cols", "rows", "int"),
+    "randQB_pb": ("cols", "rows"),
     "pivotedQR_mkl": ("cols", "rows", "idx"),
     "pivoted_QR_of_specified_rank_or_prec": ("cols", "rows", "idx", "int"),
     "id_decomp_fixed_rank_or_prec": ("idx", "f", "int"),

@@ -32,6 +32,8 @@ RANDOM_CASES = [
     ("low_rank_svd_rand_decomp_fixed_rank", (25, 7, 2, 3, 1)),
     ("low_rank_svd_blockrand_decomp_fixed_rank_or_prec", (30, 5, 0.0, 1, 10, 2, 1)),
     ("randQB_pb_new", (10, 0, 1e-3, 1, 1)),
+    ("randQB_pb", (10, 4, 1, 1)),
+    ("randQB_pb", (8, 5, 2, 2)),
     ("id_rand_decomp_fixed_rank", (25, 5, 2, 1)),
     ("id_two_sided_rand_decomp_fixed_rank", (25, 5, 1, 1)),
     ("cur_rand_decomp_fixed_rank", (25, 5, 2, 1)),
