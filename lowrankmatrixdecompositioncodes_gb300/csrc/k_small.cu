@@ -500,12 +500,28 @@ __global__ void colnorm_kernel_t(const S *W, long long ldw, int n, double *sv) {
         if (lane == 0) sv[j] = sqrt(a);
     }
 }
+// Descending rank of each value (ties by index).  The values are norms (>= +0), whose IEEE bit
+// patterns order like the values as 64-bit integers: integer compares, because GB300's FP64
+// pipe is a small fraction of its integer rate (FP64 compares made this step ~40 us at n = 272).
+// Each block stages all n keys in shared memory (n <= RANK_SMEM_MAX) and ranks its slice.
+constexpr int RANK_SMEM_MAX = 6144;
 __global__ void rank_desc_kernel(const double *sv, int n, int *rank) {
+    extern __shared__ long long s_key[];
+    const bool staged = n <= RANK_SMEM_MAX;
+    const long long *gkey = reinterpret_cast<const long long *>(sv);
+    if (staged) {
+        for (int i = threadIdx.x; i < n; i += blockDim.x) s_key[i] = gkey[i];
+        __syncthreads();
+    }
+    const long long *key = staged ? s_key : gkey;
     const int j = blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= n) return;
-    const double v = sv[j];
+    const long long v = key[j];
     int r = 0;
-    for (int i = 0; i < n; i++) r += (sv[i] > v) || (sv[i] == v && i < j);
+    for (int i = 0; i < n; i++) {
+        const long long w = key[i];
+        r += (w > v) | ((w == v) & (i < j));
+    }
     rank[j] = r;
 }
 // U(:, rank j) = W(:, j) / sv_j ; V(:, rank j) = Vacc(:, j)  (or, without Vacc, left for the caller)
@@ -631,7 +647,7 @@ int jacobi_small(cudaStream_t s, DM<double> G, DM<double> U, DM<double> V, doubl
         jacobi_kernel_t<S><<<1, 1024, 0, s>>>(W, ld, Vacc, ld, n, tol, 40, d_sweeps, d_flag);
     }
     colnorm_kernel_t<S><<<ceil_div(n, 8), 256, 0, s>>>(W, ld, n, d_raw);
-    rank_desc_kernel<<<ceil_div(n, 256), 256, 0, s>>>(d_raw, n, d_rank);
+    rank_desc_kernel<<<ceil_div(n, 256), 256, n <= RANK_SMEM_MAX ? sizeof(long long) * n : 0, s>>>(d_raw, n, d_rank);
     scatter_kernel_t<S><<<gfor((long long)n * n), 256, 0, s>>>(W, ld, Vacc, ld, d_raw, d_rank, n, U.p, U.ld, V.p, V.ld,
                                                                  d_sv);
     RSVD_LAUNCH_CK();
