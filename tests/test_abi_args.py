@@ -1,0 +1,67 @@
+"""Argument checks of the driver-facing entry points (randQB_pb, randQB_pb2, the QR helpers) in
+all three libraries: bad shapes and parameters are reported through rsvdpack_last_error()
+(RSVD_ERR_ARGUMENT) with NULL outputs, before any device work -- the reference leaves them
+undefined (rank_revealing_algorithms_intel_mkl.c:1425, matrix_vector_functions_intel_mkl.c:1214-1263).
+No GPU needed."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from lowrankmatrixdecompositioncodes_gb300 import load_engine, load_engine64, load_engine_f32
+
+LOADERS = {"int": load_engine, "int64": load_engine64, "f32": load_engine_f32}
+
+
+@pytest.fixture(params=sorted(LOADERS))
+def lib(request):
+    return LOADERS[request.param]()
+
+
+def _err(eng):
+    code, msg = eng.last_error()
+    return code, msg
+
+
+@pytest.mark.parametrize("kstep,nstep,why", [(0, 2, "kstep"), (4, 0, "nstep"), (8, 2, "exceeds")])
+def test_randQB_pb_rejects_bad_blocks(lib, kstep, nstep, why):
+    M = lib.to_mat(np.ones((12, 10)))
+    Q, B = lib.PMat(), lib.PMat()
+    lib.lib.randQB_pb(M, kstep, nstep, 1, 1, C.byref(Q), C.byref(B))
+    code, msg = _err(lib)
+    assert code == 1 and why in msg
+    assert not Q and not B
+    lib.lib.matrix_delete(M)
+
+
+def test_randQB_pb2_checks_like_randQB_pb_new(lib):
+    M = lib.to_mat(np.ones((12, 10)))
+    Q, B, fr = lib.PMat(), lib.PMat(), lib.Int(0)
+    lib.lib.randQB_pb2(M, 0, 1, 0.0, 1, 1, C.byref(fr), C.byref(Q), C.byref(B))
+    code, msg = _err(lib)
+    assert code == 1 and "randQB_pb2" in msg and "kstep" in msg
+    assert not Q and not B
+    lib.lib.matrix_delete(M)
+
+
+def test_qr_helpers_check_shapes(lib):
+    L = lib.lib
+    L.compact_QR_factorization.argtypes = [lib.PMat, lib.PMat, lib.PMat]
+    L.QR_factorization_getQ.argtypes = [lib.PMat, lib.PMat]
+    M = lib.to_mat(np.ones((8, 5)))
+    Qbad, R = L.matrix_new(8, 4), L.matrix_new(5, 5)
+    L.compact_QR_factorization(M, Qbad, R)
+    code, msg = _err(lib)
+    assert code == 1 and "Q must be m x n" in msg
+    Q, Rbad = L.matrix_new(8, 5), L.matrix_new(4, 4)
+    L.compact_QR_factorization(M, Q, Rbad)
+    code, msg = _err(lib)
+    assert code == 1 and "R must be n x n" in msg
+    W, QW = lib.to_mat(np.ones((3, 5))), L.matrix_new(3, 5)
+    L.QR_factorization_getQ(W, QW)
+    code, msg = _err(lib)
+    assert code == 1 and "rows >= columns" in msg
+    # the caller's buffers are untouched by a rejected call
+    assert np.all(lib.from_mat(Q, free=False) == 0) and np.all(lib.from_mat(R, free=False) == 0)
+    for x in (M, Qbad, R, Q, Rbad, W, QW):
+        L.matrix_delete(x)
