@@ -149,6 +149,36 @@ def measured_peaks():
         return 6800.0, 1900.0, "fallback"
 
 
+def solve_roofline(m, n, k, l, q, s, vnum, esize, ms, hbm_gbs, tensor_tflops):
+    """Whole-solve roofline of one fixed-rank rSVD (the reference's semantics: q - 1 power
+    rounds, an orthonormalisation where (2j-2) % s == 0 / (2j-1) % s == 0).  Algorithmic work:
+      products: 2q passes over A (Y = A Omega, 2(q-1) power products, B^T = A^T Q), each
+                2 m n l flops and m n esize bytes;
+      QR:       4 r l^2 flops per orthonormalisation of an r x l basis (the Householder count;
+                the engine's CholeskyQR2 is charged the same);
+      l x l:    22 l^3 (nominal SVD count) and the factor products 2 (m + n) l k.
+    roofline time = max(flops / tensor peak, bytes / HBM peak); frac = roofline / measured."""
+    orth_rows = []
+    for j in range(1, q):
+        if (2 * j - 2) % s == 0:
+            orth_rows.append(m)
+        if (2 * j - 1) % s == 0:
+            orth_rows.append(n)
+    orth_rows.append(m)
+    if vnum == 1 or vnum > 2:
+        orth_rows.append(n)
+    passes = 2 * q
+    flops = (passes * 2.0 * m * n * l + sum(4.0 * r * l * l for r in orth_rows)
+             + 22.0 * l ** 3 + 2.0 * (m + n) * l * k)
+    nbytes = passes * float(m) * n * esize
+    t_flops = flops / (tensor_tflops * 1e12) * 1e3
+    t_bytes = nbytes / (hbm_gbs * 1e9) * 1e3
+    t_roof = max(t_flops, t_bytes)
+    return {"flops": flops, "bytes": nbytes, "passes": passes, "roofline_ms": t_roof,
+            "bound": "tensor" if t_flops >= t_bytes else "hbm", "measured_ms": ms, "frac": t_roof / ms,
+            "tensor_peak_tflops": tensor_tflops, "hbm_peak_gbs": hbm_gbs}
+
+
 def cpu_solve_seconds(A_host, threads, repeats=1):
     """Time the CPU oracle (oracle/port) on the workload; returns seconds per solve."""
     from lowrankmatrixdecompositioncodes_gb300.capi import RsvdLibrary, SeededOmega
@@ -510,6 +540,11 @@ def run_ours(args):
             "kernel": "sketch product " + ("(tcgen05, one A*X and one A^T*X launch)" if mixed else "(CUDA-core GEMM)"),
             "tflops": 2.0 * m * n * l * len(forms) / tot_ms / 1e9, "tensor_peak_tflops": tc_peak, "forms": forms,
             "solve_phases_ms": phases}
+    # the whole solve against its own roofline (A's FP32 bytes per pass; the TF32 dense rate
+    # taken as half the measured BF16 rate)
+    roof["solve"] = (solve_roofline(m, n, k, l, Q, S_ORTH, VNUM, 4, ms, hbm_peak,
+                                    tc_peak / 2.0 if args.precision == "tf32" else tc_peak)
+                     if mixed else None)
 
     # ---------------- the plain FP32 GPU form of the same method (CUDA-core GEMMs, no
     # tensor cores), same matrix and sizes: the comparison point for the mixed modes

@@ -48,3 +48,21 @@ def test_reference_arm_runs_on_rank_zero_only():
                         "--steps", "1", "--warmup", "0"], capture_output=True, text=True, env=env, timeout=300)
     assert r.returncode == 0, r.stderr[-500:]
     assert r.stdout.strip() == ""
+
+
+def test_solve_roofline_of_the_headline_workload():
+    """The whole-solve roofline bench.py reports: 16384 x 8192, l = 272, q = 2 (4 passes over A),
+    s = 1, vnum = 1 (four orthonormalisations), FP32 A, the measured peaks of the pool."""
+    import bench
+    r = bench.solve_roofline(16384, 8192, 256, 272, 2, 1, 1, 4, 5.35, 6791.0, 1935.3 / 2)
+    m, n, l, k = 16384, 8192, 272, 256
+    want = 4 * 2.0 * m * n * l + 4.0 * l * l * (2 * m + 2 * n) + 22.0 * l ** 3 + 2.0 * (m + n) * l * k
+    assert r["passes"] == 4 and abs(r["flops"] - want) < 1e-6 * want
+    assert r["bytes"] == 4 * m * n * 4
+    assert r["bound"] == "tensor" and 0.3 < r["roofline_ms"] < 0.34
+    assert abs(r["frac"] - r["roofline_ms"] / 5.35) < 1e-12
+    # q = 3, s = 2: power rounds j = 1, 2 orthonormalise at 2j - 2 = 0, 2 only
+    r2 = bench.solve_roofline(1000, 500, 10, 20, 3, 2, 2, 8, 1.0, 6791.0, 1935.3)
+    assert r2["passes"] == 6
+    assert abs(r2["flops"] - (6 * 2.0 * 1000 * 500 * 20 + 4.0 * 400 * (1000 + 1000 + 1000)
+                              + 22.0 * 20 ** 3 + 2.0 * 1500 * 20 * 10)) < 1e-3
