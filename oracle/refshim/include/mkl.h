@@ -15,6 +15,7 @@
 #include <stdlib.h>
 #include <string.h>
 #include <math.h>
+#include <omp.h>   /* the oneAPI variant's sources call omp_get_wtime without including it */
 
 #ifdef __cplusplus
 extern "C" {
@@ -78,6 +79,60 @@ lapack_int refshim_LAPACKE_dgeqp3(int layout, lapack_int m, lapack_int n, double
 #define LAPACKE_dsyev  scipy_LAPACKE_dsyev
 #define LAPACKE_dtrtri scipy_LAPACKE_dtrtri
 #define LAPACKE_dgesv  scipy_LAPACKE_dgesv
+
+/* Single precision and MKL service calls, used by the oneAPI variant's sources
+ * (oneapi_code/matrix_vector_functions_one_api.c, rank_revealing_algorithms_one_api.c),
+ * compiled into oracle/_ref/librsvd_ref_f32.so the same way. */
+void scipy_cblas_sgemm(int layout, int transa, int transb, int m, int n, int k,
+                       float alpha, const float *a, int lda, const float *b, int ldb,
+                       float beta, float *c, int ldc);
+void scipy_cblas_sgemv(int layout, int trans, int m, int n, float alpha,
+                       const float *a, int lda, const float *x, int incx,
+                       float beta, float *y, int incy);
+void scipy_cblas_strsm(int layout, int side, int uplo, int transa, int diag,
+                       int m, int n, float alpha, const float *a, int lda,
+                       float *b, int ldb);
+void scipy_cblas_strsv(int layout, int uplo, int trans, int diag, int n,
+                       const float *a, int lda, float *x, int incx);
+lapack_int scipy_LAPACKE_sgeqrf(int layout, lapack_int m, lapack_int n, float *a,
+                                lapack_int lda, float *tau);
+lapack_int scipy_LAPACKE_sorgqr(int layout, lapack_int m, lapack_int n, lapack_int k,
+                                float *a, lapack_int lda, const float *tau);
+lapack_int scipy_LAPACKE_sgeqp3(int layout, lapack_int m, lapack_int n, float *a,
+                                lapack_int lda, lapack_int *jpvt, float *tau);
+lapack_int scipy_LAPACKE_sgesvd(int layout, char jobu, char jobvt, lapack_int m,
+                                lapack_int n, float *a, lapack_int lda, float *s,
+                                float *u, lapack_int ldu, float *vt, lapack_int ldvt,
+                                float *superb);
+lapack_int scipy_LAPACKE_ssyev(int layout, char jobz, char uplo, lapack_int n,
+                               float *a, lapack_int lda, float *w);
+lapack_int scipy_LAPACKE_sgesv(int layout, lapack_int n, lapack_int nrhs, float *a,
+                               lapack_int lda, lapack_int *ipiv, float *b, lapack_int ldb);
+/* the oneAPI pivotedQR_mkl passes an uninitialised jpvt too (one_api.c:830,844) */
+lapack_int refshim_LAPACKE_sgeqp3(int layout, lapack_int m, lapack_int n, float *a,
+                                  lapack_int lda, lapack_int *jpvt, float *tau);
+
+#define cblas_sgemm    scipy_cblas_sgemm
+#define cblas_sgemv    scipy_cblas_sgemv
+#define cblas_strsm    scipy_cblas_strsm
+#define cblas_strsv    scipy_cblas_strsv
+#define LAPACKE_sgeqrf scipy_LAPACKE_sgeqrf
+#define LAPACKE_sorgqr scipy_LAPACKE_sorgqr
+#define LAPACKE_sgeqp3 refshim_LAPACKE_sgeqp3
+#define LAPACKE_sgesvd scipy_LAPACKE_sgesvd
+#define LAPACKE_ssyev  scipy_LAPACKE_ssyev
+#define LAPACKE_sgesv  scipy_LAPACKE_sgesv
+
+/* MKL service functions: aligned allocation (calloc'd, as the reference relies on zeroed
+ * matrices) and the wall-clock timer */
+static inline void *mkl_calloc(size_t num, size_t size, int alignment)
+{
+    (void)alignment;
+    return calloc(num ? num : 1, size);
+}
+static inline void mkl_free(void *p) { free(p); }
+double refshim_seconds(void);
+#define dsecnd refshim_seconds
 
 #ifdef __cplusplus
 }

@@ -6,7 +6,8 @@
  *  - VSL replacement (see include/mkl_vsl.h): each vsRngGaussian request is
  *    served by the registered Gaussian-test-matrix provider, so a harness can
  *    hand the reference exactly the sketch matrices it hands the GPU engine.
- *  - LAPACKE_dgeqp3 wrapper that clears jpvt (see include/mkl.h).
+ *  - LAPACKE_dgeqp3 / LAPACKE_sgeqp3 wrappers that clear jpvt (see include/mkl.h).
+ *  - dsecnd (MKL's timer) for the oneAPI variant's sources.
  *  - Thread control for OpenBLAS and OpenMP, for timed CPU baselines.
  *
  * The provider ABI is shared with the port (oracle/port) and the GPU engine
@@ -100,3 +101,12 @@ lapack_int refshim_LAPACKE_dgeqp3(int layout, lapack_int m, lapack_int n, double
     for (lapack_int j = 0; j < n; j++) jpvt[j] = 0;
     return scipy_LAPACKE_dgeqp3(layout, m, n, a, lda, jpvt, tau);
 }
+
+lapack_int refshim_LAPACKE_sgeqp3(int layout, lapack_int m, lapack_int n, float *a,
+                                  lapack_int lda, lapack_int *jpvt, float *tau)
+{
+    for (lapack_int j = 0; j < n; j++) jpvt[j] = 0;
+    return scipy_LAPACKE_sgeqp3(layout, m, n, a, lda, jpvt, tau);
+}
+
+double refshim_seconds(void) { return omp_get_wtime(); }
