@@ -94,6 +94,9 @@ rsvd_real get_matrix_frobenius_norm(mat *M);                      /* :116-117 */
 rsvd_real get_percent_error_between_two_mats(mat *A, mat *B);     /* :288-289 */
 rsvd_real vector_get2norm(vec *v);                                /* :83 */
 void initialize_diagonal_matrix(mat *D, vec *data);               /* :199: D(i,i) = data(i) */
+void initialize_identity_matrix(mat *D);                          /* :204 (diagonal bounded by min(m, n)) */
+void matrix_get_col(mat *M, rsvd_int j, vec *column_vec);          /* :158 */
+void matrix_set_col(mat *M, rsvd_int j, vec *column_vec);          /* :161 */
 void initialize_random_matrix(mat *M);                            /* :128-129 */
 void matrix_matrix_mult(mat *A, mat *B, mat *C);                  /* :132-133 */
 void matrix_transpose_matrix_mult(mat *A, mat *B, mat *C);        /* :136-137 */
@@ -105,7 +108,11 @@ void compact_QR_factorization(mat *M, mat *Q, mat *R);
 void QR_factorization_getQ(mat *M, mat *Q);
 void form_svd_product_matrix(mat *U, mat *S, mat *V, mat *P);     /* :343-344 */
 void form_cur_product_matrix(mat *C, mat *U, mat *R, mat *P);     /* :346-347 */
+#if defined(RSVDPACK_REAL32)
+rsvd_real get_seconds_frac(rsvd_real start, rsvd_real end);  /* one_api.h:367: end - start (omp_get_wtime values) */
+#else
 double get_seconds_frac(struct timeval start_timeval, struct timeval end_timeval); /* :359-360 */
+#endif
 
 /* ---- decompositions: rank_revealing_algorithms_intel_mkl.h ---- */
 /* :5  fixed-rank randomized SVD.  q means q-1 rounds of (M M^T); vnum 1 (or >2): QR of
@@ -132,6 +139,10 @@ void pivotedQR_mkl(mat *M, mat **Q, mat **R, vec **I);
 /* :52 partial pivoted Householder QR of rank k, or of precision TOL when k <= 0 */
 void pivoted_QR_of_specified_rank_or_prec(mat *M, rsvd_int k, rsvd_real TOL, rsvd_int *frank,
                                           mat **Qk, mat **Rk, vec **I);
+/* :47 partial pivoted Householder QR of rank k >= 1 (rank_revealing_algorithms_intel_mkl.c
+ *     :1012-1157): the rank-or-precision routine's rank mode, except that only an exactly vanished
+ *     pivot column ends it early (RRA:1069; the other stops below 1e-10, RRA:1250) */
+void pivoted_QR_of_specified_rank(mat *M, rsvd_int k, rsvd_int *frank, mat **Qk, mat **Rk, vec **I);
 /* :73 column ID, T = Rk1^-1 Rk2 */
 void id_decomp_fixed_rank_or_prec(mat *M, rsvd_int k, rsvd_real TOL, rsvd_int *frank, vec **I, mat **T);
 /* :76 randomized column ID (row sketch (k+p) x n, q power rounds) */

@@ -72,6 +72,7 @@ def _algos(_I, PMat, PVec, _D=C.c_double):
         "randQB_pb": [PMat, _I, _I, _I, _I, _PPM, _PPM],
         "pivotedQR_mkl": [PMat, _PPM, _PPM, _PPV],
         "pivoted_QR_of_specified_rank_or_prec": [PMat, _I, _D, _PI, _PPM, _PPM, _PPV],
+        "pivoted_QR_of_specified_rank": [PMat, _I, _PI, _PPM, _PPM, _PPV],
         "id_decomp_fixed_rank_or_prec": [PMat, _I, _D, _PI, _PPV, _PPM],
         "id_rand_decomp_fixed_rank": [PMat, _I, _I, _I, _I, _PPV, _PPM],
         "id_blockrand_decomp_fixed_rank_or_prec": [PMat, _I, _I, _D, _I, _I, _I, _PI, _PPV, _PPM],
@@ -317,6 +318,15 @@ class RsvdLibrary:
         try:
             self.lib.pivoted_QR_of_specified_rank_or_prec(
                 M, k, float(TOL), C.byref(fr), C.byref(Q), C.byref(R), C.byref(I))
+        finally:
+            self.lib.matrix_delete(M)
+        return self.from_mat(Q), self.from_mat(R), self.from_vec(I), fr.value
+
+    def pivoted_QR_of_specified_rank(self, A, k):
+        M = self.to_mat(A)
+        Q, R, I, fr = self.PMat(), self.PMat(), self.PVec(), self.Int(-1)
+        try:
+            self.lib.pivoted_QR_of_specified_rank(M, k, C.byref(fr), C.byref(Q), C.byref(R), C.byref(I))
         finally:
             self.lib.matrix_delete(M)
         return self.from_mat(Q), self.from_mat(R), self.from_vec(I), fr.value

@@ -448,11 +448,31 @@ void initialize_diagonal_matrix(mat *D, vec *data) {
     for (rsvd_int i = 0; i < D->nrows; i++) D->d[(size_t)i * D->nrows + i] = data->d[i];
 }
 
+// MVF:504-515: D = I (the reference writes D(i,i) for every row; here the diagonal stops at
+// min(m, n), inside the matrix)
+void initialize_identity_matrix(mat *D) {
+    std::memset(D->d, 0, sizeof(real) * (size_t)D->nrows * (size_t)D->ncols);
+    for (rsvd_int i = 0; i < std::min(D->nrows, D->ncols); i++) D->d[(size_t)i * D->nrows + i] = (real)1;
+}
+
+// MVF:582-604: column j of M to / from a vector of M->nrows entries
+void matrix_get_col(mat *M, rsvd_int j, vec *column_vec) {
+    std::memcpy(column_vec->d, M->d + (size_t)j * M->nrows, sizeof(real) * (size_t)M->nrows);
+}
+void matrix_set_col(mat *M, rsvd_int j, vec *column_vec) {
+    std::memcpy(M->d + (size_t)j * M->nrows, column_vec->d, sizeof(real) * (size_t)M->nrows);
+}
+
+#if defined(RSVDPACK_REAL32)
+// oneapi_code/matrix_vector_functions_one_api.c:1511-1513
+real get_seconds_frac(real start, real end) { return end - start; }
+#else
 double get_seconds_frac(struct timeval start_timeval, struct timeval end_timeval) {
     const long secs = end_timeval.tv_sec - start_timeval.tv_sec;
     const long micros = secs * 1000000 + end_timeval.tv_usec - start_timeval.tv_usec;
     return micros / 1e6;
 }
+#endif
 
 void initialize_random_matrix(mat *M) {
     guarded("initialize_random_matrix", [&] {
@@ -630,6 +650,25 @@ void pivoted_QR_of_specified_rank_or_prec(mat *M, rsvd_int k, real TOL, rsvd_int
         auto t0 = Clock::now();
         DMat<double> A = upload<double>(M);
         PivQROut r = pivoted_qr_partial(A.v, k, TOL);
+        *Qk = download<double>(r.Q.v);
+        *Rk = download<double>(r.R.v);
+        *I = index_vec(r.I);
+        if (frank) *frank = r.frank;
+        end_call(t0);
+    });
+}
+
+void pivoted_QR_of_specified_rank(mat *M, rsvd_int k, rsvd_int *frank, mat **Qk, mat **Rk, vec **I) {
+    *Qk = *Rk = nullptr;
+    *I = nullptr;
+    guarded("pivoted_QR_of_specified_rank", [&] {
+        check_mat(M);
+        need_int(k);
+        need(k >= 1 && k <= std::min(M->nrows, M->ncols), "need 1 <= k <= min(m, n)");
+        begin_call();
+        auto t0 = Clock::now();
+        DMat<double> A = upload<double>(M);
+        PivQROut r = pivoted_qr_partial(A.v, k, 0.0, 0.0);
         *Qk = download<double>(r.Q.v);
         *Rk = download<double>(r.R.v);
         *I = index_vec(r.I);

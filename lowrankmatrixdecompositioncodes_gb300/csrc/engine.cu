@@ -765,7 +765,7 @@ PivQROut pivoted_qr_full(DM<double> A) {
     return out;
 }
 
-PivQROut pivoted_qr_partial(DM<double> A, int k, double TOL) {
+PivQROut pivoted_qr_partial(DM<double> A, int k, double TOL, double zero_tol) {
     // RRA:1159-1334 : the reference's own pivoting; Qk = first frank columns of the
     // accumulated reflectors, Rk = first frank rows of the transformed matrix
     Ctx &cx = ctx();
@@ -777,7 +777,7 @@ PivQROut pivoted_qr_partial(DM<double> A, int k, double TOL) {
     copy_dm<double>(s, A, R.v);
     DMat<double> Qk(m, std::max(1, k), s, false);
     DBuf jb(sizeof(int) * std::max<i64>(1, n), s);
-    const int f = pivqr_rsvdpack(s, R.v, Qk.v, k, TOL, tol_mode, (int *)jb.get());
+    const int f = pivqr_rsvdpack(s, R.v, Qk.v, k, TOL, tol_mode, (int *)jb.get(), zero_tol);
     PivQROut out;
     out.frank = f;
     out.Q = DMat<double>(m, f, s, false);

@@ -75,7 +75,7 @@ template <typename T>
 QBOut<T> qb_blocked(DM<T> A, int kstep, int nstep, double TOL, int q, int s, QbRule rule = QB_PB_NEW);
 
 PivQROut pivoted_qr_full(DM<double> A);
-PivQROut pivoted_qr_partial(DM<double> A, int k, double TOL);
+PivQROut pivoted_qr_partial(DM<double> A, int k, double TOL, double zero_tol = 1e-10);
 IdOut id_det(DM<double> A, int k, double TOL);
 IdOut id_rand(DM<double> A, int k, int p, int q, int s);
 IdOut id_blockrand(DM<double> A, int k, int p, double TOL, int kstep, int q, int s);

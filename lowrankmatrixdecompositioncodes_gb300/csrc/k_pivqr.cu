@@ -199,7 +199,7 @@ __global__ void sqnorm_kernel(const double *A, i64 ld, i64 m, int n, double *nrm
 
 __global__ void __launch_bounds__(1024) rsvdpack_select_kernel(double *R, i64 ld, i64 m, int n, int i, double *nrm,
                                                                int *perm, double *H, i64 ldh, PivCtl *ctl,
-                                                               int tol_mode, double TOL) {
+                                                               int tol_mode, double TOL, double zero_tol) {
     __shared__ double sc[32];
     if (ctl->stop) return;
     double bv;
@@ -221,7 +221,10 @@ __global__ void __launch_bounds__(1024) rsvdpack_select_kernel(double *R, i64 ld
     __syncthreads();
     int stop = 0;
     if (threadIdx.x == 0) {
-        if (fabs(nrm[pvt]) < 1e-10 && i > 0) stop = 1;
+        // a vanished pivot column ends the factorisation: |norm| < 1e-10 (RRA:1250), or exactly
+        // zero for the rank-only form (zero_tol = 0, RRA:1069)
+        const bool vanished = zero_tol > 0.0 ? fabs(nrm[pvt]) < zero_tol : nrm[pvt] == 0.0;
+        if (vanished && i > 0) stop = 1;
         else if (tol_mode && ctl->r22 < TOL) stop = 1;
         if (stop) ctl->stop = 1;
         else { ctl->frank = i + 1; ctl->pvt = pvt; }
@@ -372,7 +375,8 @@ void form_q_from_reflectors(cudaStream_t s, DM<double> A, const double *d_tau, i
     RSVD_LAUNCH_CK();
 }
 
-int pivqr_rsvdpack(cudaStream_t s, DM<double> R, DM<double> Qk, int k, double TOL, bool tol_mode, int *d_jpvt) {
+int pivqr_rsvdpack(cudaStream_t s, DM<double> R, DM<double> Qk, int k, double TOL, bool tol_mode, int *d_jpvt,
+                   double zero_tol) {
     const i64 m = R.r;
     const int n = (int)R.c;
     DBuf nb(sizeof(double) * std::max(1, n), s);
@@ -383,7 +387,8 @@ int pivqr_rsvdpack(cudaStream_t s, DM<double> R, DM<double> Qk, int k, double TO
     DMat<double> H(m, std::max(1, k), s);
     sqnorm_kernel<<<ceil_div(n, 128), 128, 0, s>>>(R.p, R.ld, m, n, nrm, d_jpvt);
     for (int i = 0; i < k; i++) {
-        rsvdpack_select_kernel<<<1, 1024, 0, s>>>(R.p, R.ld, m, n, i, nrm, d_jpvt, H.v.p, H.v.ld, ctl, tol_mode ? 1 : 0, TOL);
+        rsvdpack_select_kernel<<<1, 1024, 0, s>>>(R.p, R.ld, m, n, i, nrm, d_jpvt, H.v.p, H.v.ld, ctl, tol_mode ? 1 : 0, TOL,
+                                                    zero_tol);
         rsvdpack_apply_kernel<<<ceil_div((i64)n * 32, 256), 256, 0, s>>>(R.p, R.ld, m, n, i, nrm, H.v.p, H.v.ld, ctl);
     }
     RSVD_LAUNCH_CK();

@@ -190,9 +190,11 @@ void pivqr_lapack(cudaStream_t s, DM<double> A, double *d_tau, int *d_jpvt);
 // Form Q (m x qc) from the reflectors stored in A (dorgqr).
 void form_q_from_reflectors(cudaStream_t s, DM<double> A, const double *d_tau, int nrefl, DM<double> Q);
 // The reference's own partial pivoted QR (rank_revealing_algorithms_intel_mkl.c:1159-1334).
-// Returns frank; fills Q (m x m workspace) and R (m x n) in place.
+// Returns frank; fills Q (m x m workspace) and R (m x n) in place.  zero_tol: a pivot column
+// whose squared norm is below it ends the factorisation (1e-10, RRA:1250); 0 means exactly zero
+// (the rank-only pivoted_QR_of_specified_rank, RRA:1069).
 int pivqr_rsvdpack(cudaStream_t s, DM<double> R, DM<double> Q, int k, double TOL, bool tol_mode,
-                   int *d_jpvt);
+                   int *d_jpvt, double zero_tol = 1e-10);
 // Solve A X = B in place (B <- X) by LU with partial pivoting (dgesv); false if singular.
 bool lu_solve(cudaStream_t s, DM<double> A, DM<double> B, int *d_flag);
 // G = Y^T Y (c x c, FP64) for tall Y: FP64 products for double data; for float data,

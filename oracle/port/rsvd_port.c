@@ -456,12 +456,15 @@ void pivotedQR_mkl(mat *M, mat **Q, mat **R, vec **I)
     free(tau);
 }
 
-/* ===================== deterministic partial pivoted QR (RRA:1159-1334) ===================== */
-void pivoted_QR_of_specified_rank_or_prec(mat *M, int k, double TOL, int *frank,
-                                          mat **Qk, mat **Rk, vec **I)
+/* ===================== deterministic partial pivoted QR (RRA:1159-1334) =====================
+ * exact_zero = 0: pivoted_QR_of_specified_rank_or_prec, a pivot column whose squared norm is
+ * below 1e-10 ends it (RRA:1250); exact_zero = 1: the rank-only pivoted_QR_of_specified_rank
+ * (RRA:1012-1157), which stops only on an exactly zero one (RRA:1069) and has no TOL mode. */
+static void pivqr_partial_port(mat *M, int k, double TOL, int *frank, mat **Qk, mat **Rk, vec **I,
+                               int exact_zero)
 {
     int m = M->nrows, n = M->ncols;
-    int tol_mode = (k <= 0);
+    int tol_mode = !exact_zero && (k <= 0);
     if (tol_mode) k = MIN(m, n);
     mat *Qf = matrix_new(m, m), *R = dup(M), *H = matrix_new(m, 1);
     mat *QHHt = matrix_new(m, m), *HtR = matrix_new(1, n), *HHtR = matrix_new(m, n);
@@ -489,7 +492,7 @@ void pivoted_QR_of_specified_rank_or_prec(mat *M, int k, double TOL, int *frank,
                 r22 = sqrt(r22) / n;
             }
         }
-        if (fabs(nrm[piv]) < 1e-10 && i > 0) break;
+        if ((exact_zero ? nrm[piv] == 0.0 : fabs(nrm[piv]) < 1e-10) && i > 0) break;
         if (tol_mode && r22 < TOL) break;
         *frank = i + 1;
         double t = (*I)->d[i]; (*I)->d[i] = (*I)->d[piv]; (*I)->d[piv] = t;
@@ -516,6 +519,17 @@ void pivoted_QR_of_specified_rank_or_prec(mat *M, int k, double TOL, int *frank,
     matrix_delete(Qf); matrix_delete(R); matrix_delete(H); matrix_delete(QHHt);
     matrix_delete(HtR); matrix_delete(HHtR); matrix_delete(QH);
     free(nrm);
+}
+
+void pivoted_QR_of_specified_rank_or_prec(mat *M, int k, double TOL, int *frank,
+                                          mat **Qk, mat **Rk, vec **I)
+{
+    pivqr_partial_port(M, k, TOL, frank, Qk, Rk, I, 0);
+}
+
+void pivoted_QR_of_specified_rank(mat *M, int k, int *frank, mat **Qk, mat **Rk, vec **I)
+{
+    pivqr_partial_port(M, k, 0.0, frank, Qk, Rk, I, 1);
 }
 
 /* T = triu(Rk(:,1:r))^{-1} Rk(:,r+1:end) (RRA:1838-1850 and repeats) */

@@ -42,6 +42,7 @@ void randQB_pb_new(mat *M, int kstep, int nstep, double TOL, int q, int s, int *
                    mat **Q, mat **B);
 void randQB_pb(mat *M, int kstep, int nstep, int q, int s, mat **Q, mat **B);
 void pivotedQR_mkl(mat *M, mat **Q, mat **R, vec **I);
+void pivoted_QR_of_specified_rank(mat *M, int k, int *frank, mat **Qk, mat **Rk, vec **I);
 void pivoted_QR_of_specified_rank_or_prec(mat *M, int k, double TOL, int *frank,
                                           mat **Qk, mat **Rk, vec **I);
 void id_decomp_fixed_rank_or_prec(mat *M, int k, double TOL, int *frank, vec **I, mat **T);

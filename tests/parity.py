@@ -20,6 +20,7 @@ KINDS = {
     "randQB_pb": ("cols", "rows"),
     "pivotedQR_mkl": ("cols", "rows", "idx"),
     "pivoted_QR_of_specified_rank_or_prec": ("cols", "rows", "idx", "int"),
+    "pivoted_QR_of_specified_rank": ("cols", "rows", "idx", "int"),
     "id_decomp_fixed_rank_or_prec": ("idx", "f", "int"),
     "id_rand_decomp_fixed_rank": ("idx", "f"),
     "id_blockrand_decomp_fixed_rank_or_prec": ("idx", "f", "int"),

@@ -65,3 +65,36 @@ def test_qr_helpers_check_shapes(lib):
     assert np.all(lib.from_mat(Q, free=False) == 0) and np.all(lib.from_mat(R, free=False) == 0)
     for x in (M, Qbad, R, Q, Rbad, W, QW):
         L.matrix_delete(x)
+
+
+def test_identity_and_column_helpers(lib):
+    """initialize_identity_matrix, matrix_get_col, matrix_set_col (MVF:504-515, 582-604)."""
+    L = lib.lib
+    L.initialize_identity_matrix.argtypes = [lib.PMat]
+    L.matrix_get_col.argtypes = [lib.PMat, lib.Int, lib.PVec]
+    L.matrix_set_col.argtypes = [lib.PMat, lib.Int, lib.PVec]
+    D = lib.to_mat(np.full((5, 3), 9.0))
+    L.initialize_identity_matrix(D)
+    assert np.array_equal(lib.from_mat(D, free=False), np.eye(5, 3, dtype=lib.dtype))
+    v = L.vector_new(5)
+    for i in range(5):
+        v.contents.d[i] = i + 0.5
+    L.matrix_set_col(D, 2, v)
+    w = L.vector_new(5)
+    L.matrix_get_col(D, 2, w)
+    assert [w.contents.d[i] for i in range(5)] == [i + 0.5 for i in range(5)]
+    got = lib.from_mat(D)
+    assert np.array_equal(got[:, 2], np.arange(5) + 0.5) and got[0, 0] == 1 and got[1, 1] == 1
+    L.vector_delete(v)
+    L.vector_delete(w)
+
+
+def test_rank_only_pivoted_qr_checks_k(lib):
+    M = lib.to_mat(np.ones((6, 4)))
+    Q, R, I, fr = lib.PMat(), lib.PMat(), lib.PVec(), lib.Int(0)
+    for k in (0, 5):
+        lib.lib.pivoted_QR_of_specified_rank(M, k, C.byref(fr), C.byref(Q), C.byref(R), C.byref(I))
+        code, msg = _err(lib)
+        assert code == 1 and "1 <= k" in msg
+        assert not Q and not R and not I
+    lib.lib.matrix_delete(M)

@@ -69,3 +69,26 @@ def test_reference_quirks_are_kept(port):
     assert port.omega_calls() == 1
     sv = np.linalg.svd(A, compute_uv=False)[:10]
     assert np.allclose(np.diag(S)[:4], sv[:4], rtol=1e-3)
+
+
+def test_rank_only_pivoted_qr_stops_only_on_exact_zero(ref, port):
+    """pivoted_QR_of_specified_rank stops early only on an exactly vanished pivot column
+    (rank_revealing_algorithms_intel_mkl.c:1069); the rank-or-precision routine below 1e-10
+    (:1250).  A rank-5 matrix plus columns of squared norm ~1e-12: the first stops at k, the
+    second after five steps.  The port matches the reference with identical pivots and ranks, and
+    factors to 1e-12 (the reference's column norms come from an OpenMP reduction whose order
+    depends on the thread count)."""
+    g = np.random.default_rng(17)
+    B = g.standard_normal((60, 5)) @ g.standard_normal((5, 7))
+    A = np.hstack([B, 1e-7 * g.standard_normal((60, 3))])
+    outs = {}
+    for name, lib in (("ref", ref), ("port", port)):
+        outs[name] = (lib.pivoted_QR_of_specified_rank(A, 8), lib.pivoted_QR_of_specified_rank_or_prec(A, 8, 0.0))
+    (r1, p1), (r2, p2) = outs["ref"], outs["port"]
+    assert r1[3] == 8 and p1[3] == 5
+    compare_outputs("pivoted_QR_of_specified_rank", r2, r1, rtol=1e-12)
+    compare_outputs("pivoted_QR_of_specified_rank_or_prec", p2, p1, rtol=1e-12)
+    # and on a full-rank matrix, rank 12 of 110 columns
+    A = spectrum_matrix(150, 110, 0.97 ** np.arange(110), seed=3)
+    compare_outputs("pivoted_QR_of_specified_rank", port.pivoted_QR_of_specified_rank(A, 12),
+                    ref.pivoted_QR_of_specified_rank(A, 12), rtol=1e-12)
