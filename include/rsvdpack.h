@@ -18,8 +18,8 @@
  * outputs are set to NULL and rsvdpack_last_error() reports a non-zero code.
  *
  * Part 2 holds additive extensions (precision modes, sketch-matrix provider,
- * device-resident entry points, residual reporting).  They have no counterpart
- * in the reference unless stated.
+ * device-resident entry points, batched and learned paths, per-call timing).  They have
+ * no counterpart in the reference unless stated.
  */
 #ifndef RSVDPACK_H
 #define RSVDPACK_H
