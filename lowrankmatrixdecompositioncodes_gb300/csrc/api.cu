@@ -19,7 +19,7 @@
 
 using namespace rsvd;
 
-// Host element type of this build's mat / vec: double, or float in the oneAPI-variant library.
+// Host element type of the library being compiled: double, or float in the oneAPI-variant one.
 using real = rsvd_real;
 
 namespace rsvd {
