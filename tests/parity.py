@@ -30,6 +30,8 @@ KINDS = {
     "cur_decomp_fixed_rank_or_prec": ("f", "f", "f", "int"),
     "cur_rand_decomp_fixed_rank": ("f", "f", "f"),
     "cur_blockrand_decomp_fixed_rank_or_prec": ("f", "f", "f", "int"),
+    "low_rank_svd_rand_decomp_fromQB": ("cols", "f", "cols"),
+    "id_rand_decomp_fromQB": ("idx", "f"),
 }
 
 

@@ -97,3 +97,64 @@ def test_qb_split_matches_the_port(port, ref_f32):
     I2, T2 = ref_f32.id_rand_decomp_fromQB(Q, B)
     assert np.array_equal(I1, I2.astype(np.float64))
     assert np.max(np.abs(T2 - T1)) < 1e-3 * np.abs(T1).max()
+
+
+# ---------------------------------------------------------------- float golden fixtures
+GOLDEN_F32 = os.path.join(ROOT, "tests", "golden", "f32")
+
+
+def _golden_f32():
+    import json
+    with open(os.path.join(GOLDEN_F32, "index.json")) as f:
+        return json.load(f)
+
+
+def _load_f32(key, meta):
+    z = np.load(os.path.join(GOLDEN_F32, key + ".npz"))
+    outs = [z[f"out{i}"] for i in range(meta["n_out"])]
+    if meta["matrix"] is None:
+        return (z["Q"], z["B"]), outs, []
+    A = np.load(os.path.join(GOLDEN_F32, meta["matrix"]))["A"]
+    return (A,), outs, [z[f"omega{i}"] for i in range(meta["n_omega"])]
+
+
+F32_KEYS = sorted(_golden_f32())
+# the MKL-variant name of each oneAPI routine
+MKL_NAME = {"randQB_pb2": "randQB_pb_new"}
+
+
+@pytest.mark.parametrize("key", F32_KEYS)
+def test_oneapi_reference_reproduces_float_golden(ref_f32, key):
+    from lowrankmatrixdecompositioncodes_gb300.capi import ListOmega
+    from parity import compare_outputs
+    meta = _golden_f32()[key]
+    inputs, want, omegas = _load_f32(key, meta)
+    ref_f32.set_omega(ListOmega(omegas))
+    got = getattr(ref_f32, meta["routine"])(*inputs, *meta["args"])
+    got = got if isinstance(got, tuple) else (got,)
+    compare_outputs(meta["routine"].replace("randQB_pb2", "randQB_pb_new"), got, want, rtol=1e-5)
+
+
+@pytest.mark.parametrize("key", F32_KEYS)
+def test_port_matches_float_golden_to_single_precision(port, key):
+    """On every machine: the oracle port (the MKL variant's algorithms, FP64) replayed on the float
+    fixtures' inputs and test matrices gives the oneAPI reference's float outputs to single-precision
+    rounding -- identical pivots and ranks, factors to 2e-3 of each output's largest entry."""
+    from lowrankmatrixdecompositioncodes_gb300.capi import ListOmega
+    from parity import compare_outputs
+    meta = _golden_f32()[key]
+    inputs, want, omegas = _load_f32(key, meta)
+    routine = MKL_NAME.get(meta["routine"], meta["routine"])
+    port.set_omega(ListOmega(omegas))
+    got = getattr(port, routine)(*[x.astype(np.float64) for x in inputs], *meta["args"])
+    got = got if isinstance(got, tuple) else (got,)
+    want = [np.asarray(w, dtype=np.float64) for w in want]
+    if routine == "pivotedQR_mkl":
+        # a full factorisation of a matrix whose spectrum spans 1e-6: in single precision the
+        # reflectors after |R_ii| falls below ~1e-3 |R_00| act on rounding noise, so the leading
+        # part (pivots, Q columns, R rows) is what the two precisions share
+        Q, R, I = got
+        r = int(np.sum(np.abs(np.diag(R)) > 1e-3 * abs(R[0, 0])))
+        got = (Q[:, :r], R[:r, :], I[:r])
+        want = [want[0][:, :r], want[1][:r, :], want[2][:r]]
+    compare_outputs(routine, got, want, rtol=2e-3)
