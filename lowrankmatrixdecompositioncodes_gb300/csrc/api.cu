@@ -362,6 +362,8 @@ real matrix_get_element(mat *M, rsvd_int i, rsvd_int j) { return M->d[(size_t)j 
 void vector_set_element(vec *v, rsvd_int i, real val) { v->d[i] = val; }
 real vector_get_element(vec *v, rsvd_int i) { return v->d[i]; }
 
+constexpr rsvd_int FILE_ROWS = 64;   // rows per block of the binary-file transposition
+
 // m, n as rsvd_int (int32; int64 in the 64-bit-index and float libraries, as the reference's
 // 64-bit and oneAPI variants write them), then m*n values of the element type in row-major order
 // (MVF:77-133; oneapi_code/matrix_vector_functions_one_api.c:71-130)
@@ -377,16 +379,30 @@ mat *matrix_load_from_binary_file(char *fname) {
         set_error(RSVD_ERR_ARGUMENT, "bad matrix file header");
         return nullptr;
     }
-    mat *M = matrix_new(hdr[0], hdr[1]);
-    std::vector<real> row((size_t)hdr[1]);
-    for (rsvd_int i = 0; i < hdr[0]; i++) {
-        if (std::fread(row.data(), sizeof(real), (size_t)hdr[1], fp) != (size_t)hdr[1]) {
+    const rsvd_int m = hdr[0], n = hdr[1];
+    mat *M = matrix_new_output(m, n);     // every entry is written below
+    if (!M) {
+        std::fclose(fp);
+        set_error(RSVD_ERR_ALLOC, "host allocation failed");
+        return nullptr;
+    }
+    // FILE_ROWS rows at a time, transposed by FILE_ROWS x FILE_ROWS tiles into the column-major
+    // matrix: every write is a contiguous run of a column
+    std::vector<real> blk((size_t)FILE_ROWS * (size_t)n);
+    for (rsvd_int i0 = 0; i0 < m; i0 += FILE_ROWS) {
+        const rsvd_int nb = std::min<rsvd_int>(FILE_ROWS, m - i0);
+        if (std::fread(blk.data(), sizeof(real), (size_t)nb * n, fp) != (size_t)nb * n) {
             std::fclose(fp);
             matrix_delete(M);
             set_error(RSVD_ERR_ARGUMENT, "truncated matrix file");
             return nullptr;
         }
-        for (rsvd_int j = 0; j < hdr[1]; j++) M->d[(size_t)j * hdr[0] + i] = row[(size_t)j];
+        for (rsvd_int j0 = 0; j0 < n; j0 += FILE_ROWS)
+            for (rsvd_int j = j0; j < std::min<rsvd_int>(n, j0 + FILE_ROWS); j++) {
+                real *dst = M->d + (size_t)j * m + i0;
+                const real *src = blk.data() + j;
+                for (rsvd_int r = 0; r < nb; r++) dst[r] = src[(size_t)r * n];
+            }
     }
     std::fclose(fp);
     return M;
@@ -399,11 +415,18 @@ void matrix_write_to_binary_file(mat *M, char *fname) {
         return;
     }
     const rsvd_int hdr[2] = {M->nrows, M->ncols};
+    const rsvd_int m = M->nrows, n = M->ncols;
     std::fwrite(hdr, sizeof(rsvd_int), 2, fp);
-    std::vector<real> row((size_t)M->ncols);
-    for (rsvd_int i = 0; i < M->nrows; i++) {
-        for (rsvd_int j = 0; j < M->ncols; j++) row[(size_t)j] = M->d[(size_t)j * M->nrows + i];
-        std::fwrite(row.data(), sizeof(real), (size_t)M->ncols, fp);
+    std::vector<real> blk((size_t)FILE_ROWS * (size_t)n);
+    for (rsvd_int i0 = 0; i0 < m; i0 += FILE_ROWS) {
+        const rsvd_int nb = std::min<rsvd_int>(FILE_ROWS, m - i0);
+        for (rsvd_int j0 = 0; j0 < n; j0 += FILE_ROWS)
+            for (rsvd_int j = j0; j < std::min<rsvd_int>(n, j0 + FILE_ROWS); j++) {
+                const real *src = M->d + (size_t)j * m + i0;
+                real *dst = blk.data() + j;
+                for (rsvd_int r = 0; r < nb; r++) dst[(size_t)r * n] = src[r];
+            }
+        std::fwrite(blk.data(), sizeof(real), (size_t)nb * n, fp);
     }
     std::fclose(fp);
 }
