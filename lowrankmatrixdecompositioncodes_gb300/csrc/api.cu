@@ -13,6 +13,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <thread>
+#include <utility>
 #include <vector>
 
 #include <sys/mman.h>
@@ -123,6 +124,43 @@ mat *matrix_new_output(rsvd_int nrows, rsvd_int ncols) {
     M->ncols = ncols;
     M->d = (real *)p;
     return M;
+}
+
+// Host reductions over whole matrices: a fixed split into REDUCE_CHUNKS contiguous chunks, each
+// summed in double by one of up to 16 threads, the chunk sums then added in chunk order -- the
+// result does not depend on the thread count.  f(i) returns the (num, den) terms of element i.
+constexpr int REDUCE_CHUNKS = 64;
+template <typename F>
+std::pair<double, double> host_reduce(size_t n, F f) {
+    std::vector<double> num(REDUCE_CHUNKS, 0.0), den(REDUCE_CHUNKS, 0.0);
+    auto run = [&](int c) {
+        const size_t a = n * (size_t)c / REDUCE_CHUNKS, b = n * (size_t)(c + 1) / REDUCE_CHUNKS;
+        double x = 0.0, y = 0.0;
+        for (size_t i = a; i < b; i++) {
+            const auto t = f(i);
+            x += t.first;
+            y += t.second;
+        }
+        num[(size_t)c] = x;
+        den[(size_t)c] = y;
+    };
+    const int nt = n < ((size_t)1 << 20) ? 1 : (int)std::min<unsigned>(16, std::max(1u, std::thread::hardware_concurrency()));
+    if (nt == 1) {
+        for (int c = 0; c < REDUCE_CHUNKS; c++) run(c);
+    } else {
+        std::vector<std::thread> th;
+        for (int t = 0; t < nt; t++)
+            th.emplace_back([&, t] {
+                for (int c = t; c < REDUCE_CHUNKS; c += nt) run(c);
+            });
+        for (auto &x : th) x.join();
+    }
+    double x = 0.0, y = 0.0;
+    for (int c = 0; c < REDUCE_CHUNKS; c++) {
+        x += num[(size_t)c];
+        y += den[(size_t)c];
+    }
+    return {x, y};
 }
 
 // Pinned host staging for device-to-host copies (per thread, grown on demand).
@@ -435,28 +473,33 @@ void matrix_copy(mat *D, mat *S) {
     std::memcpy(D->d, S->d, sizeof(real) * (size_t)S->nrows * (size_t)S->ncols);
 }
 
+// Mt = M^T by 64 x 64 tiles
 void matrix_build_transpose(mat *Mt, mat *M) {
-    for (rsvd_int j = 0; j < M->ncols; j++)
-        for (rsvd_int i = 0; i < M->nrows; i++) Mt->d[(size_t)i * Mt->nrows + j] = M->d[(size_t)j * M->nrows + i];
+    const rsvd_int m = M->nrows, n = M->ncols, T = 64;
+    for (rsvd_int j0 = 0; j0 < n; j0 += T)
+        for (rsvd_int i0 = 0; i0 < m; i0 += T)
+            for (rsvd_int i = i0; i < std::min<rsvd_int>(m, i0 + T); i++)
+                for (rsvd_int j = j0; j < std::min<rsvd_int>(n, j0 + T); j++)
+                    Mt->d[(size_t)i * Mt->nrows + j] = M->d[(size_t)j * m + i];
 }
 
 // host reductions accumulate in double for either element type
 real get_matrix_frobenius_norm(mat *M) {
-    double acc = 0.0;
-    const size_t n = (size_t)M->nrows * (size_t)M->ncols;
-    for (size_t i = 0; i < n; i++) acc += (double)M->d[i] * (double)M->d[i];
-    return (real)std::sqrt(acc);
+    const real *a = M->d;
+    const auto r = host_reduce((size_t)M->nrows * (size_t)M->ncols, [a](size_t i) {
+        const double v = (double)a[i];
+        return std::pair<double, double>(v * v, 0.0);
+    });
+    return (real)std::sqrt(r.first);
 }
 
 real get_percent_error_between_two_mats(mat *A, mat *B) {
-    double num = 0.0, den = 0.0;
-    const size_t n = (size_t)A->nrows * (size_t)A->ncols;
-    for (size_t i = 0; i < n; i++) {
-        const double d = (double)A->d[i] - (double)B->d[i];
-        num += d * d;
-        den += (double)A->d[i] * (double)A->d[i];
-    }
-    return (real)(100.0 * std::sqrt(num) / std::sqrt(den));
+    const real *a = A->d, *b = B->d;
+    const auto r = host_reduce((size_t)A->nrows * (size_t)A->ncols, [a, b](size_t i) {
+        const double d = (double)a[i] - (double)b[i];
+        return std::pair<double, double>(d * d, (double)a[i] * (double)a[i]);
+    });
+    return (real)(100.0 * std::sqrt(r.first) / std::sqrt(r.second));
 }
 
 // MVF:299-311
