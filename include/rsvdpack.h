@@ -97,6 +97,59 @@ void initialize_diagonal_matrix(mat *D, vec *data);               /* :199: D(i,i
 void initialize_identity_matrix(mat *D);                          /* :204 (diagonal bounded by min(m, n)) */
 void matrix_get_col(mat *M, rsvd_int j, vec *column_vec);          /* :158 */
 void matrix_set_col(mat *M, rsvd_int j, vec *column_vec);          /* :161 */
+
+/* ---- the other host-side mat / vec helpers of matrix_vector_functions_intel_mkl.h (same
+ *      meanings; entries outside either object are never touched; vector_get_min_element /
+ *      vector_get_max_element compare the values truncated to rsvd_int, as the reference does) ---- */
+void matrix_print(mat *M);
+void vector_print(vec *v);
+void vector_set_data(vec *v, rsvd_real *data);
+void vector_scale(vec *v, rsvd_real scalar);
+void matrix_scale(mat *M, rsvd_real scalar);
+void vector_copy(vec *d, vec *s);
+void matrix_hard_threshold(mat *M, rsvd_real TOL);
+void vector_sub(vec *a, vec *b);
+void matrix_sub(mat *A, mat *B);
+void matrix_sub_column_times_row_vector(mat *A, vec *u, vec *v);
+void vector_get_min_element(vec *v, rsvd_int *minindex, rsvd_real *minval);
+void vector_get_max_element(vec *v, rsvd_int *maxindex, rsvd_real *maxval);
+rsvd_real vector_dot_product(vec *u, vec *v);
+rsvd_real get_matrix_max_abs_element(mat *M);
+rsvd_real get_matrix_column_norm_squared(mat *M, rsvd_int colnum);
+rsvd_real matrix_getmaxcolnorm(mat *M);
+void compute_matrix_column_norms(mat *M, vec *column_norms);
+void invert_diagonal_matrix(mat *Dinv, mat *D);
+void project_vector(vec *v, vec *u, vec *p);
+void matrix_get_row(mat *M, rsvd_int i, vec *row_vec);
+void matrix_set_row(mat *M, rsvd_int i, vec *row_vec);
+void matrix_get_selected_columns(mat *M, rsvd_int *inds, mat *Mc);
+void matrix_set_selected_columns(mat *M, rsvd_int *inds, mat *Mc);
+void matrix_get_selected_rows(mat *M, rsvd_int *inds, mat *Mr);
+void matrix_set_selected_rows(mat *M, rsvd_int *inds, mat *Mr);
+void matrix_copy_symmetric(mat *S, mat *M);
+void matrix_keep_only_upper_triangular(mat *M);
+void fill_vector_from_row_list(vec *input, vec *inds, vec *output);
+void matrix_copy_first_rows(mat *M_out, mat *M);
+void matrix_copy_first_columns(mat *M_out, mat *M);
+void matrix_copy_first_columns_with_param(mat *D, mat *S, rsvd_int num_columns);
+void matrix_copy_first_k_rows_and_columns(mat *M_out, mat *M);
+void matrix_copy_all_rows_and_last_columns_from_indexk(mat *M_out, mat *M, rsvd_int k);
+void fill_matrix_from_first_rows(mat *M, rsvd_int k, mat *M_k);
+void fill_matrix_from_last_rows(mat *M, rsvd_int k, mat *M_k);
+void fill_matrix_from_first_columns(mat *M, rsvd_int k, mat *M_k);
+void fill_matrix_from_last_columns(mat *M, rsvd_int k, mat *M_k);
+void fill_matrix_from_last_columns_from_specified_one(mat *M, rsvd_int k, mat *M_k);
+void fill_matrix_from_lower_right_corner(mat *M, rsvd_int k, mat *M_out);
+void fill_matrix_from_first_columns_from_list(mat *M, vec *I, rsvd_int k, mat *M_k);
+void fill_matrix_from_first_rows_from_list(mat *M, vec *I, rsvd_int k, mat *M_k);
+void fill_matrix_from_last_columns_from_list(mat *M, vec *I, rsvd_int k, mat *M_k);
+void resize_matrix_by_columns(mat **M, rsvd_int k);
+void resize_matrix_by_columns_from_end(mat **M, rsvd_int k);
+void resize_matrix_by_rows(mat **M, rsvd_int k);
+void resize_matrix_by_rows_from_end(mat **M, rsvd_int k);
+void append_matrices_horizontally(mat *A, mat *B, mat *C);
+void append_matrices_vertically(mat *A, mat *B, mat *C);
+void vector_build_rewrapped(vec *Iinv, vec *I);
 void initialize_random_matrix(mat *M);                            /* :128-129 */
 void matrix_matrix_mult(mat *A, mat *B, mat *C);                  /* :132-133 */
 void matrix_transpose_matrix_mult(mat *A, mat *B, mat *C);        /* :136-137 */

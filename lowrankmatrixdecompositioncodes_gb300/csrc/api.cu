@@ -529,6 +529,8 @@ void matrix_set_col(mat *M, rsvd_int j, vec *column_vec) {
     std::memcpy(M->d + (size_t)j * M->nrows, column_vec->d, sizeof(real) * (size_t)M->nrows);
 }
 
+#include "mat_helpers.h"
+
 #if defined(RSVDPACK_REAL32)
 // oneapi_code/matrix_vector_functions_one_api.c:1511-1513
 real get_seconds_frac(real start, real end) { return end - start; }
