@@ -120,6 +120,7 @@ rsvd_real matrix_getmaxcolnorm(mat *M);
 void compute_matrix_column_norms(mat *M, vec *column_norms);
 void invert_diagonal_matrix(mat *Dinv, mat *D);
 void project_vector(vec *v, vec *u, vec *p);
+void build_orthonormal_basis_from_mat(mat *A, mat *Q);
 void matrix_get_row(mat *M, rsvd_int i, vec *row_vec);
 void matrix_set_row(mat *M, rsvd_int i, vec *row_vec);
 void matrix_get_selected_columns(mat *M, rsvd_int *inds, mat *Mc);

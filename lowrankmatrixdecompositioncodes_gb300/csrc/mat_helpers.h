@@ -112,6 +112,26 @@ void project_vector(vec *v, vec *u, vec *p) {
     for (rsvd_int i = 0; i < u->nrows; i++) p->d[i] = scale * u->d[i];
 }
 
+// Q = two passes of classical Gram-Schmidt over the columns of A, in the reference's order:
+// column j minus its projections on columns 0..j-1 of the current Q, then normalised (MVF:817-844)
+void build_orthonormal_basis_from_mat(mat *A, mat *Q) {
+    const rsvd_int m = A->nrows, n = A->ncols;
+    std::memcpy(Q->d, A->d, sizeof(real) * (size_t)m * (size_t)n);
+    std::vector<real> pbuf((size_t)m);
+    vec p{m, pbuf.data()};
+    for (int pass = 0; pass < 2; pass++)
+        for (rsvd_int j = 0; j < n; j++) {
+            vec vj{m, Q->d + (size_t)j * m};
+            for (rsvd_int i = 0; i < j; i++) {
+                vec vi{m, Q->d + (size_t)i * m};
+                project_vector(&vj, &vi, &p);
+                vector_sub(&vj, &p);
+            }
+            const real nrm = vector_get2norm(&vj);
+            vector_scale(&vj, (real)1.0 / nrm);
+        }
+}
+
 // ---- rows and selections (MVF:608-790)
 void matrix_get_row(mat *M, rsvd_int i, vec *row_vec) {
     for (rsvd_int j = 0; j < M->ncols; j++) row_vec->d[j] = M->d[(size_t)j * M->nrows + i];

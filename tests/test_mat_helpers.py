@@ -1,7 +1,8 @@
 """The reference's host-side mat / vec helpers (matrix_vector_functions_intel_mkl.c) exported by the
 engine: each one run on the same inputs in librsvdpack.so and in the reference's own compiled
 helpers (oracle/_ref, where the reference tree is present) must leave identical outputs -- bit for
-bit, except vector_dot_product, matrix_getmaxcolnorm and project_vector, whose sums are OpenMP
+bit, except vector_dot_product, matrix_getmaxcolnorm, project_vector and
+build_orthonormal_basis_from_mat, whose sums are OpenMP
 reductions in the reference (matrix_vector_functions_intel_mkl.c:304,349: the order is set by the
 thread count).  Where the reference is absent the same calls
 are checked against numpy.  No GPU needed."""
@@ -55,7 +56,7 @@ class Lib:
             "resize_matrix_by_columns": [C.POINTER(PM), I], "resize_matrix_by_columns_from_end": [C.POINTER(PM), I],
             "resize_matrix_by_rows": [C.POINTER(PM), I], "resize_matrix_by_rows_from_end": [C.POINTER(PM), I],
             "append_matrices_horizontally": [PM, PM, PM], "append_matrices_vertically": [PM, PM, PM],
-            "vector_build_rewrapped": [PV, PV],
+            "vector_build_rewrapped": [PV, PV], "build_orthonormal_basis_from_mat": [PM, PM],
         }
         for name, args in sig.items():
             f = getattr(self.L, name)
@@ -157,10 +158,11 @@ def scenario(lib):
     Z = lib.zeros(7, 10); N = lib.m(B0); L.append_matrices_horizontally(M, N, Z); out["append_h"] = lib.get(Z)
     Z = lib.zeros(14, 5); L.append_matrices_vertically(M, N, Z); out["append_v"] = lib.get(Z)
     inv = lib.v(np.zeros(7)); L.vector_build_rewrapped(inv, p7); out["vector_build_rewrapped"] = lib.getv(inv)
+    Q = lib.zeros(7, 5); L.build_orthonormal_basis_from_mat(M, Q); out["build_orthonormal_basis_from_mat"] = lib.get(Q)
     return out
 
 
-NOT_EXACT = {"vector_dot_product", "matrix_getmaxcolnorm", "project_vector"}
+NOT_EXACT = {"vector_dot_product", "matrix_getmaxcolnorm", "project_vector", "build_orthonormal_basis_from_mat"}
 
 
 def test_helpers_match_the_reference_build(ref):
@@ -192,3 +194,7 @@ def test_helpers_against_numpy():
     assert np.array_equal(out["append_v"], np.vstack([A0, B0]))
     inv = out["vector_build_rewrapped"].astype(int)
     assert np.array_equal(PERM7.astype(int)[inv], np.arange(7))
+    Q = out["build_orthonormal_basis_from_mat"]
+    assert np.allclose(Q.T @ Q, np.eye(5), atol=1e-14)
+    Qn, _ = np.linalg.qr(A0)
+    assert np.allclose(np.abs(np.sum(Q * Qn, axis=0)), 1.0, atol=1e-12)
