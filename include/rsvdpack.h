@@ -231,6 +231,15 @@ void cur_rand_decomp_fixed_rank(mat *M, rsvd_int k, rsvd_int p, rsvd_int q, rsvd
 void cur_blockrand_decomp_fixed_rank_or_prec(mat *M, rsvd_int k, rsvd_int p, rsvd_real TOL, rsvd_int kstep,
                                              rsvd_int q, rsvd_int s, rsvd_int *frank,
                                              mat **C, mat **U, mat **R);
+/* :12-25 the older randomized SVD entry points, each one of the routines above with fixed parameters
+ * (rank_revealing_algorithms_intel_mkl.c:385-700): svd1 = low_rank_svd_rand_decomp_fixed_rank with
+ * p = 0, vnum = 2, q = 1; svd2 = p = 0, vnum = 1, q = 1; svd3 = p = 0, vnum = 1 with q, s; svd4 =
+ * randQB_pb(kstep, nstep, p, s = 1) followed by eig(B B^T), pairs ascending.  (The header names
+ * svd4's last argument s; the definition uses it as p.) */
+void randomized_low_rank_svd1(mat *M, rsvd_int k, mat **U, mat **S, mat **V);
+void randomized_low_rank_svd2(mat *M, rsvd_int k, mat **U, mat **S, mat **V);
+void randomized_low_rank_svd3(mat *M, rsvd_int k, rsvd_int q, rsvd_int s, mat **U, mat **S, mat **V);
+void randomized_low_rank_svd4(mat *M, rsvd_int kstep, rsvd_int nstep, rsvd_int p, mat **U, mat **S, mat **V);
 /* :105-120 approximation reports (print norms and percent error, as the reference does).
  * use_pivoted_QR_decomp_for_approximation frees Qk and Rk, as the reference does. */
 void use_low_rank_svd_for_approximation(mat *M, mat *U, mat *S, mat *V);

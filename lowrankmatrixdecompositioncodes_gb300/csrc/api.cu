@@ -7,6 +7,7 @@
 #include "engine.h"
 #include "k_common.cuh"
 
+#include <algorithm>
 #include <chrono>
 #include <climits>
 #include <cmath>
@@ -831,6 +832,41 @@ void id_rand_decomp_fromQB(mat *Q, mat *B, vec **I, mat **T) {
         *T = download<double>(r.T.v);
         end_call(t0);
     });
+}
+
+// ---- the older randomized SVD entry points (RRA:385-700).  Each is one of the entry points above
+// with fixed parameters -- identities that hold bit for bit on the reference's own build:
+// svd1 = the fixed-rank rSVD with p = 0, vnum = 2 (eig of B B^T, ascending), no power round;
+// svd2 = the same with vnum = 1 (QR of B^T, descending); svd3 = vnum = 1 with q, s;
+// svd4 = randQB_pb (kstep, nstep, p power rounds, s = 1) then the eig(B B^T) back end, ascending.
+void randomized_low_rank_svd1(mat *M, rsvd_int k, mat **U, mat **S, mat **V) {
+    low_rank_svd_rand_decomp_fixed_rank(M, k, 0, 2, 1, 1, nullptr, U, S, V);
+}
+void randomized_low_rank_svd2(mat *M, rsvd_int k, mat **U, mat **S, mat **V) {
+    low_rank_svd_rand_decomp_fixed_rank(M, k, 0, 1, 1, 1, nullptr, U, S, V);
+}
+void randomized_low_rank_svd3(mat *M, rsvd_int k, rsvd_int q, rsvd_int s, mat **U, mat **S, mat **V) {
+    low_rank_svd_rand_decomp_fixed_rank(M, k, 0, 1, q, s, nullptr, U, S, V);
+}
+void randomized_low_rank_svd4(mat *M, rsvd_int kstep, rsvd_int nstep, rsvd_int p, mat **U, mat **S, mat **V) {
+    *U = *S = *V = nullptr;
+    mat *Q = nullptr, *B = nullptr;
+    randQB_pb(M, kstep, nstep, p, 1, &Q, &B);
+    if (!Q || !B) return;                                // rsvdpack_last_error() says why
+    low_rank_svd_rand_decomp_fromQB(Q, B, U, S, V);
+    matrix_delete(Q);
+    matrix_delete(B);
+    if (!*U || !*S || !*V) return;
+    // the QB split returns the pairs descending; this entry point returns them ascending
+    auto reverse_cols = [](mat *X) {
+        for (rsvd_int a = 0, b = X->ncols - 1; a < b; a++, b--)
+            std::swap_ranges(X->d + (size_t)a * X->nrows, X->d + (size_t)(a + 1) * X->nrows, X->d + (size_t)b * X->nrows);
+    };
+    reverse_cols(*U);
+    reverse_cols(*V);
+    const rsvd_int l = (*S)->nrows;
+    for (rsvd_int a = 0, b = l - 1; a < b; a++, b--)
+        std::swap((*S)->d[(size_t)a * l + a], (*S)->d[(size_t)b * l + b]);
 }
 
 static void two_sided_outputs(TwoSidedOut &r, vec **Icol, vec **Irow, mat **T, mat **S) {

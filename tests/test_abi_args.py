@@ -98,3 +98,17 @@ def test_rank_only_pivoted_qr_checks_k(lib):
         assert code == 1 and "1 <= k" in msg
         assert not Q and not R and not I
     lib.lib.matrix_delete(M)
+
+
+def test_older_svd_entry_points_check_arguments(lib):
+    L = lib.lib
+    for name, n_int in (("randomized_low_rank_svd1", 1), ("randomized_low_rank_svd4", 3)):
+        getattr(L, name).argtypes = [lib.PMat] + [lib.Int] * n_int + [C.POINTER(lib.PMat)] * 3
+    M = lib.to_mat(np.ones((6, 4)))
+    U, S, V = lib.PMat(), lib.PMat(), lib.PMat()
+    L.randomized_low_rank_svd1(M, 5, C.byref(U), C.byref(S), C.byref(V))      # k > min(m, n)
+    assert _err(lib)[0] == 1 and not U and not S and not V
+    L.randomized_low_rank_svd4(M, 2, 0, 1, C.byref(U), C.byref(S), C.byref(V))  # nstep = 0
+    code, msg = _err(lib)
+    assert code == 1 and "randQB_pb" in msg and not U
+    L.matrix_delete(M)

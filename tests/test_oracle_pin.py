@@ -5,6 +5,8 @@ outputs.  Two anchors:
   * the reference build itself (oracle/_ref), where present -- bit-exact checks on
     fresh seeded inputs.
 """
+import ctypes as C
+
 import numpy as np
 import pytest
 
@@ -92,3 +94,42 @@ def test_rank_only_pivoted_qr_stops_only_on_exact_zero(ref, port):
     A = spectrum_matrix(150, 110, 0.97 ** np.arange(110), seed=3)
     compare_outputs("pivoted_QR_of_specified_rank", port.pivoted_QR_of_specified_rank(A, 12),
                     ref.pivoted_QR_of_specified_rank(A, 12), rtol=1e-12)
+
+
+def _old_api(lib):
+    L = lib.lib
+    for name, n_int in (("randomized_low_rank_svd1", 1), ("randomized_low_rank_svd2", 1),
+                        ("randomized_low_rank_svd3", 3), ("randomized_low_rank_svd4", 3)):
+        getattr(L, name).argtypes = [lib.PMat] + [lib.Int] * n_int + [C.POINTER(lib.PMat)] * 3
+    return L
+
+
+def test_older_svd_entry_points_are_the_current_routines(ref, port):
+    """The identities the engine's randomized_low_rank_svd1..4 rest on, checked on the reference's
+    own build: svd1..3 are low_rank_svd_rand_decomp_fixed_rank with fixed parameters (bit for bit),
+    svd4 is randQB_pb followed by the eig(B B^T) back end with the pairs ascending (the port's
+    QB split, reversed)."""
+    L = _old_api(ref)
+    A = spectrum_matrix(120, 80, 0.9 ** np.arange(80), seed=1)
+
+    def old(name, *a):
+        ref.set_omega(SeededOmega(3))
+        M = ref.to_mat(A)
+        U, S, V = ref.PMat(), ref.PMat(), ref.PMat()
+        getattr(L, name)(M, *a, C.byref(U), C.byref(S), C.byref(V))
+        L.matrix_delete(M)
+        return ref.from_mat(U), ref.from_mat(S), ref.from_mat(V)
+
+    for name, a_old, a_new in (("randomized_low_rank_svd1", (10,), (10, 0, 2, 1, 1)),
+                               ("randomized_low_rank_svd2", (10,), (10, 0, 1, 1, 1)),
+                               ("randomized_low_rank_svd3", (10, 3, 2), (10, 0, 1, 3, 2))):
+        ref.set_omega(SeededOmega(3))
+        want = ref.low_rank_svd_rand_decomp_fixed_rank(A, *a_new)
+        assert all(np.array_equal(x, y) for x, y in zip(old(name, *a_old), want)), name
+    U4, S4, V4 = old("randomized_low_rank_svd4", 6, 3, 1)
+    ref.set_omega(SeededOmega(3))
+    Q, B = ref.randQB_pb(A, 6, 3, 1, 1)
+    U, S, V = port.low_rank_svd_rand_decomp_fromQB(Q, B)
+    assert np.max(np.abs(np.diag(S4) - np.diag(S)[::-1])) < 1e-13
+    compare_outputs("low_rank_svd_rand_decomp_fixed_rank", (U4, S4, V4), (U[:, ::-1], S[::-1, ::-1], V[:, ::-1]),
+                    rtol=1e-12)
