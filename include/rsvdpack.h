@@ -190,6 +190,8 @@ void randQB_pb2(mat *M, rsvd_int kstep, rsvd_int nstep, rsvd_real TOL, rsvd_int 
 void randQB_pb(mat *M, rsvd_int kstep, rsvd_int nstep, rsvd_int q, rsvd_int s, mat **Q, mat **B);
 /* :43 full column-pivoted QR, M(:,I) = Q R (LAPACK dgeqp3 pivoting, all columns free) */
 void pivotedQR_mkl(mat *M, mat **Q, mat **R, vec **I);
+/* :45 Householder vector of x(ind1:ind2) into column 0 of H, scaled so that I - H H^T reflects it */
+void get_householder_matrix(vec *x, rsvd_int ind1, rsvd_int ind2, mat *H);
 /* :52 partial pivoted Householder QR of rank k, or of precision TOL when k <= 0 */
 void pivoted_QR_of_specified_rank_or_prec(mat *M, rsvd_int k, rsvd_real TOL, rsvd_int *frank,
                                           mat **Qk, mat **Rk, vec **I);

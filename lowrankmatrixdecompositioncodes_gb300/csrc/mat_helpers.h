@@ -132,6 +132,20 @@ void build_orthonormal_basis_from_mat(mat *A, mat *Q) {
         }
 }
 
+// H(:, 0) = the Householder vector of x(ind1:ind2) scaled so that I - H H^T reflects it: x's entries
+// in [ind1, ind2), ||x(ind1:ind2)|| taken off H(ind1, 0), then H scaled by sqrt(2) / ||H||_F
+// (rank_revealing_algorithms_intel_mkl.c:982-1004; H's other entries are left as they are)
+void get_householder_matrix(vec *x, rsvd_int ind1, rsvd_int ind2, mat *H) {
+    double nrm = 0.0;
+    for (rsvd_int i = ind1; i < ind2; i++) {
+        H->d[i] = x->d[i];
+        nrm += (double)x->d[i] * (double)x->d[i];
+    }
+    H->d[ind1] = H->d[ind1] - (real)std::sqrt(nrm);
+    const double f = (double)get_matrix_frobenius_norm(H);
+    if (f > 0) matrix_scale(H, (real)std::sqrt(2.0 / (f * f)));
+}
+
 // ---- rows and selections (MVF:608-790)
 void matrix_get_row(mat *M, rsvd_int i, vec *row_vec) {
     for (rsvd_int j = 0; j < M->ncols; j++) row_vec->d[j] = M->d[(size_t)j * M->nrows + i];

@@ -57,6 +57,7 @@ class Lib:
             "resize_matrix_by_rows": [C.POINTER(PM), I], "resize_matrix_by_rows_from_end": [C.POINTER(PM), I],
             "append_matrices_horizontally": [PM, PM, PM], "append_matrices_vertically": [PM, PM, PM],
             "vector_build_rewrapped": [PV, PV], "build_orthonormal_basis_from_mat": [PM, PM],
+            "get_householder_matrix": [PV, I, I, PM],
         }
         for name, args in sig.items():
             f = getattr(self.L, name)
@@ -159,10 +160,12 @@ def scenario(lib):
     Z = lib.zeros(14, 5); L.append_matrices_vertically(M, N, Z); out["append_v"] = lib.get(Z)
     inv = lib.v(np.zeros(7)); L.vector_build_rewrapped(inv, p7); out["vector_build_rewrapped"] = lib.getv(inv)
     Q = lib.zeros(7, 5); L.build_orthonormal_basis_from_mat(M, Q); out["build_orthonormal_basis_from_mat"] = lib.get(Q)
+    H = lib.zeros(7, 1); L.get_householder_matrix(u, 2, 7, H); out["get_householder_matrix"] = lib.get(H)
     return out
 
 
-NOT_EXACT = {"vector_dot_product", "matrix_getmaxcolnorm", "project_vector", "build_orthonormal_basis_from_mat"}
+NOT_EXACT = {"vector_dot_product", "matrix_getmaxcolnorm", "project_vector", "build_orthonormal_basis_from_mat",
+             "get_householder_matrix"}
 
 
 def test_helpers_match_the_reference_build(ref):
@@ -198,3 +201,7 @@ def test_helpers_against_numpy():
     assert np.allclose(Q.T @ Q, np.eye(5), atol=1e-14)
     Qn, _ = np.linalg.qr(A0)
     assert np.allclose(np.abs(np.sum(Q * Qn, axis=0)), 1.0, atol=1e-12)
+    h = out["get_householder_matrix"][:, 0]
+    x = np.where(np.arange(7) >= 2, V7, 0.0)
+    Hx = x - h * (h @ x)                       # (I - h h^T) x = -+||x|| e_2
+    assert np.allclose(Hx[3:], 0, atol=1e-14) and abs(abs(Hx[2]) - np.linalg.norm(x)) < 1e-14
