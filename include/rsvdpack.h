@@ -155,6 +155,15 @@ void initialize_random_matrix(mat *M);                            /* :128-129 */
 void matrix_matrix_mult(mat *A, mat *B, mat *C);                  /* :132-133 */
 void matrix_transpose_matrix_mult(mat *A, mat *B, mat *C);        /* :136-137 */
 void matrix_matrix_transpose_mult(mat *A, mat *B, mat *C);        /* :140-141 */
+void matrix_vector_mult(mat *M, vec *x, vec *y);                  /* :149: y = M x */
+void matrix_transpose_vector_mult(mat *M, vec *x, vec *y);        /* :153: y = M^T x */
+/* :213 in place inverse of an upper-triangular matrix (the strictly lower part is left as it is) */
+void invert_upper_triangular_matrix(mat *Minv);
+/* :354 A X = B for upper-triangular A of order B->nrows; solve_type 2 inverts A in place first, as
+ * the reference does; the other types give the triangular solve */
+void upper_triangular_system_solve(mat *A, mat *B, mat *X, rsvd_int solve_type);
+/* :357 A X = B by LU with partial pivoting; X and B receive the solution, A is left as it is */
+void square_matrix_system_solve(mat *A, mat *X, mat *B);
 /* :333, :338 Householder QR with LAPACK's reflector signs (dgeqrf + dorgqr), m >= n: M = Q R with
  * Q (m x n, caller-allocated) and, for compact_QR_factorization, R (n x n, caller-allocated; its
  * upper triangle is written, as the reference writes it). */

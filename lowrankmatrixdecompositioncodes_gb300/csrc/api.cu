@@ -571,6 +571,91 @@ void matrix_matrix_mult(mat *A, mat *B, mat *C) { host_gemm("matrix_matrix_mult"
 void matrix_transpose_matrix_mult(mat *A, mat *B, mat *C) { host_gemm("matrix_transpose_matrix_mult", true, false, A, B, C); }
 void matrix_matrix_transpose_mult(mat *A, mat *B, mat *C) { host_gemm("matrix_matrix_transpose_mult", false, true, A, B, C); }
 
+// y = M x, y = M^T x (MVF:565-580): the same FP64 GEMM with one column
+void matrix_vector_mult(mat *M, vec *x, vec *y) {
+    mat xm{x->nrows, 1, x->d}, ym{y->nrows, 1, y->d};
+    host_gemm("matrix_vector_mult", false, false, M, &xm, &ym);
+}
+void matrix_transpose_vector_mult(mat *M, vec *x, vec *y) {
+    mat xm{x->nrows, 1, x->d}, ym{y->nrows, 1, y->d};
+    host_gemm("matrix_transpose_vector_mult", true, false, M, &xm, &ym);
+}
+
+// Minv = Minv^-1 for an upper-triangular Minv, in place (MVF:532-535, LAPACK dtrtri 'U' 'N': the
+// upper triangle is overwritten, the strictly lower part is left as it is): the engine's FP64
+// triangular solve against the identity
+void invert_upper_triangular_matrix(mat *Minv) {
+    guarded("invert_upper_triangular_matrix", [&] {
+        check_mat(Minv);
+        need(Minv->nrows == Minv->ncols, "matrix must be square");
+        begin_call();
+        auto t0 = Clock::now();
+        cudaStream_t s = ctx().stream;
+        const i64 n = Minv->nrows;
+        DMat<double> R = upload<double>(Minv);
+        DMat<double> I(n, n, s, false), X(n, n, s, false);
+        set_identity(s, I.v);
+        trsm_left_upper(s, R.v, I.v, X.v);
+        mat *h = download<double>(X.v);
+        for (i64 j = 0; j < n; j++)
+            for (i64 i = 0; i <= j; i++) Minv->d[(size_t)j * n + i] = h->d[(size_t)j * n + i];
+        matrix_delete(h);
+        end_call(t0);
+    });
+}
+
+// A X = B for an upper-triangular A (MVF:1477-1523).  solve_type 2 inverts A in place and
+// multiplies, as the reference does; every other type (1: dtrsm; 3: the SVD pseudo-inverse, the
+// same X for the nonsingular triangular A the routine is for; others: dtrsv per column) is the
+// engine's FP64 triangular solve.  The order is B->nrows, as in the reference.
+void upper_triangular_system_solve(mat *A, mat *B, mat *X, rsvd_int solve_type) {
+    if (solve_type == 2) {
+        invert_upper_triangular_matrix(A);
+        if (rsvdpack_last_error() == RSVD_OK) matrix_matrix_mult(A, B, X);
+        return;
+    }
+    guarded("upper_triangular_system_solve", [&] {
+        check_mat(A);
+        check_mat(B);
+        check_mat(X);
+        need(A->nrows >= B->nrows && A->ncols >= B->nrows, "A must hold a B->nrows x B->nrows triangle");
+        need(X->nrows == B->nrows && X->ncols == B->ncols, "X must have B's shape");
+        begin_call();
+        auto t0 = Clock::now();
+        cudaStream_t s = ctx().stream;
+        DMat<double> dA = upload<double>(A), dB = upload<double>(B);
+        DMat<double> dX(B->nrows, B->ncols, s, false);
+        trsm_left_upper(s, dA.v.sub(0, 0, B->nrows, B->nrows), dB.v, dX.v);
+        mat *h = download<double>(dX.v);
+        std::memcpy(X->d, h->d, sizeof(real) * (size_t)X->nrows * (size_t)X->ncols);
+        matrix_delete(h);
+        end_call(t0);
+    });
+}
+
+// A X = B by LU with partial pivoting (MVF:1525-1531, LAPACK dgesv): X and B receive the solution;
+// A is left as it is (the reference leaves its LU factors there)
+void square_matrix_system_solve(mat *A, mat *X, mat *B) {
+    guarded("square_matrix_system_solve", [&] {
+        check_mat(A);
+        check_mat(B);
+        check_mat(X);
+        need(A->nrows == A->ncols && B->nrows == A->nrows, "need a square A and B with A's rows");
+        need(X->nrows == B->nrows && X->ncols == B->ncols, "X must have B's shape");
+        begin_call();
+        auto t0 = Clock::now();
+        DMat<double> dA = upload<double>(A), dB = upload<double>(B);
+        if (!lu_solve(ctx().stream, dA.v, dB.v, ctx().d_flags + FLAG_NONFINITE))
+            fail(RSVD_ERR_NUMERIC, "singular matrix");
+        mat *h = download<double>(dB.v);
+        const size_t cnt = (size_t)X->nrows * (size_t)X->ncols;
+        std::memcpy(X->d, h->d, sizeof(real) * cnt);
+        std::memcpy(B->d, h->d, sizeof(real) * cnt);
+        matrix_delete(h);
+        end_call(t0);
+    });
+}
+
 // P = U S V^T (MVF:1304-1318)
 void form_svd_product_matrix(mat *U, mat *S, mat *V, mat *P) {
     mat *SVt = matrix_new(S->nrows, V->nrows);

@@ -112,3 +112,20 @@ def test_older_svd_entry_points_check_arguments(lib):
     code, msg = _err(lib)
     assert code == 1 and "randQB_pb" in msg and not U
     L.matrix_delete(M)
+
+
+def test_blas_backed_helpers_check_shapes(lib):
+    L = lib.lib
+    L.invert_upper_triangular_matrix.argtypes = [lib.PMat]
+    L.upper_triangular_system_solve.argtypes = [lib.PMat, lib.PMat, lib.PMat, lib.Int]
+    L.square_matrix_system_solve.argtypes = [lib.PMat, lib.PMat, lib.PMat]
+    W = lib.to_mat(np.ones((4, 3)))
+    L.invert_upper_triangular_matrix(W)
+    assert _err(lib) == (1, "invert_upper_triangular_matrix: matrix must be square")
+    A, B, X = lib.to_mat(np.eye(3)), lib.to_mat(np.ones((3, 2))), lib.to_mat(np.zeros((3, 3)))
+    L.upper_triangular_system_solve(A, B, X, 1)
+    assert _err(lib)[0] == 1 and "B's shape" in _err(lib)[1]
+    L.square_matrix_system_solve(W, X, B)
+    assert _err(lib)[0] == 1 and "square A" in _err(lib)[1]
+    for x in (W, A, B, X):
+        L.matrix_delete(x)
