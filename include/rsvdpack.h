@@ -162,6 +162,9 @@ void invert_upper_triangular_matrix(mat *Minv);
 /* :354 A X = B for upper-triangular A of order B->nrows; solve_type 2 inverts A in place first, as
  * the reference does; the other types give the triangular solve */
 void upper_triangular_system_solve(mat *A, mat *B, mat *X, rsvd_int solve_type);
+/* :328 eigenvalues ascending into evals and eigenvectors into the columns of S (the upper triangle
+ * of S defines the symmetric matrix, as for LAPACK dsyev 'V' 'U') */
+void compute_evals_and_evecs_of_symm_matrix(mat *S, vec *evals);
 /* :357 A X = B by LU with partial pivoting; X and B receive the solution, A is left as it is */
 void square_matrix_system_solve(mat *A, mat *X, mat *B);
 /* :333, :338 Householder QR with LAPACK's reflector signs (dgeqrf + dorgqr), m >= n: M = Q R with

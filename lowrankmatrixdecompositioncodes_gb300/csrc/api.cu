@@ -633,6 +633,47 @@ void upper_triangular_system_solve(mat *A, mat *B, mat *X, rsvd_int solve_type) 
     });
 }
 
+// Eigenvalues ascending into evals, eigenvectors into the columns of S (MVF:1206-1209, LAPACK dsyev
+// 'V' 'U': the upper triangle of S defines the matrix).  The engine's FP64 one-sided Jacobi SVD of
+// S + sigma I with sigma = ||S||_F, which is positive semidefinite, so that its singular pairs are
+// eigenpairs: lambda = sv - sigma, to ~eps ||S|| (dsyev's bound is of the same kind).
+void compute_evals_and_evecs_of_symm_matrix(mat *S, vec *evals) {
+    guarded("compute_evals_and_evecs_of_symm_matrix", [&] {
+        check_mat(S);
+        need(S->nrows == S->ncols, "matrix must be square");
+        need(evals != nullptr && evals->d != nullptr && evals->nrows >= S->nrows, "evals shorter than S");
+        begin_call();
+        auto t0 = Clock::now();
+        cudaStream_t s = ctx().stream;
+        const i64 n = S->nrows;
+        std::vector<double> g((size_t)n * (size_t)n);
+        double fro2 = 0.0;
+        for (i64 j = 0; j < n; j++)
+            for (i64 i = 0; i <= j; i++) {
+                const double v = (double)S->d[(size_t)j * n + i];
+                g[(size_t)j * n + i] = g[(size_t)i * n + j] = v;
+                fro2 += (i == j ? 1.0 : 2.0) * v * v;
+            }
+        const double sigma = fro2 > 0.0 ? std::sqrt(fro2) : 1.0;
+        for (i64 i = 0; i < n; i++) g[(size_t)i * n + i] += sigma;
+        DMat<double> G(n, n, s, false), U(n, n, s, false), V(n, n, s, false);
+        DBuf svb(sizeof(double) * (size_t)n, s);
+        RSVD_CK(cudaMemcpy2DAsync(G.v.p, sizeof(double) * G.v.ld, g.data(), sizeof(double) * n, sizeof(double) * n, n,
+                                  cudaMemcpyHostToDevice, s));
+        jacobi_small<double>(s, G.v, U.v, V.v, (double *)svb.get(), ctx().d_flags + FLAG_JACOBI_NOCONV, false);
+        std::vector<double> sv((size_t)n);
+        RSVD_CK(cudaMemcpyAsync(sv.data(), svb.get(), sizeof(double) * n, cudaMemcpyDeviceToHost, s));
+        mat *hv = download<double>(V.v);                 // synchronises the stream
+        for (i64 j = 0; j < n; j++) {                    // the SVD is descending; eigenvalues ascending
+            const i64 src = n - 1 - j;
+            evals->d[j] = (real)(sv[(size_t)src] - sigma);
+            std::memcpy(S->d + (size_t)j * n, hv->d + (size_t)src * n, sizeof(real) * (size_t)n);
+        }
+        matrix_delete(hv);
+        end_call(t0);
+    });
+}
+
 // A X = B by LU with partial pivoting (MVF:1525-1531, LAPACK dgesv): X and B receive the solution;
 // A is left as it is (the reference leaves its LU factors there)
 void square_matrix_system_solve(mat *A, mat *X, mat *B) {

@@ -81,3 +81,23 @@ def test_square_system_solve(eng):
     np.testing.assert_allclose(eng.from_mat(pX), want, rtol=0, atol=1e-12)
     np.testing.assert_allclose(eng.from_mat(pB), want, rtol=0, atol=1e-12)
     assert np.array_equal(eng.from_mat(pA), A)
+
+
+@pytest.mark.parametrize("n", [9, 64, 150])
+def test_symmetric_eigensolver(eng, n):
+    """compute_evals_and_evecs_of_symm_matrix on an indefinite symmetric matrix whose strictly
+    lower part holds other numbers (the upper triangle defines it, as for dsyev 'U')."""
+    L = eng.lib
+    L.compute_evals_and_evecs_of_symm_matrix.argtypes = [eng.PMat, eng.PVec]
+    X = G.standard_normal((n, n))
+    Ssym = (X + X.T) / 2
+    S = np.triu(Ssym) + np.tril(G.standard_normal((n, n)), -1)
+    pS, pe = eng.to_mat(S), _vec(eng, np.zeros(n))
+    L.compute_evals_and_evecs_of_symm_matrix(pS, pe)
+    eng.check()
+    lam, Vec = eng.from_vec(pe), eng.from_mat(pS)
+    scale = np.linalg.norm(Ssym)
+    np.testing.assert_allclose(lam, np.linalg.eigvalsh(Ssym), rtol=0, atol=1e-12 * scale)
+    assert np.all(np.diff(lam) >= -1e-12 * scale)                     # ascending
+    assert np.max(np.abs(Vec.T @ Vec - np.eye(n))) < 1e-12
+    assert np.max(np.abs(Ssym @ Vec - Vec * lam)) < 1e-11 * scale
