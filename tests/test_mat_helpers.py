@@ -1,8 +1,8 @@
 """The reference's host-side mat / vec helpers (matrix_vector_functions_intel_mkl.c) exported by the
 engine: each one run on the same inputs in librsvdpack.so and in the reference's own compiled
 helpers (oracle/_ref, where the reference tree is present) must leave identical outputs -- bit for
-bit, except vector_dot_product, matrix_getmaxcolnorm, project_vector and
-build_orthonormal_basis_from_mat, whose sums are OpenMP
+bit, except vector_dot_product, project_vector, build_orthonormal_basis_from_mat and
+get_householder_matrix, whose sums are OpenMP
 reductions in the reference (matrix_vector_functions_intel_mkl.c:304,349: the order is set by the
 thread count).  Where the reference is absent the same calls
 are checked against numpy.  No GPU needed."""
@@ -164,14 +164,19 @@ def scenario(lib):
     return out
 
 
-NOT_EXACT = {"vector_dot_product", "matrix_getmaxcolnorm", "project_vector", "build_orthonormal_basis_from_mat",
-             "get_householder_matrix"}
+NOT_EXACT = {"vector_dot_product", "project_vector", "build_orthonormal_basis_from_mat", "get_householder_matrix"}
+# the reference's matrix_getmaxcolnorm shares one column buffer and the running maximum between
+# OpenMP threads without a reduction (matrix_vector_functions_intel_mkl.c:422-443): its result
+# changes from run to run, so it is checked against numpy only
+RACY_IN_REFERENCE = {"matrix_getmaxcolnorm"}
 
 
 def test_helpers_match_the_reference_build(ref):
     got, want = scenario(Lib(load_engine())), scenario(Lib(ref))
     assert got.keys() == want.keys()
     for key in want:
+        if key in RACY_IN_REFERENCE:
+            continue
         g, w = np.asarray(got[key], dtype=np.float64), np.asarray(want[key], dtype=np.float64)
         if key in NOT_EXACT:
             np.testing.assert_allclose(g, w, rtol=1e-14, atol=0, err_msg=key)
@@ -182,6 +187,7 @@ def test_helpers_match_the_reference_build(ref):
 def test_helpers_against_numpy():
     out = scenario(Lib(load_engine()))
     assert np.array_equal(out["matrix_scale"], -1.5 * A0)
+    assert abs(out["matrix_getmaxcolnorm"] - np.linalg.norm(A0, axis=0).max()) < 1e-14
     assert np.array_equal(out["matrix_sub"], A0 - B0)
     assert np.allclose(out["matrix_sub_column_times_row_vector"], A0 - np.outer(V7, V5))
     assert out["vector_get_min_element"] == (1, -3.0)      # values truncated before comparing
