@@ -401,7 +401,6 @@ int rsvdpack_dev_small_cholesky(double *dG, int n, long long ldg, int fp32);
 int rsvdpack_dev_sketch_t_noalloc(const float *dA, long long lda, int m, int n, const float *dX,
                                   long long ldx, int w, float *dY, long long ldy, void *stream);
 
-/* Per-call phase timing of the last decomposition on this thread (milliseconds). */
 /* ---- the learned rank / power-count proposal's network (no counterpart in the reference):
  * an MLP 36 -> 64 -> 64 -> 2 (ReLU) whose inputs are the R-diagonal features of a 32-column
  * probe sketch and whose outputs are log2(width / 32) of the single-shot range finder for
@@ -430,6 +429,7 @@ int rsvdpack_mlp_forward(const float *dP, const float *dnorm, const float *dX, i
 int rsvdpack_mlp_train_step(float *dP, float *dM, float *dV, const float *dnorm, const float *dX, const float *dT,
                             const float *dReached, int batch, float lr, int step, float *dloss, float *dG);
 
+/* Per-call phase timing of the last decomposition on this thread (milliseconds). */
 typedef struct {
     double upload_ms, sketch_ms, orth_ms, small_ms, download_ms, total_ms;
     long long gemm_launches, kernel_launches;

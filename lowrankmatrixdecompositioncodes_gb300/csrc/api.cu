@@ -636,7 +636,10 @@ void upper_triangular_system_solve(mat *A, mat *B, mat *X, rsvd_int solve_type) 
 // Eigenvalues ascending into evals, eigenvectors into the columns of S (MVF:1206-1209, LAPACK dsyev
 // 'V' 'U': the upper triangle of S defines the matrix).  The engine's FP64 one-sided Jacobi SVD of
 // S + sigma I with sigma = ||S||_F, which is positive semidefinite, so that its singular pairs are
-// eigenpairs: lambda = sv - sigma, to ~eps ||S|| (dsyev's bound is of the same kind).
+// eigenpairs: lambda = sv - sigma.  Absolute accuracy of every eigenvalue ~eps ||S||_F (the shift's
+// size; dsyev's bound is eps ||S||_2, at most sqrt(n) times smaller), so eigenvalues far below
+// ||S||_F carry correspondingly fewer correct digits.  A Jacobi run that hits its sweep limit
+// returns RSVD_ERR_NUMERIC instead of unconverged pairs.
 void compute_evals_and_evecs_of_symm_matrix(mat *S, vec *evals) {
     guarded("compute_evals_and_evecs_of_symm_matrix", [&] {
         check_mat(S);
@@ -664,6 +667,13 @@ void compute_evals_and_evecs_of_symm_matrix(mat *S, vec *evals) {
         std::vector<double> sv((size_t)n);
         RSVD_CK(cudaMemcpyAsync(sv.data(), svb.get(), sizeof(double) * n, cudaMemcpyDeviceToHost, s));
         mat *hv = download<double>(V.v);                 // synchronises the stream
+        int noconv = 0;
+        RSVD_CK(cudaMemcpyAsync(&noconv, ctx().d_flags + FLAG_JACOBI_NOCONV, sizeof(int), cudaMemcpyDeviceToHost, s));
+        RSVD_CK(cudaStreamSynchronize(s));
+        if (noconv) {
+            matrix_delete(hv);
+            fail(RSVD_ERR_NUMERIC, "Jacobi iteration did not converge");
+        }
         for (i64 j = 0; j < n; j++) {                    // the SVD is descending; eigenvalues ascending
             const i64 src = n - 1 - j;
             evals->d[j] = (real)(sv[(size_t)src] - sigma);

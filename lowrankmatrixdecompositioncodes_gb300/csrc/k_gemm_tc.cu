@@ -19,6 +19,7 @@
 #include <cuda.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cstring>
 #include <mutex>
 
@@ -569,18 +570,28 @@ static CUtensorMap make_map_tile(const void *ptr, long long e0, long long e1, lo
     return m;
 }
 
+// Raise a kernel's dynamic shared-memory limit on the current device to what the device's
+// opt-in per-block maximum (227 KB on GB300) leaves after the kernel's static shared memory
+// (the update epilogue's reduction scratch).
+template <typename Kern>
+static void set_max_dynamic_smem(Kern k, int dev) {
+    cudaFuncAttributes fa{};
+    RSVD_CK(cudaFuncGetAttributes(&fa, k));
+    int optin = 0;
+    RSVD_CK(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+    RSVD_CK(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, optin - (int)fa.sharedSizeBytes));
+}
+
 template <int KIND, bool A_MN, int EPI>
 static void launch(cudaStream_t s, dim3 grid, size_t smem, const Maps &maps, const Params &P) {
     auto k = tc_gemm_kernel<KIND, A_MN, EPI>;
-    static bool attr_set = false;   // per instantiation
-    if (!attr_set) {
-        // 227 KB per CTA in total: the dynamic part is what the kernel's static shared
-        // memory (the update epilogue's reduction scratch) leaves
-        cudaFuncAttributes fa{};
-        RSVD_CK(cudaFuncGetAttributes(&fa, k));
-        RSVD_CK(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     232448 - (int)fa.sharedSizeBytes));
-        attr_set = true;
+    // function attributes are per device: set once per (instantiation, device)
+    static std::atomic<bool> attr_set[128];
+    const int dev = ctx().device;
+    if (dev < 0 || dev >= 128) fail(RSVD_ERR_NO_DEVICE, "device ordinal out of range");
+    if (!attr_set[dev].load(std::memory_order_acquire)) {
+        set_max_dynamic_smem(k, dev);
+        attr_set[dev].store(true, std::memory_order_release);
     }
     k<<<grid, NTHR, smem, s>>>(maps, P);
     RSVD_LAUNCH_CK();
@@ -776,8 +787,7 @@ void *noalloc_setup(int dev) {
         cudaGetLastError();
         fail(RSVD_ERR_CUDA, std::string("cudaGetSymbolAddress(scratch) failed: ") + cudaGetErrorString(e));
     }
-    RSVD_CK(cudaFuncSetAttribute(tc::tc_gemm_kernel<tc::KIND_TF32, false, tc::EPI_PARTIAL>,
-                                 cudaFuncAttributeMaxDynamicSharedMemorySize, 232448));
+    tc::set_max_dynamic_smem(tc::tc_gemm_kernel<tc::KIND_TF32, false, tc::EPI_PARTIAL>, dev);
     g_noalloc_ptr[dev] = p;
     return p;
 }

@@ -1,7 +1,8 @@
 """Train the proposal network on the GPU with the engine's own kernels and write the weights.
 
+  python -m lowrankmatrixdecompositioncodes_gb300.learned.dataset --out train20k.npz   # (CPU, once)
   python -m lowrankmatrixdecompositioncodes_gb300.learned.train \\
-      --data lowrankmatrixdecompositioncodes_gb300/learned/train20k.npz \\
+      --data train20k.npz \\
       --out  lowrankmatrixdecompositioncodes_gb300/learned/proposal_mlp.bin
 
 The last 10% of the (seeded, shuffled) set is held out: it calibrates the safety margin and

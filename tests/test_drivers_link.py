@@ -13,7 +13,7 @@ import pytest
 
 from conftest import ROOT
 
-REF = "/root/reference"
+REF = os.environ.get("RSVDPACK_REFERENCE", "/root/reference")
 PKG = os.path.join(ROOT, "lowrankmatrixdecompositioncodes_gb300")
 DRIVERS = [
     ("multi_core_mkl_code/driver_multi_core_mkl1.c", "mkl", "rsvdpack"),

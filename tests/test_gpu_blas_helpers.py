@@ -101,3 +101,27 @@ def test_symmetric_eigensolver(eng, n):
     assert np.all(np.diff(lam) >= -1e-12 * scale)                     # ascending
     assert np.max(np.abs(Vec.T @ Vec - np.eye(n))) < 1e-12
     assert np.max(np.abs(Ssym @ Vec - Vec * lam)) < 1e-11 * scale
+
+
+def test_symmetric_eigensolver_ill_conditioned(eng):
+    """Eigenvalues spread over 12 decades (a graded positive definite matrix, condition 1e12):
+    every eigenvalue within ~eps ||S||_F absolutely of numpy.linalg.eigh, the bound stated for the
+    shifted Jacobi route, and the eigenvectors orthonormal."""
+    L = eng.lib
+    L.compute_evals_and_evecs_of_symm_matrix.argtypes = [eng.PMat, eng.PVec]
+    n = 120
+    Qm, _ = np.linalg.qr(G.standard_normal((n, n)))
+    lam_true = np.logspace(0, -12, n)
+    Ssym = (Qm * lam_true) @ Qm.T
+    Ssym = (Ssym + Ssym.T) / 2
+    pS, pe = eng.to_mat(Ssym.copy()), _vec(eng, np.zeros(n))
+    L.compute_evals_and_evecs_of_symm_matrix(pS, pe)
+    eng.check()
+    lam, Vec = eng.from_vec(pe), eng.from_mat(pS)
+    want = np.linalg.eigvalsh(Ssym)
+    fro = np.linalg.norm(Ssym)
+    bound = 64 * np.finfo(float).eps * fro
+    assert np.max(np.abs(lam - want)) < bound
+    assert np.max(np.abs(Vec.T @ Vec - np.eye(n))) < 1e-12
+    # the large eigenvalues keep their relative accuracy
+    np.testing.assert_allclose(lam[-10:], want[-10:], rtol=1e-12)

@@ -6,7 +6,8 @@ implicit synchronisation of cudaMalloc / cudaFree): its split-K partial sums liv
 scratch array inside the library instead of in workspace the call would allocate.  Its
 result must match the regular entry point (rsvdpack_dev_sketch, TF32 mode) within the
 TF32 tolerance, on two calls in a row (the second reuses the scratch the first left
-behind).  This file is collected last on purpose.
+behind), and the device's free memory must not change across calls on a warmed device.
+The file name sorts after every other test file, so pytest collects it last.
 """
 import ctypes as C
 
@@ -33,7 +34,8 @@ def _colmajor(rows, cols, ld, gen):
     return buf
 
 
-@pytest.mark.parametrize("m,n,w", [(4096, 2000, 272), (16384, 8192, 272), (3000, 700, 40)])
+# (3000, 1000, 600): w > 512, so the product runs in three 256-column tiles
+@pytest.mark.parametrize("m,n,w", [(4096, 2000, 272), (16384, 8192, 272), (3000, 700, 40), (3000, 1000, 600)])
 def test_no_alloc_matches_regular_entry_point_twice(engine, m, n, w):
     L = engine.lib
     _bind(L)
@@ -50,6 +52,8 @@ def test_no_alloc_matches_regular_entry_point_twice(engine, m, n, w):
     assert rc == 0, engine.last_error()
     ref = Y_ref[:, :n]
     scale = float(ref.abs().max())
+    # the exact FP64 product as a second anchor
+    exact = (A[:, :m].double() @ X[:, :m].double().T).T
     outs = []
     for _ in range(2):
         Y = torch.full((w, ldy), float("nan"), device="cuda", dtype=torch.float32)
@@ -59,12 +63,33 @@ def test_no_alloc_matches_regular_entry_point_twice(engine, m, n, w):
         got = Y[:, :n]
         err = float((got - ref).abs().max()) / scale
         assert err < TF32_TOL, f"relative difference {err:.3e}"
-        # exact FP64 product as a second anchor
-        exact = (A[:, :m].double() @ X[:, :m].double().T).T
         assert float((got.double() - exact).abs().max()) / float(exact.abs().max()) < TF32_TOL
         outs.append(got.clone())
     assert torch.equal(outs[0], outs[1]), "the two calls disagree"
     engine.set_precision("fp64")
+
+
+def test_no_alloc_leaves_free_memory_unchanged(engine):
+    """After a warm-up call (which loads the kernel's module, scratch array included), further
+    calls change the driver's count of free device memory by nothing."""
+    L = engine.lib
+    _bind(L)
+    m, n, w = 8192, 4096, 272
+    g = torch.Generator(device="cuda")
+    g.manual_seed(5)
+    A = _colmajor(m, n, m, g)
+    X = _colmajor(m, w, m, g)
+    Y = torch.empty(w, n, device="cuda", dtype=torch.float32)
+    rc = L.rsvdpack_dev_sketch_t_noalloc(A.data_ptr(), m, m, n, X.data_ptr(), m, w, Y.data_ptr(), n, None)
+    assert rc == 0, engine.last_error()
+    torch.cuda.synchronize()
+    free0, _ = torch.cuda.mem_get_info()
+    for _ in range(4):
+        rc = L.rsvdpack_dev_sketch_t_noalloc(A.data_ptr(), m, m, n, X.data_ptr(), m, w, Y.data_ptr(), n, None)
+        assert rc == 0, engine.last_error()
+    torch.cuda.synchronize()
+    free1, _ = torch.cuda.mem_get_info()
+    assert free1 == free0, f"free device memory changed by {free0 - free1} bytes"
 
 
 def test_no_alloc_rejects_products_beyond_its_scratch(engine):
