@@ -51,6 +51,8 @@ def parse():
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-learned", action="store_true")
     ap.add_argument("--no-batched", action="store_true")
+    ap.add_argument("--no-c1", action="store_true", help="skip the 2000 x 1000 FP64 fixed-rank leg")
+    ap.add_argument("--no-c5", action="store_true", help="skip the 20000 x 10000 two-sided ID / CUR leg")
     # bracket one leg's timed region with cudaProfilerStart/Stop (ncu --profile-from-start off)
     ap.add_argument("--profile-leg", choices=["solve", "learned", "batched"], default=None)
     # run one fixed profiling case (see PROFILE_CASES) and exit
@@ -356,6 +358,232 @@ def batched_leg(torch, eng, dev, execs=5, profile=False):
             "residual_checks": checks}
 
 
+# ------------------------------------------------------------------ checkers and extra legs
+def port_library():
+    """The CPU oracle (oracle/port: the reference's algorithms restated in C on OpenBLAS)."""
+    from lowrankmatrixdecompositioncodes_gb300.capi import RsvdLibrary
+    so = os.path.join(ROOT, "oracle", "port", "librsvd_port.so")
+    if not os.path.exists(so):
+        subprocess.check_call(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "port"])
+    return RsvdLibrary(so)
+
+
+def top_singular_values_fp64(torch, At, k):
+    """Checker: the top k singular values of A (At = column-major A as an n x m row-major tensor)
+    in FP64 -- A^T A formed in FP64 on the GPU, its top k eigenvalues by LAPACK dsyevr on the host
+    (scipy), square-rooted.  Relative accuracy ~eps (s_1 / s_i)^2: ~1e-12 for the workloads here."""
+    import numpy as np
+    import scipy.linalg as sla
+    Ad = At.double()
+    G = (Ad @ Ad.T).cpu().numpy()
+    del Ad
+    n = G.shape[0]
+    ev = sla.eigh(G, eigvals_only=True, subset_by_index=[n - k, n - 1], driver="evr", overwrite_a=True)
+    return np.sqrt(np.maximum(ev[::-1], 0.0))
+
+
+def sigma_rel_err(got, want):
+    import numpy as np
+    got = np.sort(np.asarray(got, dtype=float))[::-1][:len(want)]
+    return float(np.max(np.abs(got - want) / want))
+
+
+def sigma_rel_err_mean(got, want):
+    import numpy as np
+    got = np.sort(np.asarray(got, dtype=float))[::-1][:len(want)]
+    return float(np.mean(np.abs(got - want) / want))
+
+
+def dev_residual_norms(eng, A_ptr, dt, lda, m, n, U_ptr, ldu, S_ptr, V_ptr, ldv, k, iters=20):
+    L = eng.lib
+    L.rsvdpack_dev_residual_norms.restype = C.c_int
+    L.rsvdpack_dev_residual_norms.argtypes = [C.c_void_p, C.c_int, C.c_longlong, C.c_int, C.c_int, C.c_void_p,
+                                              C.c_longlong, C.c_void_p, C.c_void_p, C.c_longlong, C.c_int, C.c_int,
+                                              C.POINTER(C.c_double), C.POINTER(C.c_double)]
+    fro, spec = C.c_double(0), C.c_double(0)
+    rc = L.rsvdpack_dev_residual_norms(A_ptr, dt, lda, m, n, U_ptr, ldu, S_ptr, V_ptr, ldv, k, iters, C.byref(fro),
+                                       C.byref(spec))
+    if rc:
+        raise RuntimeError(f"residual norms failed: {eng.last_error()}")
+    return fro.value, spec.value
+
+
+def host_residuals(torch, eng, A, U, S, V, fro_a, spec_a):
+    """Relative Frobenius and spectral residual of a host factorisation A ~ U diag(S) V^T through
+    the engine's residual reporter (FP64 device data)."""
+    import numpy as np
+    dev = "cuda"
+    col = lambda X: torch.from_numpy(np.ascontiguousarray(X.T)).to(dev)
+    m, n = A.shape
+    k = U.shape[1]
+    dA, dU, dV = col(A), col(U), col(V)
+    dS = torch.from_numpy(np.asarray(S, dtype=np.float64).copy()).to(dev)
+    fro, spec = dev_residual_norms(eng, dA.data_ptr(), 0, m, m, n, dU.data_ptr(), m, dS.data_ptr(), dV.data_ptr(), n, k)
+    del dA, dU, dV, dS
+    return fro / fro_a, spec / spec_a
+
+
+def timed_c_call(fn, *args, reps=1):
+    """Seconds per call of a reference-API routine (host mat in, host mats out), outputs freed."""
+    ts = []
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        fn(*args)
+        ts.append(time.perf_counter() - t0)
+    return ts
+
+
+def plain_fixed_rank_leg(torch, eng, reps=10):
+    """Plain fixed-rank rSVD at the reference's own CPU-runnable size: A 2000 x 1000 FP64 =
+    U diag(10^(-6(i-1)/999)) V^T (Haar U, V from QR of seeded Gaussians), k=100, p=10, q=2, s=1,
+    vnum=1.  FP64 mode (the reference's arithmetic) and FP64X mode (double-float products, refined
+    l x l SVD): parity against the oracle on the same supplied test matrix, top-100 singular values
+    and residuals against FP64 LAPACK, and the C-API call timed from a host matrix, next to the
+    oracle on all host cores and on one."""
+    import numpy as np
+    from lowrankmatrixdecompositioncodes_gb300.capi import PMat, SeededOmega
+    m, n, k, p, q = 2000, 1000, 100, 10, 2
+    g = np.random.default_rng(2024)
+    s_all = 10.0 ** (-6.0 * np.arange(n) / (n - 1))
+    U0, _ = np.linalg.qr(g.standard_normal((m, n)))
+    V0, _ = np.linalg.qr(g.standard_normal((n, n)))
+    A = (U0 * s_all) @ V0.T
+    sv = np.linalg.svd(A, compute_uv=False)                  # FP64 LAPACK
+    fro_a, spec_a = float(np.linalg.norm(A)), float(sv[0])
+    opt_fro = float(np.sqrt(np.sum(sv[k:] ** 2)) / fro_a)
+    port = port_library()
+    threads = os.cpu_count() or 1
+    port.lib.rsvdpack_set_num_threads(threads)
+    port.set_omega(SeededOmega(99))
+    Uo, So, Vo = port.low_rank_svd_rand_decomp_fixed_rank(A, k, p, 1, q, 1)
+    so = np.diag(So)
+    out = {"workload": "plain fixed-rank rSVD 2000x1000 FP64, s_i = 10^(-6(i-1)/999), k=100 p=10 q=2 s=1 vnum=1",
+           "lapack_optimal_rel_frobenius": opt_fro,
+           "oracle": {"sigma_rel_err_top100": sigma_rel_err(so, sv[:k])}}
+    out["oracle"]["rel_frobenius"], out["oracle"]["rel_spectral"] = host_residuals(torch, eng, A, Uo, so, Vo, fro_a,
+                                                                                   spec_a)
+
+    def c_call(lib, M):
+        U, S, V, fr = lib.PMat(), lib.PMat(), lib.PMat(), lib.Int(0)
+        lib.lib.low_rank_svd_rand_decomp_fixed_rank(M, k, p, 1, q, 1, C.byref(fr), C.byref(U), C.byref(S),
+                                                    C.byref(V))
+        for x in (U, S, V):
+            lib.lib.matrix_delete(x)
+
+    for prec in ("fp64", "fp64x"):
+        eng.set_precision(prec)
+        eng.set_use_provider(True)
+        eng.set_omega(SeededOmega(99))
+        Ue, Se, Ve = eng.low_rank_svd_rand_decomp_fixed_rank(A, k, p, 1, q, 1)
+        eng.check()
+        se = np.diag(Se)
+        leg = {"parity_sigma_vs_oracle": float(np.max(np.abs(se - so) / so)),
+               "sigma_rel_err_top100": sigma_rel_err(se, sv[:k])}
+        leg["rel_frobenius"], leg["rel_spectral"] = host_residuals(torch, eng, A, Ue, se, Ve, fro_a, spec_a)
+        leg["parity_ok"] = leg["parity_sigma_vs_oracle"] < 1e-10
+        eng.set_use_provider(False)
+        M = eng.to_mat(A)
+        c_call(eng, M)
+        ts = timed_c_call(c_call, eng, M, reps=reps)
+        eng.lib.matrix_delete(M)
+        eng.check()
+        leg["c_api_ms"] = 1e3 * float(np.median(ts))
+        leg["solves_per_s"] = 1.0 / float(np.median(ts))
+        leg["h2d_bytes_per_call"] = m * n * 8
+        out[prec] = leg
+    eng.set_precision("fp64")
+    eng.set_use_provider(False)
+    port.set_omega(None)
+    M = port.to_mat(A)
+    for cores in (threads, 1):
+        port.lib.rsvdpack_set_num_threads(cores)
+        c_call(port, M)
+        ts = timed_c_call(c_call, port, M, reps=5)
+        out["cpu_cores_%d" % cores] = {"ms": 1e3 * float(np.median(ts)), "solves_per_s": 1.0 / float(np.median(ts)),
+                                       "cores": cores, "kind": "port"}
+    port.lib.matrix_delete(M)
+    port.lib.rsvdpack_set_num_threads(threads)
+    out["speedup_fp64x_vs_cpu_all_cores"] = out["fp64x"]["solves_per_s"] / out["cpu_cores_%d" % threads]["solves_per_s"]
+    return out
+
+
+def id_cur_leg(torch, eng):
+    """Two-sided ID and CUR: A 20000 x 10000 = U diag(i^-2) V^T (Haar factors; the spectrum
+    truncated at rank 1000, where i^-2 is 1e-6, so the singular values are known exactly), k=500,
+    p=20, q=2, s=1.  The engine (FP64X mode: the sketch passes as double-float products; and the
+    FP64 mode) and the oracle on all host cores get the same supplied test matrices: index sets
+    must be identical; times are of the C-API call from a host matrix; the CUR residual is
+    measured by the engine's residual reporter and set against the rank-500 optimum."""
+    import numpy as np
+    from lowrankmatrixdecompositioncodes_gb300.capi import SeededOmega
+    m, n, k, p, q, r = 20000, 10000, 500, 20, 2, 1000
+    g = torch.Generator(device="cuda")
+    g.manual_seed(5)
+    Uq, _ = torch.linalg.qr(torch.randn(m, r, device="cuda", dtype=torch.float64, generator=g))
+    Vq, _ = torch.linalg.qr(torch.randn(n, r, device="cuda", dtype=torch.float64, generator=g))
+    s = torch.arange(1, r + 1, device="cuda", dtype=torch.float64) ** -2.0
+    A = ((Uq * s) @ Vq.T).cpu().numpy()
+    del Uq, Vq
+    torch.cuda.empty_cache()
+    sv = s.cpu().numpy()
+    fro_a, spec_a = float(np.sqrt(np.sum(sv ** 2))), float(sv[0])
+    out = {"workload": "two-sided ID and CUR 20000x10000, s_i = i^-2 (rank 1000), k=500 p=20 q=2 s=1",
+           "rank_k_optimal_rel_frobenius": float(np.sqrt(np.sum(sv[k:] ** 2)) / fro_a),
+           "rank_k_optimal_rel_spectral": float(sv[k] / spec_a)}
+    port = port_library()
+    threads = os.cpu_count() or 1
+    port.lib.rsvdpack_set_num_threads(threads)
+
+    def run(lib, name, seed):
+        lib.set_omega(SeededOmega(seed))
+        M = lib.to_mat(A)
+        if name == "id":
+            o = [lib.PVec(), lib.PVec(), lib.PMat(), lib.PMat()]
+            fn = lambda: lib.lib.id_two_sided_rand_decomp_fixed_rank(M, k, p, q, 1, *[C.byref(x) for x in o])
+        else:
+            o = [lib.PMat(), lib.PMat(), lib.PMat()]
+            fn = lambda: lib.lib.cur_rand_decomp_fixed_rank(M, k, p, q, 1, *[C.byref(x) for x in o])
+        t0 = time.perf_counter()
+        fn()
+        t = time.perf_counter() - t0
+        lib.lib.matrix_delete(M)
+        if name == "id":
+            res = (lib.from_vec(o[0]), lib.from_vec(o[1]), lib.from_mat(o[2]), lib.from_mat(o[3]))
+        else:
+            res = tuple(lib.from_mat(x) for x in o)
+        return t, res
+
+    t_id_o, id_o = run(port, "id", 2026)
+    t_cur_o, cur_o = run(port, "cur", 2027)
+    out["cpu_all_cores"] = {"cores": threads, "kind": "port", "id_ms": 1e3 * t_id_o, "cur_ms": 1e3 * t_cur_o}
+
+    def cur_res(Cm, Um, Rm):
+        # A ~ C U R = (C) diag(1) (R^T U^T)^T
+        return host_residuals(torch, eng, A, Cm, np.ones(Cm.shape[1]), (Um @ Rm).T, fro_a, spec_a)
+
+    out["oracle_cur_rel_frobenius"], out["oracle_cur_rel_spectral"] = cur_res(*cur_o)
+    for prec in ("fp64x", "fp64"):
+        eng.set_precision(prec)
+        eng.set_use_provider(True)
+        run(eng, "id", 2026)                     # warm-up (module loads, pools)
+        t_id, id_e = run(eng, "id", 2026)
+        t_cur, cur_e = run(eng, "cur", 2027)
+        eng.check()
+        leg = {"id_ms": 1e3 * t_id, "cur_ms": 1e3 * t_cur,
+               "index_sets_identical": bool(np.array_equal(id_e[0], id_o[0]) and np.array_equal(id_e[1], id_o[1])),
+               "cur_gathers_identical": bool(np.array_equal(cur_e[0], cur_o[0]) and np.array_equal(cur_e[2], cur_o[2])),
+               "h2d_bytes_per_call": m * n * 8}
+        leg["cur_rel_frobenius"], leg["cur_rel_spectral"] = cur_res(*cur_e)
+        leg["speedup_id_vs_cpu"] = t_id_o / t_id
+        leg["speedup_cur_vs_cpu"] = t_cur_o / t_cur
+        out[prec] = leg
+    eng.set_precision("fp64")
+    eng.set_use_provider(False)
+    port.set_omega(None)
+    del A
+    return out
+
+
 def run_reference(args):
     rank, world, _ = dist_env()
     if rank != 0:
@@ -445,11 +673,18 @@ def run_ours(args):
         R = Ad - (Ur * Sv) @ Vr.T
         return float(torch.linalg.norm(R) / torch.linalg.norm(Ad))
 
-    # matched-error check: same test matrix for the working precision and for FP64
+    # matched-error check: same test matrix for the working precision and for FP64; singular
+    # values against FP64 LAPACK (top k of A^T A by dsyevr), residuals by the engine's reporter
+    sv_lapack = top_singular_values_fp64(torch, At, k) if rank == 0 else None
+    fro_a = float(torch.linalg.norm(At.double()))
     L.rsvdpack_reset_omega_counter()
     solve()
     res_mixed = residual()
-    res_fp64 = None
+    fro_m, spec_m = dev_residual_norms(eng, dA, dt, m, m, n, U.data_ptr(), m, Sv.data_ptr(), V.data_ptr(), n, k)
+    sig_mixed = sigma_rel_err(Sv.cpu().numpy(), sv_lapack) if sv_lapack is not None else None
+    sig_mixed16 = sigma_rel_err(Sv.cpu().numpy()[:16], sv_lapack[:16]) if sv_lapack is not None else None
+    sig_mixed_mean = sigma_rel_err_mean(Sv.cpu().numpy(), sv_lapack) if sv_lapack is not None else None
+    res_fp64 = spec_fp64 = sig_fp64 = sig_fp64_16 = sig_fp64_mean = None
     if args.precision != "fp64":
         eng.set_precision("fp64")
         A64 = At.double()
@@ -463,7 +698,14 @@ def run_ours(args):
             raise RuntimeError(f"fp64 solve failed: {eng.last_error()}")
         R = A64.T - (U64.T * S64) @ V64
         res_fp64 = float(torch.linalg.norm(R) / torch.linalg.norm(A64))
-        del A64, U64, V64, S64, R
+        del R
+        _, spec_fp64 = dev_residual_norms(eng, A64.data_ptr(), 0, m, m, n, U64.data_ptr(), m, S64.data_ptr(),
+                                          V64.data_ptr(), n, k)
+        if sv_lapack is not None:
+            sig_fp64 = sigma_rel_err(S64.cpu().numpy(), sv_lapack)
+            sig_fp64_16 = sigma_rel_err(S64.cpu().numpy()[:16], sv_lapack[:16])
+            sig_fp64_mean = sigma_rel_err_mean(S64.cpu().numpy(), sv_lapack)
+        del A64, U64, V64, S64
         eng.set_precision(args.precision)
         torch.cuda.empty_cache()
 
@@ -654,6 +896,16 @@ def run_ours(args):
         batched = batched_leg(torch, eng, dev, profile=(args.profile_leg == "batched"))
         eng.set_precision(args.precision)
 
+    # ---------------- the plain fixed-rank workload (2000 x 1000 FP64) and the two-sided ID / CUR
+    # workload (20000 x 10000), each with its oracle check
+    c1 = c5 = None
+    if rank == 0 and not args.no_c1:
+        c1 = plain_fixed_rank_leg(torch, eng)
+        eng.set_precision(args.precision)
+    if rank == 0 and not args.no_c5:
+        c5 = id_cur_leg(torch, eng)
+        eng.set_precision(args.precision)
+
     # ---------------- CPU baseline: the oracle on the host cores, one full solve
     cpu = None
     if rank == 0 and not args.no_cpu:
@@ -662,6 +914,17 @@ def run_ours(args):
         t_cpu = cpu_solve_seconds(A_host, threads, repeats=1)
         cpu = {"value": 1.0 / t_cpu[0], "unit": "solves/s", "cores": threads, "kind": "port",
                "sample": "1 full solve of the workload on the CPU oracle (reference algorithm, OpenBLAS)"}
+        # one core: the oracle with one OpenMP / BLAS thread, pinned to one core (stands in for the
+        # reference's single-core GSL build, which has no fixed-rank routine and no GSL here)
+        prev = os.sched_getaffinity(0)
+        try:
+            os.sched_setaffinity(0, {min(prev)})
+            t1 = cpu_solve_seconds(A_host, 1, repeats=1)
+        finally:
+            os.sched_setaffinity(0, prev)
+        cpu["single_core"] = {"value": 1.0 / t1[0], "unit": "solves/s", "cores": 1, "kind": "port",
+                              "sample": "1 full solve, 1 thread pinned to one core"}
+        del A_host
 
     if rank == 0:
         line = {
@@ -673,8 +936,20 @@ def run_ours(args):
                        "p": P, "q": Q, "s": S_ORTH, "precision": args.precision,
                        "l2": "inputs larger than L2 (A = 512 MiB)", "parallelism": f"replicas x{world}"},
             "residual": {"rel_frobenius": res_mixed, "fp64_same_method": res_fp64,
-                         "matched": (res_fp64 is None) or (res_mixed <= (1 + 1e-3) * res_fp64)},
+                         "rel_frobenius_engine_reporter": fro_m / fro_a,
+                         "rel_spectral": spec_m / float(sv_lapack[0]),
+                         "fp64_same_method_rel_spectral": (spec_fp64 / float(sv_lapack[0])
+                                                           if spec_fp64 is not None else None),
+                         "sigma_rel_err_topk": sig_mixed, "fp64_same_method_sigma_rel_err_topk": sig_fp64,
+                         "sigma_rel_err_top16": sig_mixed16, "fp64_same_method_sigma_rel_err_top16": sig_fp64_16,
+                         "sigma_rel_err_mean_topk": sig_mixed_mean,
+                         "fp64_same_method_sigma_rel_err_mean_topk": sig_fp64_mean,
+                         "sigma_checker": "FP64 LAPACK: top-k eigenvalues of A^T A (dsyevr), square-rooted",
+                         "matched": (res_fp64 is None) or (res_mixed <= (1 + 1e-3) * res_fp64),
+                         "matched_sigma_rule": "max top-k relative sigma error within 1% of the FP64 path's",
+                         "matched_sigma": (sig_fp64 is None) or (sig_mixed <= (1 + 1e-2) * sig_fp64 + 1e-9)},
             "roofline": roof, "plain_gpu": plain, "bf16": bf16_leg, "learned_qb": learned_leg, "batched": batched,
+            "plain_fixed_rank_2000x1000": c1, "id_cur_20000x10000": c5,
             "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches, "clocks": clocks,
             "device": name,
         }

@@ -280,13 +280,18 @@ const char *rsvdpack_last_error_string(void);
 void rsvdpack_clear_error(void);
 
 /* Arithmetic of the large products (sketch, power rounds, projections) and of the
- * storage of A on the device.  Small k x k work (Cholesky, Jacobi, triangular
- * solves, pivot decisions) is FP64 in every mode. */
+ * storage of A on the device.  Small k x k work: in RSVD_PREC_FP64, FP64 throughout (Cholesky,
+ * one-sided Jacobi, triangular solves); in the other modes the l x l SVD is the FP32 one-sided
+ * Jacobi refined to FP64 accuracy by double-float products (singular values to ~1e-14 relative
+ * of the l x l factor), and the Cholesky factorisations of FP32-data Grams run in FP32.  Pivot
+ * decisions are FP64 in every mode. */
 enum {
     RSVD_PREC_FP64 = 0,   /* everything FP64: reproduces the reference (default) */
     RSVD_PREC_FP32 = 1,   /* A and tall factors FP32, CUDA-core FP32 products */
     RSVD_PREC_TF32 = 2,   /* A FP32, tcgen05 kind::tf32 products, FP32 accumulate */
-    RSVD_PREC_BF16 = 3    /* A FP32 + BF16 copy, tcgen05 kind::f16 (bf16) sketch products */
+    RSVD_PREC_BF16 = 3,   /* A FP32 + BF16 copy, tcgen05 kind::f16 (bf16) sketch products */
+    RSVD_PREC_FP64X = 4   /* A FP64; the large products FP64-accurate on the FP32 pipe (double-
+                             float accumulation, ~2^-46 relative per term, ~5x GB300's FP64 rate) */
 };
 
 typedef struct {
@@ -358,6 +363,26 @@ int rsvdpack_dev_gemm_3xtf32(const float *dA, long long lda, const float *dX, lo
 int rsvdpack_dev_update_3xtf32(const float *dA, long long lda, const float *dX, long long ldx, int M, int N, int K,
                                float *dC, long long ldc, double *fro2);
 
+/* Residual norms of a low-rank approximation on device data (the reference reports only the
+ * Frobenius error, via get_percent_error_between_two_mats on the formed product): *fro receives
+ * ||A - U diag(S) V^T||_F and *spec the spectral norm estimate (block power iteration, `iters`
+ * rounds of 8 vectors, then Rayleigh-Ritz: a lower bound that converges to ||.||_2); either may be
+ * NULL.  A m x n (lda), U m x k (ldu), V n x k (ldv) in dtype RSVD_DT_F64 or RSVD_DT_F32; S: k
+ * doubles on the device.  The residual is formed once on the device (double-float products for
+ * FP64 data) and kept in FP32. */
+int rsvdpack_dev_residual_norms(const void *dA, int dtype, long long lda, int m, int n, const void *dU,
+                                long long ldu, const double *dS, const void *dV, long long ldv, int k, int iters,
+                                double *fro, double *spec);
+
+/* FP64-accurate product on the FP32 pipe (no counterpart in the reference):
+ * C (M x N, ldc) = alpha op(A) op(B) + beta C, op(X) = X^T when its flag is set; FP64 device
+ * data, column-major.  Each operand is split once into FP32 parts (hi + lo, scaled on the device
+ * by a power of two) and every product term is accumulated in double-float arithmetic (exact
+ * FP32 two-product, compensated two-sum): ~2^-46 relative per term, about five times the rate of
+ * GB300's FP64 pipe.  The product time is reported as rsvdpack_last_timing()->sketch_ms. */
+int rsvdpack_dev_gemm_df64(int ta, int tb, int M, int N, int K, double alpha, const double *dA, long long lda,
+                           const double *dB, long long ldb, double beta, double *dC, long long ldc);
+
 /* The calling thread's engine stream (a cudaStream_t), for event timing by callers. */
 void *rsvdpack_stream(void);
 
@@ -380,7 +405,9 @@ void rsvdpack_batch_plan_destroy(rsvdpack_batch_plan *plan);
 
 /* The l x l steps on their own (device FP64 storage, column-major; compute in FP32 when
  * fp32 != 0, else FP64).  rsvdpack_dev_small_svd: G (n x n) = U diag(S) V^T, S descending,
- * by one-sided Jacobi (the engine's l x l SVD); G is overwritten; returns the sweep count or
+ * by one-sided Jacobi (the engine's l x l SVD); fp32 == 2 selects the mixed modes' form: the
+ * FP32 Jacobi followed by four FP64-accurate refinement steps (double-float products on the
+ * FP32 pipe, exact FP64 rotations of nearly equal pairs), singular values to ~1e-14 relative; returns the FP32 or FP64 sweep count or
  * a negative RSVD_ERR_* code.  rsvdpack_dev_small_cholesky: G = R^T R in place (upper R, lower
  * part zeroed); returns RSVD_OK, RSVD_ERR_NUMERIC on breakdown, or another RSVD_ERR_* code. */
 int rsvdpack_dev_small_svd(double *dG, int n, long long ldg, double *dU, long long ldu, double *dS, double *dV,

@@ -21,7 +21,7 @@ LIB_PATH = os.path.join(PKG_DIR, "librsvdpack.so")
 LIB64_PATH = os.path.join(PKG_DIR, "librsvdpack64.so")
 LIBF32_PATH = os.path.join(PKG_DIR, "librsvdpack_f32.so")
 
-PREC = {"fp64": 0, "fp32": 1, "tf32": 2, "bf16": 3}
+PREC = {"fp64": 0, "fp32": 1, "tf32": 2, "bf16": 3, "fp64x": 4}
 
 
 class RsvdOpts(C.Structure):

@@ -77,7 +77,10 @@ void need_int(Ts... v) {
 }
 
 // Working precision of the tall products for this call.
-bool use_fp32_path() { return ctx().opts.precision != RSVD_PREC_FP64; }
+bool use_fp32_path() {
+    const int p = ctx().opts.precision;
+    return p != RSVD_PREC_FP64 && p != RSVD_PREC_FP64X;
+}
 
 template <typename T>
 DMat<T> upload(const mat *M) {
@@ -636,9 +639,9 @@ void upper_triangular_system_solve(mat *A, mat *B, mat *X, rsvd_int solve_type) 
 // Eigenvalues ascending into evals, eigenvectors into the columns of S (MVF:1206-1209, LAPACK dsyev
 // 'V' 'U': the upper triangle of S defines the matrix).  The engine's FP64 one-sided Jacobi SVD of
 // S + sigma I with sigma = ||S||_F, which is positive semidefinite, so that its singular pairs are
-// eigenpairs: lambda = sv - sigma.  Absolute accuracy of every eigenvalue ~eps ||S||_F (the shift's
-// size; dsyev's bound is eps ||S||_2, at most sqrt(n) times smaller), so eigenvalues far below
-// ||S||_F carry correspondingly fewer correct digits.  A Jacobi run that hits its sweep limit
+// eigenpairs: lambda = sv - sigma.  Absolute accuracy of every eigenvalue ~n eps ||S||_F (the
+// Jacobi's backward error on the shifted matrix; dsyev's bound is of order eps ||S||_2), so
+// eigenvalues far below ||S||_F carry correspondingly fewer correct digits.  A Jacobi run that hits its sweep limit
 // returns RSVD_ERR_NUMERIC instead of unconverged pairs.
 void compute_evals_and_evecs_of_symm_matrix(mat *S, vec *evals) {
     guarded("compute_evals_and_evecs_of_symm_matrix", [&] {
@@ -1241,6 +1244,51 @@ int rsvdpack_dev_gemm_3xtf32(const float *dA, long long lda, const float *dX, lo
     return rsvdpack_last_error();
 }
 
+int rsvdpack_dev_residual_norms(const void *dA, int dtype, long long lda, int m, int n, const void *dU,
+                                long long ldu, const double *dS, const void *dV, long long ldv, int k, int iters,
+                                double *fro, double *spec) {
+    guarded("rsvdpack_dev_residual_norms", [&] {
+        need(dA && (k == 0 || (dU && dS && dV)), "null device pointer");
+        need(m > 0 && n > 0 && k >= 0 && k <= std::min(m, n) && iters >= 0, "bad sizes");
+        need(lda >= m && (k == 0 || (ldu >= m && ldv >= n)), "bad leading dimension");
+        need(dtype == RSVD_DT_F64 || dtype == RSVD_DT_F32, "dtype must be RSVD_DT_F64 or RSVD_DT_F32");
+        begin_call();
+        order_after_default_stream();
+        if (dtype == RSVD_DT_F64) {
+            residual_norms<double>(DM<double>{(double *)dA, m, n, lda}, DM<double>{(double *)dU, m, k, ldu}, dS,
+                                   DM<double>{(double *)dV, n, k, ldv}, fro, spec, iters);
+        } else {
+            residual_norms<float>(DM<float>{(float *)dA, m, n, lda}, DM<float>{(float *)dU, m, k, ldu}, dS,
+                                  DM<float>{(float *)dV, n, k, ldv}, fro, spec, iters);
+        }
+        RSVD_CK(cudaStreamSynchronize(ctx().stream));
+        ctx().timing.kernel_launches = ctx().launches;
+    });
+    return rsvdpack_last_error();
+}
+
+int rsvdpack_dev_gemm_df64(int ta, int tb, int M, int N, int K, double alpha, const double *dA, long long lda,
+                           const double *dB, long long ldb, double beta, double *dC, long long ldc) {
+    guarded("rsvdpack_dev_gemm_df64", [&] {
+        need(dA && dB && dC, "null device pointer");
+        need(M > 0 && N > 0 && K > 0, "bad sizes");
+        need(lda >= (ta ? K : M) && ldb >= (tb ? N : K) && ldc >= M, "bad leading dimension");
+        begin_call();
+        order_after_default_stream();
+        cudaStream_t st = ctx().stream;
+        DM<double> A{const_cast<double *>(dA), ta ? K : M, ta ? M : K, lda};
+        DM<double> B{const_cast<double *>(dB), tb ? N : K, tb ? K : N, ldb};
+        Df64Split As(st, A), Bs(st, B);
+        {
+            PhaseTimer pt(&ctx().timing.sketch_ms);
+            df64_gemm(st, ta != 0, tb != 0, alpha, As, Bs, beta, DM<double>{dC, M, N, ldc});
+        }
+        phase_collect();
+        ctx().timing.kernel_launches = ctx().launches;
+    });
+    return rsvdpack_last_error();
+}
+
 int rsvdpack_dev_update_3xtf32(const float *dA, long long lda, const float *dX, long long ldx, int M, int N, int K,
                                float *dC, long long ldc, double *fro2) {
     guarded("rsvdpack_dev_update_3xtf32", [&] {
@@ -1399,7 +1447,13 @@ int rsvdpack_dev_small_svd(double *dG, int n, long long ldg, double *dU, long lo
         cudaStream_t st = ctx().stream;
         DM<double> G{dG, n, n, ldg}, U{dU, n, n, ldu}, V{dV, n, n, ldv};
         int *flag = ctx().d_flags + FLAG_JACOBI_NOCONV;
-        sweeps = fp32 ? jacobi_small<float>(st, G, U, V, dS, flag) : jacobi_small<double>(st, G, U, V, dS, flag);
+        if (fp32 == 2) {
+            // the mixed modes' l x l SVD: FP32 Jacobi, then the FP64-accurate refinement
+            sweeps = jacobi_small<float>(st, G, U, V, dS, flag);
+            svd_refine(st, G, V, U, dS, 4);
+        } else {
+            sweeps = fp32 ? jacobi_small<float>(st, G, U, V, dS, flag) : jacobi_small<double>(st, G, U, V, dS, flag);
+        }
         RSVD_CK(cudaStreamSynchronize(st));
     });
     const int e = rsvdpack_last_error();

@@ -4,6 +4,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <memory>
 #include <type_traits>
 
 namespace rsvd {
@@ -117,9 +118,60 @@ DM<__nv_bfloat16> to_bf16(cudaStream_t s, DM<float> X, DMat<__nv_bfloat16> &tmp,
     tmp = std::move(d);
     return tmp.v;
 }
+
+// FP64X mode: the double-float split of the large FP64 operand (normally A), kept for the
+// duration of one API call like the BF16 copy above.
+struct Df64Cache {
+    const void *src = nullptr;
+    i64 r = 0, c = 0, ld = 0;
+    std::unique_ptr<Df64Split> sp;
+};
+thread_local Df64Cache t_df64_a;
+
+const Df64Split &df64_operand(cudaStream_t s, DM<double> X, std::unique_ptr<Df64Split> &tmp, bool cache) {
+    if (cache && t_df64_a.sp && t_df64_a.src == X.p && t_df64_a.r == X.r && t_df64_a.c == X.c && t_df64_a.ld == X.ld)
+        return *t_df64_a.sp;
+    auto sp = std::make_unique<Df64Split>(s, X);
+    if (!cache) {
+        tmp = std::move(sp);
+        return *tmp;
+    }
+    t_df64_a.sp = std::move(sp);
+    t_df64_a.src = X.p; t_df64_a.r = X.r; t_df64_a.c = X.c; t_df64_a.ld = X.ld;
+    return *t_df64_a.sp;
+}
 }  // namespace
 
-void release_operand_cache() { t_bf16_a = Bf16Cache{}; }
+void release_operand_cache() {
+    t_bf16_a = Bf16Cache{};
+    t_df64_a = Df64Cache{};
+}
+
+bool fp64x_mode() { return ctx().opts.precision == RSVD_PREC_FP64X; }
+
+// Large FP64 products: FP64 CUDA-core GEMM, or in the FP64X mode the double-float product on
+// the FP32 pipe with the larger operand's split cached for the call.
+void prod_f64(cudaStream_t s, bool ta, bool tb, double alpha, DM<double> A, DM<double> B, double beta,
+              DM<double> C) {
+    const i64 M = ta ? A.c : A.r, K = ta ? A.r : A.c, N = tb ? B.r : B.c;
+    const bool big = (double)M * (double)N * (double)K >= 4.0e6;
+    if (fp64x_mode() && big) {
+        if (t_df64_a.src == (const void *)C.p) t_df64_a = Df64Cache{};   // C is about to change
+        // only A-sized operands (>= 2^24 entries: A itself or the QB loop's working copy, alive
+        // for the whole call) are cached; the pointer of a freed temporary may come back from
+        // the stream-ordered allocator for another matrix of the same shape
+        std::unique_ptr<Df64Split> ta_tmp, tb_tmp;
+        const bool a_big = A.r * A.c >= B.r * B.c;
+        const i64 big_n = a_big ? A.r * A.c : B.r * B.c;
+        const bool cache = big_n >= (1ll << 24);
+        const Df64Split &As = df64_operand(s, A, ta_tmp, cache && a_big);
+        const Df64Split &Bs = df64_operand(s, B, tb_tmp, cache && !a_big);
+        df64_gemm(s, ta, tb, alpha, As, Bs, beta, C);
+        return;
+    }
+    if (t_df64_a.src == (const void *)C.p) t_df64_a = Df64Cache{};
+    gemm<double>(s, ta, tb, alpha, A, B, beta, C);
+}
 
 // Tensor-core routing (FP32 data, TF32 / BF16 modes, store form C = alpha op(A) B):
 //   op(A) = A^T (A is the K-major operand): TF32 mode -> kind::tf32 on the FP32 data as is;
@@ -166,10 +218,24 @@ void prod(cudaStream_t s, bool ta, bool tb, T alpha, DM<T> A, DM<T> B, T beta, D
         }
     }
     if (t_bf16_a.src == (const void *)C.p) release_operand_cache();
+    if constexpr (std::is_same<T, double>::value) {
+        prod_f64(s, ta, tb, alpha, A, B, beta, C);
+        return;
+    }
     gemm<T>(s, ta, tb, alpha, A, B, beta, C);
 }
 template void prod<double>(cudaStream_t, bool, bool, double, DM<double>, DM<double>, double, DM<double>);
 template void prod<float>(cudaStream_t, bool, bool, float, DM<float>, DM<float>, float, DM<float>);
+
+namespace {
+// Factor formation and other products outside the sketch passes: the CUDA-core GEMM of the
+// working precision, or for FP64 data the FP64X mode's double-float product.
+template <typename T>
+void gemm_w(cudaStream_t s, bool ta, bool tb, T alpha, DM<T> A, DM<T> B, T beta, DM<T> C) {
+    if constexpr (std::is_same<T, double>::value) prod_f64(s, ta, tb, alpha, A, B, beta, C);
+    else gemm<T>(s, ta, tb, alpha, A, B, beta, C);
+}
+}  // namespace
 
 namespace {
 
@@ -217,7 +283,7 @@ static bool chol_apply(cudaStream_t s, DM<T> Y, DM<double> G, DM<T> Q, int *flag
     if (trsm_right_tiles<T>(s, Y, G, (const T *)dinv.get(), Q)) return true;
     DMat<T> Ri(c, c, s, false);
     tri_inv_tiles<T, T>(s, G, (const T *)dinv.get(), Ri.v);
-    gemm<T>(s, false, false, T(1), Y, Ri.v, T(0), Q);
+    gemm_w<T>(s, false, false, T(1), Y, Ri.v, T(0), Q);
     return true;
 }
 
@@ -277,6 +343,14 @@ void orth(DM<T> Y, DM<T> Q, DM<double> *R, int passes) {
     const i64 c = Y.c;
     if (Y.r < c) fail(RSVD_ERR_ARGUMENT, "orth: more columns than rows");
     int *flag = cx.d_flags + FLAG_CHOL_BREAKDOWN;
+    if (cx.chol_force_hh) {
+        DMat<T> W(Y.r, c, s, false);
+        copy_dm<T>(s, Y, W.v);
+        DMat<double> Rh(c, c, s, true);
+        householder_qr<T>(s, W.v, Q, Rh.v);
+        if (R) copy_dm<double>(s, Rh.v, *R);
+        return;
+    }
     if constexpr (std::is_same<T, float>::value) {
         const int prec = cx.opts.precision;
         if (c > 288 && (prec == RSVD_PREC_TF32 || prec == RSVD_PREC_BF16) && Y.r >= 128) {
@@ -366,15 +440,18 @@ static SvdOut<T> svd_from_q(DM<T> A, DM<T> Q, int k, int vnum) {
         {
             DMat<double> RhT(l, l, s, false);
             transpose<double>(s, Rh.v, RhT.v);
-            jacobi_small<T>(s, RhT.v, Vh.v, Uh.v, (double *)svb.get(), cx.d_flags + FLAG_JACOBI_NOCONV, false);
+            if (std::is_same<T, float>::value || fp64x_mode())
+                small_svd_refined(s, RhT.v, Vh.v, Uh.v, (double *)svb.get(), cx.d_flags + FLAG_JACOBI_NOCONV);
+            else
+                jacobi_small<T>(s, RhT.v, Vh.v, Uh.v, (double *)svb.get(), cx.d_flags + FLAG_JACOBI_NOCONV, false);
         }
         // the leading k singular pairs: column prefixes of Vh, Uh in the working precision
         DMat<T> Vk(l, k, s, false), Uk(l, k, s, false);
         convert<double, T>(s, Vh.v.cols(0, k), Vk.v);
         convert<double, T>(s, Uh.v.cols(0, k), Uk.v);
         // factor formation stays in the working precision (never rounded to bf16)
-        gemm<T>(s, false, false, T(1), Q, Vk.v, T(0), out.U.v);
-        gemm<T>(s, false, false, T(1), Qh.v, Uk.v, T(0), out.V.v);
+        gemm_w<T>(s, false, false, T(1), Q, Vk.v, T(0), out.U.v);
+        gemm_w<T>(s, false, false, T(1), Qh.v, Uk.v, T(0), out.V.v);
         // the one host wait of this step: singular values into pageable memory
         RSVD_CK(cudaMemcpyAsync(sv.data(), svb.get(), sizeof(double) * l, cudaMemcpyDeviceToHost, s));
         RSVD_CK(cudaStreamSynchronize(s));
@@ -383,7 +460,10 @@ static SvdOut<T> svd_from_q(DM<T> A, DM<T> Q, int k, int vnum) {
         // eig(B B^T) ascending, keep the last k; U = Q Uh; V = B^T Uh S^-1   (RRA:176-224)
         DMat<double> BBt(l, l, s, false);
         gram<T>(s, Bt.v, BBt.v);                                         // B B^T = Bt^T Bt
-        jacobi_small<T>(s, BBt.v, Uh.v, Vh.v, (double *)svb.get(), cx.d_flags + FLAG_JACOBI_NOCONV, false);
+        if (std::is_same<T, float>::value || fp64x_mode())
+            small_svd_refined(s, BBt.v, Uh.v, Vh.v, (double *)svb.get(), cx.d_flags + FLAG_JACOBI_NOCONV);
+        else
+            jacobi_small<T>(s, BBt.v, Uh.v, Vh.v, (double *)svb.get(), cx.d_flags + FLAG_JACOBI_NOCONV, false);
         RSVD_CK(cudaMemcpyAsync(sv.data(), svb.get(), sizeof(double) * l, cudaMemcpyDeviceToHost, s));
         RSVD_CK(cudaStreamSynchronize(s));
         // ascending order position i in [0,k) <- descending position k-1-i
@@ -399,8 +479,8 @@ static SvdOut<T> svd_from_q(DM<T> A, DM<T> Q, int k, int vnum) {
         DMat<T> Uk(l, k, s, false), Uks(l, k, s, false);
         select_cols<double, T>(s, Vh.v, perm, nullptr, Uk.v);
         select_cols<double, T>(s, Vh.v, perm, &inv, Uks.v);
-        gemm<T>(s, false, false, T(1), Q, Uk.v, T(0), out.U.v);
-        gemm<T>(s, false, false, T(1), Bt.v, Uks.v, T(0), out.V.v);
+        gemm_w<T>(s, false, false, T(1), Q, Uk.v, T(0), out.U.v);
+        gemm_w<T>(s, false, false, T(1), Bt.v, Uks.v, T(0), out.V.v);
     }
     RSVD_CK(cudaStreamSynchronize(s));
     return out;
@@ -408,7 +488,7 @@ static SvdOut<T> svd_from_q(DM<T> A, DM<T> Q, int k, int vnum) {
 
 // ------------------------------------------------------------------ fixed-rank rSVD (RRA:73-234)
 template <typename T>
-SvdOut<T> svd_fixed_rank(DM<T> A, int k, int p, int vnum, int q, int s_) {
+static SvdOut<T> svd_fixed_rank_once(DM<T> A, int k, int p, int vnum, int q, int s_) {
     Ctx &cx = ctx();
     cudaStream_t s = cx.stream;
     const i64 m = A.r, n = A.c, l = (i64)k + p;
@@ -424,6 +504,44 @@ SvdOut<T> svd_fixed_rank(DM<T> A, int k, int p, int vnum, int q, int s_) {
     DMat<T> Q(m, l, s, false);
     orth<T>(Y.v, Q.v, nullptr, 2);
     return svd_from_q<T>(A, Q.v, k, vnum);
+}
+// FP32 data on Philox test matrices: the orthonormalisations run without a host wait on each
+// Cholesky's breakdown flag; the flag is read once, with the singular values, and a breakdown
+// anywhere repeats the solve on the same test matrices with Householder QR throughout.  (With a
+// registered test-matrix provider, each draw is a provider request, so the per-factorisation
+// checks stay.)
+template <typename T>
+SvdOut<T> svd_fixed_rank(DM<T> A, int k, int p, int vnum, int q, int s_) {
+    Ctx &cx = ctx();
+    const bool defer = std::is_same<T, float>::value && !(cx.opts.use_provider && omega_provider_active()) &&
+                       !cx.chol_deferred && !cx.chol_force_hh;
+    if (!defer) return svd_fixed_rank_once<T>(A, k, p, vnum, q, s_);
+    const unsigned long long draws = philox_calls();
+    int *flag = cx.d_flags + FLAG_CHOL_BREAKDOWN;
+    RSVD_CK(cudaMemsetAsync(flag, 0, sizeof(int), cx.stream));
+    cx.chol_deferred = true;
+    SvdOut<T> out;
+    try {
+        out = svd_fixed_rank_once<T>(A, k, p, vnum, q, s_);
+    } catch (...) {
+        cx.chol_deferred = false;
+        throw;
+    }
+    cx.chol_deferred = false;
+    int h = 0;
+    RSVD_CK(cudaMemcpyAsync(&h, flag, sizeof(int), cudaMemcpyDeviceToHost, cx.stream));
+    RSVD_CK(cudaStreamSynchronize(cx.stream));
+    if (!h) return out;
+    philox_calls() = draws;
+    cx.chol_force_hh = true;
+    try {
+        out = svd_fixed_rank_once<T>(A, k, p, vnum, q, s_);
+    } catch (...) {
+        cx.chol_force_hh = false;
+        throw;
+    }
+    cx.chol_force_hh = false;
+    return out;
 }
 template SvdOut<double> svd_fixed_rank<double>(DM<double>, int, int, int, int, int);
 template SvdOut<float> svd_fixed_rank<float>(DM<float>, int, int, int, int, int);
@@ -822,14 +940,14 @@ IdOut id_rand(DM<double> A, int k, int p, int q, int s_) {
     const i64 m = A.r, n = A.c, l = (i64)k + p;
     DMat<double> Om = make_omega<double>(l, m);
     DMat<double> Yt(n, l, s, false), Z1(n, l, s, false), Y2(m, l, s, false), Z2(m, l, s, false);
-    gemm<double>(s, true, true, 1.0, A, Om.v, 0.0, Yt.v);               // Yt = A^T Om^T
+    prod_f64(s, true, true, 1.0, A, Om.v, 0.0, Yt.v);                   // Yt = A^T Om^T
     for (int j = 1; j <= q; j++) {
         DM<double> z1 = Yt.v;
         if ((2 * j - 2) % s_ == 0) { orth<double>(Yt.v, Z1.v, nullptr, 1); z1 = Z1.v; }
-        gemm<double>(s, false, false, 1.0, A, z1, 0.0, Y2.v);            // (Z M^T)^T = M Z^T
+        prod_f64(s, false, false, 1.0, A, z1, 0.0, Y2.v);                // (Z M^T)^T = M Z^T
         DM<double> z2 = Y2.v;
         if ((2 * j - 1) % s_ == 0) { orth<double>(Y2.v, Z2.v, nullptr, 1); z2 = Z2.v; }
-        gemm<double>(s, true, false, 1.0, A, z2, 0.0, Yt.v);             // (Z M)^T = M^T Z^T
+        prod_f64(s, true, false, 1.0, A, z2, 0.0, Yt.v);                 // (Z M)^T = M^T Z^T
     }
     DMat<double> Y(l, n, s, false);
     transpose<double>(s, Yt.v, Y.v);
@@ -896,10 +1014,10 @@ SvdOut<double> svd_from_qb(DM<double> Q, DM<double> B) {
     }
     out.U = DMat<double>(m, l, s, false);
     out.V = DMat<double>(n, l, s, false);
-    gemm<double>(s, false, false, 1.0, Q, Uh.v, 0.0, out.U.v);
+    prod_f64(s, false, false, 1.0, Q, Uh.v, 0.0, out.U.v);
     DMat<double> Us(l, l, s, false);
     select_cols<double, double>(s, Uh.v, all, &inv, Us.v);
-    gemm<double>(s, false, false, 1.0, Bt.v, Us.v, 0.0, out.V.v);
+    prod_f64(s, false, false, 1.0, Bt.v, Us.v, 0.0, out.V.v);
     RSVD_CK(cudaStreamSynchronize(s));
     return out;
 }
@@ -979,8 +1097,8 @@ CurOut cur_from_two_sided(DM<double> A, int k, const TwoSidedOut &ts) {
     gather_rows<double>(s, A, d_irow, out.R.v);
     gather_cols<double>(s, A, d_icol, out.C.v);
     DMat<double> RRt(k, k, s, false), RV(k, k, s, false);
-    gemm<double>(s, false, true, 1.0, out.R.v, out.R.v, 0.0, RRt.v);
-    gemm<double>(s, false, false, 1.0, out.R.v, V.v, 0.0, RV.v);
+    prod_f64(s, false, true, 1.0, out.R.v, out.R.v, 0.0, RRt.v);
+    prod_f64(s, false, false, 1.0, out.R.v, V.v, 0.0, RV.v);
     if (!lu_solve(s, RRt.v, RV.v, cx.d_flags + FLAG_NONFINITE))
         set_error(RSVD_ERR_NUMERIC, "cur: R R^T is singular");
     out.U = DMat<double>(k, k, s, false);

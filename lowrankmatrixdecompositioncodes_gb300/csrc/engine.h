@@ -54,6 +54,9 @@ template <typename T>
 void prod(cudaStream_t s, bool ta, bool tb, T alpha, DM<T> A, DM<T> B, T beta, DM<T> C);
 // Drop the per-call BF16 operand copies (called at the end of every API call).
 void release_operand_cache();
+// Large FP64 products (FP64 GEMM, or double-float on the FP32 pipe in the FP64X mode).
+void prod_f64(cudaStream_t s, bool ta, bool tb, double alpha, DM<double> A, DM<double> B, double beta, DM<double> C);
+bool fp64x_mode();
 
 // Gaussian test matrix (r x c): provider when registered (and enabled), else Philox.
 template <typename T>
@@ -83,5 +86,9 @@ TwoSidedOut id_two_sided(DM<double> A, IdOut col);
 SvdOut<double> svd_from_qb(DM<double> Q, DM<double> B);
 IdOut id_from_qb(DM<double> B, int k);
 CurOut cur_from_two_sided(DM<double> A, int k, const TwoSidedOut &ts);
+// ||A - U diag(S) V^T||_F and ||.||_2 (k_resid.cu); S on the device (k values); either output may be
+// null; the spectral value is the Rayleigh-Ritz estimate after `iters` block power rounds.
+template <typename T>
+void residual_norms(DM<T> A, DM<T> U, const double *dS, DM<T> V, double *fro, double *spec, int iters);
 
 }  // namespace rsvd

@@ -724,7 +724,7 @@ bool chol_factor(cudaStream_t s, DM<double> G, double rel_tol, int *d_flag, S *d
     if (G.r != G.c) fail(RSVD_ERR_ARGUMENT, "cholesky: not square");
     if (n == 0) return true;
     const int nb = (n + TB - 1) / TB;
-    RSVD_CK(cudaMemsetAsync(d_flag, 0, sizeof(int), s));
+    if (!ctx().chol_deferred) RSVD_CK(cudaMemsetAsync(d_flag, 0, sizeof(int), s));
     DBuf own(dinv ? 16 : sizeof(S) * (size_t)nb * TB * TB, s);
     S *di = dinv ? dinv : (S *)own.get();
     if (nb <= smem_nb_max<S>()) {
@@ -751,6 +751,8 @@ bool chol_factor(cudaStream_t s, DM<double> G, double rel_tol, int *d_flag, S *d
         RSVD_LAUNCH_CK();
         ctx().launches += 2 * nb + 2;
     }
+    // deferred mode: the flag stays set for the caller's one check at the end of the solve
+    if (ctx().chol_deferred) return true;
     int h = 0;
     RSVD_CK(cudaMemcpyAsync(&h, d_flag, sizeof(int), cudaMemcpyDeviceToHost, s));
     RSVD_CK(cudaStreamSynchronize(s));
@@ -798,7 +800,7 @@ bool chol_tiles_f32(cudaStream_t s, float *Gt, int n, double rel_tol, int *d_fla
     if (n == 0) return true;
     const int nb = (n + TB - 1) / TB;
     if (nb > smem_nb_max<float>()) fail(RSVD_ERR_ARGUMENT, "chol_tiles_f32: order above 288");
-    RSVD_CK(cudaMemsetAsync(d_flag, 0, sizeof(int), s));
+    if (!ctx().chol_deferred) RSVD_CK(cudaMemsetAsync(d_flag, 0, sizeof(int), s));
     const size_t smem = sizeof(float) * ((size_t)(tix(0, nb) + 1) * TE + (size_t)nb * TB);
     RSVD_CK(cudaFuncSetAttribute(chol_tiles_f32_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     chol_tiles_f32_kernel<<<1, CHOL_F32_THREADS, smem, s>>>(Gt, n, nb, rel_tol, dinv, d_flag);
@@ -811,6 +813,8 @@ bool chol_tiles_f32(cudaStream_t s, float *Gt, int n, double rel_tol, int *d_fla
         RSVD_LAUNCH_CK();
         ctx().launches++;
     }
+    // deferred mode: the flag stays set for the caller's one check at the end of the solve
+    if (ctx().chol_deferred) return true;
     int h = 0;
     RSVD_CK(cudaMemcpyAsync(&h, d_flag, sizeof(int), cudaMemcpyDeviceToHost, s));
     RSVD_CK(cudaStreamSynchronize(s));

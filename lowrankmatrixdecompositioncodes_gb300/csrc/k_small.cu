@@ -548,6 +548,174 @@ __global__ void load_kernel_t(const double *G, long long ldg, S *W, long long ld
     }
 }
 
+
+// ------------------------------------------------------------------ SVD refinement kernels
+// M = I + C, the first-order simultaneous correction of approximate right singular vectors V of X
+// (columns v_i; H = (XV)^T (XV), Sm = V^T V, both FP64-accurate): with h_i = H_ii,
+//   C_ii = (1 - Sm_ii) / 2                                  (normalisation),
+//   C_ij = (H_ij - Sm_ij (h_i + h_j) / 2) / (h_j - h_i) - Sm_ij / 2    (i != j),
+// so that V (I + C) is orthonormal and diagonalises H to second order.  A pair whose correction
+// exceeds `tight` (nearly equal h: FP32 could not separate the two vectors, and a first-order
+// step applied to many such pairs at once does not converge) gets no coupling term here and is
+// flagged (flags[i + j n] = 1, i < j) for an exact rotation by refine_tight_kernel.
+__global__ void refine_update_kernel(const double *H, i64 ldh, const double *Sm, i64 lds, int n, double tight,
+                                     double *Mm, i64 ldm, unsigned char *flags) {
+    for (i64 e = blockIdx.x * (i64)blockDim.x + threadIdx.x; e < (i64)n * n; e += (i64)gridDim.x * blockDim.x) {
+        const int i = (int)(e % n), j = (int)(e / n);
+        double c;
+        unsigned char f = 0;
+        if (i == j) {
+            c = 0.5 * (1.0 - Sm[i + (i64)i * lds]);
+        } else {
+            const double hi = H[i + (i64)i * ldh], hj = H[j + (i64)j * ldh];
+            const double hij = 0.5 * (H[i + (i64)j * ldh] + H[j + (i64)i * ldh]);
+            const double sij = 0.5 * (Sm[i + (i64)j * lds] + Sm[j + (i64)i * lds]);
+            const double num = hij - sij * 0.5 * (hi + hj);
+            const double den = hj - hi;
+            if (fabs(num) <= tight * fabs(den)) {
+                c = num / den;
+            } else {
+                c = 0.0;
+                f = (i < j && num != 0.0) ? 1 : 0;
+            }
+            c -= 0.5 * sij;
+        }
+        Mm[i + (i64)j * ldm] = (i == j ? 1.0 : 0.0) + c;
+        flags[e] = f;
+    }
+}
+
+// Exact FP64 one-sided Jacobi rotations of the flagged pairs, in a fixed order (column j
+// ascending, then i ascending), by one CTA: for pair (i, j), a = |w_i|^2, b = |w_j|^2,
+// d = w_i . w_j over the current columns of W = X V, and (w_i, w_j), (v_i, v_j) rotated by the
+// angle that zeroes d (Rutishauser's formulas), so that W = X V still holds afterwards.  VW holds
+// V in rows [0, n) and W in rows [n, 2n); its double-float split (hi, lo) is rewritten for the
+// rotated columns.  At most max_rot rotations per launch.
+__global__ void __launch_bounds__(256) refine_tight_kernel(double *VW, i64 ld, float *hi, float *lo, i64 lds, int n,
+                                                           const unsigned char *flags, int max_rot) {
+    __shared__ int list[256];
+    __shared__ int wcnt[8];
+    __shared__ double red[3][8];
+    __shared__ double rot[2];
+    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+    int done = 0;
+    for (int j = 1; j < n && done < max_rot; j++) {
+        for (int base = 0; base < j && done < max_rot; base += 256) {
+            // ordered compaction of the flagged i in [base, min(j, base + 256))
+            const int i = base + tid;
+            const bool f = i < j && flags[i + (i64)j * n];
+            const unsigned bal = __ballot_sync(0xffffffffu, f);
+            if (lane == 0) wcnt[wid] = __popc(bal);
+            __syncthreads();
+            int off = 0, tot = 0;
+            for (int w = 0; w < 8; w++) {
+                if (w < wid) off += wcnt[w];
+                tot += wcnt[w];
+            }
+            if (f) list[off + __popc(bal & ((1u << lane) - 1u))] = i;
+            __syncthreads();
+            for (int q = 0; q < tot && done < max_rot; q++, done++) {
+                const int p = list[q];
+                double a = 0.0, b = 0.0, d = 0.0;
+                for (int r = n + tid; r < 2 * n; r += 256) {
+                    const double x = VW[r + (i64)p * ld], y = VW[r + (i64)j * ld];
+                    a = fma(x, x, a);
+                    b = fma(y, y, b);
+                    d = fma(x, y, d);
+                }
+                a = warp_sum(a);
+                b = warp_sum(b);
+                d = warp_sum(d);
+                if (lane == 0) { red[0][wid] = a; red[1][wid] = b; red[2][wid] = d; }
+                __syncthreads();
+                if (tid == 0) {
+                    double A = 0.0, B = 0.0, D = 0.0;
+                    for (int w = 0; w < 8; w++) { A += red[0][w]; B += red[1][w]; D += red[2][w]; }
+                    double cs = 1.0, sn = 0.0;
+                    if (D != 0.0) {
+                        const double zeta = (B - A) / (2.0 * D);
+                        const double t = copysign(1.0, zeta) / (fabs(zeta) + sqrt(1.0 + zeta * zeta));
+                        cs = 1.0 / sqrt(1.0 + t * t);
+                        sn = cs * t;
+                    }
+                    rot[0] = cs;
+                    rot[1] = sn;
+                }
+                __syncthreads();
+                const double cs = rot[0], sn = rot[1];
+                for (int r = tid; r < 2 * n; r += 256) {
+                    const double x = VW[r + (i64)p * ld], y = VW[r + (i64)j * ld];
+                    const double nx = cs * x - sn * y, ny = sn * x + cs * y;
+                    VW[r + (i64)p * ld] = nx;
+                    VW[r + (i64)j * ld] = ny;
+                    const float hx = __double2float_rn(nx), hy = __double2float_rn(ny);
+                    hi[r + p * lds] = hx;
+                    lo[r + p * lds] = __double2float_rn(nx - (double)hx);
+                    hi[r + j * lds] = hy;
+                    lo[r + j * lds] = __double2float_rn(ny - (double)hy);
+                }
+                __syncthreads();
+            }
+        }
+    }
+}
+
+// hi = fl32(x), lo = fl32(x - hi), no scaling (entries of order one)
+__global__ void split_unit_kernel(const double *x, i64 ld, i64 r, i64 c, float *hi, float *lo, i64 ldo) {
+    for (i64 e = blockIdx.x * (i64)blockDim.x + threadIdx.x; e < r * c; e += (i64)gridDim.x * blockDim.x) {
+        const i64 j = e / r, i = e - j * r;
+        const double v = x[i + j * ld];
+        const float h = __double2float_rn(v);
+        hi[i + j * ldo] = h;
+        lo[i + j * ldo] = __double2float_rn(v - (double)h);
+    }
+}
+
+// xexp[0] <- the split's scale exponent field; the split's own exponent <- 1023 (unit), so that
+// products read the scaled matrix X 2^(1023 - xexp) itself
+__global__ void take_scale_kernel(int *split_exp, int *xexp) {
+    const int e = *split_exp;
+    *xexp = e > 0 ? e : 1023;
+    *split_exp = 1023;
+}
+
+// Column j: sv_j = |w_j| / |v_j| (the Rayleigh quotient of the unnormalised v_j), nrm = (|w_j|, |v_j|).
+__global__ void refine_norms_kernel(const double *W, i64 ldw, const double *V, i64 ldv, int n, const int *xexp,
+                                    double *sv, double *nrm) {
+    const double unscale = ldexp(1.0, *xexp - 1023);
+    const int lane = threadIdx.x & 31;
+    for (int j = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); j < n; j += gridDim.x * (blockDim.x >> 5)) {
+        double a = 0, b = 0;
+        for (int i = lane; i < n; i += 32) {
+            const double w = W[i + (i64)j * ldw], v = V[i + (i64)j * ldv];
+            a = fma(w, w, a);
+            b = fma(v, v, b);
+        }
+        a = warp_sum(a);
+        b = warp_sum(b);
+        if (lane == 0) {
+            const double nw = sqrt(a), nv = sqrt(b);
+            sv[j] = nv > 0.0 ? nw / nv * unscale : 0.0;
+            nrm[2 * j] = nw;
+            nrm[2 * j + 1] = nv;
+        }
+    }
+}
+
+// U(:, rank j) = w_j / |w_j|, V(:, rank j) = v_j / |v_j|, sv_sorted[rank j] = sv_j
+__global__ void refine_scatter_kernel(const double *W, i64 ldw, const double *Vin, i64 ldvi, const double *sv,
+                                      const double *nrm, const int *rank, int n, double *U, i64 ldu, double *V,
+                                      i64 ldv, double *sv_sorted) {
+    for (i64 e = blockIdx.x * (i64)blockDim.x + threadIdx.x; e < (i64)n * n; e += (i64)gridDim.x * blockDim.x) {
+        const int i = (int)(e % n), j = (int)(e / n);
+        const int r = rank[j];
+        const double nw = nrm[2 * j], nv = nrm[2 * j + 1];
+        U[i + (i64)r * ldu] = nw > 0.0 ? W[i + (i64)j * ldw] / nw : 0.0;
+        V[i + (i64)r * ldv] = nv > 0.0 ? Vin[i + (i64)j * ldvi] / nv : 0.0;
+        if (i == 0) sv_sorted[r] = sv[j];
+    }
+}
+
 unsigned gfor(long long n) {
     long long g = (n + 255) / 256;
     return (unsigned)std::max<long long>(1, std::min<long long>(g, (long long)std::max(1, ctx().sms) * 8));
@@ -664,5 +832,84 @@ int jacobi_small(cudaStream_t s, DM<double> G, DM<double> U, DM<double> V, doubl
 }
 template int jacobi_small<double>(cudaStream_t, DM<double>, DM<double>, DM<double>, double *, int *, bool);
 template int jacobi_small<float>(cudaStream_t, DM<double>, DM<double>, DM<double>, double *, int *, bool);
+
+// One refinement step: H = W^T W and Sm = V^T V (double-float products), the first-order
+// correction [V; W] <- [V; W] (I + C) for every pair of well-separated singular values (W = X V
+// is carried along instead of recomputed), and exact FP64 rotations of the flagged
+// nearly-equal pairs (refine_tight_kernel).  From the FP32 Jacobi's converged vectors four steps
+// bring the singular values to ~1e-15 relative (a step roughly squares the error of the separated
+// pairs; nearly-equal pairs, which FP32 cannot separate, are settled by the rotations in the first
+// steps).  X is scaled once by a power of two (its largest entry into [1, 2)), so that every
+// operand has entries of order one and is split without a scale; the products write the split of
+// their result for the next product.
+void svd_refine(cudaStream_t s, DM<double> X, DM<double> V, DM<double> U, double *d_sv, int steps) {
+    const int n = (int)X.r;
+    if (X.r != X.c || V.r != n || V.c != n || U.r != n || U.c != n) fail(RSVD_ERR_ARGUMENT, "svd_refine: shapes");
+    if (n == 0) return;
+    DBuf xe_b(sizeof(int), s), flag_b((size_t)n * n, s);
+    int *xexp = (int *)xe_b.get();
+    unsigned char *flags = (unsigned char *)flag_b.get();
+    Df64Split Xs(s, X);
+    take_scale_kernel<<<1, 1, 0, s>>>(Xs.exp, xexp);
+    RSVD_LAUNCH_CK();
+    const i64 ldvw = pad_ld(2 * (i64)n);
+    // [V; W] stacks (2n x n, FP64) and their splits, ping-pong
+    DMat<double> VWa(2 * n, n, s, false), VWb(2 * n, n, s, false), H(n, n, s, false), Sm(n, n, s, false),
+        Mm(n, n, s, false);
+    DBuf sa(sizeof(float) * 2 * (size_t)(ldvw * n), s), sb(sizeof(float) * 2 * (size_t)(ldvw * n), s),
+        sm(sizeof(float) * 2 * (size_t)(pad_ld(n) * n), s);
+    float *ha = (float *)sa.get(), *la = ha + ldvw * n, *hb = (float *)sb.get(), *lb = hb + ldvw * n;
+    float *hm = (float *)sm.get(), *lm = hm + pad_ld(n) * n;
+    const int *unit = Xs.exp;                         // 1023 after take_scale_kernel
+    RSVD_CK(cudaMemcpy2DAsync(VWa.v.p, sizeof(double) * VWa.v.ld, V.p, sizeof(double) * V.ld, sizeof(double) * n, n,
+                              cudaMemcpyDeviceToDevice, s));
+    split_unit_kernel<<<gfor((long long)n * n), 256, 0, s>>>(VWa.v.p, VWa.v.ld, n, n, ha, la, ldvw);
+    RSVD_LAUNCH_CK();
+    {
+        const Df64View Vv{ha, la, n, n, ldvw, unit};
+        const Df64Out wo{ha + n, la + n, ldvw};
+        df64_gemm(s, false, false, 1.0, Xs.view(), Vv, 0.0, VWa.v.sub(n, 0, n, n), &wo);      // W = X V
+    }
+    DM<double> cur = VWa.v, nxt = VWb.v;
+    float *ch = ha, *cl = la, *nh = hb, *nl = lb;
+    for (int it = 0; it < steps; it++) {
+        const Df64View VWv{ch, cl, 2 * (i64)n, n, ldvw, unit};
+        const Df64View Vv = VWv.rows(0, n), Wv = VWv.rows(n, n);
+        df64_gemm(s, true, false, 1.0, Wv, Wv, 0.0, H.v, nullptr);               // H = W^T W
+        df64_gemm(s, true, false, 1.0, Vv, Vv, 0.0, Sm.v, nullptr);              // Sm = V^T V
+        // the last step also settles pairs still coupled beyond 1e-4 by exact rotations, so that
+        // the columns of W come out orthogonal to ~1e-12 even for nearly equal singular values
+        const double tight = (it == steps - 1) ? 1e-4 : 0.005;
+        refine_update_kernel<<<gfor((long long)n * n), 256, 0, s>>>(H.v.p, H.v.ld, Sm.v.p, Sm.v.ld, n, tight, Mm.v.p,
+                                                                     Mm.v.ld, flags);
+        RSVD_LAUNCH_CK();
+        split_unit_kernel<<<gfor((long long)n * n), 256, 0, s>>>(Mm.v.p, Mm.v.ld, n, n, hm, lm, pad_ld(n));
+        RSVD_LAUNCH_CK();
+        const Df64View Mv{hm, lm, n, n, pad_ld(n), unit};
+        const Df64Out no{nh, nl, ldvw};
+        df64_gemm(s, false, false, 1.0, VWv, Mv, 0.0, nxt, &no);                  // [V; W] (I + C)
+        refine_tight_kernel<<<1, 256, 0, s>>>(nxt.p, nxt.ld, nh, nl, ldvw, n, flags, 4096);
+        RSVD_LAUNCH_CK();
+        std::swap(cur, nxt);
+        std::swap(ch, nh);
+        std::swap(cl, nl);
+    }
+    DBuf nb(sizeof(double) * 3 * (size_t)n, s), rb(sizeof(int) * (size_t)n, s);
+    double *raw = (double *)nb.get(), *nrm = raw + n;
+    int *rank = (int *)rb.get();
+    const double *Wp = cur.p + n, *Vp = cur.p;
+    refine_norms_kernel<<<ceil_div(n, 8), 256, 0, s>>>(Wp, cur.ld, Vp, cur.ld, n, xexp, raw, nrm);
+    rank_desc_kernel<<<ceil_div(n, 256), 256, n <= RANK_SMEM_MAX ? sizeof(long long) * n : 0, s>>>(raw, n, rank);
+    refine_scatter_kernel<<<gfor((long long)n * n), 256, 0, s>>>(Wp, cur.ld, Vp, cur.ld, raw, nrm, rank, n, U.p,
+                                                                  U.ld, V.p, V.ld, d_sv);
+    RSVD_LAUNCH_CK();
+    ctx().launches += 6 + 3 * steps;
+}
+
+void small_svd_refined(cudaStream_t s, DM<double> G, DM<double> U, DM<double> V, double *d_sv, int *d_flag) {
+    jacobi_small<float>(s, G, U, V, d_sv, d_flag, false);
+    PhaseTimer pt(&ctx().timing.small_ms);
+    svd_refine(s, G, V, U, d_sv, 4);
+}
 
 }  // namespace rsvd

@@ -95,6 +95,12 @@ struct Ctx {
     // as a two-part BF16 split (hi + lo, 16 mantissa bits) instead of one BF16 copy (7 bits).
     // Set by the fixed-precision block loop, whose sketches must resolve the deflated matrix.
     bool ax_split = false;
+    // Cholesky breakdown checks deferred to the end of a solve (FP32-data fixed-rank solves):
+    // the factorisations leave FLAG_CHOL_BREAKDOWN set instead of returning to the host after
+    // each one; if it is set at the end, the solve is repeated with chol_force_hh (Householder QR
+    // for every orthonormalisation).
+    bool chol_deferred = false;
+    bool chol_force_hh = false;
     // kernels may read pageable host memory directly (cudaDevAttrPageableMemoryAccess: GB300
     // with a Grace host, over NVLink-C2C)
     bool pageable_access = false;
@@ -293,4 +299,45 @@ template <typename S>
 // Returns the sweep count when want_sweeps (a host read of the count, i.e. a stream sync), else 0.
 int jacobi_small(cudaStream_t s, DM<double> G, DM<double> U, DM<double> V, double *d_sv, int *d_flag,
                  bool want_sweeps = true);
+}  // namespace rsvd
+
+namespace rsvd {
+// ----------------------------------------------------------------- FP64-accurate products on the FP32 pipe (k_df64.cu)
+// x = (hi + lo) * 2^(exp - 1023): an FP64 matrix split once into two FP32 parts, scaled on the
+// device by a power of two so that the largest |x| lies in [1, 2).
+struct Df64Split {
+    DBuf buf;
+    float *hi = nullptr, *lo = nullptr;
+    int *exp = nullptr;          // device scalar: biased exponent field of the largest |x| (0: no scale)
+    i64 r = 0, c = 0, ld = 0;
+    // exp_src (device, optional): the biased exponent field to scale by (e.g. 1023: no scaling,
+    // for matrices with entries of order one), instead of the largest |x| found by a pass over x
+    Df64Split(cudaStream_t s, DM<double> x, const int *exp_src = nullptr);
+    struct Df64View view() const;
+};
+// A split operand as the product kernel reads it (hi, lo: FP32 column-major, ld; exp: device scale).
+struct Df64View {
+    const float *hi = nullptr, *lo = nullptr;
+    i64 r = 0, c = 0, ld = 0;
+    const int *exp = nullptr;
+    Df64View rows(i64 r0, i64 nr) const { return Df64View{hi + r0, lo + r0, nr, c, ld, exp}; }
+};
+inline Df64View Df64Split::view() const { return Df64View{hi, lo, r, c, ld, exp}; }
+// Optional second output of a product: the result split as hi = fl32(C), lo = fl32(C - hi) (no scale).
+struct Df64Out {
+    float *hi, *lo;
+    i64 ld;
+};
+// C = alpha op(A) op(B) + beta C with double-float accumulation (~2^-47 relative per product term).
+void df64_gemm(cudaStream_t s, bool ta, bool tb, double alpha, const Df64Split &A, const Df64Split &B, double beta,
+               DM<double> C);
+void df64_gemm(cudaStream_t s, bool ta, bool tb, double alpha, Df64View A, Df64View B, double beta, DM<double> C,
+               const Df64Out *out);
+// ----------------------------------------------------------------- SVD refinement (k_small.cu)
+// X (n x n, FP64) and approximate right singular vectors V (n x n, columns; FP32-accurate, e.g.
+// from the FP32 Jacobi) -> the SVD of X to FP64 accuracy: U, V (n x n) and sv (device, n values),
+// descending.  V is overwritten; U may not alias V.  `steps` first-order corrections.
+void svd_refine(cudaStream_t s, DM<double> X, DM<double> V, DM<double> U, double *d_sv, int steps);
+// The mixed-precision l x l SVD: FP32 one-sided Jacobi, then svd_refine (FP64-accurate result).
+void small_svd_refined(cudaStream_t s, DM<double> G, DM<double> U, DM<double> V, double *d_sv, int *d_flag);
 }  // namespace rsvd

@@ -49,6 +49,7 @@ void init_opts_locked() {
         if (v == "fp32") g_opts.precision = RSVD_PREC_FP32;
         else if (v == "tf32") g_opts.precision = RSVD_PREC_TF32;
         else if (v == "bf16") g_opts.precision = RSVD_PREC_BF16;
+        else if (v == "fp64x") g_opts.precision = RSVD_PREC_FP64X;
     }
     if (const char *p = std::getenv("RSVDPACK_SEED")) g_opts.seed = std::strtoull(p, nullptr, 0);
     if (std::getenv("RSVDPACK_VERBOSE")) g_opts.verbose = 1;
@@ -262,7 +263,7 @@ void rsvdpack_set_opts(const rsvdpack_opts *opts) {
     if (!opts) return;
     std::lock_guard<std::mutex> g(g_opts_mu);
     init_opts_locked();
-    if (opts->precision < RSVD_PREC_FP64 || opts->precision > RSVD_PREC_BF16) {
+    if (opts->precision < RSVD_PREC_FP64 || opts->precision > RSVD_PREC_FP64X) {
         set_error(RSVD_ERR_ARGUMENT, "rsvdpack_set_opts: unknown precision");
         return;
     }

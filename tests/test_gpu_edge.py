@@ -89,3 +89,34 @@ def test_rank_deficient_input(engine, port, rank):
     assert np.max(np.abs(s_got[rank:])) <= 1e-10 * s_want[0]
     U = got[0]
     assert np.max(np.abs(U[:, :rank].T @ U[:, :rank] - np.eye(rank))) < 1e-8
+
+
+@pytest.mark.parametrize("prec", ["tf32", "fp32"])
+def test_rank_deficient_mixed_solve_falls_back(engine, prec):
+    """FP32-data solves on Philox test matrices defer each Cholesky's breakdown check to the end
+    of the solve; a rank-deficient input breaks CholeskyQR, so the solve is repeated on the same
+    test matrices with Householder QR: finite factors, the leading singular values of A, the
+    trailing ones near zero, and the same result on a replay of the same draws."""
+    m, n, k, p, rank = 3000, 1500, 24, 8, 10
+    g = np.random.default_rng(17)
+    A = g.standard_normal((m, rank)) @ g.standard_normal((rank, n))
+    sv = np.linalg.svd(A, compute_uv=False)
+    engine.set_precision(prec)
+    engine.set_use_provider(False)
+    try:
+        runs = []
+        for _ in range(2):
+            engine.lib.rsvdpack_reset_omega_counter()
+            runs.append(engine.low_rank_svd_rand_decomp_fixed_rank(A, k, p, 1, 2, 1))
+            engine.check()
+    finally:
+        engine.set_precision("fp64")
+        engine.set_use_provider(True)
+    U, S, V = runs[0]
+    s = np.diag(S)
+    assert np.all(np.isfinite(U)) and np.all(np.isfinite(V)) and np.all(np.isfinite(s))
+    # TF32 products carry ~1e-3 relative error (BF16 A in A X); FP32 ~1e-7
+    tol = 5e-3 if prec == "tf32" else 1e-5
+    assert np.max(np.abs(s[:rank] - sv[:rank]) / sv[:rank]) < tol
+    assert np.max(np.abs(s[rank:])) < tol * sv[0]
+    assert np.array_equal(runs[0][1], runs[1][1])

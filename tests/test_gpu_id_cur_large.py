@@ -63,3 +63,21 @@ def test_cur_full_size_matches_oracle(engine, port, matrix):
         Ct, Ut, Rt = (torch.from_numpy(np.ascontiguousarray(x)).cuda() for x in (C_, U_, R_))
         res.append(float(torch.linalg.norm(Ad - Ct @ Ut @ Rt) / torch.linalg.norm(Ad)))
     assert res[1] <= res[0] * (1 + 1e-3) + 1e-12, res
+
+
+def test_two_sided_id_full_size_fp64x(engine, port, matrix):
+    """The same workload in the FP64X mode (the sketch passes as double-float products on the
+    FP32 pipe): index sets identical to the oracle's."""
+    engine.set_precision("fp64x")
+    try:
+        (Ic_o, Ir_o, T_o, S_o), t_cpu = _run(port, "id_two_sided_rand_decomp_fixed_rank", matrix, K, P, Q, S)
+        (Ic_e, Ir_e, T_e, S_e), t_gpu = _run(engine, "id_two_sided_rand_decomp_fixed_rank", matrix, K, P, Q, S)
+        engine.check()
+        print(f"two-sided ID 20000x10000 k=500 (FP64X): oracle {t_cpu:.2f} s, engine {t_gpu:.2f} s "
+              f"(engine call {engine.last_timing().total_ms:.0f} ms)")
+    finally:
+        engine.set_precision("fp64")
+    assert np.array_equal(Ic_e, Ic_o), "column index sets differ"
+    assert np.array_equal(Ir_e, Ir_o), "row index sets differ"
+    for got, want in ((T_e, T_o), (S_e, S_o)):
+        assert np.max(np.abs(got - want)) / np.max(np.abs(want)) < 1e-6
