@@ -239,8 +239,10 @@ def learned_qb_leg(torch, eng, dev, steps=2, profile=False):
     B = torch.empty(n, cap, device=dev)
     stream = torch.cuda.ExternalStream(L.rsvdpack_stream())
     out = {"workload": "fixed-precision QB 32768x16384 FP32, s_i = exp(-i/200), TOL = 1e-5 ||A||_F",
-           "note": "TOL = 1e-6 is below the FP32 accumulation floor of B = Q^T A at m = 32768 (~6e-6 "
-                   "measured) for every FP32 path, so the FP32 comparison is taken at 1e-5"}
+           "note": "FP32-arithmetic deflation A_res -= Q_j B_j rounds each update at ~u sqrt(w/2) of its "
+                   "size; the first blocks remove ~0.5 ||A||, so the stored residual drifts from A - QB by "
+                   "~1e-6 ||A|| and TOL = 1e-6 needs FP64-class updates: the FP32/TF32 comparison is "
+                   "taken at 1e-5, and TOL = 1e-6 is run on FP64 data (fp64_tol1e-6)"}
     for name, learned, prec in (("plain_fp32", False, "fp32"), ("learned_tf32", True, "tf32")):
         eng.set_precision(prec)
         eng.set_learned(learned)
@@ -276,7 +278,43 @@ def learned_qb_leg(torch, eng, dev, steps=2, profile=False):
     eng.set_learned(False)
     eng.set_precision("fp64")
     out["speedup"] = out["plain_fp32"]["ms_per_solve"] / out["learned_tf32"]["ms_per_solve"]
-    del At, Q, B
+    del Q, B
+    torch.cuda.empty_cache()
+    # TOL = 1e-6 on FP64 data: the reference's loop (kstep 128, q = 1) with FP64 products against
+    # the FP64X mode's double-float products, one solve each, residual checked in FP64
+    tol6 = 1e-6
+    A64 = At.double()
+    del At
+    torch.cuda.empty_cache()
+    cap64 = 4096
+    Q64 = torch.empty(cap64, m, device=dev, dtype=torch.float64)
+    B64 = torch.empty(n, cap64, device=dev, dtype=torch.float64)
+    leg6 = {"workload": "the same matrix as FP64 data, TOL = 1e-6 ||A||_F, plain blocked QB, kstep 128, q = 1"}
+    for name, prec in (("fp64x", "fp64x"), ("fp64", "fp64")):
+        eng.set_precision(prec)
+        fr = C.c_int(0)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        rc = L.rsvdpack_dev_qb(A64.data_ptr(), 0, m, m, n, 128, 0, tol6 * fro, 1, 1, Q64.data_ptr(), m,
+                               B64.data_ptr(), cap64, cap64, C.byref(fr))
+        e1.record(stream)
+        e1.synchronize()
+        if rc:
+            raise RuntimeError(f"FP64 QB failed: {eng.last_error()}")
+        k = fr.value
+        Qm, Bm = Q64[:k].T, B64[:, :k].T
+        res = 0.0
+        for c0 in range(0, n, 2048):
+            c1 = min(n, c0 + 2048)
+            E = A64[c0:c1].T - Qm @ Bm[:, c0:c1]
+            res += float((E * E).sum())
+        leg6[name] = {"ms_per_solve": e0.elapsed_time(e1), "rank": k, "rel_residual": res ** 0.5 / fro,
+                      "meets_tol": bool(res ** 0.5 <= tol6 * fro)}
+    leg6["speedup_fp64x_vs_fp64"] = leg6["fp64"]["ms_per_solve"] / leg6["fp64x"]["ms_per_solve"]
+    out["fp64_tol1e-6"] = leg6
+    eng.set_precision("fp64")
+    del A64, Q64, B64
     torch.cuda.empty_cache()
     return out
 

@@ -407,7 +407,8 @@ void rsvdpack_batch_plan_destroy(rsvdpack_batch_plan *plan);
  * fp32 != 0, else FP64).  rsvdpack_dev_small_svd: G (n x n) = U diag(S) V^T, S descending,
  * by one-sided Jacobi (the engine's l x l SVD); fp32 == 2 selects the mixed modes' form: the
  * FP32 Jacobi followed by four FP64-accurate refinement steps (double-float products on the
- * FP32 pipe, exact FP64 rotations of nearly equal pairs), singular values to ~1e-14 relative; returns the FP32 or FP64 sweep count or
+ * FP32 pipe, exact FP64 rotations of nearly equal pairs): singular values to ~1e-14 relative,
+ * singular vectors orthonormal to ~1e-12 (~1e-10 for singular values closer than ~1e-6 relative); returns the FP32 or FP64 sweep count or
  * a negative RSVD_ERR_* code.  rsvdpack_dev_small_cholesky: G = R^T R in place (upper R, lower
  * part zeroed); returns RSVD_OK, RSVD_ERR_NUMERIC on breakdown, or another RSVD_ERR_* code. */
 int rsvdpack_dev_small_svd(double *dG, int n, long long ldg, double *dU, long long ldu, double *dS, double *dV,

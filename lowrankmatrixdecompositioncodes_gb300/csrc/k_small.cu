@@ -13,6 +13,7 @@
 #include "k_common.cuh"
 
 #include <algorithm>
+#include <climits>
 #include <cmath>
 #include <limits>
 #include <type_traits>
@@ -557,13 +558,12 @@ __global__ void load_kernel_t(const double *G, long long ldg, S *W, long long ld
 // so that V (I + C) is orthonormal and diagonalises H to second order.  A pair whose correction
 // exceeds `tight` (nearly equal h: FP32 could not separate the two vectors, and a first-order
 // step applied to many such pairs at once does not converge) gets no coupling term here and is
-// flagged (flags[i + j n] = 1, i < j) for an exact rotation by refine_tight_kernel.
+// listed (key j n + i, i < j; at most max_pairs) for an exact rotation by refine_tight_kernel.
 __global__ void refine_update_kernel(const double *H, i64 ldh, const double *Sm, i64 lds, int n, double tight,
-                                     double *Mm, i64 ldm, unsigned char *flags) {
+                                     double *Mm, i64 ldm, int *pair_count, int *pairs, int max_pairs) {
     for (i64 e = blockIdx.x * (i64)blockDim.x + threadIdx.x; e < (i64)n * n; e += (i64)gridDim.x * blockDim.x) {
         const int i = (int)(e % n), j = (int)(e / n);
         double c;
-        unsigned char f = 0;
         if (i == j) {
             c = 0.5 * (1.0 - Sm[i + (i64)i * lds]);
         } else {
@@ -576,87 +576,91 @@ __global__ void refine_update_kernel(const double *H, i64 ldh, const double *Sm,
                 c = num / den;
             } else {
                 c = 0.0;
-                f = (i < j && num != 0.0) ? 1 : 0;
+                if (i < j && num != 0.0) {
+                    const int k = atomicAdd(pair_count, 1);
+                    if (k < max_pairs) pairs[k] = j * n + i;
+                }
             }
             c -= 0.5 * sij;
         }
         Mm[i + (i64)j * ldm] = (i == j ? 1.0 : 0.0) + c;
-        flags[e] = f;
     }
 }
 
-// Exact FP64 one-sided Jacobi rotations of the flagged pairs, in a fixed order (column j
-// ascending, then i ascending), by one CTA: for pair (i, j), a = |w_i|^2, b = |w_j|^2,
+// Exact FP64 one-sided Jacobi rotations of the listed pairs, in a fixed order (key j n + i
+// ascending: column j, then i), by one CTA: for pair (i, j), a = |w_i|^2, b = |w_j|^2,
 // d = w_i . w_j over the current columns of W = X V, and (w_i, w_j), (v_i, v_j) rotated by the
 // angle that zeroes d (Rutishauser's formulas), so that W = X V still holds afterwards.  VW holds
 // V in rows [0, n) and W in rows [n, 2n); its double-float split (hi, lo) is rewritten for the
-// rotated columns.  At most max_rot rotations per launch.
+// rotated columns.  The list (unordered, from refine_update_kernel) is sorted in shared memory
+// (bitonic sort); an empty list costs one read.
+constexpr int REFINE_MAX_PAIRS = 2048;
 __global__ void __launch_bounds__(256) refine_tight_kernel(double *VW, i64 ld, float *hi, float *lo, i64 lds, int n,
-                                                           const unsigned char *flags, int max_rot) {
-    __shared__ int list[256];
-    __shared__ int wcnt[8];
+                                                           const int *pair_count, const int *pairs) {
+    __shared__ int keys[REFINE_MAX_PAIRS];
     __shared__ double red[3][8];
     __shared__ double rot[2];
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
-    int done = 0;
-    for (int j = 1; j < n && done < max_rot; j++) {
-        for (int base = 0; base < j && done < max_rot; base += 256) {
-            // ordered compaction of the flagged i in [base, min(j, base + 256))
-            const int i = base + tid;
-            const bool f = i < j && flags[i + (i64)j * n];
-            const unsigned bal = __ballot_sync(0xffffffffu, f);
-            if (lane == 0) wcnt[wid] = __popc(bal);
-            __syncthreads();
-            int off = 0, tot = 0;
-            for (int w = 0; w < 8; w++) {
-                if (w < wid) off += wcnt[w];
-                tot += wcnt[w];
+    const int cnt = min(*pair_count, REFINE_MAX_PAIRS);
+    if (cnt == 0) return;
+    int np2 = 1;
+    while (np2 < cnt) np2 <<= 1;
+    for (int e = tid; e < np2; e += 256) keys[e] = e < cnt ? pairs[e] : INT_MAX;
+    __syncthreads();
+    for (int k = 2; k <= np2; k <<= 1)
+        for (int jj = k >> 1; jj > 0; jj >>= 1) {
+            for (int e = tid; e < np2; e += 256) {
+                const int o = e ^ jj;
+                if (o > e) {
+                    const bool up = (e & k) == 0;
+                    const int a = keys[e], b = keys[o];
+                    if ((a > b) == up) { keys[e] = b; keys[o] = a; }
+                }
             }
-            if (f) list[off + __popc(bal & ((1u << lane) - 1u))] = i;
             __syncthreads();
-            for (int q = 0; q < tot && done < max_rot; q++, done++) {
-                const int p = list[q];
-                double a = 0.0, b = 0.0, d = 0.0;
-                for (int r = n + tid; r < 2 * n; r += 256) {
-                    const double x = VW[r + (i64)p * ld], y = VW[r + (i64)j * ld];
-                    a = fma(x, x, a);
-                    b = fma(y, y, b);
-                    d = fma(x, y, d);
-                }
-                a = warp_sum(a);
-                b = warp_sum(b);
-                d = warp_sum(d);
-                if (lane == 0) { red[0][wid] = a; red[1][wid] = b; red[2][wid] = d; }
-                __syncthreads();
-                if (tid == 0) {
-                    double A = 0.0, B = 0.0, D = 0.0;
-                    for (int w = 0; w < 8; w++) { A += red[0][w]; B += red[1][w]; D += red[2][w]; }
-                    double cs = 1.0, sn = 0.0;
-                    if (D != 0.0) {
-                        const double zeta = (B - A) / (2.0 * D);
-                        const double t = copysign(1.0, zeta) / (fabs(zeta) + sqrt(1.0 + zeta * zeta));
-                        cs = 1.0 / sqrt(1.0 + t * t);
-                        sn = cs * t;
-                    }
-                    rot[0] = cs;
-                    rot[1] = sn;
-                }
-                __syncthreads();
-                const double cs = rot[0], sn = rot[1];
-                for (int r = tid; r < 2 * n; r += 256) {
-                    const double x = VW[r + (i64)p * ld], y = VW[r + (i64)j * ld];
-                    const double nx = cs * x - sn * y, ny = sn * x + cs * y;
-                    VW[r + (i64)p * ld] = nx;
-                    VW[r + (i64)j * ld] = ny;
-                    const float hx = __double2float_rn(nx), hy = __double2float_rn(ny);
-                    hi[r + p * lds] = hx;
-                    lo[r + p * lds] = __double2float_rn(nx - (double)hx);
-                    hi[r + j * lds] = hy;
-                    lo[r + j * lds] = __double2float_rn(ny - (double)hy);
-                }
-                __syncthreads();
-            }
         }
+    for (int q = 0; q < cnt; q++) {
+        const int key = keys[q];
+        const int j = key / n, p = key - j * n;
+        double a = 0.0, b = 0.0, d = 0.0;
+        for (int r = n + tid; r < 2 * n; r += 256) {
+            const double x = VW[r + (i64)p * ld], y = VW[r + (i64)j * ld];
+            a = fma(x, x, a);
+            b = fma(y, y, b);
+            d = fma(x, y, d);
+        }
+        a = warp_sum(a);
+        b = warp_sum(b);
+        d = warp_sum(d);
+        if (lane == 0) { red[0][wid] = a; red[1][wid] = b; red[2][wid] = d; }
+        __syncthreads();
+        if (tid == 0) {
+            double A = 0.0, B = 0.0, D = 0.0;
+            for (int w = 0; w < 8; w++) { A += red[0][w]; B += red[1][w]; D += red[2][w]; }
+            double cs = 1.0, sn = 0.0;
+            if (D != 0.0) {
+                const double zeta = (B - A) / (2.0 * D);
+                const double t = copysign(1.0, zeta) / (fabs(zeta) + sqrt(1.0 + zeta * zeta));
+                cs = 1.0 / sqrt(1.0 + t * t);
+                sn = cs * t;
+            }
+            rot[0] = cs;
+            rot[1] = sn;
+        }
+        __syncthreads();
+        const double cs = rot[0], sn = rot[1];
+        for (int r = tid; r < 2 * n; r += 256) {
+            const double x = VW[r + (i64)p * ld], y = VW[r + (i64)j * ld];
+            const double nx = cs * x - sn * y, ny = sn * x + cs * y;
+            VW[r + (i64)p * ld] = nx;
+            VW[r + (i64)j * ld] = ny;
+            const float hx = __double2float_rn(nx), hy = __double2float_rn(ny);
+            hi[r + p * lds] = hx;
+            lo[r + p * lds] = __double2float_rn(nx - (double)hx);
+            hi[r + j * lds] = hy;
+            lo[r + j * lds] = __double2float_rn(ny - (double)hy);
+        }
+        __syncthreads();
     }
 }
 
@@ -846,9 +850,10 @@ void svd_refine(cudaStream_t s, DM<double> X, DM<double> V, DM<double> U, double
     const int n = (int)X.r;
     if (X.r != X.c || V.r != n || V.c != n || U.r != n || U.c != n) fail(RSVD_ERR_ARGUMENT, "svd_refine: shapes");
     if (n == 0) return;
-    DBuf xe_b(sizeof(int), s), flag_b((size_t)n * n, s);
-    int *xexp = (int *)xe_b.get();
-    unsigned char *flags = (unsigned char *)flag_b.get();
+    DBuf xe_b(sizeof(int) * (1 + steps), s), pair_b(sizeof(int) * REFINE_MAX_PAIRS, s);
+    int *xexp = (int *)xe_b.get(), *pair_count = xexp + 1;      // one pair counter per step
+    int *pairs = (int *)pair_b.get();
+    RSVD_CK(cudaMemsetAsync(pair_count, 0, sizeof(int) * steps, s));
     Df64Split Xs(s, X);
     take_scale_kernel<<<1, 1, 0, s>>>(Xs.exp, xexp);
     RSVD_LAUNCH_CK();
@@ -881,14 +886,15 @@ void svd_refine(cudaStream_t s, DM<double> X, DM<double> V, DM<double> U, double
         // the columns of W come out orthogonal to ~1e-12 even for nearly equal singular values
         const double tight = (it == steps - 1) ? 1e-4 : 0.005;
         refine_update_kernel<<<gfor((long long)n * n), 256, 0, s>>>(H.v.p, H.v.ld, Sm.v.p, Sm.v.ld, n, tight, Mm.v.p,
-                                                                     Mm.v.ld, flags);
+                                                                     Mm.v.ld, pair_count + it, pairs,
+                                                                     REFINE_MAX_PAIRS);
         RSVD_LAUNCH_CK();
         split_unit_kernel<<<gfor((long long)n * n), 256, 0, s>>>(Mm.v.p, Mm.v.ld, n, n, hm, lm, pad_ld(n));
         RSVD_LAUNCH_CK();
         const Df64View Mv{hm, lm, n, n, pad_ld(n), unit};
         const Df64Out no{nh, nl, ldvw};
         df64_gemm(s, false, false, 1.0, VWv, Mv, 0.0, nxt, &no);                  // [V; W] (I + C)
-        refine_tight_kernel<<<1, 256, 0, s>>>(nxt.p, nxt.ld, nh, nl, ldvw, n, flags, 4096);
+        refine_tight_kernel<<<1, 256, 0, s>>>(nxt.p, nxt.ld, nh, nl, ldvw, n, pair_count + it, pairs);
         RSVD_LAUNCH_CK();
         std::swap(cur, nxt);
         std::swap(ch, nh);

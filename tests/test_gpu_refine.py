@@ -8,7 +8,8 @@
   (fp32 == 0) and of LAPACK on the same matrix, for a 272 x 272 upper-triangular factor whose
   spectrum has the shape of the 16384 x 8192 noisy workload's sketch (a dozen separated values
   above ~260 values packed into 27% of their range) and for well-separated spectra; factors
-  orthonormal and reproducing the matrix to FP64 accuracy.
+  orthonormal and reproducing the matrix to FP64 accuracy (to ~1e-10 where singular values lie
+  closer than 1e-6 relative).
 * A graded matrix (singular values over 8 decades): the refined values keep an absolute accuracy
   of order 1e-12 sigma_1 (the double-float products' error relative to |X||V|); the relative
   accuracy of the smallest ones is that divided by sigma_i / sigma_1 -- the FP64 Jacobi (fp32 == 0)
@@ -106,11 +107,13 @@ def test_refined_small_svd_matches_fp64_jacobi(engine, kind, n):
     assert np.max(np.abs(S2 - S_lapack) / S_lapack) < 1e-12
     assert np.all(np.diff(S2) <= 0)
     I = np.eye(n)
-    # the sketch-like spectrum has pairs closer than 1e-6 relative, whose vectors are determined
-    # only to ~1e-15 / gap: their columns of U are orthogonal to that accuracy
-    assert np.max(np.abs(U2.T @ U2 - I)) < (1e-9 if kind == "sketch" else 1e-12)
-    assert np.max(np.abs(V2.T @ V2 - I)) < 1e-12
-    assert np.linalg.norm(X - (U2 * S2) @ V2.T) / np.linalg.norm(X) < 1e-13
+    # the sketch-like spectrum has pairs closer than 1e-6 relative: the last first-order step
+    # leaves their vectors orthogonal to ~|C|^2 ~ 1e-10 (singular values are second order in it)
+    orth = 1e-9 if kind == "sketch" else 1e-12
+    assert np.max(np.abs(U2.T @ U2 - I)) < orth
+    assert np.max(np.abs(V2.T @ V2 - I)) < orth
+    recon = np.linalg.norm(X - (U2 * S2) @ V2.T) / np.linalg.norm(X)
+    assert recon < (1e-9 if kind == "sketch" else 1e-13), recon
 
 
 def test_refined_small_svd_graded_absolute_accuracy(engine):
