@@ -98,19 +98,33 @@ __device__ __forceinline__ void renorm(float &s, float &c) {
     s = t;
 }
 
+// One launch computes up to two products of the same shape and transposition (blockIdx.z = problem
+// x K split); with `upper`, only the tiles on or above the diagonal (M == N, symmetric results).
+struct Df64Prob {
+    const float *Ah, *Al, *Bh, *Bl;
+    i64 lda, ldb, ldc, ldo;
+    const int *ea, *eb;
+    double *C, *part;
+    float *Oh, *Ol;
+};
+struct Df64Params {
+    int M, N, K, kps, splits, nprob, upper;
+    double alpha, beta;
+    Df64Prob p[2];
+};
+
 template <bool TA, bool TB>
-__global__ void __launch_bounds__(256) df64_gemm_kernel(int M, int N, int K, int k_per_split,
-                                                        const float *__restrict__ Ah, const float *__restrict__ Al,
-                                                        i64 lda, const float *__restrict__ Bh,
-                                                        const float *__restrict__ Bl, i64 ldb, const int *ea,
-                                                        const int *eb, double alpha, double beta, double *C, i64 ldc,
-                                                        double *part, i64 part_stride, float *Oh, float *Ol,
-                                                        i64 ldo) {
+__global__ void __launch_bounds__(256) df64_gemm_kernel(const __grid_constant__ Df64Params P) {
     __shared__ float As[2][DB_K][DB_M + 1];
     __shared__ float Bs[2][DB_K][DB_N + 1];
+    if (P.upper && blockIdx.x > blockIdx.y) return;
+    const int prob = blockIdx.z / P.splits, split = blockIdx.z - prob * P.splits;
+    const Df64Prob &Q = P.p[prob];
+    const float *__restrict__ Ah = Q.Ah, *__restrict__ Al = Q.Al, *__restrict__ Bh = Q.Bh, *__restrict__ Bl = Q.Bl;
+    const int M = P.M, N = P.N, K = P.K;
     const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
     const int m0 = blockIdx.x * DB_M, n0 = blockIdx.y * DB_N;
-    const int kb = blockIdx.z * k_per_split, ke = min(K, kb + k_per_split);
+    const int kb = split * P.kps, ke = min(K, kb + P.kps);
     float s[4][4], c[4][4];
 #pragma unroll
     for (int x = 0; x < 4; x++)
@@ -126,7 +140,7 @@ __global__ void __launch_bounds__(256) df64_gemm_kernel(int M, int N, int K, int
             const int gi = m0 + i, gk = k0 + kk;
             float h = 0.f, l = 0.f;
             if (gi < M && gk < ke) {
-                const i64 off = TA ? (gk + (i64)gi * lda) : (gi + (i64)gk * lda);
+                const i64 off = TA ? (gk + (i64)gi * Q.lda) : (gi + (i64)gk * Q.lda);
                 h = Ah[off];
                 l = Al[off];
             }
@@ -142,7 +156,7 @@ __global__ void __launch_bounds__(256) df64_gemm_kernel(int M, int N, int K, int
             const int gj = n0 + j, gk = k0 + kk;
             float h = 0.f, l = 0.f;
             if (gj < N && gk < ke) {
-                const i64 off = TB ? (gj + (i64)gk * ldb) : (gk + (i64)gj * ldb);
+                const i64 off = TB ? (gj + (i64)gk * Q.ldb) : (gk + (i64)gj * Q.ldb);
                 h = Bh[off];
                 l = Bl[off];
             }
@@ -175,7 +189,7 @@ __global__ void __launch_bounds__(256) df64_gemm_kernel(int M, int N, int K, int
         __syncthreads();
     }
     // undo the operand scales (exact powers of two)
-    const int sa = *ea, sb = *eb;
+    const int sa = *Q.ea, sb = *Q.eb;
     const double unscale = ldexp(1.0, (sa > 0 ? sa - 1023 : 0) + (sb > 0 ? sb - 1023 : 0));
 #pragma unroll
     for (int x = 0; x < 4; x++) {
@@ -186,35 +200,39 @@ __global__ void __launch_bounds__(256) df64_gemm_kernel(int M, int N, int K, int
             const int gj = n0 + tx + 16 * y;
             if (gj >= N) continue;
             const double v = ((double)s[x][y] + (double)c[x][y]) * unscale;
-            if (part) {
-                part[(i64)blockIdx.z * part_stride + gi + (i64)gj * M] = v;
+            if (Q.part) {
+                Q.part[(i64)split * M * N + gi + (i64)gj * M] = v;
             } else {
-                double *cp = C + gi + (i64)gj * ldc;
-                const double o = (beta == 0.0) ? alpha * v : alpha * v + beta * (*cp);
+                double *cp = Q.C + gi + (i64)gj * Q.ldc;
+                const double o = (P.beta == 0.0) ? P.alpha * v : P.alpha * v + P.beta * (*cp);
                 *cp = o;
-                if (Oh) {
+                if (Q.Oh) {
                     const float h = __double2float_rn(o);
-                    Oh[gi + (i64)gj * ldo] = h;
-                    Ol[gi + (i64)gj * ldo] = __double2float_rn(o - (double)h);
+                    Q.Oh[gi + (i64)gj * Q.ldo] = h;
+                    Q.Ol[gi + (i64)gj * Q.ldo] = __double2float_rn(o - (double)h);
                 }
             }
         }
     }
 }
 
-__global__ void df64_reduce_kernel(const double *part, i64 part_stride, int splits, int M, int N, double alpha,
-                                   double beta, double *C, i64 ldc, float *Oh, float *Ol, i64 ldo) {
-    for (i64 e = blockIdx.x * (i64)blockDim.x + threadIdx.x; e < (i64)M * N; e += (i64)gridDim.x * blockDim.x) {
+__global__ void df64_reduce_kernel(const __grid_constant__ Df64Params P) {
+    const i64 MN = (i64)P.M * P.N;
+    for (i64 e = blockIdx.x * (i64)blockDim.x + threadIdx.x; e < MN * P.nprob; e += (i64)gridDim.x * blockDim.x) {
+        const int prob = (int)(e / MN);
+        const i64 f = e - prob * MN;
+        const i64 j = f / P.M, i = f - j * P.M;
+        if (P.upper && (i / DB_M) > (j / DB_N)) continue;      // tile not computed
+        const Df64Prob &Q = P.p[prob];
         double v = 0.0;
-        for (int z = 0; z < splits; z++) v += part[z * part_stride + e];
-        const i64 j = e / M, i = e - j * M;
-        double *cp = C + i + j * ldc;
-        const double o = (beta == 0.0) ? alpha * v : alpha * v + beta * (*cp);
+        for (int z = 0; z < P.splits; z++) v += Q.part[z * MN + f];
+        double *cp = Q.C + i + j * Q.ldc;
+        const double o = (P.beta == 0.0) ? P.alpha * v : P.alpha * v + P.beta * (*cp);
         *cp = o;
-        if (Oh) {
+        if (Q.Oh) {
             const float h = __double2float_rn(o);
-            Oh[i + j * ldo] = h;
-            Ol[i + j * ldo] = __double2float_rn(o - (double)h);
+            Q.Oh[i + j * Q.ldo] = h;
+            Q.Ol[i + j * Q.ldo] = __double2float_rn(o - (double)h);
         }
     }
 }
@@ -250,48 +268,70 @@ Df64Split::Df64Split(cudaStream_t s, DM<double> x, const int *exp_src) : r(x.r),
     }
 }
 
-void df64_gemm(cudaStream_t s, bool ta, bool tb, double alpha, Df64View A, Df64View B, double beta, DM<double> C,
-               const Df64Out *out) {
-    const i64 M = ta ? A.c : A.r, K = ta ? A.r : A.c;
-    const i64 N = tb ? B.r : B.c, Kb = tb ? B.c : B.r;
-    if (K != Kb || C.r != M || C.c != N) fail(RSVD_ERR_ARGUMENT, "df64_gemm: shape mismatch");
+// Up to two products of one shape: C_p = alpha op(A_p) op(B_p) + beta C_p.
+static void df64_gemm_n(cudaStream_t s, bool ta, bool tb, double alpha, int nprob, const Df64View *A,
+                        const Df64View *B, double beta, const DM<double> *C, const Df64Out *const *out, bool upper) {
+    const i64 M = ta ? A[0].c : A[0].r, K = ta ? A[0].r : A[0].c;
+    const i64 N = tb ? B[0].r : B[0].c;
+    for (int q = 0; q < nprob; q++) {
+        const i64 Mq = ta ? A[q].c : A[q].r, Kq = ta ? A[q].r : A[q].c;
+        const i64 Nq = tb ? B[q].r : B[q].c, Kb = tb ? B[q].c : B[q].r;
+        if (Mq != M || Kq != K || Nq != N || Kb != K || C[q].r != M || C[q].c != N)
+            fail(RSVD_ERR_ARGUMENT, "df64_gemm: shape mismatch");
+    }
     if (M == 0 || N == 0) return;
     if (M >= (1ll << 31) || N >= (1ll << 31) || K >= (1ll << 31)) fail(RSVD_ERR_ARGUMENT, "df64_gemm: too large");
+    if (upper && M != N) fail(RSVD_ERR_ARGUMENT, "df64_gemm: upper needs a square result");
     const int mt = (int)ceil_div(M, DB_M), nt = (int)ceil_div(N, DB_N);
     if (nt > 65535) fail(RSVD_ERR_ARGUMENT, "df64_gemm: N too large for the tiling");
+    const i64 tiles = upper ? (i64)mt * (mt + 1) / 2 : (i64)mt * nt;
     // split K until the grid covers the GPU (each split keeps >= 2 K steps of 16)
     const int sms = std::max(1, ctx().sms);
     int splits = 1;
     const int ksteps = (int)ceil_div(std::max<i64>(K, 1), DB_K);
-    while (splits < 16 && (i64)mt * nt * splits < sms && ksteps / (2 * splits) >= 2) splits *= 2;
+    while (splits < 16 && tiles * nprob * splits < sms && ksteps / (2 * splits) >= 2) splits *= 2;
     const int kps = (int)(ceil_div(ksteps, splits) * DB_K);
     splits = (int)ceil_div(std::max<i64>(K, 1), kps);
+    if ((i64)splits * nprob > 65535) fail(RSVD_ERR_ARGUMENT, "df64_gemm: grid too large");
+    Df64Params P{};
+    P.M = (int)M; P.N = (int)N; P.K = (int)K; P.kps = kps; P.splits = splits; P.nprob = nprob; P.upper = upper;
+    P.alpha = alpha; P.beta = beta;
     DBuf pb;
-    double *part = nullptr;
-    if (splits > 1) {
-        pb = DBuf(sizeof(double) * (size_t)(M * N * splits), s);
-        part = (double *)pb.get();
+    if (splits > 1) pb = DBuf(sizeof(double) * (size_t)(M * N * splits * nprob), s);
+    for (int q = 0; q < nprob; q++) {
+        Df64Prob &Q = P.p[q];
+        Q.Ah = A[q].hi; Q.Al = A[q].lo; Q.lda = A[q].ld; Q.ea = A[q].exp;
+        Q.Bh = B[q].hi; Q.Bl = B[q].lo; Q.ldb = B[q].ld; Q.eb = B[q].exp;
+        Q.C = C[q].p; Q.ldc = C[q].ld;
+        Q.part = splits > 1 ? (double *)pb.get() + (size_t)q * M * N * splits : nullptr;
+        Q.Oh = out && out[q] ? out[q]->hi : nullptr;
+        Q.Ol = out && out[q] ? out[q]->lo : nullptr;
+        Q.ldo = out && out[q] ? out[q]->ld : 0;
     }
-    float *oh = out ? out->hi : nullptr, *ol = out ? out->lo : nullptr;
-    const i64 ldo = out ? out->ld : 0;
-    dim3 grid(mt, nt, splits);
-#define RSVD_DF64_LAUNCH(TA_, TB_)                                                                              \
-    df64_gemm_kernel<TA_, TB_><<<grid, 256, 0, s>>>((int)M, (int)N, (int)K, kps, A.hi, A.lo, A.ld, B.hi, B.lo, \
-                                                    B.ld, A.exp, B.exp, alpha, beta, C.p, C.ld, part, M * N, oh, ol, \
-                                                    ldo)
-    if (!ta && !tb) RSVD_DF64_LAUNCH(false, false);
-    else if (ta && !tb) RSVD_DF64_LAUNCH(true, false);
-    else if (!ta && tb) RSVD_DF64_LAUNCH(false, true);
-    else RSVD_DF64_LAUNCH(true, true);
-#undef RSVD_DF64_LAUNCH
+    dim3 grid(mt, nt, splits * nprob);
+    if (!ta && !tb) df64_gemm_kernel<false, false><<<grid, 256, 0, s>>>(P);
+    else if (ta && !tb) df64_gemm_kernel<true, false><<<grid, 256, 0, s>>>(P);
+    else if (!ta && tb) df64_gemm_kernel<false, true><<<grid, 256, 0, s>>>(P);
+    else df64_gemm_kernel<true, true><<<grid, 256, 0, s>>>(P);
     RSVD_LAUNCH_CK();
     ctx().launches++;
     if (splits > 1) {
-        df64_reduce_kernel<<<grid_for(M * N), 256, 0, s>>>(part, M * N, splits, (int)M, (int)N, alpha, beta, C.p, C.ld,
-                                                            oh, ol, ldo);
+        df64_reduce_kernel<<<grid_for(M * N * nprob), 256, 0, s>>>(P);
         RSVD_LAUNCH_CK();
         ctx().launches++;
     }
+}
+
+void df64_gemm(cudaStream_t s, bool ta, bool tb, double alpha, Df64View A, Df64View B, double beta, DM<double> C,
+               const Df64Out *out) {
+    const Df64Out *o[1] = {out};
+    df64_gemm_n(s, ta, tb, alpha, 1, &A, &B, beta, &C, o, false);
+}
+
+void df64_gram_pair(cudaStream_t s, Df64View A0, DM<double> C0, Df64View A1, DM<double> C1) {
+    const Df64View A[2] = {A0, A1};
+    const DM<double> C[2] = {C0, C1};
+    df64_gemm_n(s, true, false, 1.0, 2, A, A, 0.0, C, nullptr, true);
 }
 
 void df64_gemm(cudaStream_t s, bool ta, bool tb, double alpha, const Df64Split &A, const Df64Split &B, double beta,

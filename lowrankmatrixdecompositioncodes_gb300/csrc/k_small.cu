@@ -552,7 +552,8 @@ __global__ void load_kernel_t(const double *G, long long ldg, S *W, long long ld
 
 // ------------------------------------------------------------------ SVD refinement kernels
 // M = I + C, the first-order simultaneous correction of approximate right singular vectors V of X
-// (columns v_i; H = (XV)^T (XV), Sm = V^T V, both FP64-accurate): with h_i = H_ii,
+// (columns v_i; H = (XV)^T (XV), Sm = V^T V, both FP64-accurate, upper triangles read), written as
+// its double-float split (Mh + Ml): with h_i = H_ii,
 //   C_ii = (1 - Sm_ii) / 2                                  (normalisation),
 //   C_ij = (H_ij - Sm_ij (h_i + h_j) / 2) / (h_j - h_i) - Sm_ij / 2    (i != j),
 // so that V (I + C) is orthonormal and diagonalises H to second order.  A pair whose correction
@@ -560,7 +561,7 @@ __global__ void load_kernel_t(const double *G, long long ldg, S *W, long long ld
 // step applied to many such pairs at once does not converge) gets no coupling term here and is
 // listed (key j n + i, i < j; at most max_pairs) for an exact rotation by refine_tight_kernel.
 __global__ void refine_update_kernel(const double *H, i64 ldh, const double *Sm, i64 lds, int n, double tight,
-                                     double *Mm, i64 ldm, int *pair_count, int *pairs, int max_pairs) {
+                                     float *Mh, float *Ml, i64 ldm, int *pair_count, int *pairs, int max_pairs) {
     for (i64 e = blockIdx.x * (i64)blockDim.x + threadIdx.x; e < (i64)n * n; e += (i64)gridDim.x * blockDim.x) {
         const int i = (int)(e % n), j = (int)(e / n);
         double c;
@@ -568,8 +569,9 @@ __global__ void refine_update_kernel(const double *H, i64 ldh, const double *Sm,
             c = 0.5 * (1.0 - Sm[i + (i64)i * lds]);
         } else {
             const double hi = H[i + (i64)i * ldh], hj = H[j + (i64)j * ldh];
-            const double hij = 0.5 * (H[i + (i64)j * ldh] + H[j + (i64)i * ldh]);
-            const double sij = 0.5 * (Sm[i + (i64)j * lds] + Sm[j + (i64)i * lds]);
+            const int a = min(i, j), b = max(i, j);           // H and Sm hold their upper triangles
+            const double hij = H[a + (i64)b * ldh];
+            const double sij = Sm[a + (i64)b * lds];
             const double num = hij - sij * 0.5 * (hi + hj);
             const double den = hj - hi;
             if (fabs(num) <= tight * fabs(den)) {
@@ -583,7 +585,10 @@ __global__ void refine_update_kernel(const double *H, i64 ldh, const double *Sm,
             }
             c -= 0.5 * sij;
         }
-        Mm[i + (i64)j * ldm] = (i == j ? 1.0 : 0.0) + c;
+        const double mv = (i == j ? 1.0 : 0.0) + c;
+        const float mh = __double2float_rn(mv);
+        Mh[i + (i64)j * ldm] = mh;
+        Ml[i + (i64)j * ldm] = __double2float_rn(mv - (double)mh);
     }
 }
 
@@ -859,8 +864,7 @@ void svd_refine(cudaStream_t s, DM<double> X, DM<double> V, DM<double> U, double
     RSVD_LAUNCH_CK();
     const i64 ldvw = pad_ld(2 * (i64)n);
     // [V; W] stacks (2n x n, FP64) and their splits, ping-pong
-    DMat<double> VWa(2 * n, n, s, false), VWb(2 * n, n, s, false), H(n, n, s, false), Sm(n, n, s, false),
-        Mm(n, n, s, false);
+    DMat<double> VWa(2 * n, n, s, false), VWb(2 * n, n, s, false), H(n, n, s, false), Sm(n, n, s, false);
     DBuf sa(sizeof(float) * 2 * (size_t)(ldvw * n), s), sb(sizeof(float) * 2 * (size_t)(ldvw * n), s),
         sm(sizeof(float) * 2 * (size_t)(pad_ld(n) * n), s);
     float *ha = (float *)sa.get(), *la = ha + ldvw * n, *hb = (float *)sb.get(), *lb = hb + ldvw * n;
@@ -880,16 +884,13 @@ void svd_refine(cudaStream_t s, DM<double> X, DM<double> V, DM<double> U, double
     for (int it = 0; it < steps; it++) {
         const Df64View VWv{ch, cl, 2 * (i64)n, n, ldvw, unit};
         const Df64View Vv = VWv.rows(0, n), Wv = VWv.rows(n, n);
-        df64_gemm(s, true, false, 1.0, Wv, Wv, 0.0, H.v, nullptr);               // H = W^T W
-        df64_gemm(s, true, false, 1.0, Vv, Vv, 0.0, Sm.v, nullptr);              // Sm = V^T V
+        df64_gram_pair(s, Wv, H.v, Vv, Sm.v);                                   // H = W^T W, Sm = V^T V
         // the last step also settles pairs still coupled beyond 1e-4 by exact rotations, so that
         // the columns of W come out orthogonal to ~1e-12 even for nearly equal singular values
         const double tight = (it == steps - 1) ? 1e-4 : 0.005;
-        refine_update_kernel<<<gfor((long long)n * n), 256, 0, s>>>(H.v.p, H.v.ld, Sm.v.p, Sm.v.ld, n, tight, Mm.v.p,
-                                                                     Mm.v.ld, pair_count + it, pairs,
+        refine_update_kernel<<<gfor((long long)n * n), 256, 0, s>>>(H.v.p, H.v.ld, Sm.v.p, Sm.v.ld, n, tight, hm, lm,
+                                                                     pad_ld(n), pair_count + it, pairs,
                                                                      REFINE_MAX_PAIRS);
-        RSVD_LAUNCH_CK();
-        split_unit_kernel<<<gfor((long long)n * n), 256, 0, s>>>(Mm.v.p, Mm.v.ld, n, n, hm, lm, pad_ld(n));
         RSVD_LAUNCH_CK();
         const Df64View Mv{hm, lm, n, n, pad_ld(n), unit};
         const Df64Out no{nh, nl, ldvw};

@@ -333,6 +333,9 @@ void df64_gemm(cudaStream_t s, bool ta, bool tb, double alpha, const Df64Split &
                DM<double> C);
 void df64_gemm(cudaStream_t s, bool ta, bool tb, double alpha, Df64View A, Df64View B, double beta, DM<double> C,
                const Df64Out *out);
+// C0 = A0^T A0 and C1 = A1^T A1 (same shapes) in one launch, upper-triangle tiles only: entries
+// (i, j) with i <= j are exact to the product's accuracy; tiles below the diagonal are not written.
+void df64_gram_pair(cudaStream_t s, Df64View A0, DM<double> C0, Df64View A1, DM<double> C1);
 // ----------------------------------------------------------------- SVD refinement (k_small.cu)
 // X (n x n, FP64) and approximate right singular vectors V (n x n, columns; FP32-accurate, e.g.
 // from the FP32 Jacobi) -> the SVD of X to FP64 accuracy: U, V (n x n) and sv (device, n values),
