@@ -212,12 +212,14 @@ WEIGHTS = os.path.join(ROOT, "lowrankmatrixdecompositioncodes_gb300", "learned",
 
 def learned_qb_leg(torch, eng, dev, steps=2, profile=False):
     """Fixed-precision blocked QB on the 32768 x 16384 FP32 workload (s_i = exp(-i/200), Haar
-    factors), TOL = 1e-6 ||A||_F: the plain FP32 adaptive loop (randQB_pb_new semantics,
-    kstep = 128, q = 1) against the learned proposal in TF32 mode, then the plain loop on the same
-    values as FP64 data in the FP64 and FP64X modes.  Every residual is checked in FP64; times
-    are per solve with A resident (CUDA events).  The matrix is formed in FP64 at rank 4000
+    factors): the plain FP32 adaptive loop (randQB_pb_new semantics, kstep = 128, q = 1) against the
+    learned proposal in TF32 mode at TOL = 1e-5 ||A||_F, then the plain loop on the same values as
+    FP64 data in the FP64 and FP64X modes at TOL = 1e-6 ||A||_F (FP32-arithmetic deflation
+    updates A_res -= Q_j B_j err by ~u sqrt(w/2) of their size, and the first blocks remove ~0.5
+    ||A||: a floor near 1e-6 ||A||_F at this size).  Every residual is checked in FP64; times are
+    per solve with A resident (CUDA events).  The matrix is formed in FP64 at rank 4000
     (s_4000 = 2e-9) and rounded once to FP32 (rounding noise ~4e-8 ||A||_F); an FP32 product of
-    the factors would add a full-rank accumulation noise of ~5e-6 ||A||_F, above the tolerance."""
+    the factors would add a full-rank accumulation noise of ~5e-6 ||A||_F."""
     L = eng.lib
     m, n, r = 32768, 16384, 4000
     g = torch.Generator(device=dev)
@@ -229,7 +231,7 @@ def learned_qb_leg(torch, eng, dev, steps=2, profile=False):
     del U, V
     torch.cuda.empty_cache()
     fro = float(torch.linalg.norm(At.double()))
-    tol_rel = 1e-6
+    tol_rel = 1e-5
     L.rsvdpack_dev_qb.argtypes = [C.c_void_p, C.c_int, C.c_longlong, C.c_int, C.c_int, C.c_int, C.c_int,
                                   C.c_double, C.c_int, C.c_int, C.c_void_p, C.c_longlong, C.c_void_p, C.c_longlong,
                                   C.c_int, C.POINTER(C.c_int)]
@@ -237,7 +239,7 @@ def learned_qb_leg(torch, eng, dev, steps=2, profile=False):
     Q = torch.empty(cap, m, device=dev)
     B = torch.empty(n, cap, device=dev)
     stream = torch.cuda.ExternalStream(L.rsvdpack_stream())
-    out = {"workload": "fixed-precision QB 32768x16384 FP32, s_i = exp(-i/200), TOL = 1e-6 ||A||_F",
+    out = {"workload": "fixed-precision QB 32768x16384 FP32, s_i = exp(-i/200), TOL = 1e-5 ||A||_F",
            "matrix": "formed in FP64 (rank 4000), rounded once to FP32"}
     for name, learned, prec in (("plain_fp32", False, "fp32"), ("learned_tf32", True, "tf32")):
         eng.set_precision(prec)
@@ -365,6 +367,14 @@ def batched_leg(torch, eng, dev, execs=5, profile=False):
                                         arr([int(x) for x in ns], C.c_longlong), 7)
     if not plan:
         raise RuntimeError(f"batch plan failed: {eng.last_error()}")
+    L.rsvdpack_batch_plan_info.restype = C.c_int
+    L.rsvdpack_batch_plan_info.argtypes = [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int),
+                                           C.POINTER(C.c_double)]
+    lp, cu, tuned, tms = C.c_int(0), C.c_int(0), C.c_int(0), C.c_double(0)
+    L.rsvdpack_batch_plan_info(plan, C.byref(lp), C.byref(cu), C.byref(tuned), C.byref(tms))
+    tuner = {"lanes_per_jacobi_pair": lp.value, "column_group_offset": cu.value,
+             "source": {0: "default", 1: "measured at plan creation", 2: "tuning table"}[tuned.value],
+             "sample_ms": tms.value}
     stream = torch.cuda.ExternalStream(L.rsvdpack_stream())
     try:
         for _ in range(3):
@@ -398,6 +408,7 @@ def batched_leg(torch, eng, dev, execs=5, profile=False):
     nbytes = sum(int(a) * int(b) for a, b in zip(ms, ns)) * 4
     return {"workload": "4096 matrices m~U[64,1024] n~U[32,512], s_i = 0.9^i, k = min(m,n)/8, p = 8, q = 1",
             "ms_per_batch": ms_exec, "solves_per_s": cnt * 1000.0 / ms_exec, "bytes_of_A": nbytes,
+            "autotuner": tuner,
             "residual_checks": checks}
 
 

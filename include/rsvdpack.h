@@ -402,6 +402,15 @@ rsvdpack_batch_plan *rsvdpack_batch_plan_create(int count, const int *m, const i
                                                 float *const *dV, const long long *ldv, unsigned long long seed);
 int rsvdpack_batch_plan_execute(rsvdpack_batch_plan *plan);
 void rsvdpack_batch_plan_destroy(rsvdpack_batch_plan *plan);
+/* The configuration a plan runs: lanes per Jacobi pair (4, 8, 16 or 32 = one warp per pair) and
+ * the offset (0 or 1) added to the narrowest register-tile column-group count of the per-item
+ * products.  Plan creation looks the batch's class -- (max k + p, max n / 64, max m / 64, q) -- up in
+ * the autotuner's table (RSVDPACK_TUNE_FILE, else $HOME/.cache/rsvdpack/batch_tune.txt) or, when
+ * absent, times the eight candidates on a strided sample of the batch (2 x SMs matrices) and
+ * records the fastest; RSVDPACK_NO_TUNE=1 keeps the default (8, 0).  *tuned: 1 measured now, 2 read
+ * from the table, 0 default; *tune_ms: the choice's time on the sample. */
+int rsvdpack_batch_plan_info(const rsvdpack_batch_plan *plan, int *lanes_per_pair, int *col_group_offset,
+                             int *tuned, double *tune_ms);
 
 /* The l x l steps on their own (device FP64 storage, column-major; compute in FP32 when
  * fp32 != 0, else FP64).  rsvdpack_dev_small_svd: G (n x n) = U diag(S) V^T, S descending,

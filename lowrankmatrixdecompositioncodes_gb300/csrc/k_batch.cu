@@ -15,9 +15,16 @@
 #include "rsvd_internal.h"
 #include "k_common.cuh"
 
+#include <sys/stat.h>
+
 #include <algorithm>
 #include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <map>
+#include <mutex>
 #include <numeric>
+#include <string>
 #include <vector>
 
 namespace rsvd {
@@ -226,9 +233,13 @@ __device__ void gemm_At_Q_t(const float *A, long long lda, int m, int n, const f
     __syncthreads();
 }
 
+// The column-group count of a product: the smallest that covers its width, plus the tuned
+// offset cuadd (0 or 1: one more group leaves padding FMAs but fewer loop trips per row chunk).
+__device__ __forceinline__ int cu_for(int l, int cuadd) { return min(CU_MAX, (l + 15) / 16 + cuadd); }
+
 __device__ __forceinline__ void gemm_A_B(const float *A, long long lda, int m, int n, const float *Bsm, int l,
-                                         float *Y, long long ldy, float *At) {
-    switch ((l + 15) / 16) {
+                                         float *Y, long long ldy, float *At, int cuadd) {
+    switch (cu_for(l, cuadd)) {
         case 1: gemm_A_B_t<1>(A, lda, m, n, Bsm, l, Y, ldy, At); break;
         case 2: gemm_A_B_t<2>(A, lda, m, n, Bsm, l, Y, ldy, At); break;
         case 3: gemm_A_B_t<3>(A, lda, m, n, Bsm, l, Y, ldy, At); break;
@@ -237,8 +248,8 @@ __device__ __forceinline__ void gemm_A_B(const float *A, long long lda, int m, i
     }
 }
 __device__ __forceinline__ void gemm_At_Q(const float *A, long long lda, int m, int n, const float *Q, long long ldq,
-                                          int l, float *Z, long long ldz, float *At, float *Qs) {
-    switch ((l + 15) / 16) {
+                                          int l, float *Z, long long ldz, float *At, float *Qs, int cuadd) {
+    switch (cu_for(l, cuadd)) {
         case 1: gemm_At_Q_t<1>(A, lda, m, n, Q, ldq, l, Z, ldz, At, Qs); break;
         case 2: gemm_At_Q_t<2>(A, lda, m, n, Q, ldq, l, Z, ldz, At, Qs); break;
         case 3: gemm_At_Q_t<3>(A, lda, m, n, Q, ldq, l, Z, ldz, At, Qs); break;
@@ -361,7 +372,7 @@ __device__ void trinv_cta(const float *R, int l, float *X) {
 // Y <- Y R^-1 is the tiled product gemm_A_B applied in place (each 64-row tile of Y is read
 // completely before it is written), with R^-1 row-major in X.
 __device__ bool cqr_cta(float *Y, long long ldy, int rows, int l, int passes, float *R, float *G, float *X, float *T,
-                        float *Ys, float *At, int *bad) {
+                        float *Ys, float *At, int *bad, int cuadd) {
     for (int e = threadIdx.x; e < l * l; e += BT) R[e] = ((e % l) == (e / l)) ? 1.f : 0.f;
     __syncthreads();
     __shared__ float trace_sh;
@@ -386,7 +397,7 @@ __device__ bool cqr_cta(float *Y, long long ldy, int rows, int l, int passes, fl
             passes++;
         }
         trinv_cta(G, l, X);
-        gemm_A_B(Y, ldy, rows, l, X, l, Y, ldy, At);
+        gemm_A_B(Y, ldy, rows, l, X, l, Y, ldy, At, cuadd);
         // R <- G R  (both upper)
         for (int e = threadIdx.x; e < l * l; e += BT) {
             const int i = e % l, k = e / l;
@@ -402,11 +413,13 @@ __device__ bool cqr_cta(float *Y, long long ldy, int rows, int l, int passes, fl
 }
 
 // One-sided Jacobi on W (l x l, shared), V accumulated; then sort descending.
+template <int LP>
 __device__ int jacobi_cta(float *W, float *V, int l, float *sv, int *rot) {
-    // one-sided Jacobi, round-robin pairs; each pair is handled by a group of 8 lanes (32
-    // groups per CTA, so every pair of a round (l / 2 <= 36) runs at once for l <= 64)
-    const int tid = threadIdx.x, g8 = tid >> 3, gl = tid & 7;
-    const unsigned gmask = 0xffu << (tid & 24);                // the 8 lanes of this group
+    // one-sided Jacobi, round-robin pairs; each pair is handled by a group of LP lanes (4, 8, 16
+    // or 32: BT / LP groups per CTA; with LP = 8, every pair of a round (l / 2 <= 36) runs at once
+    // for l <= 64; LP = 32 is one warp per pair)
+    const int tid = threadIdx.x, g8 = tid / LP, gl = tid % LP;
+    const unsigned gmask = (LP == 32) ? 0xffffffffu : (((1u << LP) - 1u) << (tid & (32 - LP)));
     for (int e = tid; e < l * l; e += BT) V[e] = ((e % l) == (e / l)) ? 1.f : 0.f;
     const int np = l + (l & 1);
     const float tol = 4.f * sqrtf((float)l) * 1.1920929e-7f;
@@ -415,7 +428,7 @@ __device__ int jacobi_cta(float *W, float *V, int l, float *sv, int *rot) {
         if (tid == 0) *rot = 0;
         __syncthreads();
         for (int r = 0; r < np - 1; r++) {
-            for (int pi = g8; pi < np / 2; pi += BT / 8) {
+            for (int pi = g8; pi < np / 2; pi += BT / LP) {
                 int p, q;
                 const int mm = np - 1;
                 if (pi == 0) { p = 0; q = (r % mm) + 1; }
@@ -425,12 +438,12 @@ __device__ int jacobi_cta(float *W, float *V, int l, float *sv, int *rot) {
                 float a = 0, b = 0, d = 0;
                 float *wp = W + p * l, *wq = W + q * l;
                 if (valid)
-                    for (int i = gl; i < l; i += 8) {
+                    for (int i = gl; i < l; i += LP) {
                         const float x = wp[i], y = wq[i];
                         a = fmaf(x, x, a); b = fmaf(y, y, b); d = fmaf(x, y, d);
                     }
 #pragma unroll
-                for (int o = 4; o > 0; o >>= 1) {
+                for (int o = LP / 2; o > 0; o >>= 1) {
                     a += __shfl_xor_sync(gmask, a, o);
                     b += __shfl_xor_sync(gmask, b, o);
                     d += __shfl_xor_sync(gmask, d, o);
@@ -440,7 +453,7 @@ __device__ int jacobi_cta(float *W, float *V, int l, float *sv, int *rot) {
                 const float t = copysignf(1.f, zeta) / (fabsf(zeta) + sqrtf(1.f + zeta * zeta));
                 const float cs = rsqrtf(1.f + t * t), sn = cs * t;
                 float *vp = V + p * l, *vq = V + q * l;
-                for (int i = gl; i < l; i += 8) {
+                for (int i = gl; i < l; i += LP) {
                     const float x = wp[i], y = wq[i];
                     wp[i] = cs * x - sn * y;
                     wq[i] = sn * x + cs * y;
@@ -468,9 +481,10 @@ __device__ int jacobi_cta(float *W, float *V, int l, float *sv, int *rot) {
 }
 
 
+template <int LP>
 __global__ void __launch_bounds__(BT, 1)
     batch_rsvd_kernel(const BatchItem *items, int count, int *queue, float *work, long long slab, long long ldw,
-                      uint64_t seed, int q, int s, int *flag) {
+                      uint64_t seed, int q, int s, int *flag, int cuadd) {
     extern __shared__ __align__(16) float sm[];
     __shared__ int item_idx, bad, rot;
     float *slabp = work + (long long)blockIdx.x * slab;
@@ -487,7 +501,7 @@ __global__ void __launch_bounds__(BT, 1)
         float *Bsm = sm, *At = sm + ((size_t)n * l + 3) / 4 * 4;        // At: 16-byte aligned
         gen_omega(Bsm, n, l, seed, (uint64_t)B.index);
         __syncthreads();
-        gemm_A_B(B.A, B.lda, m, n, Bsm, l, Yg, ldw, At);
+        gemm_A_B(B.A, B.lda, m, n, Bsm, l, Yg, ldw, At, cuadd);
         // small-matrix areas after the phase-1 region is no longer needed
         const int L2 = l * l;
         float *R = sm, *G = R + L2, *X = G + L2, *T = X + L2, *Ys = T + L2, *W = Ys + 33 * 96, *Vs = W + L2;
@@ -495,17 +509,17 @@ __global__ void __launch_bounds__(BT, 1)
         float *At2 = sm + ((size_t)(Qs + 32 * 96 - sm) + 3) / 4 * 4;   // A chunks of the A^T Q product
         bool ok = true;
         for (int j = 1; j < q && ok; j++) {                            // q-1 power rounds, s=1 schedule
-            if ((2 * j - 2) % s == 0) ok = cqr_cta(Yg, ldw, m, l, 1, R, G, X, T, Ys, At2, &bad);
-            gemm_At_Q(B.A, B.lda, m, n, Yg, ldw, l, Zg, ldw, At2, Qs);
-            if ((2 * j - 1) % s == 0 && ok) ok = cqr_cta(Zg, ldw, n, l, 1, R, G, X, T, Ys, At2, &bad);
+            if ((2 * j - 2) % s == 0) ok = cqr_cta(Yg, ldw, m, l, 1, R, G, X, T, Ys, At2, &bad, cuadd);
+            gemm_At_Q(B.A, B.lda, m, n, Yg, ldw, l, Zg, ldw, At2, Qs, cuadd);
+            if ((2 * j - 1) % s == 0 && ok) ok = cqr_cta(Zg, ldw, n, l, 1, R, G, X, T, Ys, At2, &bad, cuadd);
             // Y = A Zo : stage Zo row-major in shared memory as the B operand
             for (int e = threadIdx.x; e < n * l; e += BT) Bsm[(e % n) * l + e / n] = Zg[(e % n) + (long long)(e / n) * ldw];
             __syncthreads();
-            gemm_A_B(B.A, B.lda, m, n, Bsm, l, Yg, ldw, At);
+            gemm_A_B(B.A, B.lda, m, n, Bsm, l, Yg, ldw, At, cuadd);
         }
-        if (ok) ok = cqr_cta(Yg, ldw, m, l, 2, R, G, X, T, Ys, At2, &bad);                // Q in Yg
-        if (ok) gemm_At_Q(B.A, B.lda, m, n, Yg, ldw, l, Zg, ldw, At2, Qs);  // Bt in Zg
-        if (ok) ok = cqr_cta(Zg, ldw, n, l, 2, R, G, X, T, Ys, At2, &bad);                // Qh in Zg, Rh in R
+        if (ok) ok = cqr_cta(Yg, ldw, m, l, 2, R, G, X, T, Ys, At2, &bad, cuadd);                // Q in Yg
+        if (ok) gemm_At_Q(B.A, B.lda, m, n, Yg, ldw, l, Zg, ldw, At2, Qs, cuadd);  // Bt in Zg
+        if (ok) ok = cqr_cta(Zg, ldw, n, l, 2, R, G, X, T, Ys, At2, &bad, cuadd);                // Qh in Zg, Rh in R
         if (!ok) {
             if (threadIdx.x == 0) atomicAdd(flag, 1);
             continue;
@@ -514,7 +528,7 @@ __global__ void __launch_bounds__(BT, 1)
         // orthogonal, so fewer sweeps): Rh^T = W diag(1/sv) ... i.e. Rh = Vs S (W / sv)^T
         for (int e = threadIdx.x; e < L2; e += BT) W[e] = R[(e / l) + (e % l) * l];
         __syncthreads();
-        jacobi_cta(W, Vs, l, sv, &rot);
+        jacobi_cta<LP>(W, Vs, l, sv, &rot);
         // order: rank of each column by descending sv
         __shared__ int rank_of[96];
         for (int c = threadIdx.x; c < l; c += BT) {
@@ -536,8 +550,8 @@ __global__ void __launch_bounds__(BT, 1)
         for (int c = threadIdx.x; c < l; c += BT)
             if (rank_of[c] < k) B.S[rank_of[c]] = (double)sv[c];
         __syncthreads();
-        gemm_A_B(Yg, ldw, m, l, T, k, B.U, B.ldu, At2);
-        gemm_A_B(Zg, ldw, n, l, G, k, B.V, B.ldv, At2);
+        gemm_A_B(Yg, ldw, m, l, T, k, B.U, B.ldu, At2, cuadd);
+        gemm_A_B(Zg, ldw, n, l, G, k, B.V, B.ldv, At2, cuadd);
         __syncthreads();
     }
 }
@@ -552,12 +566,85 @@ size_t batch_smem_bytes(int nmax, int lmax) {
     return sizeof(float) * std::max(phase1, small) + 64;
 }
 
+// A configuration of the batched kernel: lanes per Jacobi pair and the column-group offset of
+// the register-tiled products.
+struct BatchCfg {
+    int lp = 8, cuadd = 0;
+};
+
 void batch_rsvd_launch(cudaStream_t s, const BatchItem *d_items, int count, int *d_queue, float *d_work, long long slab,
-                       long long ldw, unsigned long long seed, int q, int s_, int *d_flag, int nctas, size_t smem) {
-    auto k = batch_rsvd_kernel;
+                       long long ldw, unsigned long long seed, int q, int s_, int *d_flag, int nctas, size_t smem,
+                       BatchCfg cfg) {
+    auto k = batch_rsvd_kernel<8>;
+    switch (cfg.lp) {
+        case 4: k = batch_rsvd_kernel<4>; break;
+        case 16: k = batch_rsvd_kernel<16>; break;
+        case 32: k = batch_rsvd_kernel<32>; break;
+        default: break;
+    }
     RSVD_CK(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    k<<<nctas, BT, smem, s>>>(d_items, count, d_queue, d_work, slab, ldw, seed, q, s_, d_flag);
+    k<<<nctas, BT, smem, s>>>(d_items, count, d_queue, d_work, slab, ldw, seed, q, s_, d_flag, cfg.cuadd);
     RSVD_LAUNCH_CK();
+}
+
+// ---------------------------------------------------------------- the autotuner
+// The candidates (lanes per Jacobi pair x column-group offset) are timed on a strided sample of
+// the sorted batch (every count / S-th matrix, S = min(count, 2 x SMs), so that the sample has
+// the batch's size mix) with CUDA events, one warm-up and two timed launches each, and the fastest
+// is used.  Choices are kept per batch class -- (max k + p, max n / 64, max m / 64, q) -- in a
+// table that lives for the process and in a text file (RSVDPACK_TUNE_FILE, else
+// $HOME/.cache/rsvdpack/batch_tune.txt; one "key lp cuadd ms" line per class), read at the first
+// plan of a class and appended to after each new tuning.
+struct TuneEntry {
+    BatchCfg cfg;
+    double ms = 0.0;
+};
+std::mutex g_tune_mu;
+std::map<std::string, TuneEntry> g_tune;
+bool g_tune_loaded = false;
+
+std::string tune_path() {
+    if (const char *p = std::getenv("RSVDPACK_TUNE_FILE")) return p;
+    const char *h = std::getenv("HOME");
+    return std::string(h ? h : ".") + "/.cache/rsvdpack/batch_tune.txt";
+}
+
+void tune_load_locked() {
+    if (g_tune_loaded) return;
+    g_tune_loaded = true;
+    std::FILE *f = std::fopen(tune_path().c_str(), "r");
+    if (!f) return;
+    char key[128];
+    int lp, cu;
+    double ms;
+    while (std::fscanf(f, "%127s %d %d %lf", key, &lp, &cu, &ms) == 4) {
+        if ((lp == 4 || lp == 8 || lp == 16 || lp == 32) && (cu == 0 || cu == 1)) {
+            TuneEntry e;
+            e.cfg.lp = lp;
+            e.cfg.cuadd = cu;
+            e.ms = ms;
+            g_tune[key] = e;
+        }
+    }
+    std::fclose(f);
+}
+
+void tune_store_locked(const std::string &key, const TuneEntry &e) {
+    g_tune[key] = e;
+    const std::string path = tune_path();
+    const size_t slash = path.find_last_of('/');
+    if (slash != std::string::npos) {
+        // create the directory chain (best effort: an unwritable location only loses persistence)
+        std::string dir;
+        for (size_t i = 0; i <= slash; i++) {
+            dir += path[i];
+            if (path[i] == '/' && i > 0) mkdir(dir.c_str(), 0755);
+        }
+    }
+    if (std::FILE *f = std::fopen(path.c_str(), "a")) {
+        std::fprintf(f, "%s %d %d %.6f\n", key.c_str(), e.cfg.lp, e.cfg.cuadd, e.ms);
+        std::fclose(f);
+    }
 }
 
 }  // namespace rsvd
@@ -565,6 +652,8 @@ void batch_rsvd_launch(cudaStream_t s, const BatchItem *d_items, int count, int 
 // ============================================================ plan API (extern "C")
 struct rsvdpack_batch_plan {
     int count = 0;
+    int lp = 8, cuadd = 0, tuned = 0;   // chosen configuration; tuned: 1 measured now, 2 from the table
+    double tune_ms = 0.0;               // the chosen configuration's time on the tuning sample
     rsvd::DBuf items, queue, work, flag;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
@@ -618,12 +707,74 @@ rsvdpack_batch_plan *rsvdpack_batch_plan_create(int count, const int *m, const i
         plan->queue = DBuf(sizeof(int), st);
         plan->flag = DBuf(sizeof(int), st);
         RSVD_CK(cudaStreamSynchronize(st));
+        // ---- configuration: the table entry of this batch class, else tuned on a sample
+        BatchCfg cfg;
+        {
+            char keyb[128];
+            std::snprintf(keyb, sizeof keyb, "l%d_n%d_m%d_q%d", lmax, (nmax + 63) / 64, (mmax + 63) / 64, q);
+            const std::string key = keyb;
+            std::lock_guard<std::mutex> g(g_tune_mu);
+            tune_load_locked();
+            auto it = g_tune.find(key);
+            if (it != g_tune.end()) {
+                cfg = it->second.cfg;
+                plan->tune_ms = it->second.ms;
+                plan->tuned = 2;
+            } else if (!std::getenv("RSVDPACK_NO_TUNE")) {
+                const int S = std::min(count, 2 * std::max(1, cx.sms));
+                std::vector<BatchItem> sample((size_t)S);
+                for (int i = 0; i < S; i++) sample[(size_t)i] = items[(size_t)((long long)i * count / S)];
+                DBuf sitems(sizeof(BatchItem) * (size_t)S, st);
+                RSVD_CK(cudaMemcpyAsync(sitems.get(), sample.data(), sizeof(BatchItem) * (size_t)S,
+                                        cudaMemcpyHostToDevice, st));
+                cudaEvent_t e0, e1;
+                RSVD_CK(cudaEventCreate(&e0));
+                RSVD_CK(cudaEventCreate(&e1));
+                double best = 1e300;
+                const int snct = std::max(1, std::min(cx.sms, S));
+                for (int lp : {4, 8, 16, 32})
+                    for (int cu : {0, 1}) {
+                        BatchCfg c;
+                        c.lp = lp;
+                        c.cuadd = cu;
+                        float tot = 0.f;
+                        for (int rep = 0; rep < 3; rep++) {
+                            RSVD_CK(cudaMemsetAsync(plan->queue.get(), 0, sizeof(int), st));
+                            RSVD_CK(cudaMemsetAsync(plan->flag.get(), 0, sizeof(int), st));
+                            RSVD_CK(cudaEventRecord(e0, st));
+                            batch_rsvd_launch(st, (const BatchItem *)sitems.get(), S, (int *)plan->queue.get(),
+                                              (float *)plan->work.get(), slab, ldw, seed, q, s,
+                                              (int *)plan->flag.get(), snct, smem, c);
+                            RSVD_CK(cudaEventRecord(e1, st));
+                            RSVD_CK(cudaEventSynchronize(e1));
+                            float ms = 0.f;
+                            RSVD_CK(cudaEventElapsedTime(&ms, e0, e1));
+                            if (rep > 0) tot += ms;
+                        }
+                        const double ms = tot / 2.0;
+                        if (ms < best) {
+                            best = ms;
+                            cfg = c;
+                        }
+                    }
+                cudaEventDestroy(e0);
+                cudaEventDestroy(e1);
+                TuneEntry e;
+                e.cfg = cfg;
+                e.ms = best;
+                tune_store_locked(key, e);
+                plan->tune_ms = best;
+                plan->tuned = 1;
+            }
+        }
+        plan->lp = cfg.lp;
+        plan->cuadd = cfg.cuadd;
         // one persistent launch (plus the two counter resets) captured in a CUDA graph
         RSVD_CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
         cudaMemsetAsync(plan->queue.get(), 0, sizeof(int), st);
         cudaMemsetAsync(plan->flag.get(), 0, sizeof(int), st);
         batch_rsvd_launch(st, (const BatchItem *)plan->items.get(), count, (int *)plan->queue.get(),
-                          (float *)plan->work.get(), slab, ldw, seed, q, s, (int *)plan->flag.get(), nctas, smem);
+                          (float *)plan->work.get(), slab, ldw, seed, q, s, (int *)plan->flag.get(), nctas, smem, cfg);
         RSVD_CK(cudaStreamEndCapture(st, &plan->graph));
         RSVD_CK(cudaGraphInstantiate(&plan->exec, plan->graph, 0));
         return plan;
@@ -652,6 +803,16 @@ int rsvdpack_batch_plan_execute(rsvdpack_batch_plan *plan) {
         set_error(e.code, std::string("rsvdpack_batch_plan_execute: ") + e.what());
         return e.code;
     }
+}
+
+int rsvdpack_batch_plan_info(const rsvdpack_batch_plan *plan, int *lanes_per_pair, int *col_group_offset,
+                             int *tuned, double *tune_ms) {
+    if (!plan) return RSVD_ERR_ARGUMENT;
+    if (lanes_per_pair) *lanes_per_pair = plan->lp;
+    if (col_group_offset) *col_group_offset = plan->cuadd;
+    if (tuned) *tuned = plan->tuned;
+    if (tune_ms) *tune_ms = plan->tune_ms;
+    return RSVD_OK;
 }
 
 void rsvdpack_batch_plan_destroy(rsvdpack_batch_plan *plan) {

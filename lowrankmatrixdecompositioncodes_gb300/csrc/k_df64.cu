@@ -27,6 +27,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 
 namespace rsvd {
 
@@ -98,6 +99,28 @@ __device__ __forceinline__ void renorm(float &s, float &c) {
     s = t;
 }
 
+// The same two operations on pairs of accumulators (rows x, x + 1 of one output column) with the
+// packed FP32 instructions (FMUL2 / FFMA2 / FADD2): half the instructions for the same arithmetic.
+__device__ __forceinline__ float2 neg2(float2 v) { return make_float2(-v.x, -v.y); }
+__device__ __forceinline__ void mac2(float2 ah, float2 al, float bh, float bl, float2 &s, float2 &c) {
+    const float2 b = make_float2(bh, bh), bl2 = make_float2(bl, bl);
+    const float2 p = __fmul2_rn(ah, b);
+    const float2 e = __ffma2_rn(ah, b, neg2(p));
+    const float2 t = __fadd2_rn(s, p);
+    const float2 z = __fadd2_rn(t, neg2(s));
+    const float2 err = __fadd2_rn(__fadd2_rn(s, neg2(__fadd2_rn(t, neg2(z)))), __fadd2_rn(p, neg2(z)));
+    s = t;
+    c = __fadd2_rn(c, __fadd2_rn(err, e));
+    c = __ffma2_rn(ah, bl2, c);
+    c = __ffma2_rn(al, b, c);
+}
+__device__ __forceinline__ void renorm2(float2 &s, float2 &c) {
+    const float2 t = __fadd2_rn(s, c);
+    const float2 z = __fadd2_rn(t, neg2(s));
+    c = __fadd2_rn(__fadd2_rn(s, neg2(__fadd2_rn(t, neg2(z)))), __fadd2_rn(c, neg2(z)));
+    s = t;
+}
+
 // One launch computes up to two products of the same shape and transposition (blockIdx.z = problem
 // x K split); with `upper`, only the tiles on or above the diagonal (M == N, symmetric results).
 struct Df64Prob {
@@ -113,7 +136,7 @@ struct Df64Params {
     Df64Prob p[2];
 };
 
-template <bool TA, bool TB>
+template <bool TA, bool TB, bool PK>
 __global__ void __launch_bounds__(256) df64_gemm_kernel(const __grid_constant__ Df64Params P) {
     __shared__ float As[2][DB_K][DB_M + 1];
     __shared__ float Bs[2][DB_K][DB_N + 1];
@@ -126,10 +149,15 @@ __global__ void __launch_bounds__(256) df64_gemm_kernel(const __grid_constant__ 
     const int m0 = blockIdx.x * DB_M, n0 = blockIdx.y * DB_N;
     const int kb = split * P.kps, ke = min(K, kb + P.kps);
     float s[4][4], c[4][4];
+    float2 s2[2][4], c2[2][4];          // PK: rows (2 xp, 2 xp + 1) of column y
 #pragma unroll
     for (int x = 0; x < 4; x++)
 #pragma unroll
         for (int y = 0; y < 4; y++) s[x][y] = c[x][y] = 0.f;
+#pragma unroll
+    for (int x = 0; x < 2; x++)
+#pragma unroll
+        for (int y = 0; y < 4; y++) s2[x][y] = c2[x][y] = make_float2(0.f, 0.f);
     for (int k0 = kb; k0 < ke; k0 += DB_K) {
 #pragma unroll
         for (int t = 0; t < (DB_M * DB_K) / 256; t++) {
@@ -176,17 +204,42 @@ __global__ void __launch_bounds__(256) df64_gemm_kernel(const __grid_constant__ 
                     bh[t] = Bs[0][kk][tx + 16 * t];
                     bl[t] = Bs[1][kk][tx + 16 * t];
                 }
+                if constexpr (PK) {
+#pragma unroll
+                    for (int x = 0; x < 2; x++) {
+                        const float2 a2 = make_float2(ah[2 * x], ah[2 * x + 1]), l2 = make_float2(al[2 * x], al[2 * x + 1]);
+#pragma unroll
+                        for (int y = 0; y < 4; y++) mac2(a2, l2, bh[y], bl[y], s2[x][y], c2[x][y]);
+                    }
+                } else {
+#pragma unroll
+                    for (int x = 0; x < 4; x++)
+#pragma unroll
+                        for (int y = 0; y < 4; y++) mac(ah[x], al[x], bh[y], bl[y], s[x][y], c[x][y]);
+                }
+            }
+            if constexpr (PK) {
+#pragma unroll
+                for (int x = 0; x < 2; x++)
+#pragma unroll
+                    for (int y = 0; y < 4; y++) renorm2(s2[x][y], c2[x][y]);
+            } else {
 #pragma unroll
                 for (int x = 0; x < 4; x++)
 #pragma unroll
-                    for (int y = 0; y < 4; y++) mac(ah[x], al[x], bh[y], bl[y], s[x][y], c[x][y]);
+                    for (int y = 0; y < 4; y++) renorm(s[x][y], c[x][y]);
             }
-#pragma unroll
-            for (int x = 0; x < 4; x++)
-#pragma unroll
-                for (int y = 0; y < 4; y++) renorm(s[x][y], c[x][y]);
         }
         __syncthreads();
+    }
+    if constexpr (PK) {
+#pragma unroll
+        for (int x = 0; x < 2; x++)
+#pragma unroll
+            for (int y = 0; y < 4; y++) {
+                s[2 * x][y] = s2[x][y].x; s[2 * x + 1][y] = s2[x][y].y;
+                c[2 * x][y] = c2[x][y].x; c[2 * x + 1][y] = c2[x][y].y;
+            }
     }
     // undo the operand scales (exact powers of two)
     const int sa = *Q.ea, sb = *Q.eb;
@@ -309,10 +362,21 @@ static void df64_gemm_n(cudaStream_t s, bool ta, bool tb, double alpha, int npro
         Q.ldo = out && out[q] ? out[q]->ld : 0;
     }
     dim3 grid(mt, nt, splits * nprob);
-    if (!ta && !tb) df64_gemm_kernel<false, false><<<grid, 256, 0, s>>>(P);
-    else if (ta && !tb) df64_gemm_kernel<true, false><<<grid, 256, 0, s>>>(P);
-    else if (!ta && tb) df64_gemm_kernel<false, true><<<grid, 256, 0, s>>>(P);
-    else df64_gemm_kernel<true, true><<<grid, 256, 0, s>>>(P);
+    static const bool packed = [] {
+        const char *e = std::getenv("RSVDPACK_DF64_PACKED");
+        return !(e && e[0] == '0');
+    }();
+    if (packed) {
+        if (!ta && !tb) df64_gemm_kernel<false, false, true><<<grid, 256, 0, s>>>(P);
+        else if (ta && !tb) df64_gemm_kernel<true, false, true><<<grid, 256, 0, s>>>(P);
+        else if (!ta && tb) df64_gemm_kernel<false, true, true><<<grid, 256, 0, s>>>(P);
+        else df64_gemm_kernel<true, true, true><<<grid, 256, 0, s>>>(P);
+    } else {
+        if (!ta && !tb) df64_gemm_kernel<false, false, false><<<grid, 256, 0, s>>>(P);
+        else if (ta && !tb) df64_gemm_kernel<true, false, false><<<grid, 256, 0, s>>>(P);
+        else if (!ta && tb) df64_gemm_kernel<false, true, false><<<grid, 256, 0, s>>>(P);
+        else df64_gemm_kernel<true, true, false><<<grid, 256, 0, s>>>(P);
+    }
     RSVD_LAUNCH_CK();
     ctx().launches++;
     if (splits > 1) {

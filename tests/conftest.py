@@ -14,12 +14,17 @@ import json
 import os
 import subprocess
 import sys
+import tempfile
 
 import numpy as np
 import pytest
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 sys.path.insert(0, ROOT)
+
+# the batched path's autotuner keeps its table in a file: a fresh one for every test session
+os.environ.setdefault("RSVDPACK_TUNE_FILE", os.path.join(tempfile.gettempdir(),
+                                                         f"rsvdpack_batch_tune_{os.getpid()}.txt"))
 
 GOLDEN = os.path.join(ROOT, "tests", "golden")
 PORT_SO = os.path.join(ROOT, "oracle", "port", "librsvd_port.so")

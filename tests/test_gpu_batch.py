@@ -57,9 +57,18 @@ def _bind(L):
     L.rsvdpack_batch_plan_execute.restype = C.c_int
     L.rsvdpack_batch_plan_execute.argtypes = [C.c_void_p]
     L.rsvdpack_batch_plan_destroy.argtypes = [C.c_void_p]
+    L.rsvdpack_batch_plan_info.restype = C.c_int
+    L.rsvdpack_batch_plan_info.argtypes = [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int),
+                                           C.POINTER(C.c_double)]
 
 
-def run_batch(engine, mats, ks, p, q, seed):
+def plan_info(L, plan):
+    lp, cu, tuned, ms = C.c_int(0), C.c_int(0), C.c_int(0), C.c_double(0)
+    assert L.rsvdpack_batch_plan_info(plan, C.byref(lp), C.byref(cu), C.byref(tuned), C.byref(ms)) == 0
+    return lp.value, cu.value, tuned.value, ms.value
+
+
+def run_batch(engine, mats, ks, p, q, seed, info=None):
     L = engine.lib
     _bind(L)
     cnt = len(mats)
@@ -81,6 +90,8 @@ def run_batch(engine, mats, ks, p, q, seed):
     plan = L.rsvdpack_batch_plan_create(cnt, m, n, kk, p, q, 1, ptr(dA), lda, ptr(dU), lda, ptr(dS), ptr(dV), ldv,
                                         seed)
     assert plan, engine.last_error()
+    if info is not None:
+        info.append(plan_info(L, plan))
     try:
         for _ in range(2):                      # the captured graph replays
             rc = L.rsvdpack_batch_plan_execute(plan)
@@ -127,3 +138,36 @@ def test_batch_rejects_oversized_items(engine):
     assert not plan
     code, msg = engine.last_error()
     assert code == 1 and "72" in msg
+
+
+def test_batch_autotuner_chooses_and_records(engine, port):
+    """Plan creation times the kernel's configurations (lanes per Jacobi pair x column-group
+    offset) on a sample of the batch and records the fastest for the batch's class: the first
+    plan of a new class measures, the next one reads the same choice from the table (and the
+    table file holds it); results match the oracle on the same sketches with the chosen
+    configuration."""
+    import os
+    g = np.random.default_rng(7)
+    mats, ks = [], []
+    for i in range(40):
+        m = int(g.integers(900, 1000))
+        n = int(g.integers(450, 500))
+        A = spectrum_matrix(m, n, 0.9 ** np.arange(min(m, n)), seed=2000 + i)
+        mats.append(A.astype(np.float32).astype(np.float64))
+        ks.append(42 if i == 0 else int(g.integers(20, 42)))     # k + p = 50 at most
+    p, q, seed = 8, 1, 0x55AA
+    info = []
+    Us, Ss, Vs = run_batch(engine, mats, ks, p, q, seed, info)
+    run_batch(engine, mats, ks, p, q, seed + 1, info)            # the same class
+    (lp1, cu1, t1, ms1), (lp2, cu2, t2, ms2) = info
+    assert lp1 in (4, 8, 16, 32) and cu1 in (0, 1) and t1 == 1 and ms1 > 0
+    assert (lp2, cu2, t2) == (lp1, cu1, 2)
+    with open(os.environ["RSVDPACK_TUNE_FILE"]) as f:
+        assert any(line.split()[1:3] == [str(lp1), str(cu1)] for line in f if line.startswith("l50_"))
+    for i in (0, 17, 39):
+        A, k = mats[i], ks[i]
+        n = A.shape[1]
+        port.set_omega(ListOmega([philox_gaussians(n * (k + p), seed, i)]))
+        Uo, So, Vo = port.low_rank_svd_rand_decomp_fixed_rank(A, k, p, 1, q, 1)
+        so = np.diag(So)
+        assert np.max(np.abs(Ss[i] - so) / so[0]) < 2e-4
