@@ -56,7 +56,7 @@ def parse():
     # bracket one leg's timed region with cudaProfilerStart/Stop (ncu --profile-from-start off)
     ap.add_argument("--profile-leg", choices=["solve", "learned", "batched"], default=None)
     # run one fixed profiling case (see PROFILE_CASES) and exit
-    ap.add_argument("--profile-case", choices=["update", "gemm3x", "solve", "pivot", "norm"], default=None)
+    ap.add_argument("--profile-case", choices=["update", "gemm3x", "solve", "pivot", "norm", "df64"], default=None)
     return ap.parse_args()
 
 
@@ -1034,6 +1034,8 @@ def run_ours(args):
 #            two-sided ID / CUR workload)
 #   norm     the Frobenius-norm sweep of the plain FP32 blocked QB (one block) on a 32768 x 16384
 #            FP32 matrix (2 GiB)
+#   df64     one sketch pass of the two-sided ID workload as a double-float FP64 product
+#            (520 x 20000 by 20000 x 10000, rsvdpack_dev_gemm_df64)
 
 def _prof_engine():
     from lowrankmatrixdecompositioncodes_gb300 import load_engine
@@ -1154,8 +1156,29 @@ def prof_case_norm(torch, eng):
     _prof_run(torch, call)
 
 
+def prof_case_df64(torch, eng):
+    """One sketch pass of the two-sided ID workload as a double-float FP64 product:
+    Y^T (520 x 10000) = Om (520 x 20000) A (20000 x 10000), operands already split."""
+    L = eng.lib
+    L.rsvdpack_dev_gemm_df64.restype = C.c_int
+    L.rsvdpack_dev_gemm_df64.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_double, C.c_void_p,
+                                         C.c_longlong, C.c_void_p, C.c_longlong, C.c_double, C.c_void_p,
+                                         C.c_longlong]
+    g = torch.Generator(device="cuda")
+    g.manual_seed(4)
+    M, N, K = 520, 10000, 20000
+    Om = torch.randn(M, K, device="cuda", dtype=torch.float64, generator=g)   # K x M column-major
+    A = torch.randn(N, K, device="cuda", dtype=torch.float64, generator=g)    # K x N column-major
+    Y = torch.empty(N, M, device="cuda", dtype=torch.float64)
+
+    def call():
+        if L.rsvdpack_dev_gemm_df64(1, 0, M, N, K, 1.0, Om.data_ptr(), K, A.data_ptr(), K, 0.0, Y.data_ptr(), M):
+            raise RuntimeError(eng.last_error())
+    _prof_run(torch, call)
+
+
 PROFILE_CASES = {"update": prof_case_update, "gemm3x": prof_case_gemm3x, "solve": prof_case_solve,
-                 "pivot": prof_case_pivot, "norm": prof_case_norm}
+                 "pivot": prof_case_pivot, "norm": prof_case_norm, "df64": prof_case_df64}
 
 
 def main():

@@ -27,7 +27,6 @@
 
 #include <algorithm>
 #include <cmath>
-#include <cstdlib>
 
 namespace rsvd {
 
@@ -78,29 +77,11 @@ __global__ void split_kernel(const double *x, i64 ld, i64 r, i64 c, const int *s
 // reduced by df64_reduce_kernel), else the epilogue applies alpha, beta and the scales.
 constexpr int DB_M = 64, DB_N = 64, DB_K = 16;
 
-__device__ __forceinline__ void mac(float ah, float al, float bh, float bl, float &s, float &c) {
-    const float p = __fmul_rn(ah, bh);
-    const float e = __fmaf_rn(ah, bh, -p);
-    const float t = __fadd_rn(s, p);
-    const float z = __fsub_rn(t, s);
-    const float err = __fadd_rn(__fsub_rn(s, __fsub_rn(t, z)), __fsub_rn(p, z));
-    s = t;
-    c = __fadd_rn(c, __fadd_rn(err, e));
-    c = __fmaf_rn(ah, bl, c);
-    c = __fmaf_rn(al, bh, c);
-}
-
-// (s, c) <- (s + c rounded, the exact remainder) by Knuth's two-sum (no ordering assumption: a
-// partial sum that cancels can leave |s| < |c|)
-__device__ __forceinline__ void renorm(float &s, float &c) {
-    const float t = __fadd_rn(s, c);
-    const float z = __fsub_rn(t, s);
-    c = __fadd_rn(__fsub_rn(s, __fsub_rn(t, z)), __fsub_rn(c, z));
-    s = t;
-}
-
-// The same two operations on pairs of accumulators (rows x, x + 1 of one output column) with the
-// packed FP32 instructions (FMUL2 / FFMA2 / FADD2): half the instructions for the same arithmetic.
+// One multiply-add of the double-float product, on a pair of accumulators (rows x, x + 1 of one
+// output column) with the packed FP32 instructions (FMUL2 / FFMA2 / FADD2): p = hi_a hi_b,
+// e = fma(hi_a, hi_b, -p) exact; (s, c) += p by two-sum, c += e + hi_a lo_b + lo_a hi_b.
+// renorm2: (s, c) <- two-sum(s, c) (no ordering assumption: a partial sum that cancels can
+// leave |s| < |c|).
 __device__ __forceinline__ float2 neg2(float2 v) { return make_float2(-v.x, -v.y); }
 __device__ __forceinline__ void mac2(float2 ah, float2 al, float bh, float bl, float2 &s, float2 &c) {
     const float2 b = make_float2(bh, bh), bl2 = make_float2(bl, bl);
@@ -136,7 +117,7 @@ struct Df64Params {
     Df64Prob p[2];
 };
 
-template <bool TA, bool TB, bool PK>
+template <bool TA, bool TB>
 __global__ void __launch_bounds__(256) df64_gemm_kernel(const __grid_constant__ Df64Params P) {
     __shared__ float As[2][DB_K][DB_M + 1];
     __shared__ float Bs[2][DB_K][DB_N + 1];
@@ -149,11 +130,7 @@ __global__ void __launch_bounds__(256) df64_gemm_kernel(const __grid_constant__ 
     const int m0 = blockIdx.x * DB_M, n0 = blockIdx.y * DB_N;
     const int kb = split * P.kps, ke = min(K, kb + P.kps);
     float s[4][4], c[4][4];
-    float2 s2[2][4], c2[2][4];          // PK: rows (2 xp, 2 xp + 1) of column y
-#pragma unroll
-    for (int x = 0; x < 4; x++)
-#pragma unroll
-        for (int y = 0; y < 4; y++) s[x][y] = c[x][y] = 0.f;
+    float2 s2[2][4], c2[2][4];          // rows (2 xp, 2 xp + 1) of column y
 #pragma unroll
     for (int x = 0; x < 2; x++)
 #pragma unroll
@@ -204,43 +181,27 @@ __global__ void __launch_bounds__(256) df64_gemm_kernel(const __grid_constant__ 
                     bh[t] = Bs[0][kk][tx + 16 * t];
                     bl[t] = Bs[1][kk][tx + 16 * t];
                 }
-                if constexpr (PK) {
 #pragma unroll
-                    for (int x = 0; x < 2; x++) {
-                        const float2 a2 = make_float2(ah[2 * x], ah[2 * x + 1]), l2 = make_float2(al[2 * x], al[2 * x + 1]);
+                for (int x = 0; x < 2; x++) {
+                    const float2 a2 = make_float2(ah[2 * x], ah[2 * x + 1]), l2 = make_float2(al[2 * x], al[2 * x + 1]);
 #pragma unroll
-                        for (int y = 0; y < 4; y++) mac2(a2, l2, bh[y], bl[y], s2[x][y], c2[x][y]);
-                    }
-                } else {
-#pragma unroll
-                    for (int x = 0; x < 4; x++)
-#pragma unroll
-                        for (int y = 0; y < 4; y++) mac(ah[x], al[x], bh[y], bl[y], s[x][y], c[x][y]);
+                    for (int y = 0; y < 4; y++) mac2(a2, l2, bh[y], bl[y], s2[x][y], c2[x][y]);
                 }
             }
-            if constexpr (PK) {
 #pragma unroll
-                for (int x = 0; x < 2; x++)
+            for (int x = 0; x < 2; x++)
 #pragma unroll
-                    for (int y = 0; y < 4; y++) renorm2(s2[x][y], c2[x][y]);
-            } else {
-#pragma unroll
-                for (int x = 0; x < 4; x++)
-#pragma unroll
-                    for (int y = 0; y < 4; y++) renorm(s[x][y], c[x][y]);
-            }
+                for (int y = 0; y < 4; y++) renorm2(s2[x][y], c2[x][y]);
         }
         __syncthreads();
     }
-    if constexpr (PK) {
 #pragma unroll
-        for (int x = 0; x < 2; x++)
+    for (int x = 0; x < 2; x++)
 #pragma unroll
-            for (int y = 0; y < 4; y++) {
-                s[2 * x][y] = s2[x][y].x; s[2 * x + 1][y] = s2[x][y].y;
-                c[2 * x][y] = c2[x][y].x; c[2 * x + 1][y] = c2[x][y].y;
-            }
-    }
+        for (int y = 0; y < 4; y++) {
+            s[2 * x][y] = s2[x][y].x; s[2 * x + 1][y] = s2[x][y].y;
+            c[2 * x][y] = c2[x][y].x; c[2 * x + 1][y] = c2[x][y].y;
+        }
     // undo the operand scales (exact powers of two)
     const int sa = *Q.ea, sb = *Q.eb;
     const double unscale = ldexp(1.0, (sa > 0 ? sa - 1023 : 0) + (sb > 0 ? sb - 1023 : 0));
@@ -362,21 +323,10 @@ static void df64_gemm_n(cudaStream_t s, bool ta, bool tb, double alpha, int npro
         Q.ldo = out && out[q] ? out[q]->ld : 0;
     }
     dim3 grid(mt, nt, splits * nprob);
-    static const bool packed = [] {
-        const char *e = std::getenv("RSVDPACK_DF64_PACKED");
-        return !(e && e[0] == '0');
-    }();
-    if (packed) {
-        if (!ta && !tb) df64_gemm_kernel<false, false, true><<<grid, 256, 0, s>>>(P);
-        else if (ta && !tb) df64_gemm_kernel<true, false, true><<<grid, 256, 0, s>>>(P);
-        else if (!ta && tb) df64_gemm_kernel<false, true, true><<<grid, 256, 0, s>>>(P);
-        else df64_gemm_kernel<true, true, true><<<grid, 256, 0, s>>>(P);
-    } else {
-        if (!ta && !tb) df64_gemm_kernel<false, false, false><<<grid, 256, 0, s>>>(P);
-        else if (ta && !tb) df64_gemm_kernel<true, false, false><<<grid, 256, 0, s>>>(P);
-        else if (!ta && tb) df64_gemm_kernel<false, true, false><<<grid, 256, 0, s>>>(P);
-        else df64_gemm_kernel<true, true, false><<<grid, 256, 0, s>>>(P);
-    }
+    if (!ta && !tb) df64_gemm_kernel<false, false><<<grid, 256, 0, s>>>(P);
+    else if (ta && !tb) df64_gemm_kernel<true, false><<<grid, 256, 0, s>>>(P);
+    else if (!ta && tb) df64_gemm_kernel<false, true><<<grid, 256, 0, s>>>(P);
+    else df64_gemm_kernel<true, true><<<grid, 256, 0, s>>>(P);
     RSVD_LAUNCH_CK();
     ctx().launches++;
     if (splits > 1) {
