@@ -1034,8 +1034,8 @@ def run_ours(args):
 #            two-sided ID / CUR workload)
 #   norm     the Frobenius-norm sweep of the plain FP32 blocked QB (one block) on a 32768 x 16384
 #            FP32 matrix (2 GiB)
-#   df64     one sketch pass of the two-sided ID workload as a double-float FP64 product
-#            (520 x 20000 by 20000 x 10000, rsvdpack_dev_gemm_df64)
+#   df64     a reduced sketch pass of the two-sided ID workload as a double-float FP64 product
+#            (520 x 8000 by 8000 x 4000, rsvdpack_dev_gemm_df64)
 
 def _prof_engine():
     from lowrankmatrixdecompositioncodes_gb300 import load_engine
@@ -1157,8 +1157,8 @@ def prof_case_norm(torch, eng):
 
 
 def prof_case_df64(torch, eng):
-    """One sketch pass of the two-sided ID workload as a double-float FP64 product:
-    Y^T (520 x 10000) = Om (520 x 20000) A (20000 x 10000), operands already split."""
+    """A reduced sketch pass of the two-sided ID workload as a double-float FP64 product:
+    Y^T (520 x 4000) = Om (520 x 8000) A (8000 x 4000) (A and its split: 512 MB, above L2)."""
     L = eng.lib
     L.rsvdpack_dev_gemm_df64.restype = C.c_int
     L.rsvdpack_dev_gemm_df64.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_double, C.c_void_p,
@@ -1166,7 +1166,7 @@ def prof_case_df64(torch, eng):
                                          C.c_longlong]
     g = torch.Generator(device="cuda")
     g.manual_seed(4)
-    M, N, K = 520, 10000, 20000
+    M, N, K = 520, 4000, 8000
     Om = torch.randn(M, K, device="cuda", dtype=torch.float64, generator=g)   # K x M column-major
     A = torch.randn(N, K, device="cuda", dtype=torch.float64, generator=g)    # K x N column-major
     Y = torch.empty(N, M, device="cuda", dtype=torch.float64)
