@@ -202,9 +202,21 @@ __global__ void __launch_bounds__(1024) jacobi_cluster_kernel(const double *G, l
 // Jacobi rotation (cs, sn) zeroing w_p.w_q = d, |w_p|^2 = a, |w_q|^2 = b (Rutishauser's
 // formulas); FP32 with correctly rounded reciprocal / rsqrt intrinsics instead of the
 // division and square-root sequences.
+// FP32: the tangent t only has to annihilate the pair to about FP32 precision, so it takes the
+// hardware's approximate reciprocal and reciprocal square root (the correctly rounded sequences
+// sat on the round's critical path); the cosine, whose rounding decides how orthogonal the
+// accumulated rotations stay, is correctly rounded (an approximate cosine with one Newton step
+// drifted the column norms by ~1e-4 over a 272-column solve).
 __device__ __forceinline__ void jrot(float a, float b, float d, float &cs, float &sn) {
-    const float zeta = (b - a) * __frcp_rn(2.f * d);
-    const float t = copysignf(__frcp_rn(fabsf(zeta) + __fsqrt_rn(fmaf(zeta, zeta, 1.f))), zeta);
+    const float zeta = __fdividef(b - a, 2.f * d);
+    const float az = fabsf(zeta);
+    float t;
+    if (az < 1e18f) {
+        const float z2 = fmaf(zeta, zeta, 1.f);
+        t = copysignf(__fdividef(1.f, fmaf(z2, rsqrtf(z2), az)), zeta);      // 1 / (|z| + sqrt(1 + z^2))
+    } else {
+        t = __fdividef(0.5f, zeta);
+    }
     cs = __frsqrt_rn(fmaf(t, t, 1.f));
     sn = cs * t;
 }
@@ -226,16 +238,21 @@ __device__ __forceinline__ uint32_t smem_addr(const void *p) { return (uint32_t)
 // shared memory (completing on the holder's mbarrier, waited with a bound), followed by one
 // cluster barrier.  NBLK-1 super-rounds meet every pair of blocks once: one outer sweep.
 // Outer sweeps repeat until no CTA rotated anything during a whole sweep, or (FP32) until
-// the largest |cos| = |w_p.w_q| / (|w_p||w_q|) seen in a sweep is below sqrt(tol): Jacobi
-// converges quadratically, so the next sweep would find every pair below tol.
+// the largest cos^2 = (w_p.w_q)^2 / (|w_p|^2 |w_q|^2) seen in a sweep is below stop_tol.  The
+// caller passes tol / 10: quadratic convergence would make cos^2 < tol enough for the next
+// sweep to find every pair below tol, but clustered singular values converge more slowly, and
+// on 272-column factors of the 16384 x 8192 workload that shortcut stopped one sweep early on
+// some sketches, leaving hundreds of nearly-equal pairs to the refinement's sequential rotations.
+// Each warp keeps its rotation count and largest cos^2 in registers during a sweep (no
+// shared-memory atomics in the rounds) and folds them into the CTA's totals at its end.
 // One warp per pair (blockDim = 32 bs, at most 16 warps so that the register-held chunks
 // fit): a lane keeps its 16-byte chunks of w_p and w_q in registers between the dot
 // products and the rotation (MAXIT chunks: ldr <= 32 MAXIT VW); FP32 uses packed FFMA2.
 // Shared memory per CTA: 2 buffers x 2 slots x bs x ldr x 2 (W, V) x sizeof(S).
 template <typename S, int CLN>
 __global__ void __launch_bounds__(512, 1) jacobi_block_cluster_kernel(const double *G, long long ldg, int n, int bs,
-                                                                    int ldr, S tol, int max_sweeps, S *Wout, S *Vout,
-                                                                    long long ldo, int *sweeps_out, int *flag) {
+                                                                    int ldr, S tol, S stop_tol, int max_sweeps, S *Wout,
+                                                                    S *Vout, long long ldo, int *sweeps_out, int *flag) {
     namespace cg = cooperative_groups;
     cg::cluster_group cluster = cg::this_cluster();
     const int rank = (int)cluster.block_rank();
@@ -292,6 +309,8 @@ __global__ void __launch_bounds__(512, 1) jacobi_block_cluster_kernel(const doub
     uint32_t mphase = 0;
     const int nvec = ldr / VW;               // columns are zero beyond n up to ldr (a multiple of 4)
     const uint32_t slot_bytes = (uint32_t)(slot_elems * sizeof(S));
+    float wmax = 0.f;                        // this warp's largest cos^2 and rotations in the sweep
+    int wrot = 0;
     for (; sweep < max_sweeps; sweep++) {
         for (int sr = 0; sr < NBLK - 1; sr++) {
             S *s0 = slot_ptr(buf, cur, 0), *s1 = slot_ptr(buf, cur, 1);
@@ -354,7 +373,7 @@ __global__ void __launch_bounds__(512, 1) jacobi_block_cluster_kernel(const doub
                     }
                     a = warp_sum_t(a); b = warp_sum_t(b); d = warp_sum_t(d);
                     const S ab = a * b, dd = d * d;
-                    if (lane == 0 && ab > S(0)) atomicMax(&sweep_max, __float_as_uint((float)(dd / ab)));
+                    if (ab > S(0)) wmax = fmaxf(wmax, __fdividef((float)dd, (float)ab));
                     if (d == S(0) || dd <= tol * tol * ab) continue;
                     S cs, sn;
                     jrot(a, b, d, cs, sn);
@@ -397,7 +416,7 @@ __global__ void __launch_bounds__(512, 1) jacobi_block_cluster_kernel(const doub
                             vq[iv] = vv;
                         }
                     }
-                    if (lane == 0) atomicAdd(&rot_count, 1);
+                    wrot++;
                 }
                 __syncthreads();
             }
@@ -449,6 +468,13 @@ __global__ void __launch_bounds__(512, 1) jacobi_block_cluster_kernel(const doub
             cur = nxt;
         }
         // ---- did any CTA rotate during this sweep, and how large was the largest cosine?
+        if (lane == 0) {
+            atomicMax(&sweep_max, __float_as_uint(wmax));
+            atomicAdd(&rot_count, wrot);
+        }
+        wmax = 0.f;
+        wrot = 0;
+        __syncthreads();
         if (threadIdx.x < CLN) {
             int *dstf = cluster.map_shared_rank(&sweep_rot[rank], (unsigned)threadIdx.x);
             *dstf = rot_count;
@@ -469,7 +495,7 @@ __global__ void __launch_bounds__(512, 1) jacobi_block_cluster_kernel(const doub
         if (total == 0) break;
         // FP32 only: |cos| < sqrt(tol) (cos^2 < tol).  FP64 keeps the plain criterion, so that
         // its factors match the reference's to the last sweep.
-        if (sizeof(S) == 4 && (double)cmax < (double)tol) { sweep++; break; }
+        if (sizeof(S) == 4 && (double)cmax < (double)stop_tol) { sweep++; break; }
     }
     // ---- write the columns this CTA holds
     for (int sl = 0; sl < 2; sl++) {
@@ -796,8 +822,8 @@ int jacobi_small(cudaStream_t s, DM<double> G, DM<double> U, DM<double> V, doubl
             cudaGetLastError();
             continue;
         }
-        RSVD_CK(cudaLaunchKernelEx(&cfg, kern, (const double *)G.p, (long long)G.ld, n, bs, ldr, tol, 40, W, Vacc,
-                                   (long long)ld, d_sweeps, d_flag));
+        RSVD_CK(cudaLaunchKernelEx(&cfg, kern, (const double *)G.p, (long long)G.ld, n, bs, ldr, tol, (S)(tol / 10), 40,
+                                   W, Vacc, (long long)ld, d_sweeps, d_flag));
         launched = true;
         variant = cl;
     }
@@ -911,6 +937,14 @@ void svd_refine(cudaStream_t s, DM<double> X, DM<double> V, DM<double> U, double
                                                                   U.ld, V.p, V.ld, d_sv);
     RSVD_LAUNCH_CK();
     ctx().launches += 6 + 3 * steps;
+    if (ctx().opts.verbose) {
+        std::vector<int> cnt((size_t)steps);
+        RSVD_CK(cudaMemcpyAsync(cnt.data(), pair_count, sizeof(int) * steps, cudaMemcpyDeviceToHost, s));
+        RSVD_CK(cudaStreamSynchronize(s));
+        std::fprintf(stderr, "rsvdpack: refine n=%d tight pairs per step:", n);
+        for (int c : cnt) std::fprintf(stderr, " %d", c);
+        std::fprintf(stderr, "\n");
+    }
 }
 
 void small_svd_refined(cudaStream_t s, DM<double> G, DM<double> U, DM<double> V, double *d_sv, int *d_flag) {
