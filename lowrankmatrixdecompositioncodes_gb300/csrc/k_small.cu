@@ -207,10 +207,9 @@ __global__ void __launch_bounds__(1024) jacobi_cluster_kernel(const double *G, l
 // sat on the round's critical path); the cosine, whose rounding decides how orthogonal the
 // accumulated rotations stay, is correctly rounded (an approximate cosine with one Newton step
 // drifted the column norms by ~1e-4 over a 272-column solve).
-__device__ __forceinline__ void jrot(float a, float b, float d, float &cs, float &sn) {
+__device__ __forceinline__ void jrot_t(float a, float b, float d, float &cs, float &sn, float &t) {
     const float zeta = __fdividef(b - a, 2.f * d);
     const float az = fabsf(zeta);
-    float t;
     if (az < 1e18f) {
         const float z2 = fmaf(zeta, zeta, 1.f);
         t = copysignf(__fdividef(1.f, fmaf(z2, rsqrtf(z2), az)), zeta);      // 1 / (|z| + sqrt(1 + z^2))
@@ -219,6 +218,10 @@ __device__ __forceinline__ void jrot(float a, float b, float d, float &cs, float
     }
     cs = __frsqrt_rn(fmaf(t, t, 1.f));
     sn = cs * t;
+}
+__device__ __forceinline__ void jrot(float a, float b, float d, float &cs, float &sn) {
+    float t;
+    jrot_t(a, b, d, cs, sn, t);
 }
 __device__ __forceinline__ void jrot(double a, double b, double d, double &cs, double &sn) {
     const double zeta = (b - a) / (2.0 * d);
@@ -517,6 +520,453 @@ __global__ void __launch_bounds__(512, 1) jacobi_block_cluster_kernel(const doub
     cluster.sync();
 }
 
+// FP32 block-cyclic Jacobi, register-resident Gram form, for a fixed block width BS (the
+// cluster layout, block moves, pair schedule and convergence tests of
+// jacobi_block_cluster_kernel).  A super-round of the one-sided kernel costs one block barrier,
+// two n-row passes and three warp reductions per round; here it is three phases:
+//   Gram   Gl = P^T P of the CTA's NL = 2 BS local columns P (n rows), all warps: TK x TK
+//          output blocks x row slices (consecutive lanes take consecutive 16-byte row chunks),
+//          partial sums reduced through shared memory;
+//   rounds warp 0 alone: lane i holds row i of Gl and of Z (the accumulated rotation) in
+//          registers; the round's pair pattern is a compile-time function of the (unrolled)
+//          round index, so every register index is static.  A round: lane l < BS computes the
+//          rotation of pair l from Gl_pp, Gl_qq, Gl_pq fetched by shuffles, the rotations are
+//          broadcast, every lane applies the column rotations to its rows of Gl and Z, and the
+//          row rotation of Gl by exchanging rows with its partner; the diagonal block takes
+//          a' = a - t d, b' = b + t d, d' = 0.  No barrier and no shared memory inside a round.
+//   apply  P <- P Z for the W and V columns: one thread per 4-row chunk of one matrix, Z rows
+//          broadcast from shared memory, 4 x NL accumulators (skipped when nothing rotated).
+// Gl is formed afresh at every super-round, so the rounding of the two-sided updates does not
+// accumulate; its FP32 dot products carry the one-sided kernel's ~sqrt(n) eps relative error.
+// The super-round's rounds on two warps in lockstep.  Warp 0: lane i < 2 BS holds row i of Gl
+// (g) for the columns at positions 0..2 BS-1 and dg = Gl_ii; warp 1: lane i holds row i of Z.
+// The pairs sit at fixed positions -- cross rounds (k, BS + k), the full round of a sweep's first
+// super-round (k, 2 BS - 1 - k) -- and the columns move between rounds instead: cross rounds
+// shift positions BS..2 BS-1 down by one, full rounds rotate positions 1..2 BS-1 (the circle
+// method).  So every register index is static inside one compact loop body (a loop unrolled over
+// the rounds did not fit the instruction cache).  Column moves are register moves within a lane,
+// row moves (Gl only) are shuffles between lanes; after the last round every column is back at
+// its starting position.  A round: lane k < BS of warp 0 computes the rotation of pair k from dg
+// and Gl(k, partner) and publishes it (cos, sin, ballot) in shared memory, double-buffered by
+// round parity; a named barrier over the two warps hands it to warp 1, which rotates the columns
+// of Z while warp 0 rotates its rows of Gl by columns and against the partner's row.  Only the
+// rotated pair's diagonal is updated exactly (a' = a - t d, b' = b + t d); its off-diagonal entry
+// keeps the rounding of the general formula, which is never read again in the super-round (each
+// pair meets once) and is recomputed at the next one.  Adjacent pairs are rotated as packed
+// FP32 pairs (FFMA2).
+template <int BS, bool FULLR>
+__device__ __forceinline__ void gr_move(float (&g)[2 * BS]) {
+    constexpr int NL = 2 * BS;
+    if (FULLR) {
+        const float g1 = g[1];
+#pragma unroll
+        for (int k = 1; k < NL - 1; k++) g[k] = g[k + 1];
+        g[NL - 1] = g1;
+    } else {
+        const float g0 = g[BS];
+#pragma unroll
+        for (int k = BS; k < NL - 1; k++) g[k] = g[k + 1];
+        g[NL - 1] = g0;
+    }
+}
+// column rotations of one row: new col p = c col_p - s col_q, new col q = s col_p + c col_q,
+// pairs k and k + 1 packed
+template <int BS, bool FULLR>
+__device__ __forceinline__ void gr_colrot(float (&g)[2 * BS], const float *C, const float *Sn) {
+    constexpr int NL = 2 * BS;
+#pragma unroll
+    for (int k = 0; k + 1 < BS; k += 2) {
+        const int P0 = k, Q0 = FULLR ? NL - 1 - k : BS + k;
+        const int P1 = k + 1, Q1 = FULLR ? NL - 2 - k : BS + k + 1;
+        const float2 c2 = make_float2(C[k], C[k + 1]), s2 = make_float2(Sn[k], Sn[k + 1]);
+        const float2 xp = make_float2(g[P0], g[P1]), xq = make_float2(g[Q0], g[Q1]);
+        const float2 np = __ffma2_rn(c2, xp, __fmul2_rn(make_float2(-s2.x, -s2.y), xq));
+        const float2 nq = __ffma2_rn(s2, xp, __fmul2_rn(c2, xq));
+        g[P0] = np.x; g[P1] = np.y; g[Q0] = nq.x; g[Q1] = nq.y;
+    }
+    if (BS % 2) {
+        constexpr int k = BS - 1;
+        const int P = k, Q = FULLR ? NL - 1 - k : BS + k;
+        const float xp = g[P], xq = g[Q];
+        g[P] = fmaf(C[k], xp, -Sn[k] * xq);
+        g[Q] = fmaf(Sn[k], xp, C[k] * xq);
+    }
+}
+template <int BS, bool FULLR>
+__device__ __forceinline__ void gr_rounds_g(float (&g)[2 * BS], float &dg, int lane, int b0, int b1, int n, float tol,
+                                            float &wmax, int &wrot, bool &any, float *rot_cs, float *rot_sn,
+                                            unsigned int *rot_bal) {
+    constexpr int NL = 2 * BS;
+    constexpr int NR = FULLR ? NL - 1 : BS;
+    const int partner = lane >= NL ? lane : (FULLR ? NL - 1 - lane : (lane < BS ? lane + BS : lane - BS));
+    const int pidx = lane >= NL ? 0 : (FULLR ? (lane < BS ? lane : NL - 1 - lane) : (lane < BS ? lane : lane - BS));
+    const bool is_p = lane < BS;
+    const int src = lane >= NL ? lane
+                    : (FULLR ? (lane == 0 ? 0 : (lane % (NL - 1)) + 1)
+                             : (lane < BS ? lane : BS + (lane - BS + 1) % BS));
+#pragma unroll 1
+    for (int r = 0; r < NR; r++) {
+        float op = 0.f;                                   // Gl(lane, partner)
+#pragma unroll
+        for (int k = 0; k < BS; k++) {
+            const int P = k, Q = FULLR ? NL - 1 - k : BS + k;
+            if (lane == P) op = g[Q];
+            if (lane == Q) op = g[P];
+        }
+        const float b = __shfl_sync(0xffffffffu, dg, partner);
+        const float a = dg, d = op;
+        int op_, oq_;                                     // original columns at the pair's positions
+        if (FULLR) {
+            op_ = lane == 0 ? 0 : ((lane - 1 + r) % (NL - 1)) + 1;
+            oq_ = ((partner - 1 + r) % (NL - 1)) + 1;
+        } else {
+            op_ = lane;
+            oq_ = BS + (lane + r) % BS;
+        }
+        const int gp = (op_ < BS) ? b0 * BS + op_ : b1 * BS + (op_ - BS);
+        const int gq = (oq_ < BS) ? b0 * BS + oq_ : b1 * BS + (oq_ - BS);
+        float cs = 1.f, sn = 0.f, t = 0.f;
+        bool act = false;
+        unsigned int c2 = 0u;
+        if (lane < BS && gp < n && gq < n) {
+            const float ab = a * b, dd = d * d;
+            if (ab > 0.f) c2 = __float_as_uint(__fdividef(dd, ab));
+            if (d != 0.f && dd > tol * tol * ab) {
+                jrot_t(a, b, d, cs, sn, t);
+                act = true;
+            }
+        }
+        const unsigned int bal = __ballot_sync(0xffffffffu, act);
+        const int slot = r & 1;
+        if (lane < BS) {
+            rot_cs[slot * BS + lane] = cs;
+            rot_sn[slot * BS + lane] = sn;
+        }
+        if (lane == 0) rot_bal[slot] = bal;
+        asm volatile("bar.sync 1, 64;" ::: "memory");      // hand the round to warp 1
+        wmax = fmaxf(wmax, __uint_as_float(__reduce_max_sync(0xffffffffu, c2)));
+        if (bal != 0u) {
+            wrot += __popc(bal);
+            any = true;
+            const float dgp = fmaf(-t, d, a), dgq = fmaf(t, d, b);
+            float C[BS], Sn[BS];
+#pragma unroll
+            for (int k = 0; k < BS; k++) {
+                C[k] = __shfl_sync(0xffffffffu, cs, k);
+                Sn[k] = __shfl_sync(0xffffffffu, sn, k);
+            }
+            const float c_own = __shfl_sync(0xffffffffu, cs, pidx), s_own = __shfl_sync(0xffffffffu, sn, pidx);
+            const float dp_own = __shfl_sync(0xffffffffu, dgp, pidx), dq_own = __shfl_sync(0xffffffffu, dgq, pidx);
+            const bool act_own = lane < NL && ((bal >> pidx) & 1u);
+            gr_colrot<BS, FULLR>(g, C, Sn);
+            // row rotation (J^T Gl) against the partner's row: g = c g -+ s other
+            const float cr = act_own ? c_own : 1.f, sr = act_own ? (is_p ? -s_own : s_own) : 0.f;
+            const float2 cr2 = make_float2(cr, cr), sr2 = make_float2(sr, sr);
+#pragma unroll
+            for (int k = 0; k < NL; k += 2) {
+                const float o0 = __shfl_sync(0xffffffffu, g[k], partner);
+                const float o1 = __shfl_sync(0xffffffffu, g[k + 1], partner);
+                const float2 nv = __ffma2_rn(cr2, make_float2(g[k], g[k + 1]), __fmul2_rn(sr2, make_float2(o0, o1)));
+                g[k] = nv.x;
+                g[k + 1] = nv.y;
+            }
+            if (act_own) dg = is_p ? dp_own : dq_own;
+        }
+        gr_move<BS, FULLR>(g);
+#pragma unroll
+        for (int k = 0; k < NL; k++) g[k] = __shfl_sync(0xffffffffu, g[k], src);
+        dg = __shfl_sync(0xffffffffu, dg, src);
+    }
+}
+template <int BS, bool FULLR>
+__device__ __forceinline__ void gr_rounds_z(float (&z)[2 * BS], const float *rot_cs, const float *rot_sn,
+                                            const unsigned int *rot_bal) {
+    constexpr int NL = 2 * BS;
+    constexpr int NR = FULLR ? NL - 1 : BS;
+#pragma unroll 1
+    for (int r = 0; r < NR; r++) {
+        asm volatile("bar.sync 1, 64;" ::: "memory");      // round r published by warp 0
+        const int slot = r & 1;
+        if (rot_bal[slot] != 0u) {
+            float C[BS], Sn[BS];
+#pragma unroll
+            for (int k = 0; k < BS; k++) {
+                C[k] = rot_cs[slot * BS + k];
+                Sn[k] = rot_sn[slot * BS + k];
+            }
+            gr_colrot<BS, FULLR>(z, C, Sn);
+        }
+        gr_move<BS, FULLR>(z);
+    }
+}
+
+// P <- P Z for the W and V columns of a super-round (in place): one thread per 4-row chunk of
+// one matrix, 4 x 2 BS accumulators, Z rows (pitch 2 BS + 2) broadcast from shared memory.
+// Not inlined, so that its accumulators and warp 0's register rounds are allocated apart.
+template <int BS>
+__device__ __noinline__ void gr_apply(float *s0, float *s1, int ldr, int nch, const float *zs) {
+    constexpr int NL = 2 * BS, ZP = NL + 2;
+    for (int task = threadIdx.x; task < 2 * nch; task += blockDim.x) {
+        const bool isv = task >= nch;
+        const int ch = isv ? task - nch : task;
+        // column c of W: c < BS in slot 0, else slot 1; V columns follow the W columns of a slot
+        auto col = [&](int c) {
+            return (c < BS) ? s0 + (size_t)((isv ? BS : 0) + c) * ldr : s1 + (size_t)((isv ? BS : 0) + c - BS) * ldr;
+        };
+        float2 y[4][NL / 2];
+#pragma unroll
+        for (int a = 0; a < 4; a++)
+#pragma unroll
+            for (int j = 0; j < NL / 2; j++) y[a][j] = make_float2(0.f, 0.f);
+#pragma unroll
+        for (int i = 0; i < NL; i++) {
+            const float4 x = *reinterpret_cast<const float4 *>(col(i) + 4 * ch);
+            const float xs[4] = {x.x, x.y, x.z, x.w};
+#pragma unroll
+            for (int j = 0; j < NL / 2; j++) {
+                const float2 zz = *reinterpret_cast<const float2 *>(zs + i * ZP + 2 * j);
+#pragma unroll
+                for (int a = 0; a < 4; a++) y[a][j] = __ffma2_rn(make_float2(xs[a], xs[a]), zz, y[a][j]);
+            }
+        }
+#pragma unroll
+        for (int j = 0; j < NL / 2; j++) {
+            *reinterpret_cast<float4 *>(col(2 * j) + 4 * ch) = make_float4(y[0][j].x, y[1][j].x, y[2][j].x, y[3][j].x);
+            *reinterpret_cast<float4 *>(col(2 * j + 1) + 4 * ch) = make_float4(y[0][j].y, y[1][j].y, y[2][j].y, y[3][j].y);
+        }
+    }
+}
+
+constexpr int GR_THREADS = 256;   // 8 warps: up to 255 registers a thread for warp 0's register rounds
+template <int CLN, int BS>
+__global__ void __launch_bounds__(GR_THREADS, 1) jacobi_gramreg_kernel(const double *G, long long ldg, int n, int ldr,
+                                                               float tol, float stop_tol, int max_sweeps, float *Wout,
+                                                               float *Vout, long long ldo, int *sweeps_out, int *flag) {
+    namespace cg = cooperative_groups;
+    cg::cluster_group cluster = cg::this_cluster();
+    const int rank = (int)cluster.block_rank();
+    constexpr int NBLK = 2 * CLN;
+    constexpr int NL = 2 * BS;
+    constexpr int TK = (NL % 3 == 0) ? 3 : 2;                 // Gram output blocks TK x TK
+    constexpr int NT = NL / TK, NTP = NT * (NT + 1) / 2;
+    constexpr int KS0 = GR_THREADS / NTP, KS = (KS0 % 2 == 0) ? KS0 - 1 : KS0;   // row slices (odd: conflict-free reduction)
+    constexpr int bs = BS;
+    extern __shared__ __align__(16) unsigned char shraw[];
+    const size_t slot_elems = (size_t)bs * ldr * 2;          // W columns then V columns
+    float *buf = (float *)shraw;                              // [2 buffers][2 slots][slot_elems]
+    __shared__ int blk[2][2];
+    __shared__ int rot_count, sr_rot;
+    __shared__ int sweep_rot[CLN];
+    __shared__ __align__(8) unsigned long long inbar;
+    __shared__ unsigned int sweep_max;
+    __shared__ unsigned int cl_max[CLN];
+    __shared__ float gsm[NL][NL + 1];
+    __shared__ __align__(16) float zsm[NL][NL + 2];
+    __shared__ float red[KS * NTP * TK * TK];
+    __shared__ float rot_cs[2 * BS], rot_sn[2 * BS];          // a round's rotations, by round parity
+    __shared__ unsigned int rot_bal[2];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    auto slot_ptr = [&](float *base, int b, int sl) { return base + ((size_t)b * 2 + sl) * slot_elems; };
+
+    if (threadIdx.x == 0) {
+        blk[0][0] = rank;
+        blk[0][1] = NBLK - 1 - rank;
+        rot_count = 0;
+        sweep_max = 0u;
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&inbar)) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    for (int sl = 0; sl < 2; sl++) {
+        const int b = (sl == 0) ? rank : NBLK - 1 - rank;
+        float *sp = slot_ptr(buf, 0, sl);
+        for (long long e = threadIdx.x; e < (long long)bs * ldr; e += blockDim.x) {
+            const int j = (int)(e / ldr), r = (int)(e % ldr);
+            const int c = b * bs + j;
+            const bool ok = (c < n && r < n);
+            sp[(size_t)j * ldr + r] = ok ? (float)G[r + (long long)c * ldg] : 0.f;
+            sp[(size_t)(bs + j) * ldr + r] = (ok && r == c) ? 1.f : 0.f;
+        }
+    }
+    cluster.sync();
+    int cur = 0, sweep = 0;
+    uint32_t mphase = 0;
+    const int nch = ldr / 4;                 // 16-byte row chunks; rows n..ldr-1 are zero
+    const uint32_t slot_bytes = (uint32_t)(slot_elems * sizeof(float));
+    float wmax = 0.f;                        // warp 0's largest cos^2 and rotations in the sweep
+    int wrot = 0;
+    for (; sweep < max_sweeps; sweep++) {
+        for (int sr = 0; sr < NBLK - 1; sr++) {
+            float *s0 = slot_ptr(buf, cur, 0), *s1 = slot_ptr(buf, cur, 1);
+            const int b0 = blk[cur][0], b1 = blk[cur][1];
+            auto colw = [&](int c) { return (c < bs) ? s0 + (size_t)c * ldr : s1 + (size_t)(c - bs) * ldr; };
+            auto colv = [&](int c) { return (c < bs) ? s0 + (size_t)(bs + c) * ldr : s1 + (size_t)c * ldr; };
+            // ---- Gram: partial sums per (block, row slice)
+            if (threadIdx.x < KS * NTP) {
+                const int bk = threadIdx.x / KS, sl = threadIdx.x - bk * KS;
+                int bi = 0, rem = bk;
+                while (rem >= NT - bi) { rem -= NT - bi; bi++; }
+                const int bj = bi + rem;
+                float acc[TK][TK];
+#pragma unroll
+                for (int a = 0; a < TK; a++)
+#pragma unroll
+                    for (int c = 0; c < TK; c++) acc[a][c] = 0.f;
+                for (int ch = sl; ch < nch; ch += KS) {
+                    float4 x[TK], y[TK];
+#pragma unroll
+                    for (int a = 0; a < TK; a++) x[a] = *reinterpret_cast<const float4 *>(colw(bi * TK + a) + 4 * ch);
+#pragma unroll
+                    for (int c = 0; c < TK; c++)
+                        y[c] = (bi == bj) ? x[c] : *reinterpret_cast<const float4 *>(colw(bj * TK + c) + 4 * ch);
+#pragma unroll
+                    for (int a = 0; a < TK; a++)
+#pragma unroll
+                        for (int c = 0; c < TK; c++) {
+                            float v = acc[a][c];
+                            v = fmaf(x[a].x, y[c].x, v);
+                            v = fmaf(x[a].y, y[c].y, v);
+                            v = fmaf(x[a].z, y[c].z, v);
+                            v = fmaf(x[a].w, y[c].w, v);
+                            acc[a][c] = v;
+                        }
+                }
+#pragma unroll
+                for (int a = 0; a < TK; a++)
+#pragma unroll
+                    for (int c = 0; c < TK; c++) red[((bk * TK + a) * TK + c) * KS + sl] = acc[a][c];
+            }
+            if (threadIdx.x == 0) sr_rot = 0;
+            __syncthreads();
+            for (int v = threadIdx.x; v < NTP * TK * TK; v += blockDim.x) {
+                float sum = 0.f;
+#pragma unroll 4
+                for (int k = 0; k < KS; k++) sum += red[v * KS + k];
+                const int bk = v / (TK * TK), a = (v / TK) % TK, c = v % TK;
+                int bi = 0, rem = bk;
+                while (rem >= NT - bi) { rem -= NT - bi; bi++; }
+                const int i = bi * TK + a, j = (bi + rem) * TK + c;
+                gsm[i][j] = sum;
+                gsm[j][i] = sum;
+            }
+            __syncthreads();
+            // ---- rounds: Gl on warp 0, Z on warp 1
+            if (wid == 0) {
+                float g[NL];
+                float dg = 0.f;
+#pragma unroll
+                for (int k = 0; k < NL; k++) {
+                    g[k] = lane < NL ? gsm[lane][k] : 0.f;
+                    if (k == lane) dg = g[k];
+                }
+                bool any = false;
+                if (sr == 0) gr_rounds_g<BS, true>(g, dg, lane, b0, b1, n, tol, wmax, wrot, any, rot_cs, rot_sn, rot_bal);
+                else gr_rounds_g<BS, false>(g, dg, lane, b0, b1, n, tol, wmax, wrot, any, rot_cs, rot_sn, rot_bal);
+                if (lane == 0) sr_rot = any ? 1 : 0;
+            } else if (wid == 1) {
+                float z[NL];
+#pragma unroll
+                for (int k = 0; k < NL; k++) z[k] = (k == lane) ? 1.f : 0.f;
+                if (sr == 0) gr_rounds_z<BS, true>(z, rot_cs, rot_sn, rot_bal);
+                else gr_rounds_z<BS, false>(z, rot_cs, rot_sn, rot_bal);
+                if (lane < NL) {
+#pragma unroll
+                    for (int k = 0; k < NL; k++) zsm[lane][k] = z[k];
+                }
+            }
+            __syncthreads();
+            // ---- P <- P Z (W and V), one thread per 4-row chunk of one matrix
+            if (sr_rot) gr_apply<BS>(s0, s1, ldr, nch, &zsm[0][0]);
+            // ---- move blocks to their next holders (positions 1..NBLK-1 rotate by one)
+            const int nxt = cur ^ 1;
+            int dst0, dsl0, dst1, dsl1;
+            if (rank == 0) { dst0 = 0; dsl0 = 0; }
+            else if (rank < CLN - 1) { dst0 = rank + 1; dsl0 = 0; }
+            else { dst0 = CLN - 1; dsl0 = 1; }
+            if (rank == 0) { dst1 = 1; dsl1 = 0; }
+            else { dst1 = rank - 1; dsl1 = 1; }
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            __syncthreads();
+            if (threadIdx.x == 0) {
+                asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(&inbar)),
+                             "r"(2u * slot_bytes)
+                             : "memory");
+                for (int sl = 0; sl < 2; sl++) {
+                    const int dc = sl ? dst1 : dst0, ds = sl ? dsl1 : dsl0;
+                    uint32_t rdst, rbar;
+                    asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(rdst) : "r"(smem_addr(slot_ptr(buf, nxt, ds))), "r"(dc));
+                    asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(rbar) : "r"(smem_addr(&inbar)), "r"(dc));
+                    asm volatile(
+                        "cp.async.bulk.shared::cluster.shared::cta.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(rdst),
+                        "r"(smem_addr(slot_ptr(buf, cur, sl))), "r"(slot_bytes), "r"(rbar)
+                        : "memory");
+                    int *rb = cluster.map_shared_rank(&blk[nxt][ds], dc);
+                    *rb = sl ? b1 : b0;
+                }
+            }
+            {
+                uint32_t ok = 0;
+                const long long t0 = clock64();
+                while (true) {
+                    asm volatile(
+                        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+                        "selp.u32 %0, 1, 0, p;\n\t}\n"
+                        : "=r"(ok)
+                        : "r"(smem_addr(&inbar)), "r"(mphase)
+                        : "memory");
+                    if (ok) break;
+                    if (clock64() - t0 > (1ll << 31)) { atomicExch(flag, 1); break; }
+                }
+                mphase ^= 1u;
+            }
+            cluster.sync();
+            cur = nxt;
+        }
+        // ---- did any CTA rotate during this sweep, and how large was the largest cosine?
+        if (threadIdx.x == 0) {
+            sweep_max = __float_as_uint(wmax);
+            rot_count = wrot;
+        }
+        wmax = 0.f;
+        wrot = 0;
+        __syncthreads();
+        if (threadIdx.x < CLN) {
+            int *dstf = cluster.map_shared_rank(&sweep_rot[rank], (unsigned)threadIdx.x);
+            *dstf = rot_count;
+            unsigned int *dstm = cluster.map_shared_rank(&cl_max[rank], (unsigned)threadIdx.x);
+            *dstm = sweep_max;
+        }
+        cluster.sync();
+        int total = 0;
+        float cmax = 0.f;
+#pragma unroll
+        for (int c = 0; c < CLN; c++) {
+            total += sweep_rot[c];
+            cmax = fmaxf(cmax, __uint_as_float(cl_max[c]));
+        }
+        __syncthreads();
+        cluster.sync();
+        if (total == 0) break;
+        if (cmax < stop_tol) { sweep++; break; }
+    }
+    for (int sl = 0; sl < 2; sl++) {
+        float *sp = slot_ptr(buf, cur, sl);
+        const int b = blk[cur][sl];
+        for (long long e = threadIdx.x; e < (long long)bs * n; e += blockDim.x) {
+            const int j = (int)(e / n), r = (int)(e % n);
+            const int c = b * bs + j;
+            if (c < n) {
+                Wout[r + (long long)c * ldo] = sp[(size_t)j * ldr + r];
+                Vout[r + (long long)c * ldo] = sp[(size_t)(bs + j) * ldr + r];
+            }
+        }
+    }
+    if (rank == 0 && threadIdx.x == 0) {
+        *sweeps_out = sweep;
+        if (sweep >= max_sweeps) atomicExch(flag, 1);
+    }
+    cluster.sync();
+}
+
 template <typename S>
 __global__ void colnorm_kernel_t(const S *W, long long ldw, int n, double *sv) {
     const int lane = threadIdx.x & 31;
@@ -618,80 +1068,129 @@ __global__ void refine_update_kernel(const double *H, i64 ldh, const double *Sm,
     }
 }
 
-// Exact FP64 one-sided Jacobi rotations of the listed pairs, in a fixed order (key j n + i
-// ascending: column j, then i), by one CTA: for pair (i, j), a = |w_i|^2, b = |w_j|^2,
-// d = w_i . w_j over the current columns of W = X V, and (w_i, w_j), (v_i, v_j) rotated by the
-// angle that zeroes d (Rutishauser's formulas), so that W = X V still holds afterwards.  VW holds
-// V in rows [0, n) and W in rows [n, 2n); its double-float split (hi, lo) is rewritten for the
-// rotated columns.  The list (unordered, from refine_update_kernel) is sorted in shared memory
-// (bitonic sort); an empty list costs one read.
+// Exact FP64 one-sided Jacobi rotations of the listed pairs: for pair (i, j), a = |w_i|^2,
+// b = |w_j|^2, d = w_i . w_j over the current columns of W = X V, and (w_i, w_j), (v_i, v_j)
+// rotated by the angle that zeroes d (Rutishauser's formulas), so that W = X V still holds
+// afterwards.  VW holds V in rows [0, n) and W in rows [n, 2n); its double-float split (hi, lo)
+// is rewritten for the rotated columns.  The list (unordered, from refine_update_kernel) is
+// sorted (key j n + i ascending) and scheduled into batches of disjoint pairs by first fit in
+// that order -- batch(i, j) = 1 + max(batch of the last pair that touched i, ... touched j) --
+// so pairs that share a column keep their sorted order and the pairs of a batch are
+// independent.  A cluster of TIGHT_CL CTAs runs the batches one after another (a cluster
+// barrier between them), one CTA per pair: each rotation is FP64-pipe bound on its SM (~3000
+// FP64 operations), so spreading a batch over SMs is what shortens the step.  CTA 0 sorts and
+// schedules into `sched` (count, batch offsets, keys by batch); an empty list costs one read.
+// Orders above TIGHT_SMEM_N schedule one pair per batch.
 constexpr int REFINE_MAX_PAIRS = 2048;
-__global__ void __launch_bounds__(256) refine_tight_kernel(double *VW, i64 ld, float *hi, float *lo, i64 lds, int n,
-                                                           const int *pair_count, const int *pairs) {
+constexpr int TIGHT_CL = 8;
+constexpr int TIGHT_SMEM_N = 8192;
+__global__ void __cluster_dims__(TIGHT_CL, 1, 1) __launch_bounds__(256)
+    refine_tight_kernel(double *VW, i64 ld, float *hi, float *lo, i64 lds, int n, const int *pair_count,
+                        const int *pairs, int *sched) {
+    namespace cg = cooperative_groups;
+    cg::cluster_group cluster = cg::this_cluster();
+    const int crank = (int)cluster.block_rank();
     __shared__ int keys[REFINE_MAX_PAIRS];
+    __shared__ unsigned short bat[REFINE_MAX_PAIRS];
+    __shared__ int last[TIGHT_SMEM_N];
     __shared__ double red[3][8];
     __shared__ double rot[2];
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
     const int cnt = min(*pair_count, REFINE_MAX_PAIRS);
-    if (cnt == 0) return;
-    int np2 = 1;
-    while (np2 < cnt) np2 <<= 1;
-    for (int e = tid; e < np2; e += 256) keys[e] = e < cnt ? pairs[e] : INT_MAX;
-    __syncthreads();
-    for (int k = 2; k <= np2; k <<= 1)
-        for (int jj = k >> 1; jj > 0; jj >>= 1) {
-            for (int e = tid; e < np2; e += 256) {
-                const int o = e ^ jj;
-                if (o > e) {
-                    const bool up = (e & k) == 0;
-                    const int a = keys[e], b = keys[o];
-                    if ((a > b) == up) { keys[e] = b; keys[o] = a; }
+    if (cnt == 0) return;                                  // uniform over the cluster
+    int *nbat = sched, *off = sched + 1, *skey = sched + 2 + REFINE_MAX_PAIRS;
+    if (crank == 0) {
+        int np2 = 1;
+        while (np2 < cnt) np2 <<= 1;
+        for (int e = tid; e < np2; e += 256) keys[e] = e < cnt ? pairs[e] : INT_MAX;
+        for (int e = tid; e < n && e < TIGHT_SMEM_N; e += 256) last[e] = 0;
+        __syncthreads();
+        for (int k = 2; k <= np2; k <<= 1)
+            for (int jj = k >> 1; jj > 0; jj >>= 1) {
+                for (int e = tid; e < np2; e += 256) {
+                    const int o = e ^ jj;
+                    if (o > e) {
+                        const bool up = (e & k) == 0;
+                        const int a = keys[e], b = keys[o];
+                        if ((a > b) == up) { keys[e] = b; keys[o] = a; }
+                    }
                 }
+                __syncthreads();
+            }
+        if (tid == 0) {
+            // first-fit batches in sorted order, then a counting sort of the keys by batch
+            int nb = 0;
+            for (int q = 0; q < cnt; q++) {
+                int b;
+                if (n <= TIGHT_SMEM_N) {
+                    const int j = keys[q] / n, i = keys[q] - j * n;
+                    b = max(last[i], last[j]);
+                    last[i] = last[j] = b + 1;
+                } else {
+                    b = q;
+                }
+                bat[q] = (unsigned short)b;
+                nb = max(nb, b + 1);
+            }
+            *nbat = nb;
+            for (int b = 0; b <= nb; b++) off[b] = 0;
+            for (int q = 0; q < cnt; q++) off[bat[q] + 1]++;
+            for (int b = 0; b < nb; b++) off[b + 1] += off[b];
+            int *fill = last;                      // per-batch fill counters (nb <= cnt <= 2048)
+            for (int b = 0; b < nb; b++) fill[b] = 0;
+            for (int q = 0; q < cnt; q++) {        // stable: a batch keeps the sorted order
+                const int b = bat[q];
+                skey[off[b] + fill[b]++] = keys[q];
+            }
+        }
+    }
+    cluster.sync();
+    const int nb = *nbat;
+    for (int b = 0; b < nb; b++) {
+        for (int q = off[b] + crank; q < off[b + 1]; q += TIGHT_CL) {
+            const int key = skey[q];
+            const int j = key / n, p = key - j * n;
+            double a = 0.0, bb = 0.0, d = 0.0;
+            for (int r = n + tid; r < 2 * n; r += 256) {
+                const double x = VW[r + (i64)p * ld], y = VW[r + (i64)j * ld];
+                a = fma(x, x, a);
+                bb = fma(y, y, bb);
+                d = fma(x, y, d);
+            }
+            a = warp_sum(a);
+            bb = warp_sum(bb);
+            d = warp_sum(d);
+            if (lane == 0) { red[0][wid] = a; red[1][wid] = bb; red[2][wid] = d; }
+            __syncthreads();
+            if (tid == 0) {
+                double A = 0.0, B = 0.0, D = 0.0;
+                for (int w = 0; w < 8; w++) { A += red[0][w]; B += red[1][w]; D += red[2][w]; }
+                double cs = 1.0, sn = 0.0;
+                if (D != 0.0) {
+                    const double zeta = (B - A) / (2.0 * D);
+                    const double t = copysign(1.0, zeta) / (fabs(zeta) + sqrt(1.0 + zeta * zeta));
+                    cs = 1.0 / sqrt(1.0 + t * t);
+                    sn = cs * t;
+                }
+                rot[0] = cs;
+                rot[1] = sn;
+            }
+            __syncthreads();
+            const double cs = rot[0], sn = rot[1];
+            for (int r = tid; r < 2 * n; r += 256) {
+                const double x = VW[r + (i64)p * ld], y = VW[r + (i64)j * ld];
+                const double nx = cs * x - sn * y, ny = sn * x + cs * y;
+                VW[r + (i64)p * ld] = nx;
+                VW[r + (i64)j * ld] = ny;
+                const float hx = __double2float_rn(nx), hy = __double2float_rn(ny);
+                hi[r + p * lds] = hx;
+                lo[r + p * lds] = __double2float_rn(nx - (double)hx);
+                hi[r + j * lds] = hy;
+                lo[r + j * lds] = __double2float_rn(ny - (double)hy);
             }
             __syncthreads();
         }
-    for (int q = 0; q < cnt; q++) {
-        const int key = keys[q];
-        const int j = key / n, p = key - j * n;
-        double a = 0.0, b = 0.0, d = 0.0;
-        for (int r = n + tid; r < 2 * n; r += 256) {
-            const double x = VW[r + (i64)p * ld], y = VW[r + (i64)j * ld];
-            a = fma(x, x, a);
-            b = fma(y, y, b);
-            d = fma(x, y, d);
-        }
-        a = warp_sum(a);
-        b = warp_sum(b);
-        d = warp_sum(d);
-        if (lane == 0) { red[0][wid] = a; red[1][wid] = b; red[2][wid] = d; }
-        __syncthreads();
-        if (tid == 0) {
-            double A = 0.0, B = 0.0, D = 0.0;
-            for (int w = 0; w < 8; w++) { A += red[0][w]; B += red[1][w]; D += red[2][w]; }
-            double cs = 1.0, sn = 0.0;
-            if (D != 0.0) {
-                const double zeta = (B - A) / (2.0 * D);
-                const double t = copysign(1.0, zeta) / (fabs(zeta) + sqrt(1.0 + zeta * zeta));
-                cs = 1.0 / sqrt(1.0 + t * t);
-                sn = cs * t;
-            }
-            rot[0] = cs;
-            rot[1] = sn;
-        }
-        __syncthreads();
-        const double cs = rot[0], sn = rot[1];
-        for (int r = tid; r < 2 * n; r += 256) {
-            const double x = VW[r + (i64)p * ld], y = VW[r + (i64)j * ld];
-            const double nx = cs * x - sn * y, ny = sn * x + cs * y;
-            VW[r + (i64)p * ld] = nx;
-            VW[r + (i64)j * ld] = ny;
-            const float hx = __double2float_rn(nx), hy = __double2float_rn(ny);
-            hi[r + p * lds] = hx;
-            lo[r + p * lds] = __double2float_rn(nx - (double)hx);
-            hi[r + j * lds] = hy;
-            lo[r + j * lds] = __double2float_rn(ny - (double)hy);
-        }
-        __syncthreads();
+        cluster.sync();
     }
 }
 
@@ -803,7 +1302,12 @@ int jacobi_small(cudaStream_t s, DM<double> G, DM<double> U, DM<double> V, doubl
         if (bs > 32 || 2 * bs > 64) continue;
         const size_t bsmem = sizeof(S) * (size_t)4 * bs * ldr * 2;
         if (bsmem > 200 * 1024) continue;
-        auto kern = (cl == 16) ? jacobi_block_cluster_kernel<S, 16> : jacobi_block_cluster_kernel<S, 8>;
+        // FP32 at the block widths of the common orders (l in (256, 288] on 16 CTAs, l in
+        // (96, 112] on 8): the register-resident Gram form
+        const bool greg = sizeof(S) == 4 && ((cl == 16 && bs == 9) || (cl == 8 && bs == 7));
+        const void *kern = (cl == 16) ? (const void *)jacobi_block_cluster_kernel<S, 16>
+                                      : (const void *)jacobi_block_cluster_kernel<S, 8>;
+        if (greg) kern = (cl == 16) ? (const void *)jacobi_gramreg_kernel<16, 9> : (const void *)jacobi_gramreg_kernel<8, 7>;
         if (cl == 16 && cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess) {
             cudaGetLastError();
             continue;
@@ -811,19 +1315,31 @@ int jacobi_small(cudaStream_t s, DM<double> G, DM<double> U, DM<double> V, doubl
         RSVD_CK(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bsmem));
         cudaLaunchConfig_t cfg = {};
         cfg.gridDim = dim3(cl);
-        cfg.blockDim = dim3(32 * std::min(bs, 16));
+        cfg.blockDim = dim3(greg ? GR_THREADS : 32 * std::min(bs, 16));
         cfg.dynamicSmemBytes = bsmem;
         cfg.stream = s;
         cattr[0].val.clusterDim.x = cl;
         cfg.attrs = cattr;
         cfg.numAttrs = 1;
         int nclusters = 0;
-        if (cudaOccupancyMaxActiveClusters(&nclusters, (void *)kern, &cfg) != cudaSuccess || nclusters < 1) {
+        if (cudaOccupancyMaxActiveClusters(&nclusters, kern, &cfg) != cudaSuccess || nclusters < 1) {
             cudaGetLastError();
             continue;
         }
-        RSVD_CK(cudaLaunchKernelEx(&cfg, kern, (const double *)G.p, (long long)G.ld, n, bs, ldr, tol, (S)(tol / 10), 40,
-                                   W, Vacc, (long long)ld, d_sweeps, d_flag));
+        if (greg) {
+            if constexpr (sizeof(S) == 4) {
+                auto gk = (cl == 16) ? jacobi_gramreg_kernel<16, 9> : jacobi_gramreg_kernel<8, 7>;
+                RSVD_CK(cudaLaunchKernelEx(&cfg, gk, (const double *)G.p, (long long)G.ld, n, ldr, (float)tol,
+                                           (float)(tol / 10), 40, (float *)W, (float *)Vacc, (long long)ld, d_sweeps,
+                                           d_flag));
+            }
+        } else if (cl == 16) {
+            RSVD_CK(cudaLaunchKernelEx(&cfg, jacobi_block_cluster_kernel<S, 16>, (const double *)G.p, (long long)G.ld, n,
+                                       bs, ldr, tol, (S)(tol / 10), 40, W, Vacc, (long long)ld, d_sweeps, d_flag));
+        } else {
+            RSVD_CK(cudaLaunchKernelEx(&cfg, jacobi_block_cluster_kernel<S, 8>, (const double *)G.p, (long long)G.ld, n,
+                                       bs, ldr, tol, (S)(tol / 10), 40, W, Vacc, (long long)ld, d_sweeps, d_flag));
+        }
         launched = true;
         variant = cl;
     }
@@ -881,9 +1397,10 @@ void svd_refine(cudaStream_t s, DM<double> X, DM<double> V, DM<double> U, double
     const int n = (int)X.r;
     if (X.r != X.c || V.r != n || V.c != n || U.r != n || U.c != n) fail(RSVD_ERR_ARGUMENT, "svd_refine: shapes");
     if (n == 0) return;
-    DBuf xe_b(sizeof(int) * (1 + steps), s), pair_b(sizeof(int) * REFINE_MAX_PAIRS, s);
+    DBuf xe_b(sizeof(int) * (1 + steps), s), pair_b(sizeof(int) * REFINE_MAX_PAIRS, s),
+        sched_b(sizeof(int) * (2 + 2 * (size_t)REFINE_MAX_PAIRS), s);
     int *xexp = (int *)xe_b.get(), *pair_count = xexp + 1;      // one pair counter per step
-    int *pairs = (int *)pair_b.get();
+    int *pairs = (int *)pair_b.get(), *sched = (int *)sched_b.get();
     RSVD_CK(cudaMemsetAsync(pair_count, 0, sizeof(int) * steps, s));
     Df64Split Xs(s, X);
     take_scale_kernel<<<1, 1, 0, s>>>(Xs.exp, xexp);
@@ -911,9 +1428,10 @@ void svd_refine(cudaStream_t s, DM<double> X, DM<double> V, DM<double> U, double
         const Df64View VWv{ch, cl, 2 * (i64)n, n, ldvw, unit};
         const Df64View Vv = VWv.rows(0, n), Wv = VWv.rows(n, n);
         df64_gram_pair(s, Wv, H.v, Vv, Sm.v);                                   // H = W^T W, Sm = V^T V
-        // the last step also settles pairs still coupled beyond 1e-4 by exact rotations, so that
-        // the columns of W come out orthogonal to ~1e-12 even for nearly equal singular values
-        const double tight = (it == steps - 1) ? 1e-4 : 0.005;
+        // the last step also settles pairs still coupled beyond 2e-5 by exact rotations, so that
+        // the first-order step leaves nearly equal singular values' vectors orthogonal to
+        // ~(2e-5)^2 whatever the FP32 Jacobi's last sweep left
+        const double tight = (it == steps - 1) ? 2e-5 : 0.005;
         refine_update_kernel<<<gfor((long long)n * n), 256, 0, s>>>(H.v.p, H.v.ld, Sm.v.p, Sm.v.ld, n, tight, hm, lm,
                                                                      pad_ld(n), pair_count + it, pairs,
                                                                      REFINE_MAX_PAIRS);
@@ -921,7 +1439,7 @@ void svd_refine(cudaStream_t s, DM<double> X, DM<double> V, DM<double> U, double
         const Df64View Mv{hm, lm, n, n, pad_ld(n), unit};
         const Df64Out no{nh, nl, ldvw};
         df64_gemm(s, false, false, 1.0, VWv, Mv, 0.0, nxt, &no);                  // [V; W] (I + C)
-        refine_tight_kernel<<<1, 256, 0, s>>>(nxt.p, nxt.ld, nh, nl, ldvw, n, pair_count + it, pairs);
+        refine_tight_kernel<<<TIGHT_CL, 256, 0, s>>>(nxt.p, nxt.ld, nh, nl, ldvw, n, pair_count + it, pairs, sched);
         RSVD_LAUNCH_CK();
         std::swap(cur, nxt);
         std::swap(ch, nh);
