@@ -138,37 +138,74 @@ __device__ __forceinline__ void tile_nn(const S *P, const S *Q, int k0, int k1, 
 // Factor the upper 32 x 32 tile D (row-major, pitch TP) in place, D = R^T R, and write
 // R^-1 (upper) into Di.  One warp.  diag0: the original diagonal of the whole matrix at
 // this tile (relative breakdown test d_j > rel_tol * diag0_j).  Returns false on breakdown.
+// Lane t keeps column t of the tile in registers.  Step j: lane j's pivot and its reciprocal
+// square root were formed at the end of step j - 1, so the step's critical path is one
+// broadcast, the scaling of row j, and lane j+1 forming the next pivot from its own values
+// (c[j+1] - R(j, j+1)^2); the trailing updates c[i] -= R(j, i) R(j, t) read row j of R through
+// shared memory with 16-byte broadcast loads (a shuffle per entry made the 528 broadcasts the
+// bulk of the instructions).  FP32: reciprocal square root by the hardware estimate and one
+// Newton step (R's diagonal to ~1 ulp).
+template <typename S>
+__device__ __forceinline__ S chol_rsqrt(S d) {
+    if constexpr (sizeof(S) == 4) {
+        const float r = rsqrtf(d);
+        return r * fmaf(-0.5f * d, r * r, 1.5f);
+    } else {
+        return 1.0 / sqrt(d);
+    }
+}
 template <typename S>
 __device__ __noinline__ bool factor_diag_warp(S *D, S *Di, const S *diag0, S rel_tol) {
     const int lane = threadIdx.x & 31;
-    // lane t keeps column t of the tile in registers; row j of R is broadcast by shuffles
     S c[32];
 #pragma unroll
     for (int i = 0; i < 32; i++) c[i] = (i <= lane) ? D[i * TP + lane] : S(0);
+    const S thr = rel_tol * diag0[lane];                // this lane's column: breakdown threshold
     bool bad = false;
     S own_inv = S(1);                                   // 1 / R(lane, lane)
+    // pivot of step 0 (meaningful on lane 0)
+    bool okn = (c[0] > S(0)) && isfinite(c[0]) && (c[0] > thr);
+    S invn = okn ? chol_rsqrt<S>(c[0]) : S(1);
 #pragma unroll
     for (int j = 0; j < 32; j++) {
-        const S d = __shfl_sync(FULL, c[j], j);
-        const bool ok = (d > S(0)) && isfinite(d) && (d > rel_tol * diag0[j]);
+        const S inv = __shfl_sync(FULL, invn, j);
+        const bool ok = __shfl_sync(FULL, okn ? 1 : 0, j) != 0;
         bad |= !ok;
-        S p, inv;
-        if constexpr (sizeof(S) == 4) {
-            // FP32: one correctly rounded rsqrt instead of the square-root and division
-            // sequences on this one-warp critical path; sqrt(d) = d * rsqrt(d) (1 ulp)
-            inv = ok ? __frsqrt_rn(d) : S(1);
-            p = ok ? d * inv : S(1);
-        } else {
-            p = ok ? sqrt(d) : S(1);
-            inv = S(1) / p;
+        if (lane == j) {
+            if constexpr (sizeof(S) == 4) c[j] = ok ? c[j] * inv : S(1);      // sqrt(d) = d rsqrt(d)
+            else c[j] = ok ? sqrt(c[j]) : S(1);
+            own_inv = inv;
+        } else if (lane > j) {
+            c[j] *= inv;                                // lane t now holds R(j, t)
         }
-        if (lane == j) { c[j] = p; own_inv = inv; }
-        else if (lane > j) c[j] *= inv;                 // lane t now holds R(j, t)
+        if (j + 1 < 32) {
+            // next pivot, on lane j+1: c[j+1] - R(j, j+1)^2, R(j, j+1) being its own c[j]
+            const S pn = c[j + 1] - c[j] * c[j];
+            okn = (pn > S(0)) && isfinite(pn) && (pn > thr);
+            invn = okn ? chol_rsqrt<S>(pn) : S(1);
+        }
+        // row j of R to every lane through shared memory (Di is scratch until the inverse is
+        // written): one store a lane, then 16-byte broadcast reads
+        if (lane > j) Di[lane] = c[j];
+        __syncwarp();
+        constexpr int VW = 16 / sizeof(S);
 #pragma unroll
-        for (int i = j + 1; i < 32; i++) {
-            const S rji = __shfl_sync(FULL, c[j], i);   // R(j, i) from lane i
-            if (lane >= i) c[i] -= rji * c[j];
+        for (int q = (j + 1) / VW; q < 32 / VW; q++) {
+            S r[VW];
+            if constexpr (sizeof(S) == 4) {
+                const float4 v = *reinterpret_cast<const float4 *>(Di + q * VW);
+                r[0] = v.x; r[1] = v.y; r[2] = v.z; r[3] = v.w;
+            } else {
+                const double2 v = *reinterpret_cast<const double2 *>(Di + q * VW);
+                r[0] = v.x; r[1] = v.y;
+            }
+#pragma unroll
+            for (int e = 0; e < VW; e++) {
+                const int i = q * VW + e;
+                if (i > j && lane >= i) c[i] -= r[e] * c[j];     // R(j, i) R(j, lane)
+            }
         }
+        __syncwarp();
     }
     __syncwarp();
 #pragma unroll
@@ -703,6 +740,119 @@ __global__ void __launch_bounds__(TRSM_THREADS) trsm_slab_kernel(const T *Y, lon
 template <typename S>
 constexpr int smem_nb_max() { return sizeof(S) == 4 ? 9 : 6; }
 
+// FP32 slab solve Q R = Y on the tensor cores (mma.sync m16n8k8, 3xTF32: hi x hi + hi x lo +
+// lo x hi, each operand split into a TF32 high part and the TF32 rounding of the remainder,
+// so products carry ~FP32 accuracy).  One CTA per 128-row slab, warp w owns rows
+// [16 w, 16 w + 16) of it.  Block column J: P = Q_{<J} R_{<J,J} (A fragments from the warp's
+// rows of the slab's Q, kept in shared memory row-major, pitch QP; B fragments from R's block
+// column J, staged once per J for all warps), T = Y_J - P, then Q_J = T R_JJ^-1 (T staged
+// through the warp's own rows of the slab).  Only the staging of R's block column needs block
+// barriers; a warp's rows depend on nothing but its own earlier columns.  R comes as the packed
+// FP32 upper tiles chol_tiles_f32_kernel leaves, R_JJ^-1 from its dinv (identity-padded
+// beyond n, so padded columns solve to zero).  Shared memory: 128 x QP (Q) + 256 x RPB (R block
+// column) + 32 x RPB (R_JJ^-1) floats; the pitches make every fragment load conflict-free
+// (QP = 4 mod 32 for A, RPB = 8 mod 32 for B).
+__device__ __forceinline__ uint32_t tf32_hi(float x) {
+    uint32_t h;
+    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(h) : "f"(x));
+    return h;
+}
+__device__ __forceinline__ void tf32_split(float x, uint32_t &h, uint32_t &l) {
+    h = tf32_hi(x);
+    l = tf32_hi(x - __uint_as_float(h));
+}
+__device__ __forceinline__ void mma_tf32(float (&d)[4], const uint32_t (&a)[4], uint32_t b0, uint32_t b1) {
+    asm volatile("mma.sync.aligned.m16n8k8.row.col.f32.tf32.tf32.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+                 "{%0,%1,%2,%3};\n"
+                 : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+                 : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+// acc (16 x 32: four 16 x 8 tiles) += A (the warp's 16 rows, columns [k0, k1) of As, pitch ap)
+//                                     x B (rows [k0, k1) of Bs, 32 columns, pitch bp)
+__device__ __forceinline__ void mma3_rows(float (&acc)[4][4], const float *As, int ap, const float *Bs, int bp, int k0,
+                                          int k1) {
+    const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+    for (int k = k0; k < k1; k += 8) {
+        uint32_t ah[4], al[4];
+        tf32_split(As[g * ap + k + t], ah[0], al[0]);
+        tf32_split(As[(g + 8) * ap + k + t], ah[1], al[1]);
+        tf32_split(As[g * ap + k + t + 4], ah[2], al[2]);
+        tf32_split(As[(g + 8) * ap + k + t + 4], ah[3], al[3]);
+#pragma unroll
+        for (int nt = 0; nt < 4; nt++) {
+            uint32_t bh0, bl0, bh1, bl1;
+            tf32_split(Bs[(k + t) * bp + nt * 8 + g], bh0, bl0);
+            tf32_split(Bs[(k + t + 4) * bp + nt * 8 + g], bh1, bl1);
+            mma_tf32(acc[nt], al, bh0, bh1);
+            mma_tf32(acc[nt], ah, bl0, bl1);
+            mma_tf32(acc[nt], ah, bh0, bh1);
+        }
+    }
+}
+constexpr int TRSM_MMA_BM = 128, RPB = 40;
+__global__ void __launch_bounds__(256) trsm_mma_kernel(const float *Y, long long ldy, const float *Rt, const float *dinv,
+                                                      float *Q, long long ldq, long long m, int n, int nb) {
+    extern __shared__ __align__(16) unsigned char shraw[];
+    const int QP = nb * TB + 4;                       // row pitch of the slab's Q (conflict-free fragments)
+    float *Qs = (float *)shraw;                       // 128 x QP
+    float *Rc = Qs + (size_t)TRSM_MMA_BM * QP;        // (nb - 1) * 32 x RPB: rows [0, 32 J) of block column J
+    float *Dv = Rc + (size_t)(nb - 1) * TB * RPB;     // 32 x RPB: R_JJ^-1
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, g = lane >> 2, t = lane & 3;
+    const long long row0 = (long long)blockIdx.x * TRSM_MMA_BM + wid * 16;
+    float *Qw = Qs + (size_t)wid * 16 * QP;           // this warp's 16 rows
+    constexpr int CPR = TB / 4;                       // 16-byte chunks per tile row
+    for (int J = 0; J < nb; J++) {
+        const int kr = J * TB;
+        __syncthreads();                              // every warp is done with the previous R block column
+        for (int e = threadIdx.x; e < kr * CPR; e += blockDim.x) {
+            const int I = e / (TB * CPR), r = (e / CPR) % TB, q = e % CPR;
+            cp_async16(Rc + (I * TB + r) * RPB + q * 4, Rt + (size_t)tix(I, J) * TB * TB + r * TB + q * 4);
+        }
+        for (int e = threadIdx.x; e < TB * CPR; e += blockDim.x) {
+            const int r = e / CPR, q = e % CPR;
+            cp_async16(Dv + r * RPB + q * 4, dinv + (size_t)J * TB * TB + r * TB + q * 4);
+        }
+        cp_async_wait_all();
+        __syncthreads();
+        float acc[4][4];
+#pragma unroll
+        for (int nt = 0; nt < 4; nt++)
+#pragma unroll
+            for (int e = 0; e < 4; e++) acc[nt][e] = 0.f;
+        if (kr > 0) mma3_rows(acc, Qw, QP, Rc, RPB, 0, kr);
+        // T = Y_J - P, staged into the warp's rows of column block J
+#pragma unroll
+        for (int nt = 0; nt < 4; nt++)
+#pragma unroll
+            for (int e = 0; e < 4; e++) {
+                const int r = g + (e >> 1) * 8, c = nt * 8 + 2 * t + (e & 1);
+                const long long gr = row0 + r;
+                const int gc = kr + c;
+                const float y = (gr < m && gc < n) ? Y[gr + (long long)gc * ldy] : 0.f;
+                Qw[r * QP + kr + c] = y - acc[nt][e];
+            }
+        __syncwarp();
+        float o[4][4];
+#pragma unroll
+        for (int nt = 0; nt < 4; nt++)
+#pragma unroll
+            for (int e = 0; e < 4; e++) o[nt][e] = 0.f;
+        mma3_rows(o, Qw + kr, QP, Dv, RPB, 0, TB);
+        __syncwarp();
+#pragma unroll
+        for (int nt = 0; nt < 4; nt++)
+#pragma unroll
+            for (int e = 0; e < 4; e++) {
+                const int r = g + (e >> 1) * 8, c = nt * 8 + 2 * t + (e & 1);
+                Qw[r * QP + kr + c] = o[nt][e];
+                const long long gr = row0 + r;
+                const int gc = kr + c;
+                if (gr < m && gc < n) Q[gr + (long long)gc * ldq] = o[nt][e];
+            }
+        __syncwarp();
+    }
+}
+
 template <typename T>
 constexpr int trsm_bm() { return 128; }
 
@@ -826,12 +976,12 @@ void trsm_right_tiles_f32(cudaStream_t s, DM<float> Y, int n, const float *Rt, c
     if (n == 0 || Y.r == 0) return;
     const int nb = (n + TB - 1) / TB;
     if (nb > 9) fail(RSVD_ERR_ARGUMENT, "trsm_right_tiles_f32: order above 288");
-    const size_t smem = trsm_smem<float>(nb);
-    constexpr int BM = trsm_bm<float>();
-    auto k = trsm_slab_kernel<float, float, BM>;
-    RSVD_CK(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    const long long slabs = (Y.r + BM - 1) / BM;
-    k<<<(unsigned)slabs, TRSM_THREADS, smem, s>>>(Y.p, Y.ld, nullptr, 0, Rt, dinv, Q.p, Q.ld, Y.r, n, nb);
+    // tensor cores (3xTF32 mma.sync, one warp per 16 rows)
+    const size_t smem = sizeof(float) * ((size_t)TRSM_MMA_BM * (nb * TB + 4) + (size_t)(std::max(nb - 1, 1)) * TB * RPB +
+                                         (size_t)TB * RPB);
+    RSVD_CK(cudaFuncSetAttribute(trsm_mma_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    const long long slabs = (Y.r + TRSM_MMA_BM - 1) / TRSM_MMA_BM;
+    trsm_mma_kernel<<<(unsigned)slabs, 256, smem, s>>>(Y.p, Y.ld, Rt, dinv, Q.p, Q.ld, Y.r, n, nb);
     RSVD_LAUNCH_CK();
     ctx().launches++;
 }
