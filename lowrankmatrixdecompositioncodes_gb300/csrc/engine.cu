@@ -232,8 +232,17 @@ namespace {
 // working precision, or for FP64 data the FP64X mode's double-float product.
 template <typename T>
 void gemm_w(cudaStream_t s, bool ta, bool tb, T alpha, DM<T> A, DM<T> B, T beta, DM<T> C) {
-    if constexpr (std::is_same<T, double>::value) prod_f64(s, ta, tb, alpha, A, B, beta, C);
-    else gemm<T>(s, ta, tb, alpha, A, B, beta, C);
+    if constexpr (std::is_same<T, double>::value) {
+        prod_f64(s, ta, tb, alpha, A, B, beta, C);
+    } else {
+        // tensor-core modes: plain products on the tensor cores in 3xTF32 (FP32-accurate)
+        const int prec = ctx().opts.precision;
+        if ((prec == RSVD_PREC_TF32 || prec == RSVD_PREC_BF16) && !ta && !tb && alpha == T(1) && beta == T(0) &&
+            A.r >= 256)
+            gemm_nn_3xtf32(s, A, B, C);
+        else
+            gemm<T>(s, ta, tb, alpha, A, B, beta, C);
+    }
 }
 }  // namespace
 

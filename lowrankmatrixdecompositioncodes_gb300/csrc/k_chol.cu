@@ -853,6 +853,105 @@ __global__ void __launch_bounds__(256) trsm_mma_kernel(const float *Y, long long
     }
 }
 
+// C (M x N) = A (M x K) B (K x N), FP32, all column-major, on the tensor cores in 3xTF32
+// (mma.sync m16n8k8): the factor formation U = Q Vk, V = Qh Uk of the mixed modes (K = l),
+// kept at FP32 accuracy without the CUDA-core rate.  CTA tile 128 x 64, K in chunks of 32,
+// both operands split once per chunk into TF32 high and low parts in shared memory (A as
+// [row][k] with pitch 36 and B as [k][col] with pitch 72: conflict-free fragment loads); the
+// next chunk's global loads are issued before the current chunk's products.  8 warps in a
+// 4 x 2 grid of 32 x 32 warp tiles.
+constexpr int G3_BM = 128, G3_BN = 64, G3_BK = 32, G3_AP = G3_BK + 4, G3_BP = G3_BN + 8;
+__global__ void __launch_bounds__(256) gemm_nn_3xtf32_kernel(const float *A, long long lda, const float *B,
+                                                            long long ldb, float *C, long long ldc, int M, int N,
+                                                            int K) {
+    extern __shared__ __align__(16) unsigned char shraw[];
+    uint32_t *Ah = (uint32_t *)shraw, *Al = Ah + G3_BM * G3_AP;
+    uint32_t *Bh = Al + G3_BM * G3_AP, *Bl = Bh + G3_BK * G3_BP;
+    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5, g = lane >> 2, t = lane & 3;
+    const long long row0 = (long long)blockIdx.x * G3_BM;
+    const int col0 = blockIdx.y * G3_BN;
+    const int wm = (wid & 3) * 32, wn = (wid >> 2) * 32;
+    // global -> register mapping: A rows tid % 128, k = tid / 128 + 2 i; B k = tid % 32, cols tid / 32 + 8 i
+    const int ar = tid & 127, ak = tid >> 7, bk = tid & 31, bc = tid >> 5;
+    const bool arow_ok = row0 + ar < M;
+    float ra[16], rb[8];
+    auto load = [&](int k0) {
+#pragma unroll
+        for (int i = 0; i < 16; i++) {
+            const int k = k0 + ak + 2 * i;
+            ra[i] = (arow_ok && k < K) ? A[row0 + ar + (long long)k * lda] : 0.f;
+        }
+#pragma unroll
+        for (int i = 0; i < 8; i++) {
+            const int c = col0 + bc + 8 * i, k = k0 + bk;
+            rb[i] = (c < N && k < K) ? B[k + (long long)c * ldb] : 0.f;
+        }
+    };
+    float acc[2][4][4];
+#pragma unroll
+    for (int a = 0; a < 2; a++)
+#pragma unroll
+        for (int b = 0; b < 4; b++)
+#pragma unroll
+            for (int e = 0; e < 4; e++) acc[a][b][e] = 0.f;
+    load(0);
+    for (int k0 = 0; k0 < K; k0 += G3_BK) {
+        __syncthreads();                                  // the previous chunk's fragments are read
+#pragma unroll
+        for (int i = 0; i < 16; i++) {
+            uint32_t h, l;
+            tf32_split(ra[i], h, l);
+            Ah[ar * G3_AP + ak + 2 * i] = h;
+            Al[ar * G3_AP + ak + 2 * i] = l;
+        }
+#pragma unroll
+        for (int i = 0; i < 8; i++) {
+            uint32_t h, l;
+            tf32_split(rb[i], h, l);
+            Bh[bk * G3_BP + bc + 8 * i] = h;
+            Bl[bk * G3_BP + bc + 8 * i] = l;
+        }
+        __syncthreads();
+        if (k0 + G3_BK < K) load(k0 + G3_BK);
+#pragma unroll
+        for (int kk = 0; kk < G3_BK; kk += 8) {
+            uint32_t ah[2][4], al[2][4], bh[4][2], bl[4][2];
+#pragma unroll
+            for (int a = 0; a < 2; a++) {
+                const int r = wm + a * 16 + g;
+                ah[a][0] = Ah[r * G3_AP + kk + t];           al[a][0] = Al[r * G3_AP + kk + t];
+                ah[a][1] = Ah[(r + 8) * G3_AP + kk + t];     al[a][1] = Al[(r + 8) * G3_AP + kk + t];
+                ah[a][2] = Ah[r * G3_AP + kk + t + 4];       al[a][2] = Al[r * G3_AP + kk + t + 4];
+                ah[a][3] = Ah[(r + 8) * G3_AP + kk + t + 4]; al[a][3] = Al[(r + 8) * G3_AP + kk + t + 4];
+            }
+#pragma unroll
+            for (int b = 0; b < 4; b++) {
+                const int c = wn + b * 8 + g;
+                bh[b][0] = Bh[(kk + t) * G3_BP + c];     bl[b][0] = Bl[(kk + t) * G3_BP + c];
+                bh[b][1] = Bh[(kk + t + 4) * G3_BP + c]; bl[b][1] = Bl[(kk + t + 4) * G3_BP + c];
+            }
+#pragma unroll
+            for (int a = 0; a < 2; a++)
+#pragma unroll
+                for (int b = 0; b < 4; b++) {
+                    mma_tf32(acc[a][b], al[a], bh[b][0], bh[b][1]);
+                    mma_tf32(acc[a][b], ah[a], bl[b][0], bl[b][1]);
+                    mma_tf32(acc[a][b], ah[a], bh[b][0], bh[b][1]);
+                }
+        }
+    }
+#pragma unroll
+    for (int a = 0; a < 2; a++)
+#pragma unroll
+        for (int b = 0; b < 4; b++)
+#pragma unroll
+            for (int e = 0; e < 4; e++) {
+                const long long r = row0 + wm + a * 16 + g + (e >> 1) * 8;
+                const int c = col0 + wn + b * 8 + 2 * t + (e & 1);
+                if (r < M && c < N) C[r + (long long)c * ldc] = acc[a][b][e];
+            }
+}
+
 template <typename T>
 constexpr int trsm_bm() { return 128; }
 
@@ -982,6 +1081,19 @@ void trsm_right_tiles_f32(cudaStream_t s, DM<float> Y, int n, const float *Rt, c
     RSVD_CK(cudaFuncSetAttribute(trsm_mma_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     const long long slabs = (Y.r + TRSM_MMA_BM - 1) / TRSM_MMA_BM;
     trsm_mma_kernel<<<(unsigned)slabs, 256, smem, s>>>(Y.p, Y.ld, Rt, dinv, Q.p, Q.ld, Y.r, n, nb);
+    RSVD_LAUNCH_CK();
+    ctx().launches++;
+}
+
+// C = A B (FP32, column-major) by 3xTF32 on the tensor cores (gemm_nn_3xtf32_kernel).
+void gemm_nn_3xtf32(cudaStream_t s, DM<float> A, DM<float> B, DM<float> C) {
+    const int M = (int)A.r, K = (int)A.c, N = (int)B.c;
+    if (B.r != K || C.r != M || C.c != N) fail(RSVD_ERR_ARGUMENT, "gemm_nn_3xtf32: shapes");
+    if (M == 0 || N == 0) return;
+    const size_t smem = sizeof(uint32_t) * 2 * ((size_t)G3_BM * G3_AP + (size_t)G3_BK * G3_BP);
+    RSVD_CK(cudaFuncSetAttribute(gemm_nn_3xtf32_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    const dim3 grid((unsigned)((M + G3_BM - 1) / G3_BM), (unsigned)((N + G3_BN - 1) / G3_BN));
+    gemm_nn_3xtf32_kernel<<<grid, 256, smem, s>>>(A.p, A.ld, B.p, B.ld, C.p, C.ld, M, N, K);
     RSVD_LAUNCH_CK();
     ctx().launches++;
 }
