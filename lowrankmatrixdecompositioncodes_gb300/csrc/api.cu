@@ -1450,7 +1450,7 @@ int rsvdpack_dev_small_svd(double *dG, int n, long long ldg, double *dU, long lo
         if (fp32 == 2) {
             // the mixed modes' l x l SVD: FP32 Jacobi, then the FP64-accurate refinement
             sweeps = jacobi_small<float>(st, G, U, V, dS, flag);
-            svd_refine(st, G, V, U, dS, 4);
+            svd_refine(st, G, V, U, dS, REFINE_STEPS);
         } else {
             sweeps = fp32 ? jacobi_small<float>(st, G, U, V, dS, flag) : jacobi_small<double>(st, G, U, V, dS, flag);
         }

@@ -1388,9 +1388,9 @@ template int jacobi_small<float>(cudaStream_t, DM<double>, DM<double>, DM<double
 // correction [V; W] <- [V; W] (I + C) for every pair of well-separated singular values (W = X V
 // is carried along instead of recomputed), and exact FP64 rotations of the flagged
 // nearly-equal pairs (refine_tight_kernel).  From the FP32 Jacobi's converged vectors four steps
-// bring the singular values to ~1e-15 relative (a step roughly squares the error of the separated
-// pairs; nearly-equal pairs, which FP32 cannot separate, are settled by the rotations in the first
-// steps).  X is scaled once by a power of two (its largest entry into [1, 2)), so that every
+// (REFINE_STEPS) bring the singular values to ~1e-15 relative (a step roughly squares the error of
+// the separated pairs; nearly-equal pairs, which FP32 cannot separate, are settled by the
+// rotations in the first steps).  X is scaled once by a power of two (its largest entry into [1, 2)), so that every
 // operand has entries of order one and is split without a scale; the products write the split of
 // their result for the next product.
 void svd_refine(cudaStream_t s, DM<double> X, DM<double> V, DM<double> U, double *d_sv, int steps) {
@@ -1468,7 +1468,7 @@ void svd_refine(cudaStream_t s, DM<double> X, DM<double> V, DM<double> U, double
 void small_svd_refined(cudaStream_t s, DM<double> G, DM<double> U, DM<double> V, double *d_sv, int *d_flag) {
     jacobi_small<float>(s, G, U, V, d_sv, d_flag, false);
     PhaseTimer pt(&ctx().timing.small_ms);
-    svd_refine(s, G, V, U, d_sv, 4);
+    svd_refine(s, G, V, U, d_sv, REFINE_STEPS);
 }
 
 }  // namespace rsvd

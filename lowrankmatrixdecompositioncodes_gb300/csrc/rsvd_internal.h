@@ -342,6 +342,11 @@ void df64_gram_pair(cudaStream_t s, Df64View A0, DM<double> C0, Df64View A1, DM<
 // X (n x n, FP64) and approximate right singular vectors V (n x n, columns; FP32-accurate, e.g.
 // from the FP32 Jacobi) -> the SVD of X to FP64 accuracy: U, V (n x n) and sv (device, n values),
 // descending.  V is overwritten; U may not alias V.  `steps` first-order corrections.
+// Refinement steps after the FP32 Jacobi: the first takes FP32-accurate vectors to ~1e-12, the
+// second to the FP64 floor, the last settles nearly equal pairs coupled beyond 2e-5.  Three steps
+// leave the singular values as accurate but the vectors of clustered values orthogonal only to
+// ~5e-10; the fourth brings them to ~1e-12.
+constexpr int REFINE_STEPS = 4;
 void svd_refine(cudaStream_t s, DM<double> X, DM<double> V, DM<double> U, double *d_sv, int steps);
 // The mixed-precision l x l SVD: FP32 one-sided Jacobi, then svd_refine (FP64-accurate result).
 void small_svd_refined(cudaStream_t s, DM<double> G, DM<double> U, DM<double> V, double *d_sv, int *d_flag);
