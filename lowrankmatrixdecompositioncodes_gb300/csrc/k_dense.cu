@@ -1036,12 +1036,19 @@ void gram_tiles_f32(cudaStream_t s, DM<float> Y, float *Gt, DM<double> *G) {
     if (G && (G->r != c || G->c != c)) fail(RSVD_ERR_ARGUMENT, "gram: shape mismatch");
     const int prec = ctx().opts.precision;
     if ((prec == RSVD_PREC_TF32 || prec == RSVD_PREC_BF16) && Y.r >= 2048 && c >= 64) {
-        // tensor-core modes: G = Y^T Y by 3xTF32 (FP32-accurate: hi x hi in ~256-row chains,
-        // compensated sums across chains), ~3x faster than the CUDA-core Gram at m = 16384
+        // tensor-core modes: G = Y^T Y by 3xTF32 (FP32-accurate) as ONE split-K launch of the
+        // three terms lo x hi, hi x lo, hi x hi (chains of m / 64 k-blocks across the concatenated
+        // terms, compensated sums across chains); two launches, their reductions and an add
+        // cost twice as much at m = 16384
         const int np = (c + 31) / 32 * 32;
         DMat<float> Yh(Y.r, c, s, false), Yl(Y.r, c, s, false), Gd(c, c, s, false);
         split_tf32(s, Y.p, Y.ld, Y.r, c, Yh.v.p, Yl.v.p, Yh.v.ld);
-        tc_gemm_3xtf32(s, Yh.v.p, Yl.v.p, Yh.v.ld, Yh.v.p, Yl.v.p, Yh.v.ld, c, c, (int)Y.r, Gd.v.p, Gd.v.ld);
+        const int m = (int)Y.r;
+        const TcSeg sg[3] = {{Yl.v.p, Yl.v.ld, Yh.v.p, Yh.v.ld, m}, {Yh.v.p, Yh.v.ld, Yl.v.p, Yl.v.ld, m},
+                             {Yh.v.p, Yh.v.ld, Yh.v.p, Yh.v.ld, m}};
+        const int splits = std::max(1, std::min(64, m / 256));
+        tc_gemm_segs(s, 0 /* kind::tf32 */, false, 3, sg, c, c, 1.0f, Gd.v.p, Gd.v.ld, 0 /* store */, nullptr, 0, nullptr,
+                     splits, nullptr);
         pack_gram_tiles_kernel<<<grid_for((i64)np * np), 256, 0, s>>>(Gd.v.p, Gd.v.ld, c, np, Gt, G ? G->p : nullptr,
                                                                      G ? G->ld : 0);
         RSVD_LAUNCH_CK();
