@@ -6,8 +6,9 @@ implicit synchronisation of cudaMalloc / cudaFree): its split-K partial sums liv
 scratch array inside the library instead of in workspace the call would allocate.  Its
 result must match the regular entry point (rsvdpack_dev_sketch, TF32 mode) within the
 TF32 tolerance, on two calls in a row (the second reuses the scratch the first left
-behind), and the device's free memory must not change across calls on a warmed device.
-The file name sorts after every other test file, so pytest collects it last.
+behind), and the device's free memory must not change across calls on a warmed device (the
+free-memory test synchronises the whole device first, so it does not depend on the order in
+which the suite runs).
 """
 import ctypes as C
 
