@@ -280,13 +280,13 @@ const char *rsvdpack_last_error_string(void);
 void rsvdpack_clear_error(void);
 
 /* Arithmetic of the large products (sketch, power rounds, projections) and of the
- * storage of A on the device.  Small k x k work: in RSVD_PREC_FP64, FP64 throughout (Cholesky,
- * one-sided Jacobi, triangular solves); in the other modes the l x l SVD is the FP32 one-sided
- * Jacobi refined to FP64 accuracy by double-float products (singular values to ~1e-14 relative
- * of the l x l factor), and the Cholesky factorisations of FP32-data Grams run in FP32.  Pivot
- * decisions are FP64 in every mode. */
+ * storage of A on the device.  Small k x k work: in RSVD_PREC_FP64, FP64 Cholesky and triangular
+ * solves; in every mode the l x l SVD of the randomized SVD routines is the FP32 one-sided Jacobi
+ * refined to FP64 accuracy by double-float products (singular values to ~1e-14 relative of the
+ * l x l factor; absolute ~1e-14 sigma_1 for strongly graded factors), and the Cholesky
+ * factorisations of FP32-data Grams run in FP32.  Pivot decisions are FP64 in every mode. */
 enum {
-    RSVD_PREC_FP64 = 0,   /* everything FP64: reproduces the reference (default) */
+    RSVD_PREC_FP64 = 0,   /* FP64 data and arithmetic: reproduces the reference (default) */
     RSVD_PREC_FP32 = 1,   /* A and tall factors FP32, CUDA-core FP32 products */
     RSVD_PREC_TF32 = 2,   /* A FP32, tcgen05 kind::tf32 products, FP32 accumulate */
     RSVD_PREC_BF16 = 3,   /* A FP32 + BF16 copy, tcgen05 kind::f16 (bf16) sketch products */

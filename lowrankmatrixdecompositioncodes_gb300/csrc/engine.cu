@@ -449,10 +449,10 @@ static SvdOut<T> svd_from_q(DM<T> A, DM<T> Q, int k, int vnum) {
         {
             DMat<double> RhT(l, l, s, false);
             transpose<double>(s, Rh.v, RhT.v);
-            if (std::is_same<T, float>::value || fp64x_mode())
-                small_svd_refined(s, RhT.v, Vh.v, Uh.v, (double *)svb.get(), cx.d_flags + FLAG_JACOBI_NOCONV);
-            else
-                jacobi_small<T>(s, RhT.v, Vh.v, Uh.v, (double *)svb.get(), cx.d_flags + FLAG_JACOBI_NOCONV, false);
+            // every mode: FP32 Jacobi refined to FP64 accuracy (the FP64 Jacobi took 8.6 ms at
+            // l = 110 and 40 ms at l = 272 on GB300's FP64 pipe; the refined form 1.1 / 2.8 ms, with
+            // singular values to ~1e-14 of LAPACK and the golden fixtures' parity bar met)
+            small_svd_refined(s, RhT.v, Vh.v, Uh.v, (double *)svb.get(), cx.d_flags + FLAG_JACOBI_NOCONV);
         }
         // the leading k singular pairs: column prefixes of Vh, Uh in the working precision
         DMat<T> Vk(l, k, s, false), Uk(l, k, s, false);
@@ -469,10 +469,7 @@ static SvdOut<T> svd_from_q(DM<T> A, DM<T> Q, int k, int vnum) {
         // eig(B B^T) ascending, keep the last k; U = Q Uh; V = B^T Uh S^-1   (RRA:176-224)
         DMat<double> BBt(l, l, s, false);
         gram<T>(s, Bt.v, BBt.v);                                         // B B^T = Bt^T Bt
-        if (std::is_same<T, float>::value || fp64x_mode())
-            small_svd_refined(s, BBt.v, Uh.v, Vh.v, (double *)svb.get(), cx.d_flags + FLAG_JACOBI_NOCONV);
-        else
-            jacobi_small<T>(s, BBt.v, Uh.v, Vh.v, (double *)svb.get(), cx.d_flags + FLAG_JACOBI_NOCONV, false);
+        small_svd_refined(s, BBt.v, Uh.v, Vh.v, (double *)svb.get(), cx.d_flags + FLAG_JACOBI_NOCONV);
         RSVD_CK(cudaMemcpyAsync(sv.data(), svb.get(), sizeof(double) * l, cudaMemcpyDeviceToHost, s));
         RSVD_CK(cudaStreamSynchronize(s));
         // ascending order position i in [0,k) <- descending position k-1-i
