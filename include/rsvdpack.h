@@ -374,6 +374,18 @@ int rsvdpack_dev_residual_norms(const void *dA, int dtype, long long lda, int m,
                                 long long ldu, const double *dS, const void *dV, long long ldv, int k, int iters,
                                 double *fro, double *spec);
 
+/* The reference's binary matrix files (matrix_load_from_binary_file, matrix_vector_functions_
+ * intel_mkl.c:77-133: two header integers m, n of this library's rsvd_int width, then the m x n
+ * entries of this library's rsvd_real type row by row) streamed straight into device memory.
+ * rsvdpack_binary_file_shape reads the header.  rsvdpack_dev_load_binary reads the file in
+ * ~32 MiB chunks of whole rows through two pinned staging buffers, copies each chunk to the
+ * device on its own stream and transposes it there into dA (column-major, leading dimension
+ * lda >= m, in dtype RSVD_DT_F64, RSVD_DT_F32 or RSVD_DT_BF16, round to nearest), so that file
+ * reads, copies and transposes overlap; m and n (optional) receive the shape.  Synchronous: the
+ * matrix is complete when the call returns. */
+int rsvdpack_binary_file_shape(const char *fname, long long *m, long long *n);
+int rsvdpack_dev_load_binary(const char *fname, int dtype, void *dA, long long lda, long long *m, long long *n);
+
 /* FP64-accurate product on the FP32 pipe (no counterpart in the reference):
  * C (M x N, ldc) = alpha op(A) op(B) + beta C, op(X) = X^T when its flag is set; FP64 device
  * data, column-major.  Each operand is split once into FP32 parts (hi + lo, scaled on the device

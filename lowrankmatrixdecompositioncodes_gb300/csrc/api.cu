@@ -1267,6 +1267,31 @@ int rsvdpack_dev_residual_norms(const void *dA, int dtype, long long lda, int m,
     return rsvdpack_last_error();
 }
 
+int rsvdpack_binary_file_shape(const char *fname, long long *m, long long *n) {
+    guarded("rsvdpack_binary_file_shape", [&] {
+        need(fname && m && n, "null argument");
+        if (!binary_file_shape(fname, (int)sizeof(rsvd_int), m, n))
+            fail(RSVD_ERR_ARGUMENT, std::string("cannot read a matrix file header from ") + fname);
+    });
+    return rsvdpack_last_error();
+}
+
+int rsvdpack_dev_load_binary(const char *fname, int dtype, void *dA, long long lda, long long *m, long long *n) {
+    guarded("rsvdpack_dev_load_binary", [&] {
+        need(fname && dA, "null argument");
+        need(dtype == RSVD_DT_F64 || dtype == RSVD_DT_F32 || dtype == RSVD_DT_BF16,
+             "dtype must be RSVD_DT_F64, RSVD_DT_F32 or RSVD_DT_BF16");
+        begin_call();
+        order_after_default_stream();
+        long long mm = 0, nn = 0;
+        load_binary_to_device(fname, (int)sizeof(rsvd_int), (int)sizeof(real), dtype, dA, lda, &mm, &nn);
+        if (m) *m = mm;
+        if (n) *n = nn;
+        ctx().timing.kernel_launches = ctx().launches;
+    });
+    return rsvdpack_last_error();
+}
+
 int rsvdpack_dev_gemm_df64(int ta, int tb, int M, int N, int K, double alpha, const double *dA, long long lda,
                            const double *dB, long long ldb, double beta, double *dC, long long ldc) {
     guarded("rsvdpack_dev_gemm_df64", [&] {

@@ -278,6 +278,11 @@ bool trsm_right_tiles(cudaStream_t s, DM<T> Y, DM<double> R, const T *dinv, DM<T
 // triangular solve.
 void gram_tiles_f32(cudaStream_t s, DM<float> Y, float *Gt, DM<double> *G);
 bool chol_tiles_f32(cudaStream_t s, float *Gt, int n, double rel_tol, int *d_flag, float *dinv, DM<double> *Rout);
+// Binary matrix files (k_io.cu): the header (two integers of hdr_bytes each) and the streaming
+// load of the row-major entries (real_bytes each) into a column-major device matrix of dtype.
+bool binary_file_shape(const char *fname, int hdr_bytes, long long *m, long long *n);
+void load_binary_to_device(const char *fname, int hdr_bytes, int real_bytes, int dtype, void *dA, long long lda,
+                           long long *m_out, long long *n_out);
 // C = A B (FP32, column-major) in 3xTF32 on the tensor cores (FP32-accurate products).
 void gemm_nn_3xtf32(cudaStream_t s, DM<float> A, DM<float> B, DM<float> C);
 void trsm_right_tiles_f32(cudaStream_t s, DM<float> Y, int n, const float *Rt, const float *dinv, DM<float> Q);
