@@ -88,8 +88,20 @@ DMat<T> upload(const mat *M) {
     const i64 m = M->nrows, n = M->ncols;
     if (ctx().pageable_access) {
         // the conversion kernel reads the caller's (pageable) host matrix over NVLink-C2C:
-        // one pass at the link's bandwidth, no staging copy and no device temporary
+        // one pass at the link's bandwidth, no staging copy and no device temporary.  In the
+        // tensor-core modes a large A also gets its BF16 copy (the MN-major products read it) in
+        // the same pass, where the extra device writes hide under the link-bound read.
         DMat<T> A(m, n, s, false);
+        const int prec = ctx().opts.precision;
+        if constexpr (std::is_same<T, float>::value) {
+            if ((prec == RSVD_PREC_TF32 || prec == RSVD_PREC_BF16) && m * n >= (1ll << 22)) {
+                DMat<__nv_bfloat16> Ab(m, n, s, false);
+                convert_f32_bf16<real>(s, DM<real>{M->d, m, n, m}, A.v, Ab.v);
+                RSVD_CK(cudaStreamSynchronize(s));
+                adopt_bf16_copy(A.v, std::move(Ab));
+                return A;
+            }
+        }
         convert<real, T>(s, DM<real>{M->d, m, n, m}, A.v);
         RSVD_CK(cudaStreamSynchronize(s));     // the caller may reuse M->d on return
         return A;

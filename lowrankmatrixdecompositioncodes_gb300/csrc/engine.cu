@@ -142,6 +142,14 @@ const Df64Split &df64_operand(cudaStream_t s, DM<double> X, std::unique_ptr<Df64
 }
 }  // namespace
 
+// Install a BF16 copy of X made elsewhere (the C-API upload writes it in the same pass as X)
+// as the call's cached copy.
+void adopt_bf16_copy(DM<float> X, DMat<__nv_bfloat16> &&copy) {
+    t_bf16_a = Bf16Cache{};
+    t_bf16_a.m = std::move(copy);
+    t_bf16_a.src = X.p; t_bf16_a.r = X.r; t_bf16_a.c = X.c; t_bf16_a.ld = X.ld;
+}
+
 void release_operand_cache() {
     t_bf16_a = Bf16Cache{};
     t_df64_a = Df64Cache{};

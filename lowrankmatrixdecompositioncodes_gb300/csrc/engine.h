@@ -54,6 +54,8 @@ template <typename T>
 void prod(cudaStream_t s, bool ta, bool tb, T alpha, DM<T> A, DM<T> B, T beta, DM<T> C);
 // Drop the per-call BF16 operand copies (called at the end of every API call).
 void release_operand_cache();
+// The call's cached BF16 copy of X (same shape and leading dimension as to_bf16 would make).
+void adopt_bf16_copy(DM<float> X, DMat<__nv_bfloat16> &&copy);
 // Large FP64 products (FP64 GEMM, or double-float on the FP32 pipe in the FP64X mode).
 void prod_f64(cudaStream_t s, bool ta, bool tb, double alpha, DM<double> A, DM<double> B, double beta, DM<double> C);
 bool fp64x_mode();

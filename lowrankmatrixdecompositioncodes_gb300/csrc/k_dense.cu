@@ -248,6 +248,31 @@ __global__ void convert_kernel(const Ts *src, i64 lds, Td *dst, i64 ldd, i64 r, 
         }
     }
 }
+// dst = (float)src and dst2 = bf16(dst) in one pass (the C-API upload of a matrix whose BF16
+// copy the tensor-core products will read: the second output rides on the link-bound read).
+template <typename Ts>
+__global__ void convert_f32_bf16_kernel(const Ts *src, i64 lds, float *dst, i64 ldd, __nv_bfloat16 *dst2, i64 ldd2,
+                                        i64 r, i64 c) {
+    const i64 i0 = (i64)blockIdx.x * 1024 + threadIdx.x;
+    for (i64 j = blockIdx.y; j < c; j += gridDim.y) {
+        const Ts *sc = src + j * lds;
+        Ts v[4];
+#pragma unroll
+        for (int t = 0; t < 4; t++) {
+            const i64 i = i0 + 256 * t;
+            v[t] = (i < r) ? sc[i] : Ts(0);
+        }
+#pragma unroll
+        for (int t = 0; t < 4; t++) {
+            const i64 i = i0 + 256 * t;
+            if (i < r) {
+                const float f = (float)v[t];
+                dst[i + j * ldd] = f;
+                dst2[i + j * ldd2] = __float2bfloat16_rn(f);
+            }
+        }
+    }
+}
 template <typename T>
 __global__ void fill_kernel(T *a, i64 ld, i64 r, i64 c, int identity) {
     for (i64 e = blockIdx.x * (i64)blockDim.x + threadIdx.x; e < r * c; e += (i64)gridDim.x * blockDim.x) {
@@ -364,6 +389,16 @@ void convert(cudaStream_t s, DM<Ts> src, DM<Td> dst) {
     RSVD_LAUNCH_CK();
     ctx().launches++;
 }
+template <typename Ts>
+void convert_f32_bf16(cudaStream_t s, DM<Ts> src, DM<float> dst, DM<__nv_bfloat16> dst2) {
+    if (src.r * src.c == 0) return;
+    const dim3 grid((unsigned)((src.r + 1023) / 1024), (unsigned)std::min<i64>(src.c, 65535));
+    convert_f32_bf16_kernel<Ts><<<grid, 256, 0, s>>>(src.p, src.ld, dst.p, dst.ld, dst2.p, dst2.ld, src.r, src.c);
+    RSVD_LAUNCH_CK();
+    ctx().launches++;
+}
+template void convert_f32_bf16<double>(cudaStream_t, DM<double>, DM<float>, DM<__nv_bfloat16>);
+template void convert_f32_bf16<float>(cudaStream_t, DM<float>, DM<float>, DM<__nv_bfloat16>);
 template void convert<double, float>(cudaStream_t, DM<double>, DM<float>);
 template void convert<float, double>(cudaStream_t, DM<float>, DM<double>);
 template void convert<double, double>(cudaStream_t, DM<double>, DM<double>);

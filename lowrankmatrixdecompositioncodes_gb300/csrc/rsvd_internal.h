@@ -150,6 +150,9 @@ void gemm(cudaStream_t s, bool ta, bool tb, T alpha, DM<T> A, DM<T> B, T beta, D
 
 template <typename Ts, typename Td>
 void convert(cudaStream_t s, DM<Ts> src, DM<Td> dst);      // dst = (Td)src, same shape
+// dst = (float)src and dst2 = bf16(dst), one pass (C-API upload with the BF16 copy of A)
+template <typename Ts>
+void convert_f32_bf16(cudaStream_t s, DM<Ts> src, DM<float> dst, DM<__nv_bfloat16> dst2);
 // hi = bf16(x) (round to nearest), lo = bf16(x - hi): x = hi + lo to ~2^-16 relative.
 void split_bf16(cudaStream_t s, DM<float> src, DM<__nv_bfloat16> hi, DM<__nv_bfloat16> lo);
 template <typename T>
