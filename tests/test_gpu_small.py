@@ -51,8 +51,11 @@ def test_small_cholesky_reports_breakdown(engine):
     assert engine.lib.rsvdpack_dev_small_cholesky(d.data_ptr(), n, n, 0) == 4
 
 
-@pytest.mark.parametrize("fp32", [0, 1])
-@pytest.mark.parametrize("n", [7, 40, 64, 110, 200, 272, 300, 400])
+# 97, 110, 112: the 8-CTA register-Gram form (block width 7) and its edges; 257, 272, 288: the
+# 16-CTA one (block width 9) -- 257 leaves a whole padding block -- ; the others the one-sided form.
+# fp32 = 2: the FP32 Jacobi refined to FP64 accuracy
+@pytest.mark.parametrize("fp32", [0, 1, 2])
+@pytest.mark.parametrize("n", [7, 40, 64, 97, 110, 112, 200, 257, 272, 288, 300, 400])
 def test_small_svd(engine, n, fp32):
     _bind(engine.lib)
     g = np.random.default_rng(100 + n)
@@ -69,7 +72,7 @@ def test_small_svd(engine, n, fp32):
                                                fp32)
     assert sweeps > 0, engine.last_error()
     Uh, Sh, Vh = U.cpu().numpy().T, S.cpu().numpy(), V.cpu().numpy().T
-    tol = 5e-5 if fp32 else 1e-12
+    tol = 5e-5 if fp32 == 1 else 1e-12
     assert np.all(np.diff(Sh) <= 0)
     assert np.max(np.abs(Sh - s_true)) < tol
     assert np.max(np.abs(Uh @ np.diag(Sh) @ Vh.T - A)) < 10 * tol
