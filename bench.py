@@ -9,8 +9,9 @@ Workload (one "step" = one fixed-rank randomized SVD with the reference's semant
   e2e   : solves/s through the reference C API (low_rank_svd_rand_decomp_fixed_rank)
           from a pinned host FP64 matrix: H2D of A, solve, D2H of U, S, V every step.
   A (512 MiB) is larger than L2 (129 MB), so no flush is needed between steps.
-  Residual ||A - U S V^T||_F / ||A||_F is checked against the FP64 path of the same
-  method on the same test matrix ("matched FP64-oracle error").
+  Residual ||A - U S V^T||_F / ||A||_F and the top-k singular values (against FP64 LAPACK) are
+  checked against the FP64 path of the same method on the same test matrix ("matched
+  FP64-oracle error").
 
 --impl reference times the CPU oracle (oracle/port: the reference's algorithm on
 OpenBLAS, all host cores) on the same workload and prints the same JSON line.
@@ -994,7 +995,9 @@ def run_ours(args):
         line = {
             "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": {"fp64": "f64", "fp32": "f32", "tf32": "tf32", "bf16": "bf16"}[args.precision],
+            # tf32 mode: A^T X on kind::tf32 from the FP32 A, A X on kind::f16 from A's BF16 copy (the
+            # tensor cores read 32-bit operands K-major only); the l x l steps FP32 refined to FP64
+            "vs_baseline": None, "dtype": {"fp64": "f64", "fp32": "f32", "tf32": "tf32+bf16", "bf16": "bf16"}[args.precision],
             "data": "synthetic (seeded; A = U diag(i^-1.5) V^T + 1e-4 G)",
             "config": {"workload": "single large rSVD 16384x8192 k=256 p=16 q=2 s=1 vnum=1", "m": m, "n": n, "k": k,
                        "p": P, "q": Q, "s": S_ORTH, "precision": args.precision,
