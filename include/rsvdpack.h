@@ -426,11 +426,14 @@ int rsvdpack_batch_plan_info(const rsvdpack_batch_plan *plan, int *lanes_per_pai
 
 /* The l x l steps on their own (device FP64 storage, column-major; compute in FP32 when
  * fp32 != 0, else FP64).  rsvdpack_dev_small_svd: G (n x n) = U diag(S) V^T, S descending,
- * by one-sided Jacobi (the engine's l x l SVD); fp32 == 2 selects the mixed modes' form: the
- * FP32 Jacobi followed by four FP64-accurate refinement steps (double-float products on the
- * FP32 pipe, exact FP64 rotations of nearly equal pairs): singular values to ~1e-14 relative,
- * singular vectors orthonormal to ~1e-12 (~1e-10 for singular values closer than ~1e-6 relative); returns the FP32 or FP64 sweep count or
- * a negative RSVD_ERR_* code.  rsvdpack_dev_small_cholesky: G = R^T R in place (upper R, lower
+ * by one-sided Jacobi (the engine's l x l SVD); fp32 == 2 selects the refined form the
+ * randomized SVD routines use: the FP32 Jacobi followed by four FP64-accurate refinement steps
+ * (double-float products on the FP32 pipe, exact FP64 rotations of nearly equal pairs): singular
+ * values to ~1e-14 relative, singular vectors orthonormal to ~1e-12 (~1e-10 for singular values
+ * closer than ~1e-6 relative), for factors whose singular values span up to ~6 decades (the
+ * accuracy is absolute, ~1e-13 sigma_1, so it degrades for values far below sigma_1; fp32 == 0 is
+ * the form for strongly graded factors); returns the FP32 or FP64 sweep count or a negative
+ * RSVD_ERR_* code.  rsvdpack_dev_small_cholesky: G = R^T R in place (upper R, lower
  * part zeroed); returns RSVD_OK, RSVD_ERR_NUMERIC on breakdown, or another RSVD_ERR_* code. */
 int rsvdpack_dev_small_svd(double *dG, int n, long long ldg, double *dU, long long ldu, double *dS, double *dV,
                            long long ldv, int fp32);

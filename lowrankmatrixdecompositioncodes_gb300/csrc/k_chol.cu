@@ -952,6 +952,187 @@ __global__ void __launch_bounds__(256) gemm_nn_3xtf32_kernel(const float *A, lon
             }
 }
 
+// ---------------------------------------------------------------- Cholesky and slab solve fused
+// One cooperative launch of 1 + ceil(m / 128) CTAs (all co-resident): CTA 0 runs the one-CTA
+// tiled Cholesky of chol_tiles_f32_kernel on the packed Gram and publishes block row J of R (and
+// R_JJ^-1) to global memory as soon as step J's panel is done, then releases ready[J]; the other
+// CTAs run the 3xTF32 slab solve of trsm_mma_kernel, waiting on ready[J] (acquire) before block
+// column J -- which is complete once rows 0..J are published.  The solve of block column J thus
+// runs while the Cholesky factors block J + 1 instead of after the whole factorisation.  Waits
+// are bounded (~1 s of SM cycles, then FLAG_TIMEOUT and return); a breakdown releases every
+// flag as -1 and the slabs return (the caller falls back to Householder QR as before).
+__device__ __forceinline__ int ld_acquire_gpu(const int *p) {
+    int v;
+    asm volatile("ld.acquire.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ void st_release_gpu(int *p, int v) {
+    asm volatile("st.release.gpu.global.b32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+// chol_steps with the per-step publication (FP32, tiles in shared memory).
+__device__ void chol_steps_publish(float *T, float *Dw, const float *diag0, int nb, double rel_tol, float *dinv,
+                                   int *bad, float *Gt, int *ready) {
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    if (wid == 0) {
+        const bool ok = factor_diag_warp<float>(T, Dw, diag0, (float)rel_tol);
+        if (!ok && lane == 0) *bad = 1;
+    }
+    __syncthreads();
+    for (int J = 0; J < nb; J++) {
+        if (*bad) return;
+        for (int K = J + 1 + wid; K < nb; K += nw) {
+            float *W = T + (size_t)tix(J, K) * TE;
+            float acc[4][8];
+            zero_acc(acc);
+            tile_tn<float>(Dw, W, 0, lane_r0() + 4, acc);
+            __syncwarp();
+            put_acc<float>(W, acc, false);
+        }
+        for (int e = threadIdx.x; e < TB * TB; e += blockDim.x) dinv[(size_t)J * TB * TB + e] = Dw[(e >> 5) * TP + (e & 31)];
+        __syncthreads();
+        // block row J of R is final: publish it
+        for (int e = threadIdx.x; e < (nb - J) * TB * TB; e += blockDim.x) {
+            const int K = J + e / (TB * TB), w = e % (TB * TB);
+            Gt[(size_t)tix(J, K) * TB * TB + w] = T[(size_t)tix(J, K) * TE + (w >> 5) * TP + (w & 31)];
+        }
+        __threadfence();
+        __syncthreads();
+        if (threadIdx.x == 0) st_release_gpu(ready + J, 1);
+        const int nt = nb - J - 1;
+        if (nt > 0) {
+            if (wid == 0) {
+                float acc[4][8];
+                zero_acc(acc);
+                tile_tn<float>(T + (size_t)tix(J, J + 1) * TE, T + (size_t)tix(J, J + 1) * TE, 0, TB, acc);
+                put_acc<float>(T + (size_t)tix(J + 1, J + 1) * TE, acc, true);
+                __syncwarp();
+                const bool ok = factor_diag_warp<float>(T + (size_t)tix(J + 1, J + 1) * TE, Dw, diag0 + (J + 1) * TB,
+                                                        (float)rel_tol);
+                if (!ok && lane == 0) *bad = 1;
+            } else {
+                for (int t = wid; t < nt * (nt + 1) / 2; t += nw - 1) {
+                    int Ip, Kp;
+                    untix(t, Ip, Kp);
+                    const int I = J + 1 + Ip, K = J + 1 + Kp;
+                    float acc[4][8];
+                    zero_acc(acc);
+                    tile_tn<float>(T + (size_t)tix(J, I) * TE, T + (size_t)tix(J, K) * TE, 0, TB, acc);
+                    put_acc<float>(T + (size_t)tix(I, K) * TE, acc, true);
+                }
+            }
+        }
+        __syncthreads();
+    }
+}
+
+__global__ void __launch_bounds__(256, 1) chol_trsm_fused_kernel(float *Gt, int n, int nb, double rel_tol, float *dinv,
+                                                                int *flags, int *ready, const float *Y, long long ldy,
+                                                                float *Q, long long ldq, long long m) {
+    extern __shared__ __align__(16) unsigned char shraw[];
+    __shared__ int bad, go;
+    if (blockIdx.x == 0) {
+        float *T = (float *)shraw;
+        const int ntile = tix(0, nb);
+        float *Dw = T + (size_t)ntile * TE;
+        float *diag0 = Dw + TE;
+        const int nchunk = ntile * TB * 8;
+        for (int e = threadIdx.x; e < nchunk; e += blockDim.x) {
+            const int t = e >> 8, r = (e >> 3) & 31, q = e & 7;
+            cp_async16(T + (size_t)t * TE + r * TP + q * 4, Gt + (size_t)t * TB * TB + r * TB + q * 4);
+        }
+        cp_async_wait_all();
+        if (threadIdx.x == 0) bad = 0;
+        __syncthreads();
+        for (int j = threadIdx.x; j < nb * TB; j += blockDim.x) {
+            const int J = j >> 5, jj = j & 31;
+            diag0[j] = T[(size_t)tix(J, J) * TE + jj * TP + jj];
+        }
+        __syncthreads();
+        chol_steps_publish(T, Dw, diag0, nb, rel_tol, dinv, &bad, Gt, ready);
+        __syncthreads();
+        if (bad && threadIdx.x == 0) {
+            atomicExch(flags + FLAG_CHOL_BREAKDOWN, 1);
+            __threadfence();
+            for (int J = 0; J < nb; J++) st_release_gpu(ready + J, -1);
+        }
+        return;
+    }
+    // ---- slab (blockIdx.x - 1): trsm_mma_kernel with a wait before each block column
+    const int QP = nb * TB + 4;
+    float *Qs = (float *)shraw;
+    float *Rc = Qs + (size_t)TRSM_MMA_BM * QP;
+    float *Dv = Rc + (size_t)(nb - 1) * TB * RPB;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, g = lane >> 2, t = lane & 3;
+    const long long row0 = (long long)(blockIdx.x - 1) * TRSM_MMA_BM + wid * 16;
+    float *Qw = Qs + (size_t)wid * 16 * QP;
+    constexpr int CPR = TB / 4;
+    for (int J = 0; J < nb; J++) {
+        const int kr = J * TB;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            const long long t0 = clock64();
+            int v;
+            while ((v = ld_acquire_gpu(ready + J)) == 0) {
+                if (clock64() - t0 > (1ll << 31)) {
+                    atomicExch(flags + FLAG_TIMEOUT, 1);
+                    v = -1;
+                    break;
+                }
+                __nanosleep(200);
+            }
+            go = v;
+        }
+        __syncthreads();
+        if (go < 0) return;
+        for (int e = threadIdx.x; e < kr * CPR; e += blockDim.x) {
+            const int I = e / (TB * CPR), r = (e / CPR) % TB, q = e % CPR;
+            cp_async16(Rc + (I * TB + r) * RPB + q * 4, Gt + (size_t)tix(I, J) * TB * TB + r * TB + q * 4);
+        }
+        for (int e = threadIdx.x; e < TB * CPR; e += blockDim.x) {
+            const int r = e / CPR, q = e % CPR;
+            cp_async16(Dv + r * RPB + q * 4, dinv + (size_t)J * TB * TB + r * TB + q * 4);
+        }
+        cp_async_wait_all();
+        __syncthreads();
+        float acc[4][4];
+#pragma unroll
+        for (int nt = 0; nt < 4; nt++)
+#pragma unroll
+            for (int e = 0; e < 4; e++) acc[nt][e] = 0.f;
+        if (kr > 0) mma3_rows(acc, Qw, QP, Rc, RPB, 0, kr);
+#pragma unroll
+        for (int nt = 0; nt < 4; nt++)
+#pragma unroll
+            for (int e = 0; e < 4; e++) {
+                const int r = g + (e >> 1) * 8, c = nt * 8 + 2 * t + (e & 1);
+                const long long gr = row0 + r;
+                const int gc = kr + c;
+                const float y = (gr < m && gc < n) ? Y[gr + (long long)gc * ldy] : 0.f;
+                Qw[r * QP + kr + c] = y - acc[nt][e];
+            }
+        __syncwarp();
+        float o[4][4];
+#pragma unroll
+        for (int nt = 0; nt < 4; nt++)
+#pragma unroll
+            for (int e = 0; e < 4; e++) o[nt][e] = 0.f;
+        mma3_rows(o, Qw + kr, QP, Dv, RPB, 0, TB);
+        __syncwarp();
+#pragma unroll
+        for (int nt = 0; nt < 4; nt++)
+#pragma unroll
+            for (int e = 0; e < 4; e++) {
+                const int r = g + (e >> 1) * 8, c = nt * 8 + 2 * t + (e & 1);
+                Qw[r * QP + kr + c] = o[nt][e];
+                const long long gr = row0 + r;
+                const int gc = kr + c;
+                if (gr < m && gc < n) Q[gr + (long long)gc * ldq] = o[nt][e];
+            }
+        __syncwarp();
+    }
+}
+
 template <typename T>
 constexpr int trsm_bm() { return 128; }
 
@@ -1083,6 +1264,57 @@ void trsm_right_tiles_f32(cudaStream_t s, DM<float> Y, int n, const float *Rt, c
     trsm_mma_kernel<<<(unsigned)slabs, 256, smem, s>>>(Y.p, Y.ld, Rt, dinv, Q.p, Q.ld, Y.r, n, nb);
     RSVD_LAUNCH_CK();
     ctx().launches++;
+}
+
+// Cholesky of the packed FP32 Gram and Q = Y R^-1 in one cooperative launch
+// (chol_trsm_fused_kernel).  Returns -1 when the launch is not possible here (order above 288,
+// or more slabs than can be co-resident: the caller runs chol_tiles_f32 and
+// trsm_right_tiles_f32), else 1, or 0 on a Cholesky breakdown (undeferred mode only: deferred,
+// the flag stays set for the caller's one check).  Rout (optional): R as FP64.
+int chol_trsm_fused_f32(cudaStream_t s, float *Gt, int n, double rel_tol, float *dinv, DM<double> *Rout, DM<float> Y,
+                        DM<float> Q) {
+    if (n == 0 || Y.r == 0) return -1;
+    const int nb = (n + TB - 1) / TB;
+    if (nb > smem_nb_max<float>()) return -1;
+    const long long slabs = (Y.r + TRSM_MMA_BM - 1) / TRSM_MMA_BM;
+    const size_t smem_chol = sizeof(float) * ((size_t)(tix(0, nb) + 1) * TE + (size_t)nb * TB);
+    const size_t smem_trsm = sizeof(float) * ((size_t)TRSM_MMA_BM * (nb * TB + 4) +
+                                              (size_t)std::max(nb - 1, 1) * TB * RPB + (size_t)TB * RPB);
+    const size_t smem = std::max(smem_chol, smem_trsm);
+    int dev = 0, coop = 0;
+    RSVD_CK(cudaGetDevice(&dev));
+    RSVD_CK(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev));
+    if (!coop) return -1;
+    RSVD_CK(cudaFuncSetAttribute(chol_trsm_fused_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    int per_sm = 0;
+    RSVD_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, chol_trsm_fused_kernel, 256, smem));
+    if ((long long)per_sm * std::max(1, ctx().sms) < slabs + 1) return -1;
+    int *flags = ctx().d_flags;
+    if (!ctx().chol_deferred) RSVD_CK(cudaMemsetAsync(flags + FLAG_CHOL_BREAKDOWN, 0, sizeof(int), s));
+    DBuf rb(sizeof(int) * (size_t)nb, s);
+    int *ready = (int *)rb.get();
+    RSVD_CK(cudaMemsetAsync(ready, 0, sizeof(int) * (size_t)nb, s));
+    const float *yp = Y.p;
+    long long ldy = Y.ld, ldq = Q.ld, m = Y.r;
+    float *qp = Q.p;
+    void *args[] = {(void *)&Gt, (void *)&n, (void *)&nb, (void *)&rel_tol, (void *)&dinv, (void *)&flags,
+                    (void *)&ready, (void *)&yp, (void *)&ldy, (void *)&qp, (void *)&ldq, (void *)&m};
+    RSVD_CK(cudaLaunchCooperativeKernel((const void *)chol_trsm_fused_kernel, dim3((unsigned)(slabs + 1)), dim3(256),
+                                        args, smem, s));
+    RSVD_LAUNCH_CK();
+    ctx().launches++;
+    if (Rout) {
+        const long long nn = (long long)n * n;
+        tiles_to_fp64_kernel<<<(unsigned)std::min<long long>((nn + 255) / 256, (long long)std::max(1, ctx().sms) * 4),
+                               256, 0, s>>>(Gt, n, Rout->p, Rout->ld);
+        RSVD_LAUNCH_CK();
+        ctx().launches++;
+    }
+    if (ctx().chol_deferred) return 1;
+    int h = 0;
+    RSVD_CK(cudaMemcpyAsync(&h, flags + FLAG_CHOL_BREAKDOWN, sizeof(int), cudaMemcpyDeviceToHost, s));
+    RSVD_CK(cudaStreamSynchronize(s));
+    return h == 0 ? 1 : 0;
 }
 
 // C = A B (FP32, column-major) by 3xTF32 on the tensor cores (gemm_nn_3xtf32_kernel).

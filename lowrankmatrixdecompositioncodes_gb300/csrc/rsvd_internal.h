@@ -289,6 +289,10 @@ void load_binary_to_device(const char *fname, int hdr_bytes, int real_bytes, int
 // C = A B (FP32, column-major) in 3xTF32 on the tensor cores (FP32-accurate products).
 void gemm_nn_3xtf32(cudaStream_t s, DM<float> A, DM<float> B, DM<float> C);
 void trsm_right_tiles_f32(cudaStream_t s, DM<float> Y, int n, const float *Rt, const float *dinv, DM<float> Q);
+// Both in one cooperative launch (the solve of block column J overlaps the factorisation of
+// block J + 1): -1 when not possible here (the caller runs the two above), 1, or 0 on breakdown.
+int chol_trsm_fused_f32(cudaStream_t s, float *Gt, int n, double rel_tol, float *dinv, DM<double> *Rout, DM<float> Y,
+                        DM<float> Q);
 }  // namespace rsvd
 
 namespace rsvd {
