@@ -237,17 +237,43 @@ __device__ __noinline__ bool factor_diag_warp(S *D, S *Di, const S *diag0, S rel
     return !bad;
 }
 
-// Store a lane's 4 x 8 block (optionally subtracting from the tile).
+// Store a lane's 4 x 8 block (optionally subtracting from the tile).  FP32: two 16-byte
+// accesses per row, lanes of odd row groups taking the upper half (columns c0+4..c0+7) first:
+// with the pitch TP = 36 the rows r0 and r0 + 4 lie 16 banks apart, so this order lets every
+// 8-lane phase of a 16-byte access cover the 32 banks once (scalar accesses were 8-way
+// conflicts and made the trailing update shared-memory bound).
 template <typename S>
 __device__ __forceinline__ void put_acc(S *T, const S (&acc)[4][8], bool subtract) {
     const int r0 = lane_r0(), c0 = lane_c0();
+    if constexpr (sizeof(S) == 4) {
+        const bool up = (r0 >> 2) & 1;
 #pragma unroll
-    for (int a = 0; a < 4; a++)
-#pragma unroll
-        for (int b = 0; b < 8; b++) {
-            S &t = T[(r0 + a) * TP + c0 + b];
-            t = subtract ? t - acc[a][b] : acc[a][b];
+        for (int a = 0; a < 4; a++) {
+            const float4 lo = make_float4(acc[a][0], acc[a][1], acc[a][2], acc[a][3]);
+            const float4 hi = make_float4(acc[a][4], acc[a][5], acc[a][6], acc[a][7]);
+            float4 *p0 = reinterpret_cast<float4 *>(T + (r0 + a) * TP + c0 + (up ? 4 : 0));
+            float4 *p1 = reinterpret_cast<float4 *>(T + (r0 + a) * TP + c0 + (up ? 0 : 4));
+            float4 v0 = up ? hi : lo, v1 = up ? lo : hi;
+            if (subtract) {
+                const float4 o0 = *p0;
+                v0 = make_float4(o0.x - v0.x, o0.y - v0.y, o0.z - v0.z, o0.w - v0.w);
+            }
+            *p0 = v0;
+            if (subtract) {
+                const float4 o1 = *p1;
+                v1 = make_float4(o1.x - v1.x, o1.y - v1.y, o1.z - v1.z, o1.w - v1.w);
+            }
+            *p1 = v1;
         }
+    } else {
+#pragma unroll
+        for (int a = 0; a < 4; a++)
+#pragma unroll
+            for (int b = 0; b < 8; b++) {
+                S &t = T[(r0 + a) * TP + c0 + b];
+                t = subtract ? t - acc[a][b] : acc[a][b];
+            }
+    }
 }
 
 // Load a 32 x 32 tile of a column-major FP64 matrix into a shared-memory tile (one warp).
@@ -265,6 +291,27 @@ __device__ void load_tile_g(S *T, const double *G, long long ldg, int n, int I, 
     }
 }
 
+// Trailing update of step J, G_IK -= R_JI^T R_JK for J < I <= K except tile (J+1, J+1): the
+// warps claim tiles from the shared counter *next (set to 1 before the step), so warp 0 joins
+// in once it has factored the next diagonal tile.
+template <typename S>
+__device__ __forceinline__ void trailing_update(S *T, int J, int nt, int *next) {
+    const int lane = threadIdx.x & 31, ntiles = nt * (nt + 1) / 2;
+    for (;;) {
+        int t = 0;
+        if (lane == 0) t = atomicAdd(next, 1);
+        t = __shfl_sync(FULL, t, 0);
+        if (t >= ntiles) break;
+        int Ip, Kp;
+        untix(t, Ip, Kp);
+        const int I = J + 1 + Ip, K = J + 1 + Kp;
+        S acc[4][8];
+        zero_acc(acc);
+        tile_tn<S>(T + (size_t)tix(J, I) * TE, T + (size_t)tix(J, K) * TE, 0, TB, acc);
+        put_acc<S>(T + (size_t)tix(I, K) * TE, acc, true);
+    }
+}
+
 // The J loop of the one-CTA factorisation over tiles resident in shared memory (T: packed
 // upper tiles, Dw: scratch tile, diag0: original diagonal).  *bad is set on breakdown.
 // Lookahead: while warps 1.. apply step J's trailing update, warp 0 updates the next
@@ -273,6 +320,7 @@ __device__ void load_tile_g(S *T, const double *G, long long ldg, int n, int I, 
 template <typename S>
 __device__ void chol_steps(S *T, S *Dw, const S *diag0, int nb, double rel_tol, S *dinv, int *bad) {
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    __shared__ int next_tile;
     if (wid == 0) {
         const bool ok = factor_diag_warp<S>(T, Dw, diag0, (S)rel_tol);
         if (!ok && lane == 0) *bad = 1;
@@ -290,9 +338,10 @@ __device__ void chol_steps(S *T, S *Dw, const S *diag0, int nb, double rel_tol, 
             put_acc<S>(W, acc, false);
         }
         for (int e = threadIdx.x; e < TB * TB; e += blockDim.x) dinv[(size_t)J * TB * TB + e] = Dw[(e >> 5) * TP + (e & 31)];
+        if (threadIdx.x == 0) next_tile = 1;
         __syncthreads();
         // trailing update G_IK -= R_JI^T R_JK, J < I <= K: tile (J+1, J+1) (t = 0) and the
-        // next diagonal factorisation on warp 0, the other tiles on warps 1..
+        // next diagonal factorisation on warp 0, the other tiles on whichever warp is free
         const int nt = nb - J - 1;
         if (nt > 0) {
             if (wid == 0) {
@@ -304,17 +353,8 @@ __device__ void chol_steps(S *T, S *Dw, const S *diag0, int nb, double rel_tol, 
                 const bool ok = factor_diag_warp<S>(T + (size_t)tix(J + 1, J + 1) * TE, Dw, diag0 + (J + 1) * TB,
                                                     (S)rel_tol);
                 if (!ok && lane == 0) *bad = 1;
-            } else {
-                for (int t = wid; t < nt * (nt + 1) / 2; t += nw - 1) {
-                    int Ip, Kp;
-                    untix(t, Ip, Kp);
-                    const int I = J + 1 + Ip, K = J + 1 + Kp;
-                    S acc[4][8];
-                    zero_acc(acc);
-                    tile_tn<S>(T + (size_t)tix(J, I) * TE, T + (size_t)tix(J, K) * TE, 0, TB, acc);
-                    put_acc<S>(T + (size_t)tix(I, K) * TE, acc, true);
-                }
             }
+            trailing_update<S>(T, J, nt, &next_tile);
         }
         __syncthreads();
     }
@@ -970,10 +1010,15 @@ __device__ __forceinline__ void st_release_gpu(int *p, int v) {
     asm volatile("st.release.gpu.global.b32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
 
-// chol_steps with the per-step publication (FP32, tiles in shared memory).
+// chol_steps with the per-step publication (FP32, tiles in shared memory).  Block row J is
+// published by warps 1.. (copy to Gt with R_JJ^-1 to dinv, fence, a named barrier among them,
+// then the release of ready[J]) while warp 0 already updates and factors diagonal tile J + 1:
+// the publication stays off the sequential chain of diagonal steps.
 __device__ void chol_steps_publish(float *T, float *Dw, const float *diag0, int nb, double rel_tol, float *dinv,
                                    int *bad, float *Gt, int *ready) {
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const int npub = (int)blockDim.x - 32;            // publishing threads (warps 1..)
+    __shared__ int next_tile;
     if (wid == 0) {
         const bool ok = factor_diag_warp<float>(T, Dw, diag0, (float)rel_tol);
         if (!ok && lane == 0) *bad = 1;
@@ -989,19 +1034,14 @@ __device__ void chol_steps_publish(float *T, float *Dw, const float *diag0, int 
             __syncwarp();
             put_acc<float>(W, acc, false);
         }
-        for (int e = threadIdx.x; e < TB * TB; e += blockDim.x) dinv[(size_t)J * TB * TB + e] = Dw[(e >> 5) * TP + (e & 31)];
+        // R_JJ^-1 leaves Dw before warp 0 overwrites it with step J + 1's inverse
+        if (wid > 0)
+            for (int e = threadIdx.x - 32; e < TB * TB; e += npub) dinv[(size_t)J * TB * TB + e] = Dw[(e >> 5) * TP + (e & 31)];
+        if (threadIdx.x == 0) next_tile = 1;
         __syncthreads();
-        // block row J of R is final: publish it
-        for (int e = threadIdx.x; e < (nb - J) * TB * TB; e += blockDim.x) {
-            const int K = J + e / (TB * TB), w = e % (TB * TB);
-            Gt[(size_t)tix(J, K) * TB * TB + w] = T[(size_t)tix(J, K) * TE + (w >> 5) * TP + (w & 31)];
-        }
-        __threadfence();
-        __syncthreads();
-        if (threadIdx.x == 0) st_release_gpu(ready + J, 1);
         const int nt = nb - J - 1;
-        if (nt > 0) {
-            if (wid == 0) {
+        if (wid == 0) {
+            if (nt > 0) {
                 float acc[4][8];
                 zero_acc(acc);
                 tile_tn<float>(T + (size_t)tix(J, J + 1) * TE, T + (size_t)tix(J, J + 1) * TE, 0, TB, acc);
@@ -1010,18 +1050,18 @@ __device__ void chol_steps_publish(float *T, float *Dw, const float *diag0, int 
                 const bool ok = factor_diag_warp<float>(T + (size_t)tix(J + 1, J + 1) * TE, Dw, diag0 + (J + 1) * TB,
                                                         (float)rel_tol);
                 if (!ok && lane == 0) *bad = 1;
-            } else {
-                for (int t = wid; t < nt * (nt + 1) / 2; t += nw - 1) {
-                    int Ip, Kp;
-                    untix(t, Ip, Kp);
-                    const int I = J + 1 + Ip, K = J + 1 + Kp;
-                    float acc[4][8];
-                    zero_acc(acc);
-                    tile_tn<float>(T + (size_t)tix(J, I) * TE, T + (size_t)tix(J, K) * TE, 0, TB, acc);
-                    put_acc<float>(T + (size_t)tix(I, K) * TE, acc, true);
-                }
             }
+        } else {
+            // block row J of R is final: publish it
+            for (int e = threadIdx.x - 32; e < (nb - J) * TB * TB; e += npub) {
+                const int K = J + e / (TB * TB), w = e % (TB * TB);
+                Gt[(size_t)tix(J, K) * TB * TB + w] = T[(size_t)tix(J, K) * TE + (w >> 5) * TP + (w & 31)];
+            }
+            __threadfence();
+            asm volatile("bar.sync 1, %0;" ::"r"(npub) : "memory");
+            if (threadIdx.x == 32) st_release_gpu(ready + J, 1);
         }
+        if (nt > 0) trailing_update<float>(T, J, nt, &next_tile);
         __syncthreads();
     }
 }
