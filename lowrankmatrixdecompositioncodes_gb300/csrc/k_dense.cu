@@ -9,6 +9,8 @@
 #include "k_common.cuh"
 
 #include <algorithm>
+#include <cstdint>
+#include <type_traits>
 #include <cmath>
 
 namespace rsvd {
@@ -248,6 +250,29 @@ __global__ void convert_kernel(const Ts *src, i64 lds, Td *dst, i64 ldd, i64 r, 
         }
     }
 }
+// Contiguous FP32 -> BF16 (the per-call BF16 copy of a dense operand): 16-byte loads, four per
+// thread in flight, 8-byte stores, a grid-stride loop over ~8 CTAs per SM; the n % 4 tail by
+// the first threads.  Round to nearest even, as convert_kernel.
+__global__ void convert_f32_bf16_flat_kernel(const float *__restrict__ src, __nv_bfloat16 *__restrict__ dst, i64 n) {
+    const i64 n4 = n >> 2, stride = (i64)gridDim.x * blockDim.x;
+    const float4 *s4 = reinterpret_cast<const float4 *>(src);
+    uint2 *d4 = reinterpret_cast<uint2 *>(dst);
+    auto pack = [](float4 v) {
+        const __nv_bfloat162 a = __floats2bfloat162_rn(v.x, v.y), b = __floats2bfloat162_rn(v.z, v.w);
+        return make_uint2(*reinterpret_cast<const uint32_t *>(&a), *reinterpret_cast<const uint32_t *>(&b));
+    };
+    i64 i = (i64)blockIdx.x * blockDim.x + threadIdx.x;
+    for (; i + 3 * stride < n4; i += 4 * stride) {
+        float4 v[4];
+#pragma unroll
+        for (int u = 0; u < 4; u++) v[u] = __ldcs(s4 + i + u * stride);
+#pragma unroll
+        for (int u = 0; u < 4; u++) d4[i + u * stride] = pack(v[u]);
+    }
+    for (; i < n4; i += stride) d4[i] = pack(__ldcs(s4 + i));
+    const i64 t = (i64)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < n - 4 * n4) dst[4 * n4 + t] = __float2bfloat16_rn(src[4 * n4 + t]);
+}
 // dst = (float)src and dst2 = bf16(dst) in one pass (the C-API upload of a matrix whose BF16
 // copy the tensor-core products will read: the second output rides on the link-bound read).
 template <typename Ts>
@@ -384,6 +409,17 @@ void split_bf16(cudaStream_t s, DM<float> src, DM<__nv_bfloat16> hi, DM<__nv_bfl
 template <typename Ts, typename Td>
 void convert(cudaStream_t s, DM<Ts> src, DM<Td> dst) {
     if (src.r * src.c == 0) return;
+    if constexpr (std::is_same<Ts, float>::value && std::is_same<Td, __nv_bfloat16>::value) {
+        if ((src.ld == src.r || src.c == 1) && (dst.ld == dst.r || dst.c == 1) &&
+            reinterpret_cast<uintptr_t>(src.p) % 16 == 0 && reinterpret_cast<uintptr_t>(dst.p) % 8 == 0) {
+            const i64 n = src.r * src.c;
+            const i64 blocks = std::max<i64>(1, std::min<i64>((n / 4 + 255) / 256, (i64)std::max(1, ctx().sms) * 8));
+            convert_f32_bf16_flat_kernel<<<(unsigned)blocks, 256, 0, s>>>(src.p, dst.p, n);
+            RSVD_LAUNCH_CK();
+            ctx().launches++;
+            return;
+        }
+    }
     const dim3 grid((unsigned)((src.r + 1023) / 1024), (unsigned)std::min<i64>(src.c, 65535));
     convert_kernel<Ts, Td><<<grid, 256, 0, s>>>(src.p, src.ld, dst.p, dst.ld, src.r, src.c);
     RSVD_LAUNCH_CK();
