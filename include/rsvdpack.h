@@ -449,7 +449,9 @@ int rsvdpack_dev_small_cholesky(double *dG, int n, long long ldg, int fp32);
  * and m > 32; larger products return RSVD_ERR_ARGUMENT.  The first call on each device (made
  * with that device current) looks up the scratch address; make it before any stream capture.
  * Calls share the scratch: calls that overlap on the GPU race, so serialise them.
- * A, X, Y 16-byte aligned; lda, ldx multiples of 4.  Synchronous; returns RSVD_OK or RSVD_ERR_*. */
+ * A, X, Y 16-byte aligned; lda, ldx multiples of 4.  Synchronous (it waits for its stream), so
+ * it cannot be captured: on a stream that is capturing it queues nothing and returns
+ * RSVD_ERR_ARGUMENT.  Returns RSVD_OK or RSVD_ERR_*. */
 int rsvdpack_dev_sketch_t_noalloc(const float *dA, long long lda, int m, int n, const float *dX,
                                   long long ldx, int w, float *dY, long long ldy, void *stream);
 

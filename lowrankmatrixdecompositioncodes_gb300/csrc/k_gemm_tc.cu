@@ -805,6 +805,10 @@ extern "C" int rsvdpack_dev_sketch_t_noalloc(const float *dA, long long lda, int
         if (!dA || !dX || !dY) fail(RSVD_ERR_ARGUMENT, "null device pointer");
         if (m <= 0 || n <= 0 || w <= 0) fail(RSVD_ERR_ARGUMENT, "empty product");
         if (lda < m || ldx < m || ldy < n) fail(RSVD_ERR_ARGUMENT, "bad leading dimension");
+        // the call ends by waiting for its stream, which a capturing stream cannot do
+        cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+        RSVD_CK(cudaStreamIsCapturing(s, &cap));
+        if (cap != cudaStreamCaptureStatusNone) fail(RSVD_ERR_ARGUMENT, "the stream is capturing (this call is synchronous)");
         int dev = -1;
         RSVD_CK(cudaGetDevice(&dev));
         int major = 0, minor = 0, sms = 0;

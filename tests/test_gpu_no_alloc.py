@@ -93,6 +93,33 @@ def test_no_alloc_leaves_free_memory_unchanged(engine):
     assert free1 == free0, f"free device memory changed by {free0 - free1} bytes"
 
 
+def test_no_alloc_refuses_a_capturing_stream(engine):
+    """The call ends by waiting for its stream, so under stream capture it queues nothing and
+    returns RSVD_ERR_ARGUMENT; the capture itself ends normally and the call works afterwards."""
+    L = engine.lib
+    _bind(L)
+    m, n, w = 256, 128, 16
+    A = torch.zeros(n, m, device="cuda", dtype=torch.float32)
+    X = torch.zeros(w, m, device="cuda", dtype=torch.float32)
+    Y = torch.zeros(w, n, device="cuda", dtype=torch.float32)
+    rc = L.rsvdpack_dev_sketch_t_noalloc(A.data_ptr(), m, m, n, X.data_ptr(), m, w, Y.data_ptr(), n, None)
+    assert rc == 0, engine.last_error()          # first call on the device: outside any capture
+    side = torch.cuda.Stream()
+    graph = torch.cuda.CUDAGraph()
+    with torch.cuda.stream(side):
+        graph.capture_begin()
+        try:
+            rc = L.rsvdpack_dev_sketch_t_noalloc(A.data_ptr(), m, m, n, X.data_ptr(), m, w, Y.data_ptr(), n,
+                                                 C.c_void_p(side.cuda_stream))
+        finally:
+            graph.capture_end()
+    code, msg = engine.last_error()
+    assert rc == 1 and code == 1 and "capturing" in msg
+    torch.cuda.synchronize()
+    rc = L.rsvdpack_dev_sketch_t_noalloc(A.data_ptr(), m, m, n, X.data_ptr(), m, w, Y.data_ptr(), n, None)
+    assert rc == 0, engine.last_error()
+
+
 def test_no_alloc_rejects_products_beyond_its_scratch(engine):
     L = engine.lib
     _bind(L)
