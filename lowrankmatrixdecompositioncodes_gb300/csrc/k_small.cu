@@ -738,6 +738,17 @@ __device__ __noinline__ void gr_apply(float *s0, float *s1, int ldr, int nch, co
 }
 
 constexpr int GR_THREADS = 256;   // 8 warps: up to 255 registers a thread for warp 0's register rounds
+
+// Block held in slot sl of CTA `rank` after s moves of a sweep: slot 0 is tournament position
+// rank, slot 1 position nblk-1-rank; position 0 keeps block 0 and positions 1..nblk-1 rotate by
+// one per move, so a sweep's nblk-1 moves bring every block back to its starting position.
+__device__ __forceinline__ int gr_block(int rank, int sl, int s, int nblk) {
+    const int pos = sl == 0 ? rank : nblk - 1 - rank, m = nblk - 1;
+    return pos == 0 ? 0 : ((pos - 1 - s) % m + m) % m + 1;
+}
+// The split cluster barrier of the block moves (all threads, warp-uniform).
+__device__ __forceinline__ void cluster_arrive() { asm volatile("barrier.cluster.arrive.release.aligned;" ::: "memory"); }
+__device__ __forceinline__ void cluster_wait() { asm volatile("barrier.cluster.wait.acquire.aligned;" ::: "memory"); }
 template <int CLN, int BS>
 __global__ void __launch_bounds__(GR_THREADS, 1) jacobi_gramreg_kernel(const double *G, long long ldg, int n, int ldr,
                                                                float tol, float stop_tol, int max_sweeps, float *Wout,
@@ -754,7 +765,6 @@ __global__ void __launch_bounds__(GR_THREADS, 1) jacobi_gramreg_kernel(const dou
     extern __shared__ __align__(16) unsigned char shraw[];
     const size_t slot_elems = (size_t)bs * ldr * 2;          // W columns then V columns
     float *buf = (float *)shraw;                              // [2 buffers][2 slots][slot_elems]
-    __shared__ int blk[2][2];
     __shared__ int rot_count, sr_rot;
     __shared__ int sweep_rot[CLN];
     __shared__ __align__(8) unsigned long long inbar;
@@ -769,8 +779,6 @@ __global__ void __launch_bounds__(GR_THREADS, 1) jacobi_gramreg_kernel(const dou
     auto slot_ptr = [&](float *base, int b, int sl) { return base + ((size_t)b * 2 + sl) * slot_elems; };
 
     if (threadIdx.x == 0) {
-        blk[0][0] = rank;
-        blk[0][1] = NBLK - 1 - rank;
         rot_count = 0;
         sweep_max = 0u;
         asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&inbar)) : "memory");
@@ -788,6 +796,13 @@ __global__ void __launch_bounds__(GR_THREADS, 1) jacobi_gramreg_kernel(const dou
         }
     }
     cluster.sync();
+    // Block moves: a split cluster barrier instead of a full one per move.  Each thread keeps
+    // one arrival outstanding between moves: it arrives once its incoming blocks have landed and
+    // waits just before the next move's copies, so every copy of the previous move (which read
+    // the buffers the next move writes) is complete, while the wait's latency hides behind the
+    // next super-round's Gram, rounds and update.  Sweep ends consume the arrival before their
+    // full barriers and re-arm it when another sweep follows.
+    cluster_arrive();
     int cur = 0, sweep = 0;
     uint32_t mphase = 0;
     const int nch = ldr / 4;                 // 16-byte row chunks; rows n..ldr-1 are zero
@@ -797,7 +812,7 @@ __global__ void __launch_bounds__(GR_THREADS, 1) jacobi_gramreg_kernel(const dou
     for (; sweep < max_sweeps; sweep++) {
         for (int sr = 0; sr < NBLK - 1; sr++) {
             float *s0 = slot_ptr(buf, cur, 0), *s1 = slot_ptr(buf, cur, 1);
-            const int b0 = blk[cur][0], b1 = blk[cur][1];
+            const int b0 = gr_block(rank, 0, sr, NBLK), b1 = gr_block(rank, 1, sr, NBLK);
             auto colw = [&](int c) { return (c < bs) ? s0 + (size_t)c * ldr : s1 + (size_t)(c - bs) * ldr; };
             auto colv = [&](int c) { return (c < bs) ? s0 + (size_t)(bs + c) * ldr : s1 + (size_t)c * ldr; };
             // ---- Gram: partial sums per (block, row slice)
@@ -886,6 +901,7 @@ __global__ void __launch_bounds__(GR_THREADS, 1) jacobi_gramreg_kernel(const dou
             else { dst1 = rank - 1; dsl1 = 1; }
             asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
             __syncthreads();
+            cluster_wait();                  // the previous move has landed everywhere
             if (threadIdx.x == 0) {
                 asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(&inbar)),
                              "r"(2u * slot_bytes)
@@ -899,8 +915,6 @@ __global__ void __launch_bounds__(GR_THREADS, 1) jacobi_gramreg_kernel(const dou
                         "cp.async.bulk.shared::cluster.shared::cta.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(rdst),
                         "r"(smem_addr(slot_ptr(buf, cur, sl))), "r"(slot_bytes), "r"(rbar)
                         : "memory");
-                    int *rb = cluster.map_shared_rank(&blk[nxt][ds], dc);
-                    *rb = sl ? b1 : b0;
                 }
             }
             {
@@ -918,9 +932,10 @@ __global__ void __launch_bounds__(GR_THREADS, 1) jacobi_gramreg_kernel(const dou
                 }
                 mphase ^= 1u;
             }
-            cluster.sync();
+            cluster_arrive();
             cur = nxt;
         }
+        cluster_wait();
         // ---- did any CTA rotate during this sweep, and how large was the largest cosine?
         if (threadIdx.x == 0) {
             sweep_max = __float_as_uint(wmax);
@@ -947,10 +962,11 @@ __global__ void __launch_bounds__(GR_THREADS, 1) jacobi_gramreg_kernel(const dou
         cluster.sync();
         if (total == 0) break;
         if (cmax < stop_tol) { sweep++; break; }
+        if (sweep + 1 < max_sweeps) cluster_arrive();       // the next sweep's first move waits on it
     }
     for (int sl = 0; sl < 2; sl++) {
         float *sp = slot_ptr(buf, cur, sl);
-        const int b = blk[cur][sl];
+        const int b = gr_block(rank, sl, 0, NBLK);          // a whole sweep of moves restores the start
         for (long long e = threadIdx.x; e < (long long)bs * n; e += blockDim.x) {
             const int j = (int)(e / n), r = (int)(e % n);
             const int c = b * bs + j;
