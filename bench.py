@@ -57,7 +57,8 @@ def parse():
     # bracket one leg's timed region with cudaProfilerStart/Stop (ncu --profile-from-start off)
     ap.add_argument("--profile-leg", choices=["solve", "learned", "batched"], default=None)
     # run one fixed profiling case (see PROFILE_CASES) and exit
-    ap.add_argument("--profile-case", choices=["update", "gemm3x", "solve", "pivot", "norm", "df64"], default=None)
+    ap.add_argument("--profile-case", choices=["update", "gemm3x", "solve", "pivot", "norm", "df64", "lxl"],
+                    default=None)
     return ap.parse_args()
 
 
@@ -1039,6 +1040,9 @@ def run_ours(args):
 #            FP32 matrix (2 GiB)
 #   df64     a reduced sketch pass of the two-sided ID workload as a double-float FP64 product
 #            (520 x 8000 by 8000 x 4000, rsvdpack_dev_gemm_df64)
+#   lxl      the FP32 l x l Jacobi SVD (rsvdpack_dev_small_svd(..., 1)) of a 272 x 272 factor shaped
+#            like the headline workload's: 13 separated singular values i^-1.5, then 259 packed into
+#            [0.0166, 0.0218], as the transposed triangular factor the engine hands the Jacobi
 
 def _prof_engine():
     from lowrankmatrixdecompositioncodes_gb300 import load_engine
@@ -1180,8 +1184,34 @@ def prof_case_df64(torch, eng):
     _prof_run(torch, call)
 
 
+def prof_case_lxl(torch, eng):
+    import numpy as np
+    L = eng.lib
+    L.rsvdpack_dev_small_svd.restype = C.c_int
+    L.rsvdpack_dev_small_svd.argtypes = [C.c_void_p, C.c_int, C.c_longlong, C.c_void_p, C.c_longlong, C.c_void_p,
+                                         C.c_void_p, C.c_longlong, C.c_int]
+    n = 272
+    g = np.random.default_rng(0)
+    head = np.arange(1, 14) ** -1.5
+    tail = np.sort(0.0166 + 0.0052 * g.beta(1.3, 1.0, n - 13))[::-1]
+    sv = np.concatenate([head, tail])
+    Q1, _ = np.linalg.qr(g.standard_normal((n, n)))
+    Q2, _ = np.linalg.qr(g.standard_normal((n, n)))
+    X = np.linalg.qr((Q1 * sv) @ Q2.T, mode="r").T            # lower triangular: R^T
+    G0 = torch.from_numpy(np.ascontiguousarray(X.T)).cuda()    # column-major X
+    U = torch.empty(n, n, device="cuda", dtype=torch.float64)
+    V = torch.empty_like(U)
+    S = torch.empty(n, device="cuda", dtype=torch.float64)
+
+    def call():
+        G = G0.clone()
+        if L.rsvdpack_dev_small_svd(G.data_ptr(), n, n, U.data_ptr(), n, S.data_ptr(), V.data_ptr(), n, 1) < 0:
+            raise RuntimeError(eng.last_error())
+    _prof_run(torch, call)
+
+
 PROFILE_CASES = {"update": prof_case_update, "gemm3x": prof_case_gemm3x, "solve": prof_case_solve,
-                 "pivot": prof_case_pivot, "norm": prof_case_norm, "df64": prof_case_df64}
+                 "pivot": prof_case_pivot, "norm": prof_case_norm, "df64": prof_case_df64, "lxl": prof_case_lxl}
 
 
 def main():
