@@ -521,19 +521,21 @@ __global__ void __launch_bounds__(512, 1) jacobi_block_cluster_kernel(const doub
 }
 
 // FP32 block-cyclic Jacobi, register-resident Gram form, for a fixed block width BS (the
-// cluster layout, block moves, pair schedule and convergence tests of
-// jacobi_block_cluster_kernel).  A super-round of the one-sided kernel costs one block barrier,
-// two n-row passes and three warp reductions per round; here it is three phases:
+// cluster layout, pair schedule and convergence tests of jacobi_block_cluster_kernel; its block
+// moves with a split cluster barrier, see the kernel).  A super-round of the one-sided kernel
+// costs one block barrier, two n-row passes and three warp reductions per round; here it is
+// three phases:
 //   Gram   Gl = P^T P of the CTA's NL = 2 BS local columns P (n rows), all warps: TK x TK
 //          output blocks x row slices (consecutive lanes take consecutive 16-byte row chunks),
 //          partial sums reduced through shared memory;
-//   rounds warp 0 alone: lane i holds row i of Gl and of Z (the accumulated rotation) in
-//          registers; the round's pair pattern is a compile-time function of the (unrolled)
-//          round index, so every register index is static.  A round: lane l < BS computes the
-//          rotation of pair l from Gl_pp, Gl_qq, Gl_pq fetched by shuffles, the rotations are
-//          broadcast, every lane applies the column rotations to its rows of Gl and Z, and the
-//          row rotation of Gl by exchanging rows with its partner; the diagonal block takes
-//          a' = a - t d, b' = b + t d, d' = 0.  No barrier and no shared memory inside a round.
+//   rounds lane i of warp 0 holds row i of Gl, lane i of warp 1 row i of Z (the accumulated
+//          rotation), in registers, with fixed pair positions and the columns moved between
+//          rounds so that every register index is static (gr_rounds_g / gr_rounds_z).  A round:
+//          lane l < BS of warp 0 computes the rotation of pair l from Gl_pp, Gl_qq, Gl_pq, the
+//          rotations are broadcast (shuffles within warp 0, shared memory and a named barrier
+//          to warp 1), the column rotations are applied to the rows of Gl and Z and the row
+//          rotation of Gl by exchanging rows with the partner lane; the diagonal block takes
+//          a' = a - t d, b' = b + t d, d' = 0.
 //   apply  P <- P Z for the W and V columns: one thread per 4-row chunk of one matrix, Z rows
 //          broadcast from shared memory, 4 x NL accumulators (skipped when nothing rotated).
 // Gl is formed afresh at every super-round, so the rounding of the two-sided updates does not
