@@ -551,11 +551,19 @@ __global__ void __launch_bounds__(512, 1) jacobi_block_cluster_kernel(const doub
 // its starting position.  A round: lane k < BS of warp 0 computes the rotation of pair k from dg
 // and Gl(k, partner) and publishes it (cos, sin, ballot) in shared memory, double-buffered by
 // round parity; a named barrier over the two warps hands it to warp 1, which rotates the columns
-// of Z while warp 0 rotates its rows of Gl by columns and against the partner's row.  Only the
+// of Z while warp 0 rotates its rows of Gl by columns, then takes its next row in one exchange:
+// the row rotation against the partner's row and the row and column moves fused (two shuffles
+// an entry, from the lane whose row moves here and from that lane's partner).  Only the
 // rotated pair's diagonal is updated exactly (a' = a - t d, b' = b + t d); its off-diagonal entry
 // keeps the rounding of the general formula, which is never read again in the super-round (each
 // pair meets once) and is recomputed at the next one.  Adjacent pairs are rotated as packed
 // FP32 pairs (FFMA2).
+// Position k's next occupant: a full round rotates positions 1..2 BS-1 by one (the circle
+// method), a cross round positions BS..2 BS-1; used for columns (registers) and rows (lanes).
+template <int BS, bool FULLR>
+__host__ __device__ constexpr int gr_next(int k) {
+    return FULLR ? (k == 0 ? 0 : (k == 2 * BS - 1 ? 1 : k + 1)) : (k < BS ? k : (k == 2 * BS - 1 ? BS : k + 1));
+}
 template <int BS, bool FULLR>
 __device__ __forceinline__ void gr_move(float (&g)[2 * BS]) {
     constexpr int NL = 2 * BS;
@@ -601,11 +609,13 @@ __device__ __forceinline__ void gr_rounds_g(float (&g)[2 * BS], float &dg, int l
     constexpr int NL = 2 * BS;
     constexpr int NR = FULLR ? NL - 1 : BS;
     const int partner = lane >= NL ? lane : (FULLR ? NL - 1 - lane : (lane < BS ? lane + BS : lane - BS));
-    const int pidx = lane >= NL ? 0 : (FULLR ? (lane < BS ? lane : NL - 1 - lane) : (lane < BS ? lane : lane - BS));
-    const bool is_p = lane < BS;
     const int src = lane >= NL ? lane
                     : (FULLR ? (lane == 0 ? 0 : (lane % (NL - 1)) + 1)
                              : (lane < BS ? lane : BS + (lane - BS + 1) % BS));
+    // the row this lane takes next is the rotated row of lane src: c_src row_src +- s_src row_psrc
+    const int psrc = src >= NL ? src : (FULLR ? NL - 1 - src : (src < BS ? src + BS : src - BS));
+    const int pidx_s = src >= NL ? 0 : (FULLR ? (src < BS ? src : NL - 1 - src) : (src < BS ? src : src - BS));
+    const bool isp_s = src < BS;
 #pragma unroll 1
     for (int r = 0; r < NR; r++) {
         float op = 0.f;                                   // Gl(lane, partner)
@@ -657,27 +667,37 @@ __device__ __forceinline__ void gr_rounds_g(float (&g)[2 * BS], float &dg, int l
                 C[k] = __shfl_sync(0xffffffffu, cs, k);
                 Sn[k] = __shfl_sync(0xffffffffu, sn, k);
             }
-            const float c_own = __shfl_sync(0xffffffffu, cs, pidx), s_own = __shfl_sync(0xffffffffu, sn, pidx);
-            const float dp_own = __shfl_sync(0xffffffffu, dgp, pidx), dq_own = __shfl_sync(0xffffffffu, dgq, pidx);
-            const bool act_own = lane < NL && ((bal >> pidx) & 1u);
+            const float c_s = __shfl_sync(0xffffffffu, cs, pidx_s), s_s = __shfl_sync(0xffffffffu, sn, pidx_s);
+            const float dp_s = __shfl_sync(0xffffffffu, dgp, pidx_s), dq_s = __shfl_sync(0xffffffffu, dgq, pidx_s);
+            const float dg_s = __shfl_sync(0xffffffffu, dg, src);
+            const bool act_s = src < NL && ((bal >> pidx_s) & 1u);
             gr_colrot<BS, FULLR>(g, C, Sn);
-            // row rotation (J^T Gl) against the partner's row: g = c g -+ s other
-            const float cr = act_own ? c_own : 1.f, sr = act_own ? (is_p ? -s_own : s_own) : 0.f;
+            // row rotation (J^T Gl) and the move in one exchange: position k of the next row is
+            // column gr_next(k) of src's rotated row, c row_src -+ s row_psrc (the arithmetic
+            // lane src would have done itself)
+            const float cr = act_s ? c_s : 1.f, sr = act_s ? (isp_s ? -s_s : s_s) : 0.f;
             const float2 cr2 = make_float2(cr, cr), sr2 = make_float2(sr, sr);
+            float ng[NL];
 #pragma unroll
             for (int k = 0; k < NL; k += 2) {
-                const float o0 = __shfl_sync(0xffffffffu, g[k], partner);
-                const float o1 = __shfl_sync(0xffffffffu, g[k + 1], partner);
-                const float2 nv = __ffma2_rn(cr2, make_float2(g[k], g[k + 1]), __fmul2_rn(sr2, make_float2(o0, o1)));
-                g[k] = nv.x;
-                g[k + 1] = nv.y;
+                const int m0 = gr_next<BS, FULLR>(k), m1 = gr_next<BS, FULLR>(k + 1);
+                const float x0 = __shfl_sync(0xffffffffu, g[m0], src), x1 = __shfl_sync(0xffffffffu, g[m1], src);
+                const float o0 = __shfl_sync(0xffffffffu, g[m0], psrc), o1 = __shfl_sync(0xffffffffu, g[m1], psrc);
+                const float2 nv = __ffma2_rn(cr2, make_float2(x0, x1), __fmul2_rn(sr2, make_float2(o0, o1)));
+                ng[k] = nv.x;
+                ng[k + 1] = nv.y;
             }
-            if (act_own) dg = is_p ? dp_own : dq_own;
-        }
-        gr_move<BS, FULLR>(g);
 #pragma unroll
-        for (int k = 0; k < NL; k++) g[k] = __shfl_sync(0xffffffffu, g[k], src);
-        dg = __shfl_sync(0xffffffffu, dg, src);
+            for (int k = 0; k < NL; k++) g[k] = ng[k];
+            dg = act_s ? (isp_s ? dp_s : dq_s) : dg_s;
+        } else {
+            float ng[NL];
+#pragma unroll
+            for (int k = 0; k < NL; k++) ng[k] = __shfl_sync(0xffffffffu, g[gr_next<BS, FULLR>(k)], src);
+#pragma unroll
+            for (int k = 0; k < NL; k++) g[k] = ng[k];
+            dg = __shfl_sync(0xffffffffu, dg, src);
+        }
     }
 }
 template <int BS, bool FULLR>
